@@ -1,0 +1,276 @@
+"""Benchmark: signed-distance voxels/s of calcFromGridWithDistances at 512^3 on the 1,310,720-triangle
+noisy icosphere (beta = 2, maxDistSq = +inf), one JSON line.
+
+  value        device-resident throughput: the mesh, tree and output live in HBM, each step is one
+               grid call on the GPU, L2 flushed (a 512 MB write) between steps outside the timed
+               events;
+  e2e          the public host API: every step creates the FastWindingNumber from host arrays
+               (upload + tree + dipoles) and returns the 512^3 result in host memory;
+  roofline     dominant kernel (the signed-distance grid kernel) against measured HBM bandwidth,
+               with the algorithmic bytes per voxel counted from the reference traversal;
+  cpu_baseline the oracle's FP32 reference algorithm on a bounded voxel sample, all host cores.
+
+`--impl reference` times the CPU reference algorithm alone (the reference's own code path is
+C++ that cannot travel to this machine; the restatement in oracle/ is timed instead).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+METRIC = "signed-dist voxels/s at 512³, 1M tris: plain vs surrogate-banded, ≤1e-5·diag"
+GRID = 512
+LEVEL = 8  # 20 * 4^8 = 1,310,720 triangles
+
+
+def _peaks():
+    try:
+        with open(PEAKS_FILE) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload():
+    from meshlib_gb300 import meshgen as mg
+    v, f = mg.noisy_icosphere(seed=0, level=LEVEL)
+    dims, xf = mg.grid_for(v, GRID)
+    return v, f, dims, xf
+
+
+def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=True):
+    """Oracle FP32 reference signed distance on a seeded random sample of voxels of the same grid.
+    Returns (voxels/s, threads, sample description, traversal counts per voxel or None)."""
+    import oracle as O
+    threads = threads or O.default_threads()
+    o = O.Oracle(v, f)
+    rng = np.random.default_rng(12345)
+    n_total = int(np.prod(dims))
+    A = np.asarray(xf[:9], np.float32).reshape(3, 3)
+    b = np.asarray(xf[9:], np.float32)
+
+    def sample(n):
+        idx = rng.integers(0, n_total, n)
+        z, rem = np.divmod(idx, dims[0] * dims[1])
+        y, x = np.divmod(rem, dims[0])
+        p = np.stack([x, y, z], 1).astype(np.float32)
+        return ((p[:, 0:1] * A[:, 0] + p[:, 1:2] * A[:, 1]) + p[:, 2:3] * A[:, 2] + b).astype(np.float32)
+
+    counts = None
+    if want_counts:
+        pts = sample(65536)
+        c = o.traversal_counts(pts)
+        counts = {"cp_nodes": float(c[0]) / len(pts), "cp_leaves": float(c[1]) / len(pts),
+                  "fwn_nodes": float(c[2]) / len(pts), "fwn_leaves": float(c[3]) / len(pts), "sample": len(pts)}
+    # calibrate then time a bounded sample
+    n = 4096 * threads
+    t0 = time.perf_counter()
+    o.vector_with_distances(sample(n), prec=0, threads=threads)
+    dt = time.perf_counter() - t0
+    n = int(max(n, min(64 << 20, n * seconds / max(dt, 1e-3))))
+    pts = sample(n)
+    t0 = time.perf_counter()
+    o.vector_with_distances(pts, prec=0, threads=threads)
+    dt = time.perf_counter() - t0
+    desc = f"{n} seeded random voxels of the {dims[0]}^3 grid, oracle FP32 reference algorithm, {threads} threads"
+    return n / dt, threads, desc, counts
+
+
+def bytes_per_voxel(c):
+    # 4 (output) + 32 per AABB node + 32 per dipole + 48 per leaf triangle (3 ids + 3 vertices)
+    return 4 + 32 * c["cp_nodes"] + 32 * c["fwn_nodes"] + 48 * (c["cp_leaves"] + c["fwn_leaves"])
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    v, f, dims, xf = make_workload()
+    rates = []
+    thr = None
+    desc = ""
+    for i in range(args.warmup + args.steps):
+        r, thr, desc, _ = cpu_reference_rate(v, f, dims, xf, seconds=4.0, want_counts=False)
+        if i >= args.warmup:
+            rates.append(r)
+    val = float(np.mean(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "voxels/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": GRID ** 3 / val * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded noisy icosphere)",
+            "config": {"workload": "calcFromGridWithDistances 512^3, noisy icosphere 1,310,720 tris, beta=2, maxDistSq=inf",
+                       "grid": GRID, "triangles": int(len(f))},
+            "cpu_baseline": {"value": val, "unit": "voxels/s", "cores": thr, "kind": "port", "sample": desc},
+            "e2e": {"value": val, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--grid", type=int, default=GRID)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import meshlib_gb300 as M
+    from meshlib_gb300 import build as B
+
+    B.build()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    grid = args.grid
+    from meshlib_gb300 import meshgen as mg
+    v, f = mg.noisy_icosphere(seed=0, level=LEVEL)
+    dims, xf = mg.grid_for(v, grid)
+    nvox = int(np.prod(dims))
+
+    # ---- device-resident leg: replicas, one full grid per rank per step (replicas only: the
+    # mesh is replicated and each rank computes its own grid; no collective on the data path)
+    fwn = M.FastWindingNumber(v, f, device=local)
+    out = torch.empty(nvox, dtype=torch.float32, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for _ in range(args.warmup):
+        fwn.calcFromGridWithDistances_dev(dims, xf, out.data_ptr(), stream=sp)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            fwn.calcFromGridWithDistances_dev(dims, xf, out.data_ptr(), stream=sp)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ms = float(np.sum([a.elapsed_time(b) for a, b in evs]))
+    ms_step = ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * nvox / (ms_step * 1e-3)
+    nan_frac = float(torch.isnan(out).float().mean().item())
+
+    # ---- end to end through the public host API
+    out_h = np.empty(nvox, np.float32)
+    e2e_times = []
+    for i in range(max(1, args.steps // 2) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = M.FastWindingNumber(v, f, device=local)
+        g.calcFromGridWithDistances(dims, xf, out=out_h)
+        t1 = time.perf_counter()
+        g.close()
+        if i > 0:
+            e2e_times.append(t1 - t0)
+    e2e_s = float(np.mean(e2e_times))
+    e2e_val = world * nvox / e2e_s
+
+    peak, peak_kind = _peaks()
+    line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded noisy icosphere, value noise)",
+            "config": {"workload": f"calcFromGridWithDistances {grid}^3, noisy icosphere {len(f):,} tris, beta=2, "
+                                   "maxDistSq=inf (plain)", "grid": grid, "triangles": int(len(f)),
+                       "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas x{world}"},
+            "gpu_launches": 2 * args.steps,
+            "e2e": {"value": e2e_val, "unit": "voxels/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
+                    "d2h_bytes_per_step": int(nvox * 4), "s_per_step": e2e_s},
+            "clocks": clk.summary(), "nan_fraction": nan_frac, "wall_s_timed": wall}
+    if rank == 0 and not args.no_cpu:
+        rate, thr, desc, counts = cpu_reference_rate(v, f, dims, xf)
+        bpv = bytes_per_voxel(counts)
+        achieved = bpv * nvox / (ms_step * 1e-3) / 1e9
+        line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                            "traffic": None, "peak_source": peak_kind, "bytes_per_voxel": bpv, "work_per_voxel": counts}
+        line["cpu_baseline"] = {"value": rate, "unit": "voxels/s", "cores": thr, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,174 @@
+/*
+ * gbfwn.h -- C ABI of the GB300-native fast-winding-number / signed-distance library.
+ *
+ * This is the drop-in boundary for MeshLib's `MR::IFastWindingNumber` hot path.  Every entry
+ * point is plain C: pointers, sizes and status codes, no C++ or torch types, so that a C++
+ * adapter (include/gbfwn.hpp), a ctypes stub or any other FFI can bind it.  Each function cites
+ * the reference interface it replaces (paths inside the MeshLib project).
+ *
+ * Conventions shared by all calls
+ *  - Meshes are indexed triangle lists: `verts` = nv x 3 floats, `tris` = nt x 3 int32 vertex
+ *    ids.  A triangle with any negative vertex id is an invalid (deleted) face: it is not part
+ *    of the tree and is never reported as self-intersecting -- MeshLib's `getValidFaces()`.
+ *  - Grids: voxel (x, y, z), x fastest, is written at x + y*dims[0] + z*dims[0]*dims[1]
+ *    (MRMesh/MRVolumeIndexer.h:131-139).  The voxel centre is gridToMeshXf applied to the float
+ *    vector (x, y, z); `xf` is 12 floats: the 3x3 linear part row by row, then the translation
+ *    (MRMesh/MRAffineXf.h:46).
+ *  - Calls without a `_dev` suffix take and return HOST memory and are synchronous, like
+ *    `MR::Cuda::FastWindingNumber`.  `_dev` calls take DEVICE pointers and only enqueue work on
+ *    `stream` (NULL = the handle's own stream).
+ *  - Progress callbacks receive a fraction in [0, 1] and return nonzero to continue, zero to
+ *    cancel (MRMesh/MRProgressCallback.h); a cancelled call returns GBFWN_CANCELLED.
+ *  - Errors: a nonzero status; `gbfwn_last_error()` gives the message of the last failure on the
+ *    calling thread (MeshLib's Expected<void> error string, MRCuda/MRCudaBasic.cpp:109-129).
+ */
+#ifndef GBFWN_H
+#define GBFWN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define GBFWN_API __declspec(dllexport)
+#else
+#define GBFWN_API __attribute__((visibility("default")))
+#endif
+
+enum gbfwn_status {
+    GBFWN_OK = 0,
+    GBFWN_CANCELLED = 1,      /* progress callback returned 0 (MeshLib: unexpectedOperationCanceled) */
+    GBFWN_OUT_OF_MEMORY = 2,  /* a device or pinned allocation failed */
+    GBFWN_CUDA_ERROR = 3,     /* any other CUDA runtime error ("NVIDIA GPU error: ...") */
+    GBFWN_INVALID = 4,        /* bad argument: null pointer, non-positive dims, vertex id out of range */
+    GBFWN_TIMEOUT = 5,        /* a bounded device-side wait gave up */
+    GBFWN_TRAVERSAL_OVERFLOW = 6 /* a traversal stack exceeded its fixed depth (tree too deep) */
+};
+
+typedef struct gbfwn_mesh_s* gbfwn_handle;
+
+/* MR::DistanceToMeshOptions (MRMesh/MRDistanceToMeshOptions.h:10-33); same field meaning and
+ * defaults: minDistSq = 0, maxDistSq = FLT_MAX, nullOutsideMinMax = 1, threshold = 0.5, beta = 2. */
+typedef struct gbfwn_dist_opts {
+    float minDistSq;
+    float maxDistSq;
+    int32_t nullOutsideMinMax;
+    float windingNumberThreshold;
+    float windingNumberBeta;
+} gbfwn_dist_opts;
+
+typedef int (*gbfwn_progress_cb)(float progress, void* user);
+
+/* IFastWindingNumberByParts::GridByPartsFunc (MRMesh/MRFastWindingNumber.h:88): receives one
+ * z-slab of `dims[2]` whole XY layers starting at layer `zOffset`, in host memory that stays valid
+ * only during the call.  Return 0 to continue; any other value aborts the whole call with that
+ * status. */
+typedef int (*gbfwn_slab_cb)(const float* data, const int32_t dims[3], int32_t zOffset, void* user);
+
+/* Computation knobs.  precise = 1 (default): compensated (Kahan) summation of the winding-number
+ * terms and FP64 re-evaluation of solid angles and point-triangle projections for queries within
+ * a few ulps of a triangle plane.  precise = 0: the reference's FP32 arithmetic, plain sums. */
+GBFWN_API void gbfwn_set_precise(gbfwn_handle h, int precise);
+
+/* Library version string. */
+GBFWN_API const char* gbfwn_version(void);
+
+/* Message of the last failure on this thread ("" if none). */
+GBFWN_API const char* gbfwn_last_error(void);
+
+/* Replaces MR::Cuda::FastWindingNumber::FastWindingNumber(const Mesh&) (MRCuda/MRCudaFastWindingNumber.h:21)
+ * together with its lazy prepareData_ (MRCuda/MRCudaFastWindingNumber.cpp:46-85): uploads the mesh to
+ * `device` and builds the AABB tree and dipoles there.  The tree is the reference's tree
+ * (MRMesh/MRAABBTreeMaker.hpp:51-165), node for node. */
+GBFWN_API int gbfwn_create(const float* verts, int64_t nv, const int32_t* tris, int64_t nt, int device,
+                           gbfwn_handle* out);
+
+/* Same, but the vertex and triangle arrays are already in device memory of `device`. */
+GBFWN_API int gbfwn_create_dev(const float* d_verts, int64_t nv, const int32_t* d_tris, int64_t nt, int device,
+                               gbfwn_handle* out);
+
+/* Frees the device data of the handle. */
+GBFWN_API int gbfwn_destroy(gbfwn_handle h);
+
+/* Number of triangles (faces, valid or not) and of tree nodes (2 * valid - 1). */
+GBFWN_API int64_t gbfwn_num_faces(gbfwn_handle h);
+GBFWN_API int64_t gbfwn_num_nodes(gbfwn_handle h);
+
+/* Copies the tree to host memory in the reference layout (MRMesh/MRAABBTreeNode.h:29-46):
+ * per node 8 words = box min xyz, box max xyz (float), l, r (int32; leaf <=> r < 0, then l = face),
+ * nodes in the reference's pre-order.  `dipoles` (may be NULL) receives 8 floats per node:
+ * pos xyz, area, dirArea xyz, rr (MRMesh/MRDipole.h:10-28). */
+GBFWN_API int gbfwn_get_tree(gbfwn_handle h, void* nodes, float* dipoles);
+
+/* IFastWindingNumber::calcFromVector (MRMesh/MRFastWindingNumber.h:26;
+ * MRCuda/MRCudaFastWindingNumber.cpp:87-127): winding numbers at n points (3 floats each).
+ * skipFace < 0: none. */
+GBFWN_API int gbfwn_from_vector(gbfwn_handle h, const float* pts, int64_t n, float beta, int32_t skipFace, float* out,
+                                gbfwn_progress_cb cb, void* user);
+GBFWN_API int gbfwn_from_vector_dev(gbfwn_handle h, const float* d_pts, int64_t n, float beta, int32_t skipFace,
+                                    float* d_out, void* stream);
+
+/* IFastWindingNumber::calcSelfIntersections (MRMesh/MRFastWindingNumber.h:31;
+ * MRCuda/MRCudaFastWindingNumber.cpp:129-173): bit f of `bits` (ceil(nt/64) little-endian 64-bit
+ * words, MeshLib's FaceBitSet block layout) is set when the winding number at the centroid of valid
+ * face f, skipping f itself, is < 0 or > 1.  `wn` (may be NULL) receives those winding numbers
+ * (NaN for invalid faces). */
+GBFWN_API int gbfwn_self_intersections(gbfwn_handle h, float beta, uint64_t* bits, float* wn, gbfwn_progress_cb cb,
+                                       void* user);
+GBFWN_API int gbfwn_self_intersections_dev(gbfwn_handle h, float beta, uint64_t* d_bits, float* d_wn, void* stream);
+
+/* IFastWindingNumber::calcFromGrid (MRMesh/MRFastWindingNumber.h:38;
+ * MRCuda/MRCudaFastWindingNumber.cpp:175-228): winding number at every voxel centre. */
+GBFWN_API int gbfwn_from_grid(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta, float* out,
+                              gbfwn_progress_cb cb, void* user);
+GBFWN_API int gbfwn_from_grid_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta, float* d_out,
+                                  void* stream);
+
+/* IFastWindingNumber::calcFromGridWithDistances (MRMesh/MRFastWindingNumber.h:44;
+ * MRMesh/MRFastWindingNumber.cpp:69-94; MRCuda/MRCudaFastWindingNumber.cpp:230-283): distance to the
+ * mesh with the winding-number sign (negative where the winding number > threshold); NaN where the
+ * squared distance is outside [minDistSq, maxDistSq) and nullOutsideMinMax is set. */
+GBFWN_API int gbfwn_from_grid_with_distances(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                             const gbfwn_dist_opts* opts, float* out, gbfwn_progress_cb cb, void* user);
+GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                 const gbfwn_dist_opts* opts, float* d_out, void* stream);
+
+/* MR::FastWindingNumber::calcWithDistances at arbitrary points (MRMesh/MRFastWindingNumber.h:62; the CPU
+ * class has it, the interface does not). */
+GBFWN_API int gbfwn_vector_with_distances(gbfwn_handle h, const float* pts, int64_t n, const gbfwn_dist_opts* opts,
+                                          float* out, gbfwn_progress_cb cb, void* user);
+GBFWN_API int gbfwn_vector_with_distances_dev(gbfwn_handle h, const float* d_pts, int64_t n,
+                                              const gbfwn_dist_opts* opts, float* d_out, void* stream);
+
+/* IFastWindingNumberByParts::calcFromGridByParts / calcFromGridWithDistancesByParts
+ * (MRMesh/MRFastWindingNumber.h:96-106; MRCuda/MRCudaFastWindingNumber.cpp:285-431): the grid is
+ * produced in z-slabs of whole XY layers, consecutive slabs overlapping by `layerOverlap` layers,
+ * and handed to `slab` in order while the GPU computes the next slab.  `maxLayersPerSlab` <= 0
+ * picks the slab height from free device memory. */
+GBFWN_API int gbfwn_from_grid_by_parts(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta,
+                                       int32_t layerOverlap, int32_t maxLayersPerSlab, gbfwn_slab_cb slab,
+                                       void* slabUser, gbfwn_progress_cb cb, void* user);
+GBFWN_API int gbfwn_from_grid_with_distances_by_parts(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                      const gbfwn_dist_opts* opts, int32_t layerOverlap,
+                                                      int32_t maxLayersPerSlab, gbfwn_slab_cb slab, void* slabUser,
+                                                      gbfwn_progress_cb cb, void* user);
+
+/* GPU memory estimators, MR::CudaAccessor::fastWindingNumberMeshMemory / fromGridMemory /
+ * fromVectorMemory / selfIntersectionsMemory (MRViewer/MRCudaAccessor.cpp:162-194). */
+GBFWN_API size_t gbfwn_mesh_memory(int64_t nv, int64_t nt);
+GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t dims[3]);
+GBFWN_API size_t gbfwn_from_vector_memory(int64_t nv, int64_t nt, int64_t npts);
+GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt);
+
+/* Test hook: makes the next `count` device allocations of this thread fail with
+ * GBFWN_OUT_OF_MEMORY (host-side fault injection; no device fault is involved). */
+GBFWN_API void gbfwn_debug_fail_next_allocs(int count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFWN_H */

@@ -1,0 +1,295 @@
+"""GB300-native fast winding number / signed distance for triangle meshes.
+
+Python front-end over the C ABI in ``include/gbfwn.h`` (library ``libgbfwn.so`` built in-tree by
+``meshlib_gb300.build``).  The class :class:`FastWindingNumber` mirrors MeshLib's
+``MR::IFastWindingNumber`` / ``IFastWindingNumberByParts`` (MRMesh/MRFastWindingNumber.h:11-107)
+method for method -- the same names as the reference's Python bindings
+(``mrcudapy.FastWindingNumber(mesh)``), numpy arrays in and out.  Errors raise
+:class:`FwnError` (the reference returns ``Expected<void>``; its bindings raise).
+
+There is no CPU fallback: every call goes to the CUDA library, and importing the module on a
+machine without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Callable, Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgbfwn.so")
+FLT_MAX = 3.4028234663852886e38
+
+OK, CANCELLED, OUT_OF_MEMORY, CUDA_ERROR, INVALID, TIMEOUT, TRAVERSAL_OVERFLOW = range(7)
+
+
+class FwnError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class _DistOpts(ctypes.Structure):
+    _fields_ = [("minDistSq", ctypes.c_float), ("maxDistSq", ctypes.c_float), ("nullOutsideMinMax", ctypes.c_int32),
+                ("windingNumberThreshold", ctypes.c_float), ("windingNumberBeta", ctypes.c_float)]
+
+
+@dataclass
+class DistanceToMeshOptions:
+    """MR::DistanceToMeshOptions (MRMesh/MRDistanceToMeshOptions.h:10-33), same defaults."""
+    minDistSq: float = 0.0
+    maxDistSq: float = FLT_MAX
+    nullOutsideMinMax: bool = True
+    windingNumberThreshold: float = 0.5
+    windingNumberBeta: float = 2.0
+
+    def _c(self) -> _DistOpts:
+        return _DistOpts(self.minDistSq, self.maxDistSq, int(bool(self.nullOutsideMinMax)), self.windingNumberThreshold,
+                         self.windingNumberBeta)
+
+
+PROGRESS = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_float, ctypes.c_void_p)
+SLAB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                        ctypes.c_void_p)
+
+# (name, restype, argtypes) of every exported symbol of include/gbfwn.h
+_vp, _i32, _i64, _f = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float
+_SIGS = [
+    ("gbfwn_version", ctypes.c_char_p, []),
+    ("gbfwn_last_error", ctypes.c_char_p, []),
+    ("gbfwn_set_precise", None, [_vp, ctypes.c_int]),
+    ("gbfwn_create", ctypes.c_int, [_vp, _i64, _vp, _i64, ctypes.c_int, ctypes.POINTER(_vp)]),
+    ("gbfwn_create_dev", ctypes.c_int, [_vp, _i64, _vp, _i64, ctypes.c_int, ctypes.POINTER(_vp)]),
+    ("gbfwn_destroy", ctypes.c_int, [_vp]),
+    ("gbfwn_num_faces", _i64, [_vp]),
+    ("gbfwn_num_nodes", _i64, [_vp]),
+    ("gbfwn_get_tree", ctypes.c_int, [_vp, _vp, _vp]),
+    ("gbfwn_from_vector", ctypes.c_int, [_vp, _vp, _i64, _f, _i32, _vp, PROGRESS, _vp]),
+    ("gbfwn_from_vector_dev", ctypes.c_int, [_vp, _vp, _i64, _f, _i32, _vp, _vp]),
+    ("gbfwn_self_intersections", ctypes.c_int, [_vp, _f, _vp, _vp, PROGRESS, _vp]),
+    ("gbfwn_self_intersections_dev", ctypes.c_int, [_vp, _f, _vp, _vp, _vp]),
+    ("gbfwn_from_grid", ctypes.c_int, [_vp, _vp, _vp, _f, _vp, PROGRESS, _vp]),
+    ("gbfwn_from_grid_dev", ctypes.c_int, [_vp, _vp, _vp, _f, _vp, _vp]),
+    ("gbfwn_from_grid_with_distances", ctypes.c_int, [_vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, PROGRESS, _vp]),
+    ("gbfwn_from_grid_with_distances_dev", ctypes.c_int, [_vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, _vp]),
+    ("gbfwn_vector_with_distances", ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(_DistOpts), _vp, PROGRESS, _vp]),
+    ("gbfwn_vector_with_distances_dev", ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(_DistOpts), _vp, _vp]),
+    ("gbfwn_from_grid_by_parts", ctypes.c_int, [_vp, _vp, _vp, _f, _i32, _i32, SLAB, _vp, PROGRESS, _vp]),
+    ("gbfwn_from_grid_with_distances_by_parts", ctypes.c_int,
+     [_vp, _vp, _vp, ctypes.POINTER(_DistOpts), _i32, _i32, SLAB, _vp, PROGRESS, _vp]),
+    ("gbfwn_mesh_memory", ctypes.c_size_t, [_i64, _i64]),
+    ("gbfwn_from_grid_memory", ctypes.c_size_t, [_i64, _i64, _vp]),
+    ("gbfwn_from_vector_memory", ctypes.c_size_t, [_i64, _i64, _i64]),
+    ("gbfwn_self_intersections_memory", ctypes.c_size_t, [_i64, _i64]),
+    ("gbfwn_debug_fail_next_allocs", None, [ctypes.c_int]),
+]
+EXPORTED = [s[0] for s in _SIGS]
+
+_lib = None
+
+
+def lib():
+    """Loads ``libgbfwn.so`` (raises if it has not been built: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m meshlib_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in _SIGS:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(st: int):
+    if st != OK:
+        raise FwnError(st, lib().gbfwn_last_error().decode())
+
+
+def _progress(cb: Optional[Callable[[float], bool]]):
+    if cb is None:
+        return PROGRESS(), None
+    fn = PROGRESS(lambda p, _u: 1 if cb(float(p)) else 0)
+    return fn, fn
+
+
+def _xf12(xf) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(xf, np.float32).reshape(-1))
+    if a.size != 12:
+        raise ValueError("gridToMeshXf must be 12 floats: 3x3 rows then translation")
+    return a
+
+
+class FastWindingNumber:
+    """GB300 implementation of ``MR::IFastWindingNumber`` + ``IFastWindingNumberByParts``.
+
+    ``verts``: (nv, 3) float32, ``faces``: (nt, 3) int32 (a face with a negative id is invalid).
+    The tree and dipoles are built on the device at construction and cached, as
+    ``MR::Cuda::FastWindingNumber::prepareData_`` caches them (MRCuda/MRCudaFastWindingNumber.cpp:46-85).
+    """
+
+    def __init__(self, verts: np.ndarray, faces: np.ndarray, device: int = 0, precise: bool = True):
+        self.verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        self.faces = np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
+        self._h = ctypes.c_void_p()
+        self._L = lib()
+        _check(self._L.gbfwn_create(_p(self.verts), len(self.verts), _p(self.faces), len(self.faces), device,
+                                    ctypes.byref(self._h)))
+        self.set_precise(precise)
+
+    @classmethod
+    def from_device(cls, d_verts_ptr: int, nv: int, d_faces_ptr: int, nt: int, device: int = 0, precise: bool = True):
+        self = cls.__new__(cls)
+        self.verts = self.faces = None
+        self._h = ctypes.c_void_p()
+        self._L = lib()
+        _check(self._L.gbfwn_create_dev(ctypes.c_void_p(d_verts_ptr), nv, ctypes.c_void_p(d_faces_ptr), nt, device,
+                                        ctypes.byref(self._h)))
+        self.set_precise(precise)
+        return self
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gbfwn_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def set_precise(self, precise: bool):
+        self._L.gbfwn_set_precise(self._h, 1 if precise else 0)
+
+    def num_faces(self) -> int:
+        return int(self._L.gbfwn_num_faces(self._h))
+
+    def tree(self):
+        """(nodes, dipoles): the reference-layout tree (structured array) and (n, 8) float32 dipoles."""
+        n = int(self._L.gbfwn_num_nodes(self._h))
+        dt = np.dtype([("min", np.float32, 3), ("max", np.float32, 3), ("l", np.int32), ("r", np.int32)])
+        nodes = np.empty(n, dt)
+        dip = np.empty((n, 8), np.float32)
+        _check(self._L.gbfwn_get_tree(self._h, _p(nodes), _p(dip)))
+        return nodes, dip
+
+    # -- MR::IFastWindingNumber
+    def calcFromVector(self, points: np.ndarray, beta: float = 2.0, skipFace: int = -1, cb=None) -> np.ndarray:
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        out = np.empty(len(pts), np.float32)
+        c, _keep = _progress(cb)
+        _check(self._L.gbfwn_from_vector(self._h, _p(pts), len(pts), beta, int(skipFace), _p(out), c, None))
+        return out
+
+    def calcSelfIntersections(self, beta: float = 2.0, cb=None, with_wn: bool = False):
+        """Bool array over faces (MeshLib's FaceBitSet); optionally the centroid winding numbers too."""
+        nt = self.num_faces()
+        words = np.zeros((nt + 63) // 64, np.uint64)
+        wn = np.empty(nt, np.float32) if with_wn else None
+        c, _keep = _progress(cb)
+        _check(self._L.gbfwn_self_intersections(self._h, beta, _p(words), _p(wn), c, None))
+        bits = np.unpackbits(words.view(np.uint8), bitorder="little")[:nt].astype(bool)
+        return (bits, wn) if with_wn else bits
+
+    def calcFromGrid(self, dims, gridToMeshXf, beta: float = 2.0, cb=None) -> np.ndarray:
+        d = np.asarray(dims, np.int32)
+        out = np.empty(int(np.prod(d.astype(np.int64))), np.float32)
+        c, _keep = _progress(cb)
+        _check(self._L.gbfwn_from_grid(self._h, _p(d), _p(_xf12(gridToMeshXf)), beta, _p(out), c, None))
+        return out
+
+    def calcFromGridWithDistances(self, dims, gridToMeshXf, options: Optional[DistanceToMeshOptions] = None, cb=None,
+                                  out: Optional[np.ndarray] = None) -> np.ndarray:
+        d = np.asarray(dims, np.int32)
+        n = int(np.prod(d.astype(np.int64)))
+        if out is None:
+            out = np.empty(n, np.float32)
+        o = (options or DistanceToMeshOptions())._c()
+        c, _keep = _progress(cb)
+        _check(self._L.gbfwn_from_grid_with_distances(self._h, _p(d), _p(_xf12(gridToMeshXf)), ctypes.byref(o), _p(out),
+                                                       c, None))
+        return out
+
+    def calcWithDistances(self, points: np.ndarray, options: Optional[DistanceToMeshOptions] = None, cb=None) -> np.ndarray:
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        out = np.empty(len(pts), np.float32)
+        o = (options or DistanceToMeshOptions())._c()
+        c, _keep = _progress(cb)
+        _check(self._L.gbfwn_vector_with_distances(self._h, _p(pts), len(pts), ctypes.byref(o), _p(out), c, None))
+        return out
+
+    # -- MR::IFastWindingNumberByParts
+    def calcFromGridByParts(self, resFunc, dims, gridToMeshXf, beta: float = 2.0, layerOverlap: int = 0, cb=None,
+                            maxLayersPerSlab: int = 0):
+        self._by_parts(resFunc, dims, gridToMeshXf, None, beta, layerOverlap, cb, maxLayersPerSlab)
+
+    def calcFromGridWithDistancesByParts(self, resFunc, dims, gridToMeshXf, options=None, layerOverlap: int = 0, cb=None,
+                                         maxLayersPerSlab: int = 0):
+        self._by_parts(resFunc, dims, gridToMeshXf, options or DistanceToMeshOptions(), 2.0, layerOverlap, cb,
+                       maxLayersPerSlab)
+
+    def _by_parts(self, resFunc, dims, xf, options, beta, layerOverlap, cb, maxLayers):
+        d = np.asarray(dims, np.int32)
+        err = []
+
+        def slab(data, sd, zoff, _u):
+            try:
+                n = int(sd[0]) * int(sd[1]) * int(sd[2])
+                arr = np.ctypeslib.as_array(data, shape=(n,)).copy()
+                r = resFunc(arr, (int(sd[0]), int(sd[1]), int(sd[2])), int(zoff))
+                return 0 if (r is None or r is True) else int(r) or 1
+            except Exception as ex:  # surfaced after the call
+                err.append(ex)
+                return CANCELLED
+
+        s = SLAB(slab)
+        c, _keep = _progress(cb)
+        if options is None:
+            st = self._L.gbfwn_from_grid_by_parts(self._h, _p(d), _p(_xf12(xf)), beta, layerOverlap, maxLayers, s, None, c,
+                                                 None)
+        else:
+            o = options._c()
+            st = self._L.gbfwn_from_grid_with_distances_by_parts(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o),
+                                                                layerOverlap, maxLayers, s, None, c, None)
+        if err:
+            raise err[0]
+        _check(st)
+
+    # -- device-pointer variants (torch tensors or any CUDA pointer); enqueue only
+    def calcFromGridWithDistances_dev(self, dims, xf, d_out_ptr: int, options=None, stream: int = 0):
+        d = np.asarray(dims, np.int32)
+        o = (options or DistanceToMeshOptions())._c()
+        _check(self._L.gbfwn_from_grid_with_distances_dev(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o),
+                                                           ctypes.c_void_p(d_out_ptr), ctypes.c_void_p(stream or None)))
+
+    def calcFromGrid_dev(self, dims, xf, d_out_ptr: int, beta: float = 2.0, stream: int = 0):
+        d = np.asarray(dims, np.int32)
+        _check(self._L.gbfwn_from_grid_dev(self._h, _p(d), _p(_xf12(xf)), beta, ctypes.c_void_p(d_out_ptr),
+                                           ctypes.c_void_p(stream or None)))
+
+    def calcFromVector_dev(self, d_pts_ptr: int, n: int, d_out_ptr: int, beta: float = 2.0, skipFace: int = -1,
+                           stream: int = 0):
+        _check(self._L.gbfwn_from_vector_dev(self._h, ctypes.c_void_p(d_pts_ptr), n, beta, skipFace,
+                                             ctypes.c_void_p(d_out_ptr), ctypes.c_void_p(stream or None)))
+
+
+def memory_estimates(nv: int, nt: int, dims=None, npts: int = 0) -> dict:
+    L = lib()
+    d = np.asarray(dims if dims is not None else (0, 0, 0), np.int32)
+    return {"mesh": int(L.gbfwn_mesh_memory(nv, nt)), "from_grid": int(L.gbfwn_from_grid_memory(nv, nt, _p(d))),
+            "from_vector": int(L.gbfwn_from_vector_memory(nv, nt, npts)),
+            "self_intersections": int(L.gbfwn_self_intersections_memory(nv, nt))}

@@ -1,0 +1,375 @@
+// Tree and dipole construction.
+//
+// The tree must be the reference's tree node for node: the far-field decisions of the winding
+// number (MRMesh/MRDipole.h:18-27) depend on how triangles are grouped, so any other tree gives
+// different (equally approximate) winding numbers.  The reference builds it by recursive median
+// splits (MRMesh/MRAABBTreeMaker.hpp:51-165): the leaves of a node are ordered by the box-centre
+// coordinate (min + max) along the node box's largest dimension, then the second largest, then
+// the smallest, then by face id; the first floor(n/2) go left; nodes are stored in pre-order.
+// Because that order is total, the split sets do not depend on how the partition is computed.
+//
+// This file is compiled with -fmad=false: every float expression below rounds each operation
+// separately, exactly like the reference's CPU code, so boxes, dipoles and radii are
+// bit-identical to the reference's.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gbfwn {
+
+namespace {
+
+struct HBox {
+    float mn[3], mx[3];
+};
+
+struct HLeaf {
+    int32_t id;
+    float c[3];  // min + max per dimension: the comparison key
+    HBox box;
+};
+
+// MRMesh/MRAABBTree.cpp:15-29 + MRMesh/MRBox.h:260-270
+inline HBox faceBox(const float* v, const int32_t* t) {
+    HBox b;
+    for (int d = 0; d < 3; ++d) {
+        float lo = FLT_MAX, hi = -FLT_MAX;
+        for (int k = 0; k < 3; ++k) {
+            const float x = v[3 * t[k] + d];
+            if (x < lo) lo = x;
+            if (x > hi) hi = x;
+        }
+        b.mn[d] = std::nextafter(lo, -FLT_MAX);
+        b.mx[d] = std::nextafter(hi, FLT_MAX);
+    }
+    return b;
+}
+
+// MRMesh/MRBox.h:376-396: dims ascending by (extent, index)
+inline void sortedDims(const HBox& b, int sd[3]) {
+    float e[3];
+    int id[3] = {0, 1, 2};
+    for (int i = 0; i < 3; ++i) e[i] = b.mx[i] - b.mn[i];
+    for (int i = 0; i + 1 < 3; ++i)
+        for (int j = i + 1; j < 3; ++j)
+            if (e[j] < e[i] || (e[j] == e[i] && id[j] < id[i])) {
+                std::swap(e[i], e[j]);
+                std::swap(id[i], id[j]);
+            }
+    for (int i = 0; i < 3; ++i) sd[i] = id[i];
+}
+
+struct Sub {
+    int32_t root, first, num;
+};
+
+void buildRange(std::vector<HLeaf>& leaves, std::vector<RefNode>& nodes, Sub s0, int threads) {
+    std::vector<Sub> st;
+    st.push_back(s0);
+    std::vector<std::thread> spawned;
+    while (!st.empty()) {
+        Sub s = st.back();
+        st.pop_back();
+        RefNode& nd = nodes[s.root];
+        if (s.num == 1) {
+            const HLeaf& L = leaves[s.first];
+            nd = RefNode{L.box.mn[0], L.box.mn[1], L.box.mn[2], L.box.mx[0], L.box.mx[1], L.box.mx[2], L.id, -1};
+            continue;
+        }
+        HBox b{{FLT_MAX, FLT_MAX, FLT_MAX}, {-FLT_MAX, -FLT_MAX, -FLT_MAX}};
+        for (int i = 0; i < s.num; ++i) {
+            const HBox& lb = leaves[s.first + i].box;
+            for (int d = 0; d < 3; ++d) {
+                if (lb.mn[d] < b.mn[d]) b.mn[d] = lb.mn[d];
+                if (lb.mx[d] > b.mx[d]) b.mx[d] = lb.mx[d];
+            }
+        }
+        int sd[3];
+        sortedDims(b, sd);
+        const int d2 = sd[2], d1 = sd[1], d0 = sd[0];
+        auto less = [d2, d1, d0](const HLeaf& x, const HLeaf& y) {
+            if (x.c[d2] != y.c[d2]) return x.c[d2] < y.c[d2];
+            if (x.c[d1] != y.c[d1]) return x.c[d1] < y.c[d1];
+            if (x.c[d0] != y.c[d0]) return x.c[d0] < y.c[d0];
+            return x.id < y.id;
+        };
+        const int mid = s.first + s.num / 2;
+        std::nth_element(leaves.begin() + s.first, leaves.begin() + mid, leaves.begin() + s.first + s.num, less);
+        const int nl = mid - s.first;
+        nd = RefNode{b.mn[0], b.mn[1], b.mn[2], b.mx[0], b.mx[1], b.mx[2], s.root + 1, s.root + 2 * nl};
+        const Sub L{s.root + 1, s.first, nl}, R{s.root + 2 * nl, mid, s.num - nl};
+        if (threads >= 2 && s.num >= 4096) {
+            const int rt = threads / 2;
+            spawned.emplace_back([&leaves, &nodes, R, rt] { buildRange(leaves, nodes, R, rt); });
+            threads -= rt;
+            st.push_back(L);
+        } else {
+            st.push_back(R);
+            st.push_back(L);
+        }
+    }
+    for (auto& t : spawned) t.join();
+}
+
+}  // namespace
+
+// Host construction of the reference topology (the reference builds it on the CPU too,
+// MRCuda/MRCudaFastWindingNumber.cpp:70-80).
+void hostBuildTopology(const float* verts, int64_t nv, const int32_t* tris, int64_t nt, std::vector<RefNode>& nodes) {
+    (void)nv;
+    std::vector<HLeaf> leaves;
+    leaves.reserve(size_t(nt));
+    for (int64_t f = 0; f < nt; ++f) {
+        const int32_t* t = tris + 3 * f;
+        if (t[0] < 0 || t[1] < 0 || t[2] < 0) continue;  // invalid face: not in the tree
+        HLeaf L;
+        L.id = int32_t(f);
+        L.box = faceBox(verts, t);
+        for (int d = 0; d < 3; ++d) L.c[d] = L.box.mn[d] + L.box.mx[d];
+        leaves.push_back(L);
+    }
+    const int n = int(leaves.size());
+    nodes.assign(n > 0 ? size_t(2 * n - 1) : 0, RefNode{});
+    if (n == 0) return;
+    int threads = int(std::thread::hardware_concurrency());
+    if (threads < 1) threads = 1;
+    buildRange(leaves, nodes, Sub{0, 0, n}, threads);
+}
+
+// ------------------------------------------------------------------------------------ device
+namespace {
+
+__device__ __forceinline__ float3 vload(const float* v, int i) { return make_float3(v[3 * i], v[3 * i + 1], v[3 * i + 2]); }
+
+// MRMesh/MRDipole.cpp:29-44 leaf dipoles: pos = area * triCenter, area = |dirArea|,
+// dirArea = 0.5 * cross(b - a, c - a) (MRMesh/MRMeshMath.cpp:119-124,140-149).
+__global__ void leafDipolesKernel(const RefNode* __restrict__ nodes, int64_t nNodes, const float* __restrict__ verts,
+                                  const int32_t* __restrict__ tris, float* __restrict__ dip8, int* __restrict__ arrive) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    arrive[i] = 0;
+    const RefNode nd = nodes[i];
+    float* d = dip8 + 8 * i;
+    if (nd.r >= 0) return;
+    const int32_t* t = tris + 3 * int64_t(nd.l);
+    const float3 a = vload(verts, t[0]), b = vload(verts, t[1]), c = vload(verts, t[2]);
+    const float3 ab = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+    const float3 ac = make_float3(c.x - a.x, c.y - a.y, c.z - a.z);
+    const float3 da = make_float3(0.5f * (ab.y * ac.z - ab.z * ac.y), 0.5f * (ab.z * ac.x - ab.x * ac.z),
+                                  0.5f * (ab.x * ac.y - ab.y * ac.x));
+    const float area = sqrtf(da.x * da.x + da.y * da.y + da.z * da.z);
+    const float third = 1 / 3.0f;
+    const float3 ctr = make_float3(third * (a.x + b.x + c.x), third * (a.y + b.y + c.y), third * (a.z + b.z + c.z));
+    d[0] = area * ctr.x;
+    d[1] = area * ctr.y;
+    d[2] = area * ctr.z;
+    d[3] = area;
+    d[4] = da.x;
+    d[5] = da.y;
+    d[6] = da.z;
+    d[7] = 0;
+}
+
+__global__ void parentsKernel(const RefNode* __restrict__ nodes, int64_t nNodes, int32_t* __restrict__ parent) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    if (i == 0) parent[0] = -1;
+    const RefNode nd = nodes[i];
+    if (nd.r < 0) return;
+    parent[nd.l] = int32_t(i);
+    parent[nd.r] = int32_t(i);
+}
+
+// MRMesh/MRDipole.cpp:47-60: internal dipole = left + right (pos and dirArea are still
+// area-weighted sums here).  Each leaf thread climbs; the second child to arrive at a parent
+// computes it.  dl + dr is commutative, so the result is the reference's whatever arrives first.
+__global__ void sumUpKernel(const RefNode* __restrict__ nodes, int64_t nNodes, const int32_t* __restrict__ parent,
+                            float* dip8, int* arrive) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    if (nodes[i].r >= 0) return;
+    int32_t p = parent[i];
+    while (p >= 0) {
+        __threadfence();
+        if (atomicAdd(&arrive[p], 1) == 0) return;  // first arrival: the sibling's thread finishes p
+        __threadfence();
+        const RefNode nd = nodes[p];
+        const volatile float* dl = dip8 + 8 * int64_t(nd.l);
+        const volatile float* dr = dip8 + 8 * int64_t(nd.r);
+        float* d = dip8 + 8 * int64_t(p);
+        for (int k = 0; k < 7; ++k) d[k] = dl[k] + dr[k];
+        d[7] = 0;
+        p = parent[p];
+    }
+}
+
+// MRMesh/MRDipole.cpp:63-70 + 11-21: centre of mass and squared distance to the farthest box corner.
+__global__ void finalizeKernel(const RefNode* __restrict__ nodes, int64_t nNodes, float* __restrict__ dip8) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    float* d = dip8 + 8 * i;
+    float px = d[0], py = d[1], pz = d[2];
+    const float area = d[3];
+    if (area > 0) {
+        const float inv = 1 / area;
+        px = px * inv;
+        py = py * inv;
+        pz = pz * inv;
+    }
+    const RefNode nd = nodes[i];
+    const float mn[3] = {nd.minx, nd.miny, nd.minz}, mx[3] = {nd.maxx, nd.maxy, nd.maxz}, p[3] = {px, py, pz};
+    float rr = 0;
+    for (int k = 0; k < 3; ++k) {
+        const float a = p[k] - mn[k], b = p[k] - mx[k];
+        rr = rr + fmaxf(a * a, b * b);
+    }
+    d[0] = px;
+    d[1] = py;
+    d[2] = pz;
+    d[7] = rr;
+}
+
+// Wide query records (layout in common.cuh).  irank[i] = internal index of node i (or -1),
+// slot[i] = leaf slot of node i (or -1).
+__device__ __forceinline__ int32_t linkOf(int32_t node, const int32_t* irank, const int32_t* slot) {
+    const int32_t k = irank[node];
+    return k >= 0 ? k : ~slot[node];
+}
+
+__global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, const float* __restrict__ dip8,
+                           const int32_t* __restrict__ irank, const int32_t* __restrict__ slot,
+                           const float* __restrict__ verts, const int32_t* __restrict__ tris, float4* __restrict__ cp,
+                           float4* __restrict__ dip, float4* __restrict__ tri, int32_t* __restrict__ faceSlot) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    const RefNode nd = nodes[i];
+    if (nd.r < 0) {
+        const int32_t s = slot[i];
+        const int32_t* t = tris + 3 * int64_t(nd.l);
+        const float3 a = vload(verts, t[0]), b = vload(verts, t[1]), c = vload(verts, t[2]);
+        tri[3 * int64_t(s) + 0] = make_float4(a.x, a.y, a.z, __int_as_float(nd.l));
+        tri[3 * int64_t(s) + 1] = make_float4(b.x, b.y, b.z, 0.f);
+        tri[3 * int64_t(s) + 2] = make_float4(c.x, c.y, c.z, 0.f);
+        faceSlot[nd.l] = s;
+        return;
+    }
+    const int64_t k = irank[i];
+    const RefNode L = nodes[nd.l], R = nodes[nd.r];
+    const int32_t ll = linkOf(nd.l, irank, slot), rl = linkOf(nd.r, irank, slot);
+    cp[4 * k + 0] = make_float4(L.minx, L.miny, L.minz, __int_as_float(ll));
+    cp[4 * k + 1] = make_float4(L.maxx, L.maxy, L.maxz, __int_as_float(rl));
+    cp[4 * k + 2] = make_float4(R.minx, R.miny, R.minz, 0.f);
+    cp[4 * k + 3] = make_float4(R.maxx, R.maxy, R.maxz, 0.f);
+    const float* dl = dip8 + 8 * int64_t(nd.l);
+    const float* dr = dip8 + 8 * int64_t(nd.r);
+    dip[4 * k + 0] = make_float4(dl[0], dl[1], dl[2], dl[7]);
+    dip[4 * k + 1] = make_float4(dl[4], dl[5], dl[6], __int_as_float(ll));
+    dip[4 * k + 2] = make_float4(dr[0], dr[1], dr[2], dr[7]);
+    dip[4 * k + 3] = make_float4(dr[4], dr[5], dr[6], __int_as_float(rl));
+}
+
+__global__ void fillInt(int32_t* p, int64_t n, int32_t v) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+inline unsigned blocksFor(int64_t n, int t) { return unsigned((n + t - 1) / t); }
+
+}  // namespace
+
+// Computes dipoles and the query layout on the device from reference nodes already in `out.nodes`.
+cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const int32_t* hIrankSlot, DeviceTree& out,
+                             Allocator& A, cudaStream_t s) {
+    const int64_t nNodes = out.nLeaves > 0 ? 2 * out.nLeaves - 1 : 0;
+    cudaError_t e;
+    int32_t *parent = nullptr, *arrive = nullptr, *irs = nullptr;
+    if ((e = A.alloc((void**)&out.faceSlot, sizeof(int32_t) * size_t(std::max<int64_t>(out.nFaces, 1))))) return e;
+    fillInt<<<blocksFor(std::max<int64_t>(out.nFaces, 1), 256), 256, 0, s>>>(out.faceSlot, out.nFaces, -1);
+    if (nNodes == 0) return cudaGetLastError();
+    if ((e = A.alloc((void**)&out.dip8, sizeof(float) * 8 * size_t(nNodes)))) return e;
+    if ((e = A.alloc((void**)&parent, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = A.alloc((void**)&arrive, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = A.alloc((void**)&irs, sizeof(int32_t) * 2 * size_t(nNodes)))) return e;
+    const int64_t nInt = std::max<int64_t>(out.nInternal, 1);
+    if ((e = A.alloc((void**)&out.cp, sizeof(float4) * 4 * size_t(nInt)))) return e;
+    if ((e = A.alloc((void**)&out.dip, sizeof(float4) * 4 * size_t(nInt)))) return e;
+    if ((e = A.alloc((void**)&out.tri, sizeof(float4) * 3 * size_t(out.nLeaves)))) return e;
+    if ((e = cudaMemcpyAsync(irs, hIrankSlot, sizeof(int32_t) * 2 * size_t(nNodes), cudaMemcpyHostToDevice, s))) return e;
+    const unsigned B = blocksFor(nNodes, 256);
+    leafDipolesKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, dVerts, dTris, out.dip8, arrive);
+    parentsKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, parent);
+    sumUpKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, parent, out.dip8, arrive);
+    finalizeKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, out.dip8);
+    packKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, out.dip8, irs, irs + nNodes, dVerts, dTris, out.cp, out.dip, out.tri,
+                                 out.faceSlot);
+    return cudaGetLastError();
+}
+
+cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, DeviceTree& out,
+                            Allocator& A, cudaStream_t s, std::string& err) {
+    // Topology on the host (same as the reference's GPU path); dipoles and layout on the device.
+    std::vector<float> hv(size_t(nv) * 3);
+    std::vector<int32_t> ht(size_t(nt) * 3);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(hv.data(), dVerts, hv.size() * sizeof(float), cudaMemcpyDeviceToHost, s))) return e;
+    if ((e = cudaMemcpyAsync(ht.data(), dTris, ht.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s))) return e;
+    if ((e = cudaStreamSynchronize(s))) return e;
+    for (size_t i = 0; i < ht.size(); ++i)
+        if (ht[i] >= nv) {
+            err = "triangle vertex id out of range";
+            return cudaErrorInvalidValue;
+        }
+    std::vector<RefNode> nodes;
+    hostBuildTopology(hv.data(), nv, ht.data(), nt, nodes);
+    const int64_t nNodes = int64_t(nodes.size());
+    out.nFaces = nt;
+    out.nLeaves = nNodes > 0 ? (nNodes + 1) / 2 : 0;
+    out.nInternal = out.nLeaves > 0 ? out.nLeaves - 1 : 0;
+    std::vector<int32_t> irs(size_t(2 * nNodes));
+    int32_t ni = 0, nl = 0;
+    for (int64_t i = 0; i < nNodes; ++i) {
+        if (nodes[i].r >= 0) {
+            irs[i] = ni++;
+            irs[nNodes + i] = -1;
+        } else {
+            irs[i] = -1;
+            irs[nNodes + i] = nl++;
+        }
+    }
+    if (nNodes > 0) {
+        if ((e = A.alloc((void**)&out.nodes, sizeof(RefNode) * size_t(nNodes)))) return e;
+        if ((e = cudaMemcpyAsync(out.nodes, nodes.data(), sizeof(RefNode) * size_t(nNodes), cudaMemcpyHostToDevice, s)))
+            return e;
+    }
+    if ((e = finishDeviceTree(dVerts, dTris, irs.data(), out, A, s))) return e;
+    if ((e = cudaStreamSynchronize(s))) return e;  // host vectors above must outlive the copies
+    // root data for the kernels' parameter block
+    QueryTree& q = out.q;
+    q.cp = out.cp;
+    q.dip = out.dip;
+    q.tri = out.tri;
+    q.faceSlot = out.faceSlot;
+    q.nLeaves = int32_t(out.nLeaves);
+    q.nFaces = int32_t(out.nFaces);
+    if (nNodes > 0) {
+        float rd[8];
+        if ((e = cudaMemcpy(rd, out.dip8, sizeof(rd), cudaMemcpyDeviceToHost))) return e;
+        const RefNode& r = nodes[0];
+        const int32_t rootLink = r.r >= 0 ? 0 : ~0;
+        int32_t li = rootLink;
+        float lf;
+        std::memcpy(&lf, &li, 4);
+        q.rootDip0 = make_float4(rd[0], rd[1], rd[2], rd[7]);
+        q.rootDip1 = make_float4(rd[4], rd[5], rd[6], lf);
+        q.rootBox0 = make_float4(r.minx, r.miny, r.minz, lf);
+        q.rootBox1 = make_float4(r.maxx, r.maxy, r.maxz, 0.f);
+    }
+    return cudaSuccess;
+}
+
+}  // namespace gbfwn

@@ -1,0 +1,598 @@
+// C ABI (include/gbfwn.h): handle management, host <-> device staging, slab pipelining.
+//
+// Host-facing calls behave like MR::Cuda::FastWindingNumber (MRCuda/MRCudaFastWindingNumber.cpp):
+// synchronous, results in host memory, progress reported at phase boundaries and per z-slab,
+// cancellation honoured between slabs.  Unlike the reference, the output is produced in z-slabs on
+// one stream while finished slabs are copied to the host on a second stream, so the device->host
+// copy of slab k overlaps the computation of slabs k+1...
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gbfwn.h"
+#include "common.cuh"
+
+using namespace gbfwn;
+
+namespace gbfwn {
+cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const int32_t* hIrankSlot, DeviceTree& out,
+                             Allocator& A, cudaStream_t s);
+}
+
+namespace {
+
+thread_local std::string g_lastError;
+thread_local int g_failAllocs = 0;
+
+int fail(int status, const std::string& msg) {
+    g_lastError = msg;
+    return status;
+}
+
+int cudaFail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) return fail(GBFWN_OUT_OF_MEMORY, std::string("NVIDIA GPU error: out of memory in ") + what);
+    return fail(GBFWN_CUDA_ERROR, std::string("NVIDIA GPU error: ") + cudaGetErrorString(e) + " in " + what);
+}
+
+cudaError_t devMalloc(void** p, size_t bytes) {
+    if (g_failAllocs > 0) {
+        --g_failAllocs;
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes ? bytes : 16);
+}
+
+struct ListAllocator : Allocator {
+    std::vector<void*> ptrs;
+    cudaError_t alloc(void** p, size_t bytes) override {
+        cudaError_t e = devMalloc(p, bytes);
+        if (e == cudaSuccess) ptrs.push_back(*p);
+        return e;
+    }
+    void freeAll() {
+        for (void* p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+bool progress(gbfwn_progress_cb cb, void* user, float p) { return !cb || cb(p, user) != 0; }
+
+}  // namespace
+
+struct gbfwn_mesh_s {
+    int device = 0;
+    cudaStream_t stream = nullptr, copyStream = nullptr;
+    ListAllocator treeMem;
+    DeviceTree tree;
+    float* dVerts = nullptr;
+    int32_t* dTris = nullptr;
+    int64_t nv = 0, nt = 0;
+    unsigned* scratch = nullptr;  // [0] ticket counter, [1] status bits
+    int precise = 1;
+    // device staging reused across host-API calls
+    void* outBuf = nullptr;
+    size_t outCap = 0;
+    void* inBuf = nullptr;
+    size_t inCap = 0;
+    std::vector<cudaEvent_t> events;
+    std::mutex mu;  // calls on one handle are serialised (the reference is not re-entrant per object)
+
+    cudaError_t ensure(void** buf, size_t* cap, size_t bytes) {
+        if (*cap >= bytes) return cudaSuccess;
+        if (*buf) cudaFree(*buf);
+        *buf = nullptr;
+        *cap = 0;
+        cudaError_t e = devMalloc(buf, bytes);
+        if (e == cudaSuccess) *cap = bytes;
+        return e;
+    }
+    cudaError_t ensureEvents(size_t n) {
+        while (events.size() < n) {
+            cudaEvent_t ev;
+            cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e) return e;
+            events.push_back(ev);
+        }
+        return cudaSuccess;
+    }
+    int checkStatus() {
+        unsigned st[2] = {0, 0};
+        cudaError_t e = cudaMemcpyAsync(st, scratch, sizeof(st), cudaMemcpyDeviceToHost, stream);
+        if (!e) e = cudaStreamSynchronize(stream);
+        if (e) return cudaFail(e, "status read");
+        if (st[1] & kStatusStackOverflow)
+            return fail(GBFWN_TRAVERSAL_OVERFLOW, "traversal stack overflow (tree deeper than 32 levels)");
+        if (st[1] & kStatusTimeout) return fail(GBFWN_TIMEOUT, "device-side wait timed out");
+        return GBFWN_OK;
+    }
+    cudaError_t resetStatus(cudaStream_t s) { return cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned), s); }
+};
+
+namespace {
+
+bool toXf(const float* xf, Xf& out) {
+    if (!xf) return false;
+    for (int i = 0; i < 9; ++i) out.a[i] = xf[i];
+    for (int i = 0; i < 3; ++i) out.b[i] = xf[9 + i];
+    return true;
+}
+
+DistOpts toOpts(const gbfwn_dist_opts* o) {
+    DistOpts d;
+    if (!o) {
+        d = DistOpts{0.f, FLT_MAX, 1, 0.5f, 2.f};
+    } else {
+        d = DistOpts{o->minDistSq, o->maxDistSq, o->nullOutsideMinMax, o->windingNumberThreshold, o->windingNumberBeta};
+    }
+    return d;
+}
+
+bool validDims(const int32_t* dims) { return dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0; }
+
+int createCommon(gbfwn_mesh_s* h, const std::string& where) {
+    std::string err;
+    cudaError_t e = buildDeviceTree(h->dVerts, h->nv, h->dTris, h->nt, h->tree, h->treeMem, h->stream, err);
+    if (e == cudaErrorInvalidValue && !err.empty()) return fail(GBFWN_INVALID, err);
+    if (e) return cudaFail(e, where.c_str());
+    return GBFWN_OK;
+}
+
+int newHandle(int device, gbfwn_mesh_s** out) {
+    auto* h = new gbfwn_mesh_s;
+    h->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (!e) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (!e) e = cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking);
+    if (!e) e = h->treeMem.alloc((void**)&h->scratch, 64);
+    if (!e) e = cudaMemsetAsync(h->scratch, 0, 64, h->stream);
+    if (e) {
+        int st = cudaFail(e, "gbfwn_create");
+        gbfwn_destroy(h);
+        return st;
+    }
+    *out = h;
+    return GBFWN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+GBFWN_API const char* gbfwn_version(void) { return "gbfwn 0.1 (sm_103a)"; }
+
+GBFWN_API const char* gbfwn_last_error(void) { return g_lastError.c_str(); }
+
+GBFWN_API void gbfwn_debug_fail_next_allocs(int count) { g_failAllocs = count; }
+
+GBFWN_API void gbfwn_set_precise(gbfwn_handle h, int precise) {
+    if (h) h->precise = precise ? 1 : 0;
+}
+
+GBFWN_API int gbfwn_create(const float* verts, int64_t nv, const int32_t* tris, int64_t nt, int device, gbfwn_handle* out) {
+    if (!out || nv < 0 || nt < 0 || (nv > 0 && !verts) || (nt > 0 && !tris)) return fail(GBFWN_INVALID, "gbfwn_create: bad arguments");
+    if (nt > INT32_MAX / 2) return fail(GBFWN_INVALID, "gbfwn_create: too many triangles");
+    *out = nullptr;
+    for (int64_t i = 0; i < 3 * nt; ++i)
+        if (tris[i] >= nv) return fail(GBFWN_INVALID, "gbfwn_create: triangle vertex id out of range");
+    gbfwn_mesh_s* h = nullptr;
+    int st = newHandle(device, &h);
+    if (st) return st;
+    DeviceGuard g(device);
+    h->nv = nv;
+    h->nt = nt;
+    cudaError_t e = h->treeMem.alloc((void**)&h->dVerts, sizeof(float) * 3 * size_t(nv));
+    if (!e) e = h->treeMem.alloc((void**)&h->dTris, sizeof(int32_t) * 3 * size_t(nt));
+    if (!e && nv) e = cudaMemcpyAsync(h->dVerts, verts, sizeof(float) * 3 * size_t(nv), cudaMemcpyHostToDevice, h->stream);
+    if (!e && nt) e = cudaMemcpyAsync(h->dTris, tris, sizeof(int32_t) * 3 * size_t(nt), cudaMemcpyHostToDevice, h->stream);
+    if (e) {
+        st = cudaFail(e, "gbfwn_create upload");
+        gbfwn_destroy(h);
+        return st;
+    }
+    if ((st = createCommon(h, "gbfwn_create"))) {
+        gbfwn_destroy(h);
+        return st;
+    }
+    *out = h;
+    return GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_create_dev(const float* d_verts, int64_t nv, const int32_t* d_tris, int64_t nt, int device,
+                               gbfwn_handle* out) {
+    if (!out || nv < 0 || nt < 0 || (nv > 0 && !d_verts) || (nt > 0 && !d_tris)) return fail(GBFWN_INVALID, "gbfwn_create_dev: bad arguments");
+    if (nt > INT32_MAX / 2) return fail(GBFWN_INVALID, "gbfwn_create_dev: too many triangles");
+    *out = nullptr;
+    gbfwn_mesh_s* h = nullptr;
+    int st = newHandle(device, &h);
+    if (st) return st;
+    DeviceGuard g(device);
+    h->nv = nv;
+    h->nt = nt;
+    cudaError_t e = h->treeMem.alloc((void**)&h->dVerts, sizeof(float) * 3 * size_t(nv));
+    if (!e) e = h->treeMem.alloc((void**)&h->dTris, sizeof(int32_t) * 3 * size_t(nt));
+    if (!e && nv) e = cudaMemcpyAsync(h->dVerts, d_verts, sizeof(float) * 3 * size_t(nv), cudaMemcpyDeviceToDevice, h->stream);
+    if (!e && nt) e = cudaMemcpyAsync(h->dTris, d_tris, sizeof(int32_t) * 3 * size_t(nt), cudaMemcpyDeviceToDevice, h->stream);
+    if (e) {
+        st = cudaFail(e, "gbfwn_create_dev copy");
+        gbfwn_destroy(h);
+        return st;
+    }
+    if ((st = createCommon(h, "gbfwn_create_dev"))) {
+        gbfwn_destroy(h);
+        return st;
+    }
+    *out = h;
+    return GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_destroy(gbfwn_handle h) {
+    if (!h) return GBFWN_OK;
+    {
+        DeviceGuard g(h->device);
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        if (h->copyStream) cudaStreamSynchronize(h->copyStream);
+        h->treeMem.freeAll();
+        if (h->outBuf) cudaFree(h->outBuf);
+        if (h->inBuf) cudaFree(h->inBuf);
+        for (auto ev : h->events) cudaEventDestroy(ev);
+        if (h->stream) cudaStreamDestroy(h->stream);
+        if (h->copyStream) cudaStreamDestroy(h->copyStream);
+    }
+    delete h;
+    return GBFWN_OK;
+}
+
+GBFWN_API int64_t gbfwn_num_faces(gbfwn_handle h) { return h ? h->nt : 0; }
+GBFWN_API int64_t gbfwn_num_nodes(gbfwn_handle h) { return h && h->tree.nLeaves ? 2 * h->tree.nLeaves - 1 : 0; }
+
+GBFWN_API int gbfwn_get_tree(gbfwn_handle h, void* nodes, float* dipoles) {
+    if (!h) return fail(GBFWN_INVALID, "gbfwn_get_tree: null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    const int64_t n = gbfwn_num_nodes(h);
+    if (n == 0) return GBFWN_OK;
+    cudaError_t e = cudaSuccess;
+    if (nodes) e = cudaMemcpyAsync(nodes, h->tree.nodes, sizeof(RefNode) * size_t(n), cudaMemcpyDeviceToHost, h->stream);
+    if (!e && dipoles) e = cudaMemcpyAsync(dipoles, h->tree.dip8, sizeof(float) * 8 * size_t(n), cudaMemcpyDeviceToHost, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cudaFail(e, "gbfwn_get_tree");
+    return GBFWN_OK;
+}
+
+// ------------------------------------------------------------------------- device-pointer calls
+GBFWN_API int gbfwn_from_vector_dev(gbfwn_handle h, const float* d_pts, int64_t n, float beta, int32_t skipFace,
+                                    float* d_out, void* stream) {
+    if (!h || n < 0 || (n > 0 && (!d_pts || !d_out))) return fail(GBFWN_INVALID, "gbfwn_from_vector_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaError_t e = launchVectorFwn(h->tree.q, d_pts, n, beta, skipFace, h->precise, d_out, h->scratch, s);
+    return e ? cudaFail(e, "gbfwn_from_vector_dev") : GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_vector_with_distances_dev(gbfwn_handle h, const float* d_pts, int64_t n, const gbfwn_dist_opts* opts,
+                                              float* d_out, void* stream) {
+    if (!h || n < 0 || (n > 0 && (!d_pts || !d_out))) return fail(GBFWN_INVALID, "gbfwn_vector_with_distances_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaError_t e = launchVectorSdf(h->tree.q, d_pts, n, toOpts(opts), h->precise, d_out, h->scratch, s);
+    return e ? cudaFail(e, "gbfwn_vector_with_distances_dev") : GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_self_intersections_dev(gbfwn_handle h, float beta, uint64_t* d_bits, float* d_wn, void* stream) {
+    if (!h || !d_bits) return fail(GBFWN_INVALID, "gbfwn_self_intersections_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaError_t e = launchSelfIntersections(h->tree.q, beta, h->precise, d_bits, d_wn, h->scratch, s);
+    return e ? cudaFail(e, "gbfwn_self_intersections_dev") : GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_from_grid_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta, float* d_out,
+                                  void* stream) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !d_out) return fail(GBFWN_INVALID, "gbfwn_from_grid_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
+    cudaError_t e = launchGridFwn(h->tree.q, r, X, beta, h->precise, d_out, h->scratch, s);
+    return e ? cudaFail(e, "gbfwn_from_grid_dev") : GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                 const gbfwn_dist_opts* opts, float* d_out, void* stream) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !d_out) return fail(GBFWN_INVALID, "gbfwn_from_grid_with_distances_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
+    cudaError_t e = launchGridSdf(h->tree.q, r, X, toOpts(opts), h->precise, d_out, h->scratch, s);
+    return e ? cudaFail(e, "gbfwn_from_grid_with_distances_dev") : GBFWN_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------- host-memory calls
+namespace {
+
+// Computes a grid in slabs of whole XY layers.  Each slab's kernel writes into the device output
+// buffer; the copy stream waits for it and moves it to `hostOut` (if not null) and/or hands it to
+// `slab` (by-parts mode, with `overlap` layers shared between consecutive slabs).
+template <typename LaunchFn>
+int runGrid(gbfwn_mesh_s* h, const int32_t dims[3], LaunchFn launch, float* hostOut, int32_t overlap, int32_t maxLayers,
+            gbfwn_slab_cb slab, void* slabUser, gbfwn_progress_cb cb, void* user, const char* what) {
+    const size_t layer = size_t(dims[0]) * dims[1];
+    const int nz = dims[2];
+    if (!progress(cb, user, 0.f)) return fail(GBFWN_CANCELLED, "operation canceled");
+    // slab height: about 16 M voxels per slab, at least 1 layer
+    int slabLayers = int(std::max<size_t>(1, (size_t(16) << 20) / layer));
+    if (maxLayers > 0) slabLayers = std::min(slabLayers, int(maxLayers));
+    if (overlap < 0) overlap = 0;
+    if (slab && slabLayers <= overlap) slabLayers = overlap + 1;
+    slabLayers = std::min(slabLayers, nz);
+    struct SlabR {
+        int z0, z1;  // layers computed [z0, z1)
+    };
+    std::vector<SlabR> slabs;
+    if (!slab) {
+        for (int z = 0; z < nz; z += slabLayers) slabs.push_back({z, std::min(nz, z + slabLayers)});
+    } else {
+        // MRMesh/MRChunkIterator.h:44-47 semantics: chunks of slabLayers layers stepping by
+        // slabLayers - overlap
+        const int step = slabLayers - overlap;
+        for (int z = 0;; z += step) {
+            const int z1 = std::min(nz, z + slabLayers);
+            slabs.push_back({z, z1});
+            if (z1 >= nz) break;
+        }
+    }
+    // device buffer: the whole grid in host mode, two slab buffers in by-parts mode
+    const bool whole = !slab;
+    const size_t slabBytes = layer * size_t(slabLayers) * sizeof(float);
+    const size_t need = whole ? layer * size_t(nz) * sizeof(float) : 2 * slabBytes;
+    cudaError_t e = h->ensure(&h->outBuf, &h->outCap, need);
+    if (!e) e = h->ensureEvents(2 * slabs.size() + 2);
+    if (e) return cudaFail(e, what);
+    if ((e = h->resetStatus(h->stream))) return cudaFail(e, what);
+    float* dOut = (float*)h->outBuf;
+    std::vector<float> pinnedless;  // by-parts host slab
+    if (slab) pinnedless.resize(layer * size_t(slabLayers));
+    // in by-parts mode slab i reuses buffer i%2, so the kernel of slab i waits for the copy of slab i-2
+    for (size_t i = 0; i < slabs.size(); ++i) {
+        const SlabR& sr = slabs[i];
+        float* buf = whole ? dOut + layer * size_t(sr.z0) : dOut + (i % 2) * (slabBytes / sizeof(float));
+        if (!whole && i >= 2) cudaStreamWaitEvent(h->stream, h->events[2 * (i - 2) + 1], 0);
+        GridRange r{dims[0], dims[1], dims[2], sr.z0, sr.z1, sr.z0};
+        if ((e = launch(r, buf, h->stream))) return cudaFail(e, what);
+        cudaEventRecord(h->events[2 * i], h->stream);
+        if (!whole) {
+            // by-parts: launches run ahead by at most one slab; hand slabs over in order
+            if (i >= 1) {
+                const size_t j = i - 1;
+                const SlabR& pr = slabs[j];
+                const float* pbuf = dOut + (j % 2) * (slabBytes / sizeof(float));
+                const size_t cnt = layer * size_t(pr.z1 - pr.z0);
+                cudaStreamWaitEvent(h->copyStream, h->events[2 * j], 0);
+                if ((e = cudaMemcpyAsync(pinnedless.data(), pbuf, cnt * sizeof(float), cudaMemcpyDeviceToHost, h->copyStream)))
+                    return cudaFail(e, what);
+                cudaEventRecord(h->events[2 * j + 1], h->copyStream);
+                if ((e = cudaStreamSynchronize(h->copyStream))) return cudaFail(e, what);
+                const int32_t sd[3] = {dims[0], dims[1], pr.z1 - pr.z0};
+                const int rc = slab(pinnedless.data(), sd, pr.z0, slabUser);
+                if (rc) {
+                    cudaStreamSynchronize(h->stream);
+                    return fail(rc, "slab callback returned an error");
+                }
+                if (!progress(cb, user, float(j + 1) / float(slabs.size()))) {
+                    cudaStreamSynchronize(h->stream);
+                    return fail(GBFWN_CANCELLED, "operation canceled");
+                }
+            }
+        }
+    }
+    if (whole) {
+        for (size_t i = 0; i < slabs.size(); ++i) {
+            const SlabR& sr = slabs[i];
+            const size_t off = layer * size_t(sr.z0), cnt = layer * size_t(sr.z1 - sr.z0);
+            cudaStreamWaitEvent(h->copyStream, h->events[2 * i], 0);
+            if (hostOut && (e = cudaMemcpyAsync(hostOut + off, dOut + off, cnt * sizeof(float), cudaMemcpyDeviceToHost, h->copyStream)))
+                return cudaFail(e, what);
+            if (cb) {
+                if ((e = cudaStreamSynchronize(h->copyStream))) return cudaFail(e, what);
+                if (!progress(cb, user, float(i + 1) / float(slabs.size()))) {
+                    cudaStreamSynchronize(h->stream);
+                    return fail(GBFWN_CANCELLED, "operation canceled");
+                }
+            }
+        }
+        if ((e = cudaStreamSynchronize(h->copyStream))) return cudaFail(e, what);
+    } else {
+        const size_t j = slabs.size() - 1;
+        const SlabR& pr = slabs[j];
+        const float* pbuf = dOut + (j % 2) * (slabBytes / sizeof(float));
+        const size_t cnt = layer * size_t(pr.z1 - pr.z0);
+        cudaStreamWaitEvent(h->copyStream, h->events[2 * j], 0);
+        if ((e = cudaMemcpyAsync(pinnedless.data(), pbuf, cnt * sizeof(float), cudaMemcpyDeviceToHost, h->copyStream)))
+            return cudaFail(e, what);
+        if ((e = cudaStreamSynchronize(h->copyStream))) return cudaFail(e, what);
+        int stc = h->checkStatus();
+        if (stc) return stc;
+        const int32_t sd[3] = {dims[0], dims[1], pr.z1 - pr.z0};
+        const int rc = slab(pinnedless.data(), sd, pr.z0, slabUser);
+        if (rc) return fail(rc, "slab callback returned an error");
+        if (!progress(cb, user, 1.f)) return fail(GBFWN_CANCELLED, "operation canceled");
+    }
+    if ((e = cudaStreamSynchronize(h->stream))) return cudaFail(e, what);
+    return h->checkStatus();
+}
+
+template <typename LaunchFn>
+int runPoints(gbfwn_mesh_s* h, const float* pts, int64_t n, float* out, LaunchFn launch, gbfwn_progress_cb cb, void* user,
+              const char* what) {
+    if (!progress(cb, user, 0.f)) return fail(GBFWN_CANCELLED, "operation canceled");
+    if (n == 0) return progress(cb, user, 1.f) ? GBFWN_OK : fail(GBFWN_CANCELLED, "operation canceled");
+    cudaError_t e = h->ensure(&h->inBuf, &h->inCap, sizeof(float) * 3 * size_t(n));
+    if (!e) e = h->ensure(&h->outBuf, &h->outCap, sizeof(float) * size_t(n));
+    if (!e) e = h->resetStatus(h->stream);
+    if (!e) e = cudaMemcpyAsync(h->inBuf, pts, sizeof(float) * 3 * size_t(n), cudaMemcpyHostToDevice, h->stream);
+    if (e) return cudaFail(e, what);
+    if ((e = launch((const float*)h->inBuf, (float*)h->outBuf, h->stream))) return cudaFail(e, what);
+    if ((e = cudaMemcpyAsync(out, h->outBuf, sizeof(float) * size_t(n), cudaMemcpyDeviceToHost, h->stream))) return cudaFail(e, what);
+    if ((e = cudaStreamSynchronize(h->stream))) return cudaFail(e, what);
+    int st = h->checkStatus();
+    if (st) return st;
+    return progress(cb, user, 1.f) ? GBFWN_OK : fail(GBFWN_CANCELLED, "operation canceled");
+}
+
+}  // namespace
+
+extern "C" {
+
+GBFWN_API int gbfwn_from_vector(gbfwn_handle h, const float* pts, int64_t n, float beta, int32_t skipFace, float* out,
+                                gbfwn_progress_cb cb, void* user) {
+    if (!h || n < 0 || (n > 0 && (!pts || !out))) return fail(GBFWN_INVALID, "gbfwn_from_vector: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    return runPoints(
+        h, pts, n, out,
+        [&](const float* dp, float* dout, cudaStream_t s) {
+            return launchVectorFwn(h->tree.q, dp, n, beta, skipFace, h->precise, dout, h->scratch, s);
+        },
+        cb, user, "gbfwn_from_vector");
+}
+
+GBFWN_API int gbfwn_vector_with_distances(gbfwn_handle h, const float* pts, int64_t n, const gbfwn_dist_opts* opts,
+                                          float* out, gbfwn_progress_cb cb, void* user) {
+    if (!h || n < 0 || (n > 0 && (!pts || !out))) return fail(GBFWN_INVALID, "gbfwn_vector_with_distances: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    const DistOpts o = toOpts(opts);
+    return runPoints(
+        h, pts, n, out,
+        [&](const float* dp, float* dout, cudaStream_t s) {
+            return launchVectorSdf(h->tree.q, dp, n, o, h->precise, dout, h->scratch, s);
+        },
+        cb, user, "gbfwn_vector_with_distances");
+}
+
+GBFWN_API int gbfwn_self_intersections(gbfwn_handle h, float beta, uint64_t* bits, float* wn, gbfwn_progress_cb cb,
+                                       void* user) {
+    if (!h || !bits) return fail(GBFWN_INVALID, "gbfwn_self_intersections: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    if (!progress(cb, user, 0.f)) return fail(GBFWN_CANCELLED, "operation canceled");
+    const size_t words = size_t((h->nt + 63) / 64);
+    const size_t bytes = words * sizeof(uint64_t) + (wn ? sizeof(float) * size_t(h->nt) : 0);
+    cudaError_t e = h->ensure(&h->outBuf, &h->outCap, bytes + 16);
+    if (!e) e = h->resetStatus(h->stream);
+    if (e) return cudaFail(e, "gbfwn_self_intersections");
+    uint64_t* dBits = (uint64_t*)h->outBuf;
+    float* dWn = wn ? (float*)(dBits + words) : nullptr;
+    if ((e = launchSelfIntersections(h->tree.q, beta, h->precise, dBits, dWn, h->scratch, h->stream)))
+        return cudaFail(e, "gbfwn_self_intersections");
+    if (words && (e = cudaMemcpyAsync(bits, dBits, words * sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream)))
+        return cudaFail(e, "gbfwn_self_intersections");
+    if (wn && h->nt && (e = cudaMemcpyAsync(wn, dWn, sizeof(float) * size_t(h->nt), cudaMemcpyDeviceToHost, h->stream)))
+        return cudaFail(e, "gbfwn_self_intersections");
+    if ((e = cudaStreamSynchronize(h->stream))) return cudaFail(e, "gbfwn_self_intersections");
+    int st = h->checkStatus();
+    if (st) return st;
+    return progress(cb, user, 1.f) ? GBFWN_OK : fail(GBFWN_CANCELLED, "operation canceled");
+}
+
+GBFWN_API int gbfwn_from_grid(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta, float* out,
+                              gbfwn_progress_cb cb, void* user) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !out) return fail(GBFWN_INVALID, "gbfwn_from_grid: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    return runGrid(
+        h, dims,
+        [&](const GridRange& r, float* buf, cudaStream_t s) {
+            return launchGridFwn(h->tree.q, r, X, beta, h->precise, buf, h->scratch, s);
+        },
+        out, 0, 0, nullptr, nullptr, cb, user, "gbfwn_from_grid");
+}
+
+GBFWN_API int gbfwn_from_grid_with_distances(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                             const gbfwn_dist_opts* opts, float* out, gbfwn_progress_cb cb, void* user) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !out) return fail(GBFWN_INVALID, "gbfwn_from_grid_with_distances: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    const DistOpts o = toOpts(opts);
+    return runGrid(
+        h, dims,
+        [&](const GridRange& r, float* buf, cudaStream_t s) {
+            return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s);
+        },
+        out, 0, 0, nullptr, nullptr, cb, user, "gbfwn_from_grid_with_distances");
+}
+
+GBFWN_API int gbfwn_from_grid_by_parts(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta,
+                                       int32_t layerOverlap, int32_t maxLayersPerSlab, gbfwn_slab_cb slab,
+                                       void* slabUser, gbfwn_progress_cb cb, void* user) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !slab || layerOverlap < 0)
+        return fail(GBFWN_INVALID, "gbfwn_from_grid_by_parts: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    return runGrid(
+        h, dims,
+        [&](const GridRange& r, float* buf, cudaStream_t s) {
+            return launchGridFwn(h->tree.q, r, X, beta, h->precise, buf, h->scratch, s);
+        },
+        nullptr, layerOverlap, maxLayersPerSlab, slab, slabUser, cb, user, "gbfwn_from_grid_by_parts");
+}
+
+GBFWN_API int gbfwn_from_grid_with_distances_by_parts(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                      const gbfwn_dist_opts* opts, int32_t layerOverlap,
+                                                      int32_t maxLayersPerSlab, gbfwn_slab_cb slab, void* slabUser,
+                                                      gbfwn_progress_cb cb, void* user) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !slab || layerOverlap < 0)
+        return fail(GBFWN_INVALID, "gbfwn_from_grid_with_distances_by_parts: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    const DistOpts o = toOpts(opts);
+    return runGrid(
+        h, dims,
+        [&](const GridRange& r, float* buf, cudaStream_t s) {
+            return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s);
+        },
+        nullptr, layerOverlap, maxLayersPerSlab, slab, slabUser, cb, user, "gbfwn_from_grid_with_distances_by_parts");
+}
+
+// Memory estimators: mesh data (verts, tris, reference nodes + dipoles kept for export, wide query
+// records, leaf triangles, face->slot) plus the per-call staging.
+GBFWN_API size_t gbfwn_mesh_memory(int64_t nv, int64_t nt) {
+    const size_t n = size_t(std::max<int64_t>(nt, 0));
+    return size_t(nv) * 12 + n * 12 + (2 * n) * (32 + 32) + n * (64 + 64) + n * 48 + n * 4 + (2 * n) * 16 + 4096;
+}
+GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t dims[3]) {
+    const size_t vox = dims ? size_t(std::max(dims[0], 0)) * size_t(std::max(dims[1], 0)) * size_t(std::max(dims[2], 0)) : 0;
+    return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float);
+}
+GBFWN_API size_t gbfwn_from_vector_memory(int64_t nv, int64_t nt, int64_t npts) {
+    return gbfwn_mesh_memory(nv, nt) + size_t(std::max<int64_t>(npts, 0)) * 16;
+}
+GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt) {
+    return gbfwn_mesh_memory(nv, nt) + size_t(std::max<int64_t>(nt, 0)) * 4 + size_t((nt + 63) / 64) * 8;
+}
+
+}  // extern "C"

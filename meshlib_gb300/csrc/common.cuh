@@ -1,0 +1,106 @@
+// Shared definitions of the GB300 winding-number library: device data layout, kernel entry
+// points and host helpers.  Everything here is internal; the public surface is include/gbfwn.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace gbfwn {
+
+// ---------------------------------------------------------------------------------------------
+// Reference tree layout (MRMesh/MRAABBTreeNode.h:29-46): box + l + r, leaf <=> r < 0 with l = face.
+// Nodes are in the reference's pre-order: the left child of internal node i is i + 1.
+struct RefNode {
+    float minx, miny, minz, maxx, maxy, maxz;
+    int32_t l, r;
+};
+static_assert(sizeof(RefNode) == 32, "reference node is 32 bytes");
+
+// ---------------------------------------------------------------------------------------------
+// Query layout in HBM ("wide" records: a parent stores both children, so one 64-byte record
+// read gives everything a traversal step needs; children are fetched as float4, all lanes of a
+// warp read the same record, so each load is a broadcast).
+//
+//  cp  [internal k] 4 x float4 : {lmin.xyz, lLink} {lmax.xyz, rLink} {rmin.xyz, 0} {rmax.xyz, 0}
+//  dip [internal k] 4 x float4 : {lpos.xyz, l rr}  {l dirArea.xyz, lLink} {rpos.xyz, r rr} {r dirArea.xyz, rLink}
+//  tri [leaf slot s] 3 x float4: {a.xyz, face} {b.xyz, 0} {c.xyz, 0}
+//
+// A link >= 0 is an internal-node index k (internal nodes numbered in pre-order), a link < 0 is
+// ~slot of a leaf; leaf slots are the leaves in pre-order.  Root data travels in the kernel
+// parameters.
+struct QueryTree {
+    const float4* __restrict__ cp;
+    const float4* __restrict__ dip;
+    const float4* __restrict__ tri;
+    const int32_t* __restrict__ faceSlot;  // face -> slot, -1 for invalid faces
+    float4 rootDip0, rootDip1;             // {pos.xyz, rr} {dirArea.xyz, rootLink}
+    float4 rootBox0, rootBox1;             // {min.xyz, rootLink} {max.xyz, 0}
+    int32_t nLeaves;
+    int32_t nFaces;
+};
+
+struct Xf {
+    float a[9];  // rows
+    float b[3];
+};
+
+struct DistOpts {
+    float minDistSq, maxDistSq;
+    int32_t nullOutsideMinMax;
+    float threshold, beta;
+};
+
+// Grid sub-range handled by one launch: layers [z0, z1) of a dims grid, written to out with the
+// layer z at (z - zOut) * nx * ny.
+struct GridRange {
+    int32_t nx, ny, nz;
+    int32_t z0, z1, zOut;
+};
+
+// Device status word bits.
+enum : unsigned {
+    kStatusStackOverflow = 1u,
+    kStatusTimeout = 2u,
+};
+
+// ---------------------------------------------------------------------------------------------
+// Kernel launchers (query.cu).  All take a `scratch` pointer to two device words: [0] = work
+// queue ticket counter, [1] = status bits.  The launchers reset the ticket counter themselves.
+cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
+                          unsigned* scratch, cudaStream_t s);
+cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
+                          float* out, unsigned* scratch, cudaStream_t s);
+cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,
+                            float* out, unsigned* scratch, cudaStream_t s);
+cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, const DistOpts& o, int precise, float* out,
+                            unsigned* scratch, cudaStream_t s);
+cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise, uint64_t* bits, float* wn,
+                                    unsigned* scratch, cudaStream_t s);
+
+// ---------------------------------------------------------------------------------------------
+// Tree/dipole construction (build.cu).
+struct DeviceTree {
+    int64_t nFaces = 0, nLeaves = 0, nInternal = 0;
+    RefNode* nodes = nullptr;   // 2n-1 reference nodes
+    float* dip8 = nullptr;      // 2n-1 x 8 reference dipoles
+    float4* cp = nullptr;
+    float4* dip = nullptr;
+    float4* tri = nullptr;
+    int32_t* faceSlot = nullptr;
+    QueryTree q{};
+};
+
+// Builds the tree on the device from device verts / tris (build.cu).  Allocation goes through
+// `alloc`, which the caller frees as a whole.
+struct Allocator {
+    virtual cudaError_t alloc(void** p, size_t bytes) = 0;
+    virtual ~Allocator() = default;
+};
+cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, DeviceTree& out,
+                            Allocator& a, cudaStream_t s, std::string& err);
+
+int numSMs();
+
+}  // namespace gbfwn

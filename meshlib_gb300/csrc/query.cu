@@ -1,0 +1,530 @@
+// Winding-number and closest-point traversals (the per-voxel hot loops).
+//
+// Reference semantics (paths inside the MeshLib project):
+//   winding number  MRMesh/MRDipole.cpp:94-128 (+ MRMesh/MRDipole.h:18-27, MRDipole.cpp:81-92):
+//     DFS from the root; a node whose dipole is far from q (|pos - q|^2 > beta^2 * rr) contributes
+//     dot(pos - q, dirArea) / |pos - q|^3 and is not opened; a near leaf contributes the exact
+//     triangle solid angle; sum / (4 pi).
+//   closest point   MRMesh/MRMeshProject.cpp:13-104: near-first DFS over box distances, pruning
+//     boxes not closer than the best distance so far, leaf = point-triangle projection, stop once
+//     the best distance is <= minDistSq.
+//   signed distance MRMesh/MRFastWindingNumber.cpp:69-94, MRCuda/MRCudaFastWindingNumber.cu:205-243.
+//
+// GB300 design: one warp = one packet of 32 neighbouring queries (a 4x4x2 voxel tile for grids).
+// The warp walks the UNION of the 32 per-query traversals once: a stack entry is (node, lane mask
+// of the queries that still need this node), kept in registers with one entry per lane and
+// moved with shuffles; node records are read once per warp (all lanes read the same address, so
+// each 16-byte load is a broadcast).  Every query still makes exactly its own per-node decisions,
+// so the set of dipole terms and exact solid angles summed for a query is the reference's set.
+// Work is handed out by a persistent grid pulling tiles from an atomic ticket counter.
+#include <cfloat>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace gbfwn {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int kStackDepth = 32;  // the reference's InplaceStack<..., 32>; a median-split tree of
+                                 // n <= 2^31 leaves never needs more
+
+__device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+
+// ---- reference arithmetic helpers (no FMA contraction where decisions depend on the bits)
+__device__ __forceinline__ float dot3rn(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// voxel centre: A * (x, y, z) + b, each row a left-to-right dot (MRMesh/MRMatrix3.h:127-130)
+__device__ __forceinline__ float3 xfPoint(const Xf& xf, int x, int y, int z) {
+    const float fx = float(x), fy = float(y), fz = float(z);
+    return make_float3(__fadd_rn(dot3rn(xf.a[0], xf.a[1], xf.a[2], fx, fy, fz), xf.b[0]),
+                       __fadd_rn(dot3rn(xf.a[3], xf.a[4], xf.a[5], fx, fy, fz), xf.b[1]),
+                       __fadd_rn(dot3rn(xf.a[6], xf.a[7], xf.a[8], fx, fy, fz), xf.b[2]));
+}
+
+// Summation: compensated (Kahan) in precise mode, plain otherwise.
+template <bool PRECISE> struct Acc {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        if (PRECISE) {
+            const float y = __fsub_rn(v, c);
+            const float t = __fadd_rn(s, y);
+            c = __fsub_rn(__fsub_rn(t, s), y);
+            s = t;
+        } else {
+            s = __fadd_rn(s, v);
+        }
+    }
+};
+
+// MRMesh/MRDipole.h:18-27.  Returns true (and adds the term) when the dipole is a good
+// approximation for q.  The far-field test uses separately rounded operations like the reference.
+template <bool PRECISE>
+__device__ __forceinline__ bool dipoleTerm(const float4& p, const float4& da, const float3& q, float betaSq, Acc<PRECISE>& acc) {
+    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+    const float dd = dot3rn(dx, dy, dz, dx, dy, dz);
+    if (dd <= __fmul_rn(betaSq, p.w)) return false;
+    if (dd > 0.f) {
+        const float num = dot3rn(dx, dy, dz, da.x, da.y, da.z);
+        if (PRECISE) {
+            const float r = rsqrtf(dd);
+            acc.add(num * (r * r * r));
+        } else {
+            const float d = __fsqrt_rn(dd);
+            acc.add(__fdiv_rn(num, __fmul_rn(d, dd)));
+        }
+    }
+    return true;
+}
+
+// MRMesh/MRDipole.cpp:81-92: 2 * atan2(det[a-q, b-q, c-q], den) (Van Oosterom-Strackee).  In
+// precise mode a query within a few ulps of the triangle plane (|det| small against the product of
+// the three lengths, where the FP32 sign of det is not reliable) is re-evaluated in FP64.
+template <bool PRECISE>
+__device__ __forceinline__ float solidAngle(const float3& q, const float4& A, const float4& B, const float4& C) {
+    const float mxx = A.x - q.x, mxy = A.y - q.y, mxz = A.z - q.z;
+    const float myx = B.x - q.x, myy = B.y - q.y, myz = B.z - q.z;
+    const float mzx = C.x - q.x, mzy = C.y - q.y, mzz = C.z - q.z;
+    const float x = __fsqrt_rn(dot3rn(mxx, mxy, mxz, mxx, mxy, mxz));
+    const float y = __fsqrt_rn(dot3rn(myx, myy, myz, myx, myy, myz));
+    const float z = __fsqrt_rn(dot3rn(mzx, mzy, mzz, mzx, mzy, mzz));
+    const float xyz = __fmul_rn(__fmul_rn(x, y), z);
+    const float den = __fadd_rn(__fadd_rn(__fadd_rn(xyz, __fmul_rn(dot3rn(mxx, mxy, mxz, myx, myy, myz), z)),
+                                          __fmul_rn(dot3rn(myx, myy, myz, mzx, mzy, mzz), x)),
+                                __fmul_rn(dot3rn(mzx, mzy, mzz, mxx, mxy, mxz), y));
+    const float det = __fadd_rn(__fsub_rn(__fmul_rn(mxx, __fsub_rn(__fmul_rn(myy, mzz), __fmul_rn(myz, mzy))),
+                                          __fmul_rn(mxy, __fsub_rn(__fmul_rn(myx, mzz), __fmul_rn(myz, mzx)))),
+                                __fmul_rn(mxz, __fsub_rn(__fmul_rn(myx, mzy), __fmul_rn(myy, mzx))));
+    if (PRECISE && fabsf(det) <= 1e-5f * xyz) {
+        const double ax = double(A.x) - q.x, ay = double(A.y) - q.y, az = double(A.z) - q.z;
+        const double bx = double(B.x) - q.x, by = double(B.y) - q.y, bz = double(B.z) - q.z;
+        const double cx = double(C.x) - q.x, cy = double(C.y) - q.y, cz = double(C.z) - q.z;
+        const double lx = sqrt(ax * ax + ay * ay + az * az);
+        const double ly = sqrt(bx * bx + by * by + bz * bz);
+        const double lz = sqrt(cx * cx + cy * cy + cz * cz);
+        const double dd = lx * ly * lz + (ax * bx + ay * by + az * bz) * lz + (bx * cx + by * cy + bz * cz) * lx +
+                          (cx * ax + cy * ay + cz * az) * ly;
+        const double dt = ax * (by * cz - bz * cy) - ay * (bx * cz - bz * cx) + az * (bx * cy - by * cx);
+        return float(2.0 * atan2(dt, dd));
+    }
+    return 2.f * atan2f(det, den);
+}
+
+// ------------------------------------------------------------------ winding number (packet DFS)
+// Lane-distributed stack: entry k lives in lane k's (stNode, stMask).
+struct WarpStack {
+    int node = 0;
+    unsigned mask = 0;
+    int sp = 0;  // warp-uniform
+    __device__ __forceinline__ bool push(int lane, int n, unsigned m) {
+        if (sp >= kStackDepth) return false;
+        if (lane == sp) {
+            node = n;
+            mask = m;
+        }
+        ++sp;
+        return true;
+    }
+    __device__ __forceinline__ void pop(int& n, unsigned& m) {
+        --sp;
+        n = __shfl_sync(FULL, node, sp);
+        m = __shfl_sync(FULL, mask, sp);
+    }
+};
+
+template <bool PRECISE>
+__device__ __forceinline__ void leafSolidAngle(const QueryTree& t, int slot, const float3& q, bool need, int skipSlot,
+                                               Acc<PRECISE>& acc) {
+    const float4* tr = t.tri + 3 * int64_t(slot);
+    const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+    if (need && slot != skipSlot) acc.add(solidAngle<PRECISE>(q, A, B, C));
+}
+
+// Winding number of q (lanes with active == false only ride along).  Returns sum / (4 pi).
+template <bool PRECISE>
+__device__ float fwnPacket(const QueryTree& t, const float3& q, bool active, float betaSq, int skipSlot, unsigned* status) {
+    const int lane = threadIdx.x & 31;
+    Acc<PRECISE> acc;
+    if (__ballot_sync(FULL, active) == 0 || t.nLeaves == 0) return 0.f;
+    bool need = active && !dipoleTerm<PRECISE>(t.rootDip0, t.rootDip1, q, betaSq, acc);
+    const unsigned rootNeed = __ballot_sync(FULL, need);
+    WarpStack st;
+    if (rootNeed) {
+        const int rootLink = __float_as_int(t.rootDip1.w);
+        if (rootLink < 0)
+            leafSolidAngle<PRECISE>(t, ~rootLink, q, need, skipSlot, acc);
+        else
+            st.push(lane, rootLink, rootNeed);
+    }
+    bool overflow = false;
+    while (st.sp > 0) {
+        int node;
+        unsigned m;
+        st.pop(node, m);
+        const float4* rec = t.dip + 4 * int64_t(node);
+        const float4 l0 = ld4(rec), l1 = ld4(rec + 1), r0 = ld4(rec + 2), r1 = ld4(rec + 3);
+        const bool mine = (m >> lane) & 1u;
+        bool nl = false, nr = false;
+        if (mine) {
+            nl = !dipoleTerm<PRECISE>(l0, l1, q, betaSq, acc);
+            nr = !dipoleTerm<PRECISE>(r0, r1, q, betaSq, acc);
+        }
+        const unsigned ml = __ballot_sync(FULL, nl), mr = __ballot_sync(FULL, nr);
+        const int ll = __float_as_int(l1.w), rl = __float_as_int(r1.w);
+        // right subtree below left on the stack, so the left subtree is summed first (reference order)
+        if (mr) {
+            if (rl < 0)
+                leafSolidAngle<PRECISE>(t, ~rl, q, nr, skipSlot, acc);
+            else if (!st.push(lane, rl, mr))
+                overflow = true;
+        }
+        if (ml) {
+            if (ll < 0)
+                leafSolidAngle<PRECISE>(t, ~ll, q, nl, skipSlot, acc);
+            else if (!st.push(lane, ll, ml))
+                overflow = true;
+        }
+        if (overflow) break;
+    }
+    if (overflow && lane == 0) atomicOr(status, kStatusStackOverflow);
+    const float INV_4PI = 1.0f / (4 * 3.14159265358979f);
+    return __fmul_rn(INV_4PI, PRECISE ? __fsub_rn(acc.s, acc.c) : acc.s);
+}
+
+// ------------------------------------------------------------------ closest point (packet DFS)
+__device__ __forceinline__ float boxDistSq(const float4& mn, const float4& mx, const float3& p) {
+    // MRMesh/MRBox.h:207-220 (reference arithmetic)
+    float r = 0.f, d;
+    if (p.x < mn.x) { d = p.x - mn.x; r = __fadd_rn(r, __fmul_rn(d, d)); }
+    else if (p.x > mx.x) { d = p.x - mx.x; r = __fadd_rn(r, __fmul_rn(d, d)); }
+    if (p.y < mn.y) { d = p.y - mn.y; r = __fadd_rn(r, __fmul_rn(d, d)); }
+    else if (p.y > mx.y) { d = p.y - mx.y; r = __fadd_rn(r, __fmul_rn(d, d)); }
+    if (p.z < mn.z) { d = p.z - mn.z; r = __fadd_rn(r, __fmul_rn(d, d)); }
+    else if (p.z > mx.z) { d = p.z - mx.z; r = __fadd_rn(r, __fmul_rn(d, d)); }
+    return r;
+}
+
+template <typename T> struct V3T {
+    T x, y, z;
+};
+template <typename T> __device__ __forceinline__ V3T<T> vsub(V3T<T> a, V3T<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename T> __device__ __forceinline__ T vdot(V3T<T> a, V3T<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename T> __device__ __forceinline__ V3T<T> vmad(V3T<T> a, T s, V3T<T> b) { return {a.x + s * b.x, a.y + s * b.y, a.z + s * b.z}; }
+
+// MRMesh/MRClosestPointInTriangle.h:28-91 (Voronoi-region projection).
+template <typename T> __device__ __forceinline__ V3T<T> closestPoint(V3T<T> p, V3T<T> a, V3T<T> b, V3T<T> c) {
+    const V3T<T> ab = vsub(b, a), ac = vsub(c, a), ap = vsub(p, a);
+    const T d1 = vdot(ab, ap), d2 = vdot(ac, ap);
+    if (d1 <= 0 && d2 <= 0) return a;
+    const V3T<T> bp = vsub(p, b);
+    const T d3 = vdot(ab, bp), d4 = vdot(ac, bp);
+    if (d3 >= 0 && d4 <= d3) return b;
+    const V3T<T> cp = vsub(p, c);
+    const T d5 = vdot(ab, cp), d6 = vdot(ac, cp);
+    if (d6 >= 0 && d5 <= d6) return c;
+    const T vc = d1 * d4 - d3 * d2;
+    if (vc <= 0 && d1 >= 0 && d3 <= 0) return vmad(a, d1 / (d1 - d3), ab);
+    const T vb = d5 * d2 - d1 * d6;
+    if (vb <= 0 && d6 <= 0 && d2 >= 0) return vmad(a, d2 / (d2 - d6), ac);
+    const T va = d3 * d6 - d5 * d4;
+    if (va <= 0) {
+        if (d4 < d3) return b;
+        if (d5 < d6) return c;
+        return vmad(b, (d4 - d3) / ((d4 - d3) + (d5 - d6)), vsub(c, b));
+    }
+    const T denom = T(1) / (va + vb + vc);
+    return vmad(vmad(a, vb * denom, ab), vc * denom, ac);
+}
+
+// Squared distance from p to a triangle.  FP32 projection; in precise mode a query that lands
+// within ~1e-4 triangle edge lengths of the triangle is re-projected in FP64.
+template <bool PRECISE>
+__device__ __forceinline__ float triDistSq(const float3& p, const float4& A, const float4& B, const float4& C) {
+    const V3T<float> pf{p.x, p.y, p.z}, af{A.x, A.y, A.z}, bf{B.x, B.y, B.z}, cf{C.x, C.y, C.z};
+    const V3T<float> pr = closestPoint<float>(pf, af, bf, cf);
+    const V3T<float> d = vsub(pr, pf);
+    float ds = dot3rn(d.x, d.y, d.z, d.x, d.y, d.z);
+    if (PRECISE) {
+        const V3T<float> ab = vsub(bf, af), ac = vsub(cf, af);
+        const float scale = vdot(ab, ab) + vdot(ac, ac);
+        if (ds < 1e-8f * scale) {
+            const V3T<double> pd{p.x, p.y, p.z}, ad{A.x, A.y, A.z}, bd{B.x, B.y, B.z}, cd{C.x, C.y, C.z};
+            const V3T<double> q = closestPoint<double>(pd, ad, bd, cd);
+            // the reference rounds the FP64 projection to float and measures in float
+            const float qx = float(q.x) - p.x, qy = float(q.y) - p.y, qz = float(q.z) - p.z;
+            ds = dot3rn(qx, qy, qz, qx, qy, qz);
+        }
+    }
+    return ds;
+}
+
+template <bool PRECISE>
+__device__ __forceinline__ void leafDist(const QueryTree& t, int slot, const float3& q, bool go, float& resSq, bool& done,
+                                         float loSq) {
+    const float4* tr = t.tri + 3 * int64_t(slot);
+    const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+    if (go) {
+        const float ds = triDistSq<PRECISE>(q, A, B, C);
+        if (ds < resSq) {
+            resSq = ds;
+            if (ds <= loSq) done = true;
+        }
+    }
+}
+
+// Closest squared distance from q to the mesh, starting from the bound upSq (the reference's
+// maxDistSq) and stopping once <= loSq; returns upSq when nothing is closer.
+template <bool PRECISE>
+__device__ float cpPacket(const QueryTree& t, const float3& q, bool active, float upSq, float loSq, unsigned* status) {
+    const int lane = threadIdx.x & 31;
+    float resSq = upSq;
+    bool done = !active;
+    if (__ballot_sync(FULL, active) == 0 || t.nLeaves == 0) return resSq;
+    const bool inRoot = active && boxDistSq(t.rootBox0, t.rootBox1, q) < resSq;
+    const unsigned m0 = __ballot_sync(FULL, inRoot);
+    if (!m0) return resSq;
+    const int rootLink = __float_as_int(t.rootBox0.w);
+    if (rootLink < 0) {
+        leafDist<PRECISE>(t, ~rootLink, q, inRoot, resSq, done, loSq);
+        return resSq;
+    }
+    WarpStack st;
+    st.push(lane, rootLink, m0);
+    bool overflow = false;
+    while (st.sp > 0) {
+        int node;
+        unsigned m;
+        st.pop(node, m);
+        const float4* rec = t.cp + 4 * int64_t(node);
+        const float4 lmn = ld4(rec), lmx = ld4(rec + 1), rmn = ld4(rec + 2), rmx = ld4(rec + 3);
+        const bool mine = ((m >> lane) & 1u) && !done;
+        float dl = FLT_MAX, dr = FLT_MAX;
+        if (mine) {
+            dl = boxDistSq(lmn, lmx, q);
+            dr = boxDistSq(rmn, rmx, q);
+        }
+        const bool gl = mine && dl < resSq, gr = mine && dr < resSq;
+        const unsigned ml = __ballot_sync(FULL, gl), mr = __ballot_sync(FULL, gr);
+        if ((ml | mr) == 0) continue;
+        // near first: the child more queries prefer (ties: right first, as the reference does
+        // when the two distances are equal)
+        const unsigned preferL = __ballot_sync(FULL, gl && gr ? dl < dr : gl);
+        const unsigned both = ml | mr;
+        const bool leftFirst = 2 * __popc(preferL & both) > __popc(both);
+        const int ll = __float_as_int(lmn.w), rl = __float_as_int(lmx.w);
+        // leaves are evaluated at once (near one first), inner children pushed far-then-near
+        const int nearLink = leftFirst ? ll : rl, farLink = leftFirst ? rl : ll;
+        const unsigned nearM = leftFirst ? ml : mr, farM = leftFirst ? mr : ml;
+        const float nearD = leftFirst ? dl : dr, farD = leftFirst ? dr : dl;
+        const bool nearGo = leftFirst ? gl : gr, farGo = leftFirst ? gr : gl;
+        if (nearM && nearLink < 0) leafDist<PRECISE>(t, ~nearLink, q, nearGo && !done, resSq, done, loSq);
+        if (farM && farLink < 0) leafDist<PRECISE>(t, ~farLink, q, farGo && !done && farD < resSq, resSq, done, loSq);
+        if (farM && farLink >= 0 && !st.push(lane, farLink, farM)) overflow = true;
+        if (nearM && nearLink >= 0 && !st.push(lane, nearLink, nearM)) overflow = true;
+        (void)nearD;
+        if (overflow) break;
+    }
+    if (overflow && lane == 0) atomicOr(status, kStatusStackOverflow);
+    return resSq;
+}
+
+// ------------------------------------------------------------------ kernels
+constexpr int kThreads = 256;
+constexpr int kTX = 4, kTY = 4, kTZ = 2;  // voxel tile of one warp
+
+struct TileGrid {
+    int32_t tilesX, tilesY, tilesZ;
+    uint32_t numTiles;
+};
+
+__device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1u);
+    return __shfl_sync(FULL, t, 0);
+}
+
+template <bool PRECISE, bool DIST>
+__global__ void __launch_bounds__(kThreads) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
+                                                       float* __restrict__ out, unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
+    const float betaSq = __fmul_rn(o.beta, o.beta);
+    const size_t sxy = size_t(g.nx) * g.ny;
+    for (;;) {
+        const unsigned tile = nextTicket(scratch, lane);
+        if (tile >= tg.numTiles) break;
+        const int tx = int(tile % unsigned(tg.tilesX));
+        const unsigned rest = tile / unsigned(tg.tilesX);
+        const int ty = int(rest % unsigned(tg.tilesY));
+        const int tz = int(rest / unsigned(tg.tilesY));
+        const int x = tx * kTX + lx, y = ty * kTY + ly, z = g.z0 + tz * kTZ + lz;
+        const bool active = x < g.nx && y < g.ny && z < g.z1;
+        const float3 q = xfPoint(xf, x, y, z);
+        float res;
+        if (DIST) {
+            const float dsq = cpPacket<PRECISE>(t, q, active, o.maxDistSq, o.minDistSq, scratch + 1);
+            const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
+            const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
+            const float d = __fsqrt_rn(dsq);
+            res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+        } else {
+            res = fwnPacket<PRECISE>(t, q, active, betaSq, -1, scratch + 1);
+        }
+        if (active) out[size_t(z - g.zOut) * sxy + size_t(y) * g.nx + x] = res;
+    }
+}
+
+template <bool PRECISE, bool DIST>
+__global__ void __launch_bounds__(kThreads) vectorKernel(QueryTree t, const float* __restrict__ pts, int64_t n, DistOpts o,
+                                                         int32_t skipFace, float* __restrict__ out, unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const float betaSq = __fmul_rn(o.beta, o.beta);
+    const int skipSlot = (skipFace >= 0 && skipFace < t.nFaces) ? t.faceSlot[skipFace] : -1;
+    const uint64_t numTiles = (uint64_t(n) + 31) / 32;
+    for (;;) {
+        const unsigned tile = nextTicket(scratch, lane);
+        if (tile >= numTiles) break;
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool active = i < n;
+        float3 q = make_float3(0.f, 0.f, 0.f);
+        if (active) q = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+        float res;
+        if (DIST) {
+            const float dsq = cpPacket<PRECISE>(t, q, active, o.maxDistSq, o.minDistSq, scratch + 1);
+            const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
+            const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
+            const float d = __fsqrt_rn(dsq);
+            res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+        } else {
+            res = fwnPacket<PRECISE>(t, q, active, betaSq, skipSlot, scratch + 1);
+        }
+        if (active) out[i] = res;
+    }
+}
+
+// MRMesh/MRFastWindingNumber.cpp:40-52: query = triCenter(f) = (1/3) * (v0 + v1 + v2), skipping f.
+// Lanes take consecutive leaf slots, which are spatially coherent.
+template <bool PRECISE>
+__global__ void __launch_bounds__(kThreads) selfIntKernel(QueryTree t, float beta, uint64_t* __restrict__ bits,
+                                                          float* __restrict__ wn, unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const float betaSq = __fmul_rn(beta, beta);
+    const uint64_t numTiles = (uint64_t(t.nLeaves) + 31) / 32;
+    for (;;) {
+        const unsigned tile = nextTicket(scratch, lane);
+        if (tile >= numTiles) break;
+        const int slot = int(tile) * 32 + lane;
+        const bool active = slot < t.nLeaves;
+        float3 q = make_float3(0.f, 0.f, 0.f);
+        int face = -1;
+        if (active) {
+            const float4* tr = t.tri + 3 * int64_t(slot);
+            const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+            const float third = 1 / 3.0f;
+            q = make_float3(__fmul_rn(third, __fadd_rn(__fadd_rn(A.x, B.x), C.x)),
+                            __fmul_rn(third, __fadd_rn(__fadd_rn(A.y, B.y), C.y)),
+                            __fmul_rn(third, __fadd_rn(__fadd_rn(A.z, B.z), C.z)));
+            face = __float_as_int(A.w);
+        }
+        const float w = fwnPacket<PRECISE>(t, q, active, betaSq, active ? slot : -1, scratch + 1);
+        if (active) {
+            if (wn) wn[face] = w;
+            if (w < 0.f || w > 1.f) atomicOr((unsigned long long*)bits + (face >> 6), 1ull << (face & 63));
+        }
+    }
+}
+
+__global__ void fillNan(float* p, int64_t n) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < n) p[i] = __int_as_float(0x7fc00000);
+}
+
+int gridBlocks(const void* kernel) {
+    static int sms = 0;
+    if (!sms) sms = numSMs();
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kThreads, 0);
+    if (perSm < 1) perSm = 1;
+    return sms * perSm;
+}
+
+template <typename K, typename... Args>
+cudaError_t launchPersistent(K kernel, uint64_t work, unsigned* scratch, cudaStream_t s, Args... args) {
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned), s);
+    if (e) return e;
+    if (work == 0) return cudaSuccess;
+    int blocks = gridBlocks((const void*)kernel);
+    const uint64_t warpsNeeded = work;
+    const uint64_t maxBlocks = (warpsNeeded + kThreads / 32 - 1) / (kThreads / 32);
+    if (uint64_t(blocks) > maxBlocks) blocks = int(maxBlocks);
+    kernel<<<blocks, kThreads, 0, s>>>(args...);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int numSMs() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+static TileGrid tileGridFor(const GridRange& g) {
+    TileGrid tg;
+    tg.tilesX = (g.nx + kTX - 1) / kTX;
+    tg.tilesY = (g.ny + kTY - 1) / kTY;
+    tg.tilesZ = (g.z1 - g.z0 + kTZ - 1) / kTZ;
+    tg.numTiles = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.tilesZ);
+    return tg;
+}
+
+cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
+                          unsigned* scratch, cudaStream_t s) {
+    const TileGrid tg = tileGridFor(g);
+    DistOpts o{0.f, FLT_MAX, 0, 0.5f, beta};
+    if (precise)
+        return launchPersistent(gridKernel<true, false>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+    return launchPersistent(gridKernel<false, false>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+}
+
+cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
+                          unsigned* scratch, cudaStream_t s) {
+    const TileGrid tg = tileGridFor(g);
+    if (precise)
+        return launchPersistent(gridKernel<true, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+    return launchPersistent(gridKernel<false, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+}
+
+cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,
+                            float* out, unsigned* scratch, cudaStream_t s) {
+    DistOpts o{0.f, FLT_MAX, 0, 0.5f, beta};
+    const uint64_t tiles = (uint64_t(n) + 31) / 32;
+    if (precise) return launchPersistent(vectorKernel<true, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch);
+    return launchPersistent(vectorKernel<false, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch);
+}
+
+cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, const DistOpts& o, int precise, float* out,
+                            unsigned* scratch, cudaStream_t s) {
+    const uint64_t tiles = (uint64_t(n) + 31) / 32;
+    if (precise) return launchPersistent(vectorKernel<true, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch);
+    return launchPersistent(vectorKernel<false, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch);
+}
+
+cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise, uint64_t* bits, float* wn,
+                                    unsigned* scratch, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bits, 0, sizeof(uint64_t) * size_t((t.nFaces + 63) / 64), s);
+    if (e) return e;
+    if (wn && t.nFaces > 0) {
+        fillNan<<<unsigned((t.nFaces + 255) / 256), 256, 0, s>>>(wn, t.nFaces);
+        if ((e = cudaGetLastError())) return e;
+    }
+    const uint64_t tiles = (uint64_t(t.nLeaves) + 31) / 32;
+    if (precise) return launchPersistent(selfIntKernel<true>, tiles, scratch, s, t, beta, bits, wn, scratch);
+    return launchPersistent(selfIntKernel<false>, tiles, scratch, s, t, beta, bits, wn, scratch);
+}
+
+}  // namespace gbfwn

@@ -1,0 +1,189 @@
+"""ctypes front-end of the CPU oracle (oracle/fwn_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py -- never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "liboracle.so")
+_lib = None
+
+
+class Options(ctypes.Structure):
+    """Mirror of MR::DistanceToMeshOptions (MRMesh/MRDistanceToMeshOptions.h:10-33)."""
+    _fields_ = [("minDistSq", ctypes.c_float), ("maxDistSq", ctypes.c_float), ("nullOutsideMinMax", ctypes.c_int),
+                ("windingNumberThreshold", ctypes.c_float), ("windingNumberBeta", ctypes.c_float)]
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with the host compiler (no FMA contraction, so FP32 follows the reference)."""
+    src = os.path.join(_HERE, "fwn_oracle.cpp")
+    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+                               "-o", _SO, src])
+    return _SO
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_SO)
+        vp, fp, ip, dp = ctypes.c_void_p, ctypes.c_float, ctypes.c_int, ctypes.c_double
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [vp, ip, vp, ip]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_num_nodes.restype = ip
+        L.orc_num_nodes.argtypes = [vp]
+        L.orc_get_nodes.argtypes = [vp, vp]
+        L.orc_get_dipoles_f.argtypes = [vp, vp]
+        L.orc_get_dipoles_d.argtypes = [vp, vp]
+        L.orc_solid_angle_f.restype = fp
+        L.orc_solid_angle_f.argtypes = [vp, vp]
+        L.orc_solid_angle_d.restype = dp
+        L.orc_solid_angle_d.argtypes = [vp, vp]
+        L.orc_closest_point_d.argtypes = [vp, vp, vp]
+        L.orc_from_vector.argtypes = [vp, vp, ctypes.c_int64, fp, ip, ip, ip, vp]
+        L.orc_self_intersections.argtypes = [vp, fp, ip, ip, vp, vp]
+        L.orc_from_grid.argtypes = [vp, vp, vp, fp, ip, ip, vp]
+        L.orc_from_grid_with_distances.argtypes = [vp, vp, vp, ctypes.POINTER(Options), ip, ip, vp, vp]
+        L.orc_vector_with_distances.argtypes = [vp, vp, ctypes.c_int64, ctypes.POINTER(Options), ip, ip, vp]
+        L.orc_dist_sq.argtypes = [vp, vp, ctypes.c_int64, fp, fp, ip, vp]
+        L.orc_traversal_counts.argtypes = [vp, vp, ctypes.c_int64, ctypes.POINTER(Options), vp]
+        L.orc_exact_wn.argtypes = [vp, vp, ctypes.c_int64, ip, vp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_threads() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+def make_options(minDistSq=0.0, maxDistSq=3.4028234663852886e38, nullOutsideMinMax=True, windingNumberThreshold=0.5,
+                 windingNumberBeta=2.0) -> Options:
+    return Options(minDistSq, maxDistSq, int(bool(nullOutsideMinMax)), windingNumberThreshold, windingNumberBeta)
+
+
+class Oracle:
+    """The reference CPU FastWindingNumber restated: tree, dipoles, and the four queries,
+    in FP32 (prec=0, the reference arithmetic) or FP64 (prec=1)."""
+
+    def __init__(self, verts: np.ndarray, faces: np.ndarray):
+        self.verts = np.ascontiguousarray(verts, np.float32)
+        self.faces = np.ascontiguousarray(faces, np.int32)
+        self.L = lib()
+        self.h = self.L.orc_create(_ptr(self.verts), len(self.verts), _ptr(self.faces), len(self.faces))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def nodes(self) -> np.ndarray:
+        """Reference node array: structured (min float3, max float3, l int, r int)."""
+        dt = np.dtype([("min", np.float32, 3), ("max", np.float32, 3), ("l", np.int32), ("r", np.int32)])
+        out = np.empty(self.L.orc_num_nodes(self.h), dt)
+        self.L.orc_get_nodes(self.h, _ptr(out))
+        return out
+
+    def dipoles(self, prec: int = 0) -> np.ndarray:
+        n = self.L.orc_num_nodes(self.h)
+        if prec == 0:
+            out = np.empty((n, 8), np.float32)
+            self.L.orc_get_dipoles_f(self.h, _ptr(out))
+        else:
+            out = np.empty((n, 8), np.float64)
+            self.L.orc_get_dipoles_d(self.h, _ptr(out))
+        return out
+
+    def from_vector(self, pts, beta=2.0, skip_face=-1, prec=0, threads=None):
+        pts = np.ascontiguousarray(pts, np.float32)
+        out = np.empty(len(pts), np.float64)
+        self.L.orc_from_vector(self.h, _ptr(pts), len(pts), beta, skip_face, prec, threads or default_threads(), _ptr(out))
+        return out
+
+    def self_intersections(self, beta=2.0, prec=0, threads=None):
+        bits = np.empty(len(self.faces), np.uint8)
+        wn = np.empty(len(self.faces), np.float64)
+        self.L.orc_self_intersections(self.h, beta, prec, threads or default_threads(), _ptr(bits), _ptr(wn))
+        return bits.astype(bool), wn
+
+    def from_grid(self, dims, xf, beta=2.0, prec=0, threads=None):
+        d = np.asarray(dims, np.int32)
+        xf = np.ascontiguousarray(xf, np.float32)
+        out = np.empty(int(np.prod(d.astype(np.int64))), np.float64)
+        self.L.orc_from_grid(self.h, _ptr(d), _ptr(xf), beta, prec, threads or default_threads(), _ptr(out))
+        return out
+
+    def from_grid_with_distances(self, dims, xf, opts: Options | None = None, prec=0, threads=None, want_fwn=False):
+        d = np.asarray(dims, np.int32)
+        xf = np.ascontiguousarray(xf, np.float32)
+        n = int(np.prod(d.astype(np.int64)))
+        out = np.empty(n, np.float64)
+        fwn = np.empty(n, np.float64) if want_fwn else None
+        o = opts or make_options()
+        self.L.orc_from_grid_with_distances(self.h, _ptr(d), _ptr(xf), ctypes.byref(o), prec, threads or default_threads(),
+                                            _ptr(out), _ptr(fwn) if fwn is not None else None)
+        return (out, fwn) if want_fwn else out
+
+    def vector_with_distances(self, pts, opts: Options | None = None, prec=0, threads=None):
+        pts = np.ascontiguousarray(pts, np.float32)
+        out = np.empty(len(pts), np.float64)
+        o = opts or make_options()
+        self.L.orc_vector_with_distances(self.h, _ptr(pts), len(pts), ctypes.byref(o), prec, threads or default_threads(), _ptr(out))
+        return out
+
+    def dist_sq(self, pts, maxDistSq=3.4028234663852886e38, minDistSq=0.0, threads=None):
+        pts = np.ascontiguousarray(pts, np.float32)
+        out = np.empty(len(pts), np.float32)
+        self.L.orc_dist_sq(self.h, _ptr(pts), len(pts), maxDistSq, minDistSq, threads or default_threads(), _ptr(out))
+        return out
+
+    def traversal_counts(self, pts, opts: Options | None = None):
+        pts = np.ascontiguousarray(pts, np.float32)
+        out = np.zeros(4, np.uint64)
+        o = opts or make_options()
+        self.L.orc_traversal_counts(self.h, _ptr(pts), len(pts), ctypes.byref(o), _ptr(out))
+        return out
+
+    def exact_wn(self, pts, threads=None):
+        pts = np.ascontiguousarray(pts, np.float32)
+        out = np.empty(len(pts), np.float64)
+        self.L.orc_exact_wn(self.h, _ptr(pts), len(pts), threads or default_threads(), _ptr(out))
+        return out
+
+
+def solid_angle_f(p, tri) -> float:
+    p = np.ascontiguousarray(p, np.float32)
+    tri = np.ascontiguousarray(tri, np.float32)
+    return float(lib().orc_solid_angle_f(_ptr(p), _ptr(tri)))
+
+
+def solid_angle_d(p, tri) -> float:
+    p = np.ascontiguousarray(p, np.float64)
+    tri = np.ascontiguousarray(tri, np.float64)
+    return float(lib().orc_solid_angle_d(_ptr(p), _ptr(tri)))
+
+
+def grid_points(dims, xf) -> np.ndarray:
+    """Voxel centres in the reference order (x fastest), computed in float like the reference."""
+    nx, ny, nz = dims
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    p = np.stack([x.ravel(), y.ravel(), z.ravel()], 1).astype(np.float32)
+    A = np.asarray(xf[:9], np.float32).reshape(3, 3)
+    b = np.asarray(xf[9:12], np.float32)
+    out = np.empty_like(p)
+    for r in range(3):
+        out[:, r] = (p[:, 0] * A[r, 0] + p[:, 1] * A[r, 1]) + p[:, 2] * A[r, 2] + b[r]
+    return out

@@ -1,0 +1,65 @@
+"""CPU-only checks of the C ABI: the library builds and loads, exports exactly what include/gbfwn.h
+declares, and rejects bad arguments without touching a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            names += re.findall(r"GBFWN_API\s+[\w\s\*]+?\b(gbfwn_\w+)\s*\(", txt)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(fwn_lib):
+    import meshlib_gb300
+    decl = _declared()
+    assert len(decl) >= 20
+    for name in decl:
+        assert hasattr(fwn_lib, name), name
+    assert sorted(meshlib_gb300.EXPORTED) == decl
+
+
+def test_bad_arguments_rejected_without_gpu(fwn_lib):
+    import meshlib_gb300 as M
+    L = M.lib()
+    out = ctypes.c_void_p()
+    assert L.gbfwn_create(None, 3, None, 1, 0, ctypes.byref(out)) == M.INVALID
+    assert b"bad arguments" in L.gbfwn_last_error()
+    dims = np.array([4, 4, 4], np.int32)
+    xf = np.zeros(12, np.float32)
+    assert L.gbfwn_from_grid(None, dims.ctypes.data, xf.ctypes.data, 2.0, None, M.PROGRESS(), None) == M.INVALID
+    assert L.gbfwn_destroy(None) == M.OK
+    assert L.gbfwn_num_faces(None) == 0
+    v = np.zeros((3, 3), np.float32)
+    t = np.array([[0, 1, 5]], np.int32)  # vertex id out of range: rejected before any device work
+    assert L.gbfwn_create(v.ctypes.data, 3, t.ctypes.data, 1, 0, ctypes.byref(out)) == M.INVALID
+
+
+def test_memory_estimators(fwn_lib):
+    import meshlib_gb300 as M
+    est = M.memory_estimates(655362, 1310720, dims=(512, 512, 512), npts=4_000_000)
+    assert est["mesh"] > 200e6
+    assert est["from_grid"] - est["mesh"] == 512 ** 3 * 4
+    assert est["from_vector"] > est["mesh"]
+
+
+def test_version(fwn_lib):
+    import meshlib_gb300 as M
+    assert b"sm_103a" in M.lib().gbfwn_version()
+
+
+def test_no_cpu_fallback_when_library_missing(tmp_path, monkeypatch):
+    import meshlib_gb300 as M
+    monkeypatch.setattr(M, "_lib", None)
+    monkeypatch.setattr(M, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(ImportError):
+        M.lib()

@@ -1,0 +1,135 @@
+"""CPU-only checks of the oracle against the reference's own known answers, and oracle self-consistency.
+
+Known answers restated from the reference's tests:
+  * MRTest/MRDipoleTests.cpp:25-51 -- triangle solid angle: -2pi / +2pi just above / below the
+    centroid (tolerance 1e-3), exactly 0 at the vertices and at in-plane exterior points;
+  * MRTest/MRAABBTreeTests.cpp:10-27 -- 2n-1 nodes, root box = mesh bounding box expanded by one
+    ulp each way (Box::insignificantlyExpanded), both root children valid, a 1-face tree has 1 node.
+"""
+import math
+
+import numpy as np
+
+import oracle as O
+from meshlib_gb300 import meshgen as mg
+
+TRI = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+
+
+def test_solid_angle_known_answers():
+    c = TRI.mean(0)
+    above = O.solid_angle_f(c + np.float32([0, 0, 1e-5]), TRI)
+    below = O.solid_angle_f(c - np.float32([0, 0, 1e-5]), TRI)
+    assert abs(above - (-2 * math.pi)) < 1e-3
+    assert abs(below - (2 * math.pi)) < 1e-3
+    for i in range(3):
+        assert O.solid_angle_f(TRI[i], TRI) == 0.0
+    assert O.solid_angle_f(TRI[1] + TRI[2], TRI) == 0.0
+    assert O.solid_angle_f(-TRI[1], TRI) == 0.0
+    assert O.solid_angle_f(-TRI[2], TRI) == 0.0
+    # FP64 oracle agrees
+    assert abs(O.solid_angle_d(c.astype(np.float64) + [0, 0, 1e-5], TRI.astype(np.float64)) + 2 * math.pi) < 1e-3
+
+
+def test_tree_known_answers():
+    v, f = mg.noisy_torus(seed=4, nu=16, nv=8)
+    o = O.Oracle(v, f)
+    nodes = o.nodes()
+    assert len(nodes) == 2 * len(f) - 1
+    lo = np.nextafter(v.min(0), np.float32(-np.inf))
+    hi = np.nextafter(v.max(0), np.float32(np.inf))
+    assert np.array_equal(nodes[0]["min"], lo) and np.array_equal(nodes[0]["max"], hi)
+    assert nodes[0]["l"] == 1 and nodes[0]["r"] > 1
+    one = O.Oracle(v, f[:1])
+    assert len(one.nodes()) == 1 and one.nodes()[0]["r"] < 0
+
+
+def test_tree_structure_invariants():
+    v, f = mg.noisy_icosphere(seed=2, level=3)
+    nodes = O.Oracle(v, f).nodes()
+    leaves = nodes[nodes["r"] < 0]
+    assert sorted(leaves["l"].tolist()) == list(range(len(f)))
+    internal = np.nonzero(nodes["r"] >= 0)[0]
+    for i in internal:
+        l, r = nodes[i]["l"], nodes[i]["r"]
+        assert l == i + 1
+        for c in (l, r):
+            assert (nodes[c]["min"] >= nodes[i]["min"]).all() and (nodes[c]["max"] <= nodes[i]["max"]).all()
+
+
+def test_dipole_sums():
+    v, f = mg.noisy_torus(seed=1)
+    o = O.Oracle(v, f)
+    d = o.dipoles(1)
+    a, b, c = (v[f[:, k]].astype(np.float64) for k in range(3))
+    da = 0.5 * np.cross(b - a, c - a)
+    assert abs(d[0, 3] - np.linalg.norm(da, axis=1).sum()) < 1e-9 * d[0, 3]
+    assert np.allclose(d[0, 4:7], da.sum(0), atol=1e-9)
+    df = o.dipoles(0)
+    assert np.allclose(df[:, :7], d[:, :7], rtol=1e-4, atol=1e-5)
+
+
+def test_fwn_closed_mesh_far_field():
+    v, f = mg.noisy_torus(seed=0)
+    o = O.Oracle(v, f)
+    pts = np.array([[1.0, 0, 0], [-1, 0, 0], [0, 1, 0], [0, 0, 0], [3, 0, 0], [0, 0, 2]], np.float32)
+    ex = o.exact_wn(pts)
+    assert np.allclose(ex, [1, 1, 1, 0, 0, 0], atol=1e-9)
+    w = o.from_vector(pts, prec=1)
+    assert np.abs(w - ex).max() < 0.1  # beta=2 dipole approximation
+    w32 = o.from_vector(pts, prec=0)
+    assert np.abs(w32 - w).max() < 1e-5
+
+
+def test_fp32_vs_fp64_grid():
+    v, f = mg.noisy_torus(seed=0)
+    dims, xf = mg.grid_for(v, 16)
+    o = O.Oracle(v, f)
+    d32 = o.from_grid_with_distances(dims, xf, prec=0)
+    d64 = o.from_grid_with_distances(dims, xf, prec=1)
+    assert np.abs(d32 - d64).max() < 1e-6
+    g32 = o.from_grid(dims, xf, prec=0)
+    g64 = o.from_grid(dims, xf, prec=1)
+    assert np.abs(g32 - g64).max() < 1e-5
+
+
+def test_distance_is_brute_force_min():
+    v, f = mg.noisy_icosphere(seed=1, level=2)
+    o = O.Oracle(v, f)
+    rng = np.random.default_rng(0)
+    pts = rng.uniform(-1.5, 1.5, (50, 3)).astype(np.float32)
+    dsq = o.dist_sq(pts)
+    brute = np.empty(len(pts))
+    for i, p in enumerate(pts.astype(np.float64)):
+        best = np.inf
+        for t in f:
+            q = np.empty(3)
+            O.lib().orc_closest_point_d(p.ctypes.data, np.ascontiguousarray(v[t].astype(np.float64)).ctypes.data, q.ctypes.data)
+            best = min(best, float(((q - p) ** 2).sum()))
+        brute[i] = best
+    assert np.allclose(dsq, brute, rtol=1e-5, atol=1e-9)
+
+
+def test_grid_points_convention():
+    v, f = mg.noisy_torus(seed=0)
+    dims, xf = mg.grid_for(v, 8)
+    p = O.grid_points(dims, xf)
+    assert p.shape == (512, 3)
+    assert np.allclose(p[0], xf[9:12]) and np.allclose(p[1] - p[0], [xf[0], 0, 0])
+
+
+def test_self_intersections_known():
+    v, f = mg.figure8_torus()
+    bits, wn = O.Oracle(v, f).self_intersections()
+    assert bits.any() and not bits.all()
+    v2, f2 = mg.noisy_torus(seed=0)
+    b2, _ = O.Oracle(v2, f2).self_intersections()
+    assert not b2.any()
+
+
+def test_traversal_counts():
+    v, f = mg.noisy_torus(seed=0)
+    dims, xf = mg.grid_for(v, 8)
+    o = O.Oracle(v, f)
+    c = o.traversal_counts(O.grid_points(dims, xf))
+    assert all(int(x) > 0 for x in c)
