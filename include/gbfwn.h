@@ -16,7 +16,8 @@
  *    (MRMesh/MRAffineXf.h:46).
  *  - Calls without a `_dev` suffix take and return HOST memory and are synchronous, like
  *    `MR::Cuda::FastWindingNumber`.  `_dev` calls take DEVICE pointers and only enqueue work on
- *    `stream` (NULL = the handle's own stream).
+ *    `stream`: NULL = the handle's own stream; any cudaStream_t, including cudaStreamLegacy
+ *    (0x1) and cudaStreamPerThread (0x2), is accepted.
  *  - Progress callbacks receive a fraction in [0, 1] and return nonzero to continue, zero to
  *    cancel (MRMesh/MRProgressCallback.h); a cancelled call returns GBFWN_CANCELLED.
  *  - Errors: a nonzero status; `gbfwn_last_error()` gives the message of the last failure on the

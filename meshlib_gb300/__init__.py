@@ -122,6 +122,13 @@ def _progress(cb: Optional[Callable[[float], bool]]):
     return fn, fn
 
 
+def _stream(s) -> ctypes.c_void_p:
+    """None: the handle's own stream; 0: the legacy default stream (cudaStreamLegacy); else a cudaStream_t."""
+    if s is None:
+        return ctypes.c_void_p(None)
+    return ctypes.c_void_p(1 if int(s) == 0 else int(s))
+
+
 def _xf12(xf) -> np.ndarray:
     a = np.ascontiguousarray(np.asarray(xf, np.float32).reshape(-1))
     if a.size != 12:
@@ -270,21 +277,21 @@ class FastWindingNumber:
         _check(st)
 
     # -- device-pointer variants (torch tensors or any CUDA pointer); enqueue only
-    def calcFromGridWithDistances_dev(self, dims, xf, d_out_ptr: int, options=None, stream: int = 0):
+    def calcFromGridWithDistances_dev(self, dims, xf, d_out_ptr: int, options=None, stream=None):
         d = np.asarray(dims, np.int32)
         o = (options or DistanceToMeshOptions())._c()
         _check(self._L.gbfwn_from_grid_with_distances_dev(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o),
-                                                           ctypes.c_void_p(d_out_ptr), ctypes.c_void_p(stream or None)))
+                                                           ctypes.c_void_p(d_out_ptr), _stream(stream)))
 
-    def calcFromGrid_dev(self, dims, xf, d_out_ptr: int, beta: float = 2.0, stream: int = 0):
+    def calcFromGrid_dev(self, dims, xf, d_out_ptr: int, beta: float = 2.0, stream=None):
         d = np.asarray(dims, np.int32)
         _check(self._L.gbfwn_from_grid_dev(self._h, _p(d), _p(_xf12(xf)), beta, ctypes.c_void_p(d_out_ptr),
-                                           ctypes.c_void_p(stream or None)))
+                                           _stream(stream)))
 
     def calcFromVector_dev(self, d_pts_ptr: int, n: int, d_out_ptr: int, beta: float = 2.0, skipFace: int = -1,
-                           stream: int = 0):
+                           stream=None):
         _check(self._L.gbfwn_from_vector_dev(self._h, ctypes.c_void_p(d_pts_ptr), n, beta, skipFace,
-                                             ctypes.c_void_p(d_out_ptr), ctypes.c_void_p(stream or None)))
+                                             ctypes.c_void_p(d_out_ptr), _stream(stream)))
 
 
 def memory_estimates(nv: int, nt: int, dims=None, npts: int = 0) -> dict:

@@ -8,8 +8,10 @@
 // Every routine is templated on the arithmetic type T:
 //   T = float  : the reference's own FP32 arithmetic, operation by operation
 //                (compile with -ffp-contract=off so no FMA is formed);
-//   T = double : the FP64 oracle (same tree, same far-field criterion,
-//                evaluated in double) that the precision figures are quoted on.
+//   T = double : the FP64 oracle that the precision figures are quoted on: the same tree and
+//                the reference's own FP32 far-field decisions (so the same set of dipole terms
+//                and exact solid angles), every term and sum evaluated in double.  Winding
+//                numbers with no approximation at all come from orc_exact_wn.
 //
 // Reference files restated here (paths inside the MeshLib project):
 //   source/MRMesh/MRAABBTree.cpp:15-60          face boxes, tree construction
@@ -31,6 +33,7 @@
 #include <limits>
 #include <stack>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace orc {
@@ -254,12 +257,16 @@ struct Counters {
     uint64_t cpLeaves = 0;   // point-triangle projections evaluated
 };
 
-// MRDipole.cpp:94-128 calcFastWindingNumber (stack of 32, right pushed first, left popped first)
+// MRDipole.cpp:94-128 calcFastWindingNumber (stack of 32, right pushed first, left popped first).
+// With `decide` (FP64 oracle), the far-field test of every node is the reference's FP32 test on
+// the FP32 dipoles and FP32 query `qf`, so the FP64 sum covers exactly the reference's set of
+// dipole terms and solid angles -- only the arithmetic differs.
 template <typename T>
 static T calcFWN(const Mesh& m, const std::vector<Node>& nodes, const std::vector<Dipole<T>>& dip, const V3<T>& q, T beta,
-                 int skipFace, Counters* cnt) {
+                 int skipFace, Counters* cnt, const std::vector<Dipole<float>>* decide = nullptr, V3<float> qf = {}) {
     if (dip.empty()) return 0;
     const T betaSq = beta * beta;
+    const float betaSqF = float(beta) * float(beta);
     int stack[64];
     int sp = 0;
     stack[sp++] = 0;
@@ -268,7 +275,19 @@ static T calcFWN(const Mesh& m, const std::vector<Node>& nodes, const std::vecto
         const int i = stack[--sp];
         const Node& node = nodes[i];
         if (cnt) cnt->fwnNodes++;
-        if (dip[i].addIfGoodApprox(q, betaSq, res)) continue;
+        if (decide) {
+            const Dipole<float>& df = (*decide)[i];
+            const V3<float> dpf = df.pos - qf;
+            if (lengthSq(dpf) > betaSqF * df.rr) {
+                const V3<T> dp = dip[i].pos - q;
+                const T dd = lengthSq(dp);
+                const T d = std::sqrt(dd);
+                if (d > 0) res += dot(dp, dip[i].dirArea) / (d * dd);
+                continue;
+            }
+        } else if (dip[i].addIfGoodApprox(q, betaSq, res)) {
+            continue;
+        }
         if (node.r >= 0) {
             stack[sp++] = node.r;
             stack[sp++] = node.l;
@@ -440,7 +459,8 @@ static T withDistances(const Oracle* o, const std::vector<Dipole<T>>& dip, const
         if (fwnOut) *fwnOut = std::numeric_limits<double>::quiet_NaN();
         return std::numeric_limits<T>::quiet_NaN();
     }
-    const T w = calcFWN<T>(o->mesh, o->nodes, dip, p, T(op.windingNumberBeta), -1, cnt);
+    const std::vector<Dipole<float>>* decide = std::is_same<T, double>::value ? &o->dipF : nullptr;
+    const T w = calcFWN<T>(o->mesh, o->nodes, dip, p, T(op.windingNumberBeta), -1, cnt, decide, cvt<float>(p));
     if (fwnOut) *fwnOut = w;
     const T sign = w > T(op.windingNumberThreshold) ? T(-1) : T(1);
     return sign * std::sqrt(resSq);
@@ -515,7 +535,7 @@ void orc_from_vector(void* h, const float* pts, int64_t n, float beta, int skipF
         if (prec == 0)
             out[i] = calcFWN<float>(o->mesh, o->nodes, o->dipF, q, beta, skipFace, nullptr);
         else
-            out[i] = calcFWN<double>(o->mesh, o->nodes, o->dipD, cvt<double>(q), double(beta), skipFace, nullptr);
+            out[i] = calcFWN<double>(o->mesh, o->nodes, o->dipD, cvt<double>(q), double(beta), skipFace, nullptr, &o->dipF, q);
     });
 }
 
@@ -535,7 +555,7 @@ void orc_self_intersections(void* h, float beta, int prec, int threads, uint8_t*
         if (prec == 0)
             w = calcFWN<float>(o->mesh, o->nodes, o->dipF, q, beta, int(f), nullptr);
         else
-            w = calcFWN<double>(o->mesh, o->nodes, o->dipD, cvt<double>(q), double(beta), int(f), nullptr);
+            w = calcFWN<double>(o->mesh, o->nodes, o->dipD, cvt<double>(q), double(beta), int(f), nullptr, &o->dipF, q);
         if (wn) wn[f] = w;
         bits[f] = (w < 0 || w > 1) ? 1 : 0;
     });
@@ -551,7 +571,8 @@ void orc_from_grid(void* h, const int* dims, const float* xf, float beta, int pr
         if (prec == 0)
             out[i] = calcFWN<float>(o->mesh, o->nodes, o->dipF, xfPoint<float>(xf, x, y, z), beta, -1, nullptr);
         else
-            out[i] = calcFWN<double>(o->mesh, o->nodes, o->dipD, xfPoint<double>(xf, x, y, z), double(beta), -1, nullptr);
+            out[i] = calcFWN<double>(o->mesh, o->nodes, o->dipD, xfPoint<double>(xf, x, y, z), double(beta), -1, nullptr, &o->dipF,
+                                     xfPoint<float>(xf, x, y, z));
     });
 }
 
