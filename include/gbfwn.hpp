@@ -1,0 +1,144 @@
+// gbfwn.hpp -- header-only C++ adapter over the C ABI (gbfwn.h) with the shape of MeshLib's
+// MR::IFastWindingNumber / MR::IFastWindingNumberByParts (MRMesh/MRFastWindingNumber.h:11-107).
+//
+// It depends on nothing but the C++ standard library, so it compiles inside or outside MeshLib;
+// INTEGRATION.md shows the thin MeshLib-side class that derives from MR::IFastWindingNumber and
+// forwards to this one.  Method names, argument meaning and error behaviour follow the reference:
+// results are written to caller-owned std::vector / bitset words that the callee resizes, and
+// every call returns an Expected-like value whose error is the library's message.
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gbfwn.h"
+
+namespace gbfwn {
+
+// Minimal Expected<void>: ok() or an error string ("NVIDIA GPU error: ...", "operation canceled").
+class Result {
+public:
+    Result() = default;
+    static Result fromStatus(int st) {
+        Result r;
+        r.status_ = st;
+        if (st != GBFWN_OK) r.error_ = gbfwn_last_error();
+        return r;
+    }
+    explicit operator bool() const { return status_ == GBFWN_OK; }
+    int status() const { return status_; }
+    const std::string& error() const { return error_; }
+
+private:
+    int status_ = GBFWN_OK;
+    std::string error_;
+};
+
+using ProgressCallback = std::function<bool(float)>;  // MR::ProgressCallback
+// MR::IFastWindingNumberByParts::GridByPartsFunc: (slab data, slab dims, zOffset) -> Result
+using GridByPartsFunc = std::function<Result(std::vector<float>&& data, const int32_t dims[3], int zOffset)>;
+
+struct DistanceToMeshOptions {  // MR::DistanceToMeshOptions
+    float minDistSq = 0.f;
+    float maxDistSq = 3.402823466e+38f;
+    bool nullOutsideMinMax = true;
+    float windingNumberThreshold = 0.5f;
+    float windingNumberBeta = 2.f;
+    gbfwn_dist_opts c() const {
+        return gbfwn_dist_opts{minDistSq, maxDistSq, nullOutsideMinMax ? 1 : 0, windingNumberThreshold, windingNumberBeta};
+    }
+};
+
+namespace detail {
+inline int progressThunk(float p, void* user) { return (*static_cast<const ProgressCallback*>(user))(p) ? 1 : 0; }
+struct SlabCtx {
+    GridByPartsFunc* fn;
+    Result err;
+};
+inline int slabThunk(const float* data, const int32_t dims[3], int32_t zOffset, void* user) {
+    auto* ctx = static_cast<SlabCtx*>(user);
+    const size_t n = size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]);
+    std::vector<float> v(data, data + n);
+    ctx->err = (*ctx->fn)(std::move(v), dims, zOffset);
+    return ctx->err ? 0 : (ctx->err.status() ? ctx->err.status() : GBFWN_CANCELLED);
+}
+}  // namespace detail
+
+// GPU fast winding number of one mesh.  Like MR::Cuda::FastWindingNumber it keeps the device data
+// (mesh, tree, dipoles) for the lifetime of the object; calls on one object are serialised.
+class FastWindingNumber {
+public:
+    // verts: nv x 3 floats; tris: nt x 3 vertex ids (a face with a negative id is invalid).
+    FastWindingNumber(const float* verts, int64_t nv, const int32_t* tris, int64_t nt, int device = 0) {
+        gbfwn_handle h = nullptr;
+        created_ = Result::fromStatus(gbfwn_create(verts, nv, tris, nt, device, &h));
+        h_.reset(h);
+    }
+    const Result& creation() const { return created_; }
+    gbfwn_handle handle() const { return h_.get(); }
+
+    Result calcFromVector(std::vector<float>& res, const std::vector<float>& points /* 3 per point */, float beta,
+                          int32_t skipFace = -1, const ProgressCallback& cb = {}) {
+        res.resize(points.size() / 3);
+        return Result::fromStatus(gbfwn_from_vector(h_.get(), points.data(), int64_t(res.size()), beta, skipFace, res.data(),
+                                                    cb ? &detail::progressThunk : nullptr, cbUser(cb)));
+    }
+
+    // res: one bit per face in 64-bit words (MeshLib FaceBitSet blocks)
+    Result calcSelfIntersections(std::vector<uint64_t>& res, float beta, const ProgressCallback& cb = {}) {
+        res.assign(size_t((gbfwn_num_faces(h_.get()) + 63) / 64), 0);
+        return Result::fromStatus(gbfwn_self_intersections(h_.get(), beta, res.data(), nullptr,
+                                                           cb ? &detail::progressThunk : nullptr, cbUser(cb)));
+    }
+
+    // gridToMeshXf: 3x3 rows then translation (MR::AffineXf3f)
+    Result calcFromGrid(std::vector<float>& res, const int32_t dims[3], const float gridToMeshXf[12], float beta,
+                        const ProgressCallback& cb = {}) {
+        res.resize(size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]));
+        return Result::fromStatus(gbfwn_from_grid(h_.get(), dims, gridToMeshXf, beta, res.data(),
+                                                  cb ? &detail::progressThunk : nullptr, cbUser(cb)));
+    }
+
+    Result calcFromGridWithDistances(std::vector<float>& res, const int32_t dims[3], const float gridToMeshXf[12],
+                                     const DistanceToMeshOptions& options, const ProgressCallback& cb = {}) {
+        res.resize(size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]));
+        const gbfwn_dist_opts o = options.c();
+        return Result::fromStatus(gbfwn_from_grid_with_distances(h_.get(), dims, gridToMeshXf, &o, res.data(),
+                                                                 cb ? &detail::progressThunk : nullptr, cbUser(cb)));
+    }
+
+    Result calcFromGridByParts(GridByPartsFunc resFunc, const int32_t dims[3], const float gridToMeshXf[12], float beta,
+                               int layerOverlap, const ProgressCallback& cb = {}) {
+        detail::SlabCtx ctx{&resFunc, Result{}};
+        const int st = gbfwn_from_grid_by_parts(h_.get(), dims, gridToMeshXf, beta, layerOverlap, 0, &detail::slabThunk, &ctx,
+                                                cb ? &detail::progressThunk : nullptr, cbUser(cb));
+        if (!ctx.err) return ctx.err;
+        return Result::fromStatus(st);
+    }
+
+    Result calcFromGridWithDistancesByParts(GridByPartsFunc resFunc, const int32_t dims[3], const float gridToMeshXf[12],
+                                            const DistanceToMeshOptions& options, int layerOverlap,
+                                            const ProgressCallback& cb = {}) {
+        detail::SlabCtx ctx{&resFunc, Result{}};
+        const gbfwn_dist_opts o = options.c();
+        const int st = gbfwn_from_grid_with_distances_by_parts(h_.get(), dims, gridToMeshXf, &o, layerOverlap, 0,
+                                                               &detail::slabThunk, &ctx,
+                                                               cb ? &detail::progressThunk : nullptr, cbUser(cb));
+        if (!ctx.err) return ctx.err;
+        return Result::fromStatus(st);
+    }
+
+private:
+    static void* cbUser(const ProgressCallback& cb) { return cb ? const_cast<ProgressCallback*>(&cb) : nullptr; }
+    struct Del {
+        void operator()(gbfwn_handle h) const { gbfwn_destroy(h); }
+    };
+    std::unique_ptr<gbfwn_mesh_s, Del> h_;
+    Result created_;
+};
+
+}  // namespace gbfwn
