@@ -144,7 +144,9 @@ DistOpts toOpts(const gbfwn_dist_opts* o) {
     return d;
 }
 
-bool validDims(const int32_t* dims) { return dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0; }
+bool validDims(const int32_t* dims) {
+    return dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0 && gridTiles(dims[0], dims[1], dims[2]) <= kMaxTilesPerLaunch;
+}
 
 int createCommon(gbfwn_mesh_s* h, const std::string& where) {
     std::string err;

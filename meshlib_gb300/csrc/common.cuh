@@ -103,4 +103,9 @@ cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTri
 
 int numSMs();
 
+// Number of warp tiles a grid of nx x ny x nz voxels is cut into; the work-queue ticket counter is
+// 32 bits, so a single launch covers at most 2^32 - 1 tiles.
+uint64_t gridTiles(int32_t nx, int32_t ny, int32_t nz);
+constexpr uint64_t kMaxTilesPerLaunch = 0xffffffffull;
+
 }  // namespace gbfwn

@@ -473,6 +473,10 @@ int numSMs() {
     return n > 0 ? n : 1;
 }
 
+uint64_t gridTiles(int32_t nx, int32_t ny, int32_t nz) {
+    return uint64_t((nx + kTX - 1) / kTX) * uint64_t((ny + kTY - 1) / kTY) * uint64_t((nz + kTZ - 1) / kTZ);
+}
+
 static TileGrid tileGridFor(const GridRange& g) {
     TileGrid tg;
     tg.tilesX = (g.nx + kTX - 1) / kTX;
