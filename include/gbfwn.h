@@ -137,6 +137,21 @@ GBFWN_API int gbfwn_from_grid_with_distances(gbfwn_handle h, const int32_t dims[
 GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
                                                  const gbfwn_dist_opts* opts, float* d_out, void* stream);
 
+/* No counterpart in the reference.  Allocation-free variant of gbfwn_from_grid_with_distances_dev for
+ * callers that may not call cudaMalloc/cudaFree when they need a grid -- a host application that
+ * owns the device-memory budget and gives plugins preallocated buffers only, or a latency-bound loop
+ * that cannot take cudaFree's implicit device synchronisation.  Create the handle beforehand (that
+ * allocates); this call then allocates nothing: the output is the caller's device buffer and the
+ * kernel's scratch (work-queue counter + status word) is a fixed 256-byte device array that every
+ * GPU loading the library keeps until exit.  The first call on a device resolves that array's
+ * device address (cudaGetSymbolAddress), so make that first call before any stream capture.  Every
+ * call shares the array and clears it first, so calls that overlap on the GPU (concurrent streams,
+ * threads or handles) race: serialise them.  Limit: at most 2^32-1 warp tiles of 4x4x2 voxels per
+ * call (the counter is 32 bits); larger grids are rejected with GBFWN_INVALID.  Enqueues on
+ * `stream` (NULL = the handle's stream) and returns without waiting. */
+GBFWN_API int gbfwn_from_grid_with_distances_noalloc(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                     const gbfwn_dist_opts* opts, float* d_out, void* stream);
+
 /* MR::FastWindingNumber::calcWithDistances at arbitrary points (MRMesh/MRFastWindingNumber.h:62; the CPU
  * class has it, the interface does not). */
 GBFWN_API int gbfwn_vector_with_distances(gbfwn_handle h, const float* pts, int64_t n, const gbfwn_dist_opts* opts,

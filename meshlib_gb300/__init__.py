@@ -75,6 +75,8 @@ _SIGS = [
     ("gbfwn_from_grid_dev", ctypes.c_int, [_vp, _vp, _vp, _f, _vp, _vp]),
     ("gbfwn_from_grid_with_distances", ctypes.c_int, [_vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, PROGRESS, _vp]),
     ("gbfwn_from_grid_with_distances_dev", ctypes.c_int, [_vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, _vp]),
+    ("gbfwn_from_grid_with_distances_noalloc", ctypes.c_int,
+     [_vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, _vp]),
     ("gbfwn_vector_with_distances", ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(_DistOpts), _vp, PROGRESS, _vp]),
     ("gbfwn_vector_with_distances_dev", ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(_DistOpts), _vp, _vp]),
     ("gbfwn_from_grid_by_parts", ctypes.c_int, [_vp, _vp, _vp, _f, _i32, _i32, SLAB, _vp, PROGRESS, _vp]),
@@ -282,6 +284,13 @@ class FastWindingNumber:
         o = (options or DistanceToMeshOptions())._c()
         _check(self._L.gbfwn_from_grid_with_distances_dev(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o),
                                                            ctypes.c_void_p(d_out_ptr), _stream(stream)))
+
+    def calcFromGridWithDistances_noalloc(self, dims, xf, d_out_ptr: int, options=None, stream=None):
+        """Allocation-free variant of calcFromGridWithDistances_dev (see gbfwn_from_grid_with_distances_noalloc)."""
+        d = np.asarray(dims, np.int32)
+        o = (options or DistanceToMeshOptions())._c()
+        _check(self._L.gbfwn_from_grid_with_distances_noalloc(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o),
+                                                               ctypes.c_void_p(d_out_ptr), _stream(stream)))
 
     def calcFromGrid_dev(self, dims, xf, d_out_ptr: int, beta: float = 2.0, stream=None):
         d = np.asarray(dims, np.int32)

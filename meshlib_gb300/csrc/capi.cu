@@ -598,3 +598,60 @@ GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free signed-distance grid.
+//
+// Some callers must not call cudaMalloc / cudaFree at the moment they need a distance grid: a host
+// application that owns the whole device-memory budget and hands its plugins preallocated buffers
+// only, or a latency-bound loop (an interactive viewer's frame, a tool-path planner's inner step)
+// where cudaFree's implicit device-wide synchronisation or an allocation failure halfway through
+// is not acceptable.  Such a caller creates the mesh handle once, at set-up time, and then calls
+// gbfwn_from_grid_with_distances_noalloc with its own device output buffer.  The kernel's only
+// scratch -- the work-queue ticket counter and the status word -- lives in the fixed device array
+// below, which every GPU that loads this library keeps until the process exits.
+namespace {
+
+// 256 bytes per device; words [0] ticket counter, [1] status bits, the rest unused.
+static __device__ __align__(256) unsigned g_noallocScratch[64];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noallocMu;
+unsigned* g_noallocAddr[kNoallocMaxDevices] = {};
+
+// Device address of g_noallocScratch on `device` (which must be current).  Resolved once per
+// device: in host code the array's name is only a host-side stand-in, not a device address.
+int noallocScratch(int device, unsigned** out) {
+    if (device < 0 || device >= kNoallocMaxDevices) return fail(GBFWN_INVALID, "gbfwn_from_grid_with_distances_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noallocMu);
+    if (!g_noallocAddr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess) return cudaFail(e, "gbfwn_from_grid_with_distances_noalloc: cudaGetSymbolAddress");
+        g_noallocAddr[device] = static_cast<unsigned*>(p);
+    }
+    *out = g_noallocAddr[device];
+    return GBFWN_OK;
+}
+
+}  // namespace
+
+extern "C" GBFWN_API int gbfwn_from_grid_with_distances_noalloc(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                                const gbfwn_dist_opts* opts, float* d_out, void* stream) {
+    Xf X;
+    if (!h || !dims || !toXf(xf, X) || !d_out || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0)
+        return fail(GBFWN_INVALID, "gbfwn_from_grid_with_distances_noalloc: bad arguments");
+    if (gridTiles(dims[0], dims[1], dims[2]) > kMaxTilesPerLaunch)
+        return fail(GBFWN_INVALID,
+                    "gbfwn_from_grid_with_distances_noalloc: grid too large for the fixed scratch (its 32-bit work-queue "
+                    "counter covers at most 2^32-1 tiles of 4x4x2 voxels)");
+    DeviceGuard g(h->device);
+    unsigned* scratch = nullptr;
+    if (int st = noallocScratch(h->device, &scratch)) return st;
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    // the array keeps the previous call's contents: the ticket counter and the status word must start at zero
+    cudaError_t e = cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned), s);
+    GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
+    if (!e) e = launchGridSdf(h->tree.q, r, X, toOpts(opts), h->precise, d_out, scratch, s);
+    return e ? cudaFail(e, "gbfwn_from_grid_with_distances_noalloc") : GBFWN_OK;
+}
