@@ -259,18 +259,77 @@ __global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, co
         return;
     }
     const int64_t k = irank[i];
-    const RefNode L = nodes[nd.l], R = nodes[nd.r];
     const int32_t ll = linkOf(nd.l, irank, slot), rl = linkOf(nd.r, irank, slot);
-    cp[4 * k + 0] = make_float4(L.minx, L.miny, L.minz, __int_as_float(ll));
-    cp[4 * k + 1] = make_float4(L.maxx, L.maxy, L.maxz, __int_as_float(rl));
-    cp[4 * k + 2] = make_float4(R.minx, R.miny, R.minz, 0.f);
-    cp[4 * k + 3] = make_float4(R.maxx, R.maxy, R.maxz, 0.f);
+    (void)cp;
     const float* dl = dip8 + 8 * int64_t(nd.l);
     const float* dr = dip8 + 8 * int64_t(nd.r);
     dip[4 * k + 0] = make_float4(dl[0], dl[1], dl[2], dl[7]);
     dip[4 * k + 1] = make_float4(dl[4], dl[5], dl[6], __int_as_float(ll));
     dip[4 * k + 2] = make_float4(dr[0], dr[1], dr[2], dr[7]);
     dip[4 * k + 3] = make_float4(dr[4], dr[5], dr[6], __int_as_float(rl));
+}
+
+// Oriented bounding box of every non-root node, written into its parent's closest-point record
+// (layout in common.cuh).  Frame: n = the node's dipole direction dirArea (the area-weighted
+// normal of its triangles), t and u completing an orthonormal basis; extents = the range of the
+// projections of all the node's triangle vertices, widened by a relative margin that covers the
+// FP32 rounding of the projections here and at query time, so the box distance stays a lower
+// bound of the distance to every triangle inside.  One warp per node; the node's leaves are the
+// contiguous slots range[i] = (first, count).
+__global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const int2* __restrict__ range,
+                          const float4* __restrict__ tri, const int32_t* __restrict__ parent,
+                          const int32_t* __restrict__ irank, const int32_t* __restrict__ slot, float4* __restrict__ cp) {
+    const int64_t i = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= nNodes || i == 0) return;
+    const float* d = dip8 + 8 * i;
+    float nx = d[4], ny = d[5], nz = d[6];
+    const float len = sqrtf(nx * nx + ny * ny + nz * nz);
+    if (!(len > 1e-30f)) {
+        nx = 0.f; ny = 0.f; nz = 1.f;
+    } else {
+        nx /= len; ny /= len; nz /= len;
+    }
+    float ax = 1.f, ay = 0.f;
+    if (fabsf(nx) > 0.6f) { ax = 0.f; ay = 1.f; }
+    const float an = ax * nx + ay * ny;
+    float tx = ax - an * nx, ty = ay - an * ny, tz = -an * nz;
+    const float tl = sqrtf(tx * tx + ty * ty + tz * tz);
+    tx /= tl; ty /= tl; tz /= tl;
+    const float ux = ny * tz - nz * ty, uy = nz * tx - nx * tz, uz = nx * ty - ny * tx;
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    const int2 r = range[i];
+    for (int sidx = r.x + lane; sidx < r.x + r.y; sidx += 32) {
+        for (int k = 0; k < 3; ++k) {
+            const float4 v = tri[3 * int64_t(sidx) + k];
+            const float p[3] = {tx * v.x + ty * v.y + tz * v.z, ux * v.x + uy * v.y + uz * v.z, nx * v.x + ny * v.y + nz * v.z};
+            for (int j = 0; j < 3; ++j) {
+                lo[j] = fminf(lo[j], p[j]);
+                hi[j] = fmaxf(hi[j], p[j]);
+            }
+        }
+    }
+    for (int off = 16; off; off >>= 1)
+        for (int j = 0; j < 3; ++j) {
+            lo[j] = fminf(lo[j], __shfl_xor_sync(0xffffffffu, lo[j], off));
+            hi[j] = fmaxf(hi[j], __shfl_xor_sync(0xffffffffu, hi[j], off));
+        }
+    if (lane) return;
+    float c[3], e[3];
+    for (int j = 0; j < 3; ++j) {
+        c[j] = 0.5f * (lo[j] + hi[j]);
+        const float h = 0.5f * (hi[j] - lo[j]);
+        e[j] = h + 2e-6f * (fabsf(c[j]) + h) + 1e-30f;
+    }
+    const int32_t p = parent[i];
+    const int side = (i == int64_t(p) + 1) ? 0 : 1;
+    const int32_t k = irank[i];
+    const int32_t link = k >= 0 ? k : ~slot[i];
+    float4* dst = cp + 8 * int64_t(irank[p]) + 4 * side;
+    dst[0] = make_float4(tx, ty, tz, c[0]);
+    dst[1] = make_float4(ux, uy, uz, c[1]);
+    dst[2] = make_float4(nx, ny, nz, c[2]);
+    dst[3] = make_float4(e[0], e[1], e[2], __int_as_float(link));
 }
 
 __global__ void fillInt(int32_t* p, int64_t n, int32_t v) {
@@ -283,8 +342,8 @@ inline unsigned blocksFor(int64_t n, int t) { return unsigned((n + t - 1) / t); 
 }  // namespace
 
 // Computes dipoles and the query layout on the device from reference nodes already in `out.nodes`.
-cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const int32_t* hIrankSlot, DeviceTree& out,
-                             Allocator& A, cudaStream_t s) {
+cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const int32_t* hIrankSlot, const int32_t* hRange,
+                             DeviceTree& out, Allocator& A, cudaStream_t s) {
     const int64_t nNodes = out.nLeaves > 0 ? 2 * out.nLeaves - 1 : 0;
     cudaError_t e;
     int32_t *parent = nullptr, *arrive = nullptr, *irs = nullptr;
@@ -296,7 +355,10 @@ cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const in
     if ((e = A.alloc((void**)&arrive, sizeof(int32_t) * size_t(nNodes)))) return e;
     if ((e = A.alloc((void**)&irs, sizeof(int32_t) * 2 * size_t(nNodes)))) return e;
     const int64_t nInt = std::max<int64_t>(out.nInternal, 1);
-    if ((e = A.alloc((void**)&out.cp, sizeof(float4) * 4 * size_t(nInt)))) return e;
+    int2* range = nullptr;
+    if ((e = A.alloc((void**)&range, sizeof(int2) * size_t(nNodes)))) return e;
+    if ((e = cudaMemcpyAsync(range, hRange, sizeof(int2) * size_t(nNodes), cudaMemcpyHostToDevice, s))) return e;
+    if ((e = A.alloc((void**)&out.cp, sizeof(float4) * 8 * size_t(nInt)))) return e;
     if ((e = A.alloc((void**)&out.dip, sizeof(float4) * 4 * size_t(nInt)))) return e;
     if ((e = A.alloc((void**)&out.tri, sizeof(float4) * 3 * size_t(out.nLeaves)))) return e;
     if ((e = cudaMemcpyAsync(irs, hIrankSlot, sizeof(int32_t) * 2 * size_t(nNodes), cudaMemcpyHostToDevice, s))) return e;
@@ -307,6 +369,7 @@ cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const in
     finalizeKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, out.dip8);
     packKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, out.dip8, irs, irs + nNodes, dVerts, dTris, out.cp, out.dip, out.tri,
                                  out.faceSlot);
+    obbKernel<<<blocksFor(nNodes * 32, 256), 256, 0, s>>>(nNodes, out.dip8, range, out.tri, parent, irs, irs + nNodes, out.cp);
     return cudaGetLastError();
 }
 
@@ -341,12 +404,23 @@ cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTri
             irs[nNodes + i] = nl++;
         }
     }
+    // leaf slot range of every subtree (children have larger pre-order indices)
+    std::vector<int32_t> range(size_t(2 * nNodes));
+    for (int64_t i = nNodes - 1; i >= 0; --i) {
+        if (nodes[i].r < 0) {
+            range[2 * i] = irs[nNodes + i];
+            range[2 * i + 1] = 1;
+        } else {
+            range[2 * i] = range[2 * int64_t(nodes[i].l)];
+            range[2 * i + 1] = range[2 * int64_t(nodes[i].l) + 1] + range[2 * int64_t(nodes[i].r) + 1];
+        }
+    }
     if (nNodes > 0) {
         if ((e = A.alloc((void**)&out.nodes, sizeof(RefNode) * size_t(nNodes)))) return e;
         if ((e = cudaMemcpyAsync(out.nodes, nodes.data(), sizeof(RefNode) * size_t(nNodes), cudaMemcpyHostToDevice, s)))
             return e;
     }
-    if ((e = finishDeviceTree(dVerts, dTris, irs.data(), out, A, s))) return e;
+    if ((e = finishDeviceTree(dVerts, dTris, irs.data(), range.data(), out, A, s))) return e;
     if ((e = cudaStreamSynchronize(s))) return e;  // host vectors above must outlive the copies
     // root data for the kernels' parameter block
     QueryTree& q = out.q;

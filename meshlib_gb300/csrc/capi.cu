@@ -18,8 +18,6 @@
 using namespace gbfwn;
 
 namespace gbfwn {
-cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const int32_t* hIrankSlot, DeviceTree& out,
-                             Allocator& A, cudaStream_t s);
 }
 
 namespace {

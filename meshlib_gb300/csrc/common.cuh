@@ -23,7 +23,9 @@ static_assert(sizeof(RefNode) == 32, "reference node is 32 bytes");
 // read gives everything a traversal step needs; children are fetched as float4, all lanes of a
 // warp read the same record, so each load is a broadcast).
 //
-//  cp  [internal k] 4 x float4 : {lmin.xyz, lLink} {lmax.xyz, rLink} {rmin.xyz, 0} {rmax.xyz, 0}
+//  cp  [internal k] 8 x float4 : per child (left, then right) an oriented bounding box
+//                                {t.xyz, ct} {u.xyz, cu} {n.xyz, cn} {et, eu, en, link}
+//                                (orthonormal frame t,u,n; centre and half extents along it)
 //  dip [internal k] 4 x float4 : {lpos.xyz, l rr}  {l dirArea.xyz, lLink} {rpos.xyz, r rr} {r dirArea.xyz, rLink}
 //  tri [leaf slot s] 3 x float4: {a.xyz, face} {b.xyz, 0} {c.xyz, 0}
 //
