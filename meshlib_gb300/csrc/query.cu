@@ -84,6 +84,21 @@ __device__ __forceinline__ bool dipoleTerm(const float4& p, const float4& da, co
     return true;
 }
 
+// FP64 solid angle for near-plane queries; kept out of line so the rare path does not inflate the
+// register allocation of the traversal loop.
+__device__ __noinline__ float solidAngleFp64(const float3 q, const float4 A, const float4 B, const float4 C) {
+    const double ax = double(A.x) - q.x, ay = double(A.y) - q.y, az = double(A.z) - q.z;
+    const double bx = double(B.x) - q.x, by = double(B.y) - q.y, bz = double(B.z) - q.z;
+    const double cx = double(C.x) - q.x, cy = double(C.y) - q.y, cz = double(C.z) - q.z;
+    const double lx = sqrt(ax * ax + ay * ay + az * az);
+    const double ly = sqrt(bx * bx + by * by + bz * bz);
+    const double lz = sqrt(cx * cx + cy * cy + cz * cz);
+    const double dd = lx * ly * lz + (ax * bx + ay * by + az * bz) * lz + (bx * cx + by * cy + bz * cz) * lx +
+                      (cx * ax + cy * ay + cz * az) * ly;
+    const double dt = ax * (by * cz - bz * cy) - ay * (bx * cz - bz * cx) + az * (bx * cy - by * cx);
+    return float(2.0 * atan2(dt, dd));
+}
+
 // MRMesh/MRDipole.cpp:81-92: 2 * atan2(det[a-q, b-q, c-q], den) (Van Oosterom-Strackee).  In
 // precise mode a query within a few ulps of the triangle plane (|det| small against the product of
 // the three lengths, where the FP32 sign of det is not reliable) is re-evaluated in FP64.
@@ -102,18 +117,7 @@ __device__ __forceinline__ float solidAngle(const float3& q, const float4& A, co
     const float det = __fadd_rn(__fsub_rn(__fmul_rn(mxx, __fsub_rn(__fmul_rn(myy, mzz), __fmul_rn(myz, mzy))),
                                           __fmul_rn(mxy, __fsub_rn(__fmul_rn(myx, mzz), __fmul_rn(myz, mzx)))),
                                 __fmul_rn(mxz, __fsub_rn(__fmul_rn(myx, mzy), __fmul_rn(myy, mzx))));
-    if (PRECISE && fabsf(det) <= 1e-5f * xyz) {
-        const double ax = double(A.x) - q.x, ay = double(A.y) - q.y, az = double(A.z) - q.z;
-        const double bx = double(B.x) - q.x, by = double(B.y) - q.y, bz = double(B.z) - q.z;
-        const double cx = double(C.x) - q.x, cy = double(C.y) - q.y, cz = double(C.z) - q.z;
-        const double lx = sqrt(ax * ax + ay * ay + az * az);
-        const double ly = sqrt(bx * bx + by * by + bz * bz);
-        const double lz = sqrt(cx * cx + cy * cy + cz * cz);
-        const double dd = lx * ly * lz + (ax * bx + ay * by + az * bz) * lz + (bx * cx + by * cy + bz * cz) * lx +
-                          (cx * ax + cy * ay + cz * az) * ly;
-        const double dt = ax * (by * cz - bz * cy) - ay * (bx * cz - bz * cx) + az * (bx * cy - by * cx);
-        return float(2.0 * atan2(dt, dd));
-    }
+    if (PRECISE && fabsf(det) <= 1e-5f * xyz) return solidAngleFp64(q, A, B, C);
     return 2.f * atan2f(det, den);
 }
 
@@ -254,6 +258,15 @@ template <typename T> __device__ __forceinline__ V3T<T> closestPoint(V3T<T> p, V
     return vmad(vmad(a, vb * denom, ab), vc * denom, ac);
 }
 
+// FP64 projection (as the reference CPU does for every leaf, MRMesh/MRMeshProject.cpp:66-72): the
+// projection is rounded to float and the distance measured in float.  Out of line: rare path.
+__device__ __noinline__ float triDistSqFp64(const float3 p, const float4 A, const float4 B, const float4 C) {
+    const V3T<double> pd{p.x, p.y, p.z}, ad{A.x, A.y, A.z}, bd{B.x, B.y, B.z}, cd{C.x, C.y, C.z};
+    const V3T<double> q = closestPoint<double>(pd, ad, bd, cd);
+    const float qx = float(q.x) - p.x, qy = float(q.y) - p.y, qz = float(q.z) - p.z;
+    return dot3rn(qx, qy, qz, qx, qy, qz);
+}
+
 // Squared distance from p to a triangle.  FP32 projection; in precise mode a query that lands
 // within ~1e-4 triangle edge lengths of the triangle is re-projected in FP64.
 template <bool PRECISE>
@@ -265,13 +278,7 @@ __device__ __forceinline__ float triDistSq(const float3& p, const float4& A, con
     if (PRECISE) {
         const V3T<float> ab = vsub(bf, af), ac = vsub(cf, af);
         const float scale = vdot(ab, ab) + vdot(ac, ac);
-        if (ds < 1e-8f * scale) {
-            const V3T<double> pd{p.x, p.y, p.z}, ad{A.x, A.y, A.z}, bd{B.x, B.y, B.z}, cd{C.x, C.y, C.z};
-            const V3T<double> q = closestPoint<double>(pd, ad, bd, cd);
-            // the reference rounds the FP64 projection to float and measures in float
-            const float qx = float(q.x) - p.x, qy = float(q.y) - p.y, qz = float(q.z) - p.z;
-            ds = dot3rn(qx, qy, qz, qx, qy, qz);
-        }
+        if (ds < 1e-8f * scale) ds = triDistSqFp64(p, A, B, C);
     }
     return ds;
 }
@@ -367,7 +374,7 @@ __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
 }
 
 template <bool PRECISE, bool DIST>
-__global__ void __launch_bounds__(kThreads) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
+__global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
                                                        float* __restrict__ out, unsigned* scratch) {
     const int lane = threadIdx.x & 31;
     const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
@@ -398,7 +405,7 @@ __global__ void __launch_bounds__(kThreads) gridKernel(QueryTree t, GridRange g,
 }
 
 template <bool PRECISE, bool DIST>
-__global__ void __launch_bounds__(kThreads) vectorKernel(QueryTree t, const float* __restrict__ pts, int64_t n, DistOpts o,
+__global__ void __launch_bounds__(kThreads, 4) vectorKernel(QueryTree t, const float* __restrict__ pts, int64_t n, DistOpts o,
                                                          int32_t skipFace, float* __restrict__ out, unsigned* scratch) {
     const int lane = threadIdx.x & 31;
     const float betaSq = __fmul_rn(o.beta, o.beta);
@@ -428,7 +435,7 @@ __global__ void __launch_bounds__(kThreads) vectorKernel(QueryTree t, const floa
 // MRMesh/MRFastWindingNumber.cpp:40-52: query = triCenter(f) = (1/3) * (v0 + v1 + v2), skipping f.
 // Lanes take consecutive leaf slots, which are spatially coherent.
 template <bool PRECISE>
-__global__ void __launch_bounds__(kThreads) selfIntKernel(QueryTree t, float beta, uint64_t* __restrict__ bits,
+__global__ void __launch_bounds__(kThreads, 4) selfIntKernel(QueryTree t, float beta, uint64_t* __restrict__ bits,
                                                           float* __restrict__ wn, unsigned* scratch) {
     const int lane = threadIdx.x & 31;
     const float betaSq = __fmul_rn(beta, beta);
