@@ -17,8 +17,8 @@ LIB = os.path.join(HERE, "libgbfwn.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden", "--expt-relaxed-constexpr"]
 # build.cu must round every float operation separately (bit-identical boxes and dipoles)
-PER_FILE = {"build.cu": ["-fmad=false"]}
-SOURCES = ["capi.cu", "build.cu", "query.cu"]
+PER_FILE = {"build.cu": ["-fmad=false"], "treebuild.cu": ["-fmad=false"]}
+SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu"]
 
 
 def nvcc() -> str:

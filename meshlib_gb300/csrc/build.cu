@@ -9,8 +9,8 @@
 // Because that order is total, the split sets do not depend on how the partition is computed.
 //
 // This file is compiled with -fmad=false: every float expression below rounds each operation
-// separately, exactly like the reference's CPU code, so boxes, dipoles and radii are
-// bit-identical to the reference's.
+// separately, exactly like the reference's CPU code, so dipoles and radii are bit-identical to the
+// reference's.  The tree topology itself is built on the device by treebuild.cu.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -21,125 +21,6 @@
 #include "common.cuh"
 
 namespace gbfwn {
-
-namespace {
-
-struct HBox {
-    float mn[3], mx[3];
-};
-
-struct HLeaf {
-    int32_t id;
-    float c[3];  // min + max per dimension: the comparison key
-    HBox box;
-};
-
-// MRMesh/MRAABBTree.cpp:15-29 + MRMesh/MRBox.h:260-270
-inline HBox faceBox(const float* v, const int32_t* t) {
-    HBox b;
-    for (int d = 0; d < 3; ++d) {
-        float lo = FLT_MAX, hi = -FLT_MAX;
-        for (int k = 0; k < 3; ++k) {
-            const float x = v[3 * t[k] + d];
-            if (x < lo) lo = x;
-            if (x > hi) hi = x;
-        }
-        b.mn[d] = std::nextafter(lo, -FLT_MAX);
-        b.mx[d] = std::nextafter(hi, FLT_MAX);
-    }
-    return b;
-}
-
-// MRMesh/MRBox.h:376-396: dims ascending by (extent, index)
-inline void sortedDims(const HBox& b, int sd[3]) {
-    float e[3];
-    int id[3] = {0, 1, 2};
-    for (int i = 0; i < 3; ++i) e[i] = b.mx[i] - b.mn[i];
-    for (int i = 0; i + 1 < 3; ++i)
-        for (int j = i + 1; j < 3; ++j)
-            if (e[j] < e[i] || (e[j] == e[i] && id[j] < id[i])) {
-                std::swap(e[i], e[j]);
-                std::swap(id[i], id[j]);
-            }
-    for (int i = 0; i < 3; ++i) sd[i] = id[i];
-}
-
-struct Sub {
-    int32_t root, first, num;
-};
-
-void buildRange(std::vector<HLeaf>& leaves, std::vector<RefNode>& nodes, Sub s0, int threads) {
-    std::vector<Sub> st;
-    st.push_back(s0);
-    std::vector<std::thread> spawned;
-    while (!st.empty()) {
-        Sub s = st.back();
-        st.pop_back();
-        RefNode& nd = nodes[s.root];
-        if (s.num == 1) {
-            const HLeaf& L = leaves[s.first];
-            nd = RefNode{L.box.mn[0], L.box.mn[1], L.box.mn[2], L.box.mx[0], L.box.mx[1], L.box.mx[2], L.id, -1};
-            continue;
-        }
-        HBox b{{FLT_MAX, FLT_MAX, FLT_MAX}, {-FLT_MAX, -FLT_MAX, -FLT_MAX}};
-        for (int i = 0; i < s.num; ++i) {
-            const HBox& lb = leaves[s.first + i].box;
-            for (int d = 0; d < 3; ++d) {
-                if (lb.mn[d] < b.mn[d]) b.mn[d] = lb.mn[d];
-                if (lb.mx[d] > b.mx[d]) b.mx[d] = lb.mx[d];
-            }
-        }
-        int sd[3];
-        sortedDims(b, sd);
-        const int d2 = sd[2], d1 = sd[1], d0 = sd[0];
-        auto less = [d2, d1, d0](const HLeaf& x, const HLeaf& y) {
-            if (x.c[d2] != y.c[d2]) return x.c[d2] < y.c[d2];
-            if (x.c[d1] != y.c[d1]) return x.c[d1] < y.c[d1];
-            if (x.c[d0] != y.c[d0]) return x.c[d0] < y.c[d0];
-            return x.id < y.id;
-        };
-        const int mid = s.first + s.num / 2;
-        std::nth_element(leaves.begin() + s.first, leaves.begin() + mid, leaves.begin() + s.first + s.num, less);
-        const int nl = mid - s.first;
-        nd = RefNode{b.mn[0], b.mn[1], b.mn[2], b.mx[0], b.mx[1], b.mx[2], s.root + 1, s.root + 2 * nl};
-        const Sub L{s.root + 1, s.first, nl}, R{s.root + 2 * nl, mid, s.num - nl};
-        if (threads >= 2 && s.num >= 4096) {
-            const int rt = threads / 2;
-            spawned.emplace_back([&leaves, &nodes, R, rt] { buildRange(leaves, nodes, R, rt); });
-            threads -= rt;
-            st.push_back(L);
-        } else {
-            st.push_back(R);
-            st.push_back(L);
-        }
-    }
-    for (auto& t : spawned) t.join();
-}
-
-}  // namespace
-
-// Host construction of the reference topology (the reference builds it on the CPU too,
-// MRCuda/MRCudaFastWindingNumber.cpp:70-80).
-void hostBuildTopology(const float* verts, int64_t nv, const int32_t* tris, int64_t nt, std::vector<RefNode>& nodes) {
-    (void)nv;
-    std::vector<HLeaf> leaves;
-    leaves.reserve(size_t(nt));
-    for (int64_t f = 0; f < nt; ++f) {
-        const int32_t* t = tris + 3 * f;
-        if (t[0] < 0 || t[1] < 0 || t[2] < 0) continue;  // invalid face: not in the tree
-        HLeaf L;
-        L.id = int32_t(f);
-        L.box = faceBox(verts, t);
-        for (int d = 0; d < 3; ++d) L.c[d] = L.box.mn[d] + L.box.mx[d];
-        leaves.push_back(L);
-    }
-    const int n = int(leaves.size());
-    nodes.assign(n > 0 ? size_t(2 * n - 1) : 0, RefNode{});
-    if (n == 0) return;
-    int threads = int(std::thread::hardware_concurrency());
-    if (threads < 1) threads = 1;
-    buildRange(leaves, nodes, Sub{0, 0, n}, threads);
-}
 
 // ------------------------------------------------------------------------------------ device
 namespace {
@@ -341,27 +222,28 @@ inline unsigned blocksFor(int64_t n, int t) { return unsigned((n + t - 1) / t); 
 
 }  // namespace
 
-// Computes dipoles and the query layout on the device from reference nodes already in `out.nodes`.
-cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const int32_t* hIrankSlot, const int32_t* hRange,
-                             DeviceTree& out, Allocator& A, cudaStream_t s) {
+// Device tree construction of the reference topology (treebuild.cu).
+cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, int64_t& nLeaves,
+                             RefNode*& nodes, int32_t*& irs, int2*& range, Allocator& P, Allocator& A, cudaStream_t s,
+                             std::string& err);
+
+// Dipoles and the query layout on the device from the reference nodes in `out.nodes`; `irs` holds
+// the internal rank and leaf slot of every node, `range` its leaf-slot range (device arrays).
+static cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const int32_t* irs, const int2* range,
+                                    DeviceTree& out, Allocator& P, Allocator& T, cudaStream_t s) {
     const int64_t nNodes = out.nLeaves > 0 ? 2 * out.nLeaves - 1 : 0;
     cudaError_t e;
-    int32_t *parent = nullptr, *arrive = nullptr, *irs = nullptr;
-    if ((e = A.alloc((void**)&out.faceSlot, sizeof(int32_t) * size_t(std::max<int64_t>(out.nFaces, 1))))) return e;
+    int32_t *parent = nullptr, *arrive = nullptr;
+    if ((e = P.alloc((void**)&out.faceSlot, sizeof(int32_t) * size_t(std::max<int64_t>(out.nFaces, 1))))) return e;
     fillInt<<<blocksFor(std::max<int64_t>(out.nFaces, 1), 256), 256, 0, s>>>(out.faceSlot, out.nFaces, -1);
     if (nNodes == 0) return cudaGetLastError();
-    if ((e = A.alloc((void**)&out.dip8, sizeof(float) * 8 * size_t(nNodes)))) return e;
-    if ((e = A.alloc((void**)&parent, sizeof(int32_t) * size_t(nNodes)))) return e;
-    if ((e = A.alloc((void**)&arrive, sizeof(int32_t) * size_t(nNodes)))) return e;
-    if ((e = A.alloc((void**)&irs, sizeof(int32_t) * 2 * size_t(nNodes)))) return e;
+    if ((e = P.alloc((void**)&out.dip8, sizeof(float) * 8 * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&parent, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&arrive, sizeof(int32_t) * size_t(nNodes)))) return e;
     const int64_t nInt = std::max<int64_t>(out.nInternal, 1);
-    int2* range = nullptr;
-    if ((e = A.alloc((void**)&range, sizeof(int2) * size_t(nNodes)))) return e;
-    if ((e = cudaMemcpyAsync(range, hRange, sizeof(int2) * size_t(nNodes), cudaMemcpyHostToDevice, s))) return e;
-    if ((e = A.alloc((void**)&out.cp, sizeof(float4) * 8 * size_t(nInt)))) return e;
-    if ((e = A.alloc((void**)&out.dip, sizeof(float4) * 4 * size_t(nInt)))) return e;
-    if ((e = A.alloc((void**)&out.tri, sizeof(float4) * 3 * size_t(out.nLeaves)))) return e;
-    if ((e = cudaMemcpyAsync(irs, hIrankSlot, sizeof(int32_t) * 2 * size_t(nNodes), cudaMemcpyHostToDevice, s))) return e;
+    if ((e = P.alloc((void**)&out.cp, sizeof(float4) * 8 * size_t(nInt)))) return e;
+    if ((e = P.alloc((void**)&out.dip, sizeof(float4) * 4 * size_t(nInt)))) return e;
+    if ((e = P.alloc((void**)&out.tri, sizeof(float4) * 3 * size_t(out.nLeaves)))) return e;
     const unsigned B = blocksFor(nNodes, 256);
     leafDipolesKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, dVerts, dTris, out.dip8, arrive);
     parentsKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, parent);
@@ -374,55 +256,16 @@ cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, const in
 }
 
 cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, DeviceTree& out,
-                            Allocator& A, cudaStream_t s, std::string& err) {
-    // Topology on the host (same as the reference's GPU path); dipoles and layout on the device.
-    std::vector<float> hv(size_t(nv) * 3);
-    std::vector<int32_t> ht(size_t(nt) * 3);
+                            Allocator& P, Allocator& T, cudaStream_t s, std::string& err) {
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(hv.data(), dVerts, hv.size() * sizeof(float), cudaMemcpyDeviceToHost, s))) return e;
-    if ((e = cudaMemcpyAsync(ht.data(), dTris, ht.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s))) return e;
-    if ((e = cudaStreamSynchronize(s))) return e;
-    for (size_t i = 0; i < ht.size(); ++i)
-        if (ht[i] >= nv) {
-            err = "triangle vertex id out of range";
-            return cudaErrorInvalidValue;
-        }
-    std::vector<RefNode> nodes;
-    hostBuildTopology(hv.data(), nv, ht.data(), nt, nodes);
-    const int64_t nNodes = int64_t(nodes.size());
+    int64_t nLeaves = 0;
+    int32_t* irs = nullptr;
+    int2* range = nullptr;
+    if ((e = gpuBuildTopology(dVerts, nv, dTris, nt, nLeaves, out.nodes, irs, range, P, T, s, err))) return e;
     out.nFaces = nt;
-    out.nLeaves = nNodes > 0 ? (nNodes + 1) / 2 : 0;
-    out.nInternal = out.nLeaves > 0 ? out.nLeaves - 1 : 0;
-    std::vector<int32_t> irs(size_t(2 * nNodes));
-    int32_t ni = 0, nl = 0;
-    for (int64_t i = 0; i < nNodes; ++i) {
-        if (nodes[i].r >= 0) {
-            irs[i] = ni++;
-            irs[nNodes + i] = -1;
-        } else {
-            irs[i] = -1;
-            irs[nNodes + i] = nl++;
-        }
-    }
-    // leaf slot range of every subtree (children have larger pre-order indices)
-    std::vector<int32_t> range(size_t(2 * nNodes));
-    for (int64_t i = nNodes - 1; i >= 0; --i) {
-        if (nodes[i].r < 0) {
-            range[2 * i] = irs[nNodes + i];
-            range[2 * i + 1] = 1;
-        } else {
-            range[2 * i] = range[2 * int64_t(nodes[i].l)];
-            range[2 * i + 1] = range[2 * int64_t(nodes[i].l) + 1] + range[2 * int64_t(nodes[i].r) + 1];
-        }
-    }
-    if (nNodes > 0) {
-        if ((e = A.alloc((void**)&out.nodes, sizeof(RefNode) * size_t(nNodes)))) return e;
-        if ((e = cudaMemcpyAsync(out.nodes, nodes.data(), sizeof(RefNode) * size_t(nNodes), cudaMemcpyHostToDevice, s)))
-            return e;
-    }
-    if ((e = finishDeviceTree(dVerts, dTris, irs.data(), range.data(), out, A, s))) return e;
-    if ((e = cudaStreamSynchronize(s))) return e;  // host vectors above must outlive the copies
-    // root data for the kernels' parameter block
+    out.nLeaves = nLeaves;
+    out.nInternal = nLeaves > 0 ? nLeaves - 1 : 0;
+    if ((e = finishDeviceTree(dVerts, dTris, irs, range, out, P, T, s))) return e;
     QueryTree& q = out.q;
     q.cp = out.cp;
     q.dip = out.dip;
@@ -430,20 +273,21 @@ cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTri
     q.faceSlot = out.faceSlot;
     q.nLeaves = int32_t(out.nLeaves);
     q.nFaces = int32_t(out.nFaces);
-    if (nNodes > 0) {
+    if (nLeaves > 0) {  // root data for the kernels' parameter block
         float rd[8];
-        if ((e = cudaMemcpy(rd, out.dip8, sizeof(rd), cudaMemcpyDeviceToHost))) return e;
-        const RefNode& r = nodes[0];
+        RefNode r;
+        if ((e = cudaMemcpyAsync(rd, out.dip8, sizeof(rd), cudaMemcpyDeviceToHost, s))) return e;
+        if ((e = cudaMemcpyAsync(&r, out.nodes, sizeof(r), cudaMemcpyDeviceToHost, s))) return e;
+        if ((e = cudaStreamSynchronize(s))) return e;
         const int32_t rootLink = r.r >= 0 ? 0 : ~0;
-        int32_t li = rootLink;
         float lf;
-        std::memcpy(&lf, &li, 4);
+        std::memcpy(&lf, &rootLink, 4);
         q.rootDip0 = make_float4(rd[0], rd[1], rd[2], rd[7]);
         q.rootDip1 = make_float4(rd[4], rd[5], rd[6], lf);
         q.rootBox0 = make_float4(r.minx, r.miny, r.minz, lf);
         q.rootBox1 = make_float4(r.maxx, r.maxy, r.maxz, 0.f);
     }
-    return cudaSuccess;
+    return cudaStreamSynchronize(s);
 }
 
 }  // namespace gbfwn

@@ -148,7 +148,10 @@ bool validDims(const int32_t* dims) {
 
 int createCommon(gbfwn_mesh_s* h, const std::string& where) {
     std::string err;
-    cudaError_t e = buildDeviceTree(h->dVerts, h->nv, h->dTris, h->nt, h->tree, h->treeMem, h->stream, err);
+    ListAllocator tmp;  // build work arrays, freed once the build has finished
+    cudaError_t e = buildDeviceTree(h->dVerts, h->nv, h->dTris, h->nt, h->tree, h->treeMem, tmp, h->stream, err);
+    cudaStreamSynchronize(h->stream);
+    tmp.freeAll();
     if (e == cudaErrorInvalidValue && !err.empty()) return fail(GBFWN_INVALID, err);
     if (e) return cudaFail(e, where.c_str());
     return GBFWN_OK;

@@ -100,8 +100,9 @@ struct Allocator {
     virtual cudaError_t alloc(void** p, size_t bytes) = 0;
     virtual ~Allocator() = default;
 };
+// P: allocations that live with the handle; T: work arrays the caller frees after the build.
 cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, DeviceTree& out,
-                            Allocator& a, cudaStream_t s, std::string& err);
+                            Allocator& P, Allocator& T, cudaStream_t s, std::string& err);
 
 int numSMs();
 

@@ -54,6 +54,38 @@ def test_tree_bit_exact_large(fwncls):
     assert np.array_equal(dip.view(np.uint32), o.dipoles(0).view(np.uint32))
 
 
+def _plane_grid(n):
+    i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    v = np.stack([i.ravel(), j.ravel(), np.zeros((n + 1) ** 2)], 1).astype(np.float32) / n
+    a = (i[:-1, :-1] * (n + 1) + j[:-1, :-1]).ravel()
+    f = np.concatenate([np.stack([a, a + n + 1, a + n + 2], 1), np.stack([a, a + n + 2, a + 1], 1)]).astype(np.int32)
+    return v, f
+
+
+@pytest.mark.parametrize("n, dup", [(20, 2), (110, 2), (64, 1)])
+def test_tree_bit_exact_with_ties(fwncls, n, dup):
+    """Flat grids (every box centre ties in z) with duplicated faces (identical boxes: only the face
+    id breaks the tie); the larger cases go through the multi-level radix-select path."""
+    v, f = _plane_grid(n)
+    f = np.concatenate([f] * dup)
+    o = O.Oracle(v, f)
+    g = fwncls(v, f)
+    nodes, dip = g.tree()
+    assert np.array_equal(nodes.view(np.uint8), o.nodes().view(np.uint8))
+    assert np.array_equal(dip.view(np.uint32), o.dipoles(0).view(np.uint32))
+
+
+def test_tree_bit_exact_sizes(fwncls):
+    """Leaf counts around the shared-memory threshold and odd sizes."""
+    for level, keep in [(3, 1), (5, 1023), (5, 1024), (5, 1025), (6, 2049), (6, 4095), (4, 1), (4, 2), (4, 3)]:
+        v, f = mg.noisy_icosphere(seed=level, level=level)
+        f = f[:keep]
+        o = O.Oracle(v, f)
+        nodes, dip = fwncls(v, f).tree()
+        assert np.array_equal(nodes.view(np.uint8), o.nodes().view(np.uint8)), (level, keep)
+        assert np.array_equal(dip.view(np.uint32), o.dipoles(0).view(np.uint32)), (level, keep)
+
+
 @pytest.mark.parametrize("precise", [False, True])
 def test_from_grid_matches_oracle(fwncls, torus, precise):
     v, f = torus
