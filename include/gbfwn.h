@@ -179,6 +179,13 @@ GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t di
 GBFWN_API size_t gbfwn_from_vector_memory(int64_t nv, int64_t nt, int64_t npts);
 GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt);
 
+/* Diagnostic (no counterpart in the reference): D[m x n] (+)= A[m x k] * B[n x k]^T on the tcgen05 tensor
+ * cores, bf16 inputs (row-major, k contiguous), FP32 output (row-major); m % 128 == 0, n in {128, 192},
+ * k % 64 == 0; with split_k > 1 the output is accumulated atomically (zero it first).  Device pointers,
+ * enqueued on `stream`.  Used by the tests of the surrogate network's GEMM. */
+GBFWN_API int gbfwn_debug_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32_t m, int32_t n, int32_t k,
+                                    int32_t split_k, void* stream);
+
 /* Test hook: makes the next `count` device allocations of this thread fail with
  * GBFWN_OUT_OF_MEMORY (host-side fault injection; no device fault is involved). */
 GBFWN_API void gbfwn_debug_fail_next_allocs(int count);

@@ -87,6 +87,7 @@ _SIGS = [
     ("gbfwn_from_vector_memory", ctypes.c_size_t, [_i64, _i64, _i64]),
     ("gbfwn_self_intersections_memory", ctypes.c_size_t, [_i64, _i64]),
     ("gbfwn_debug_fail_next_allocs", None, [ctypes.c_int]),
+    ("gbfwn_debug_gemm_bf16", ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
 ]
 EXPORTED = [s[0] for s in _SIGS]
 
