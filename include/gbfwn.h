@@ -179,6 +179,71 @@ GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t di
 GBFWN_API size_t gbfwn_from_vector_memory(int64_t nv, int64_t nt, int64_t npts);
 GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt);
 
+/* ---------------------------------------------------------------------------------------------
+ * Learned band culling (no counterpart in the reference).  A small per-mesh network predicts the
+ * signed distance; bricks of 8x8x8 voxels whose predicted |d|, less a validated error margin and
+ * less the brick's half diagonal, is still >= the band are known to be NaN and are skipped; every
+ * other voxel goes through the exact traversal, so the result is the reference's banded result
+ * (maxDistSq = band^2, nullOutsideMinMax) wherever the margin holds.  Network: Fourier features
+ * of the point (32 frequencies x 3 axes x sin/cos = 192) -> 4 x 128 SiLU -> 1; BF16 weights and
+ * activations on the tcgen05 tensor cores, FP32 accumulation; trained on the GPU on samples whose
+ * targets come from the exact traversal (half uniform in the grid box, half near the surface). */
+typedef struct gbfwn_surrogate_s* gbfwn_surrogate;
+
+typedef struct gbfwn_surrogate_opts {
+    int64_t samples;     /* training samples (2,000,000) */
+    int64_t validation;  /* held-out samples that set the error margin (1,000,000) */
+    int32_t steps;       /* optimizer steps (3000) */
+    int32_t batch;       /* rows per step (16384) */
+    float learningRate;  /* peak Adam step size, cosine decay to 1/100 (2e-3) */
+    float band;          /* distance band the network serves, world units (required, > 0) */
+    float beta;          /* winding-number beta of the exact targets (2) */
+    uint64_t seed;
+} gbfwn_surrogate_opts;
+
+typedef struct gbfwn_surrogate_stats {
+    float trainLoss;           /* last mean squared error (targets clamped to +-6 band) */
+    float validationMaxError;  /* max |prediction - clamped target| on the held-out samples */
+    float margin;              /* margin used for culling: 1.25 x validationMaxError + 0.001 band */
+    float sampleSeconds;       /* sample generation + exact targets */
+    float trainSeconds;        /* optimizer steps */
+    int32_t steps;
+} gbfwn_surrogate_stats;
+
+typedef struct gbfwn_banded_stats {
+    int32_t bricks, keptBricks;  /* 8x8x8-voxel bricks in the grid / sent to the exact traversal */
+    float cullMs, exactMs;       /* time of the culling pass and of the exact pass */
+} gbfwn_banded_stats;
+
+GBFWN_API void gbfwn_surrogate_default_opts(gbfwn_surrogate_opts* opts);
+
+/* Trains a network for the grid (dims, xf): its box is the sampling box. */
+GBFWN_API int gbfwn_surrogate_train(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                    const gbfwn_surrogate_opts* opts, gbfwn_surrogate* out, gbfwn_surrogate_stats* stats);
+GBFWN_API int gbfwn_surrogate_destroy(gbfwn_surrogate s);
+
+/* Parameters (74,369 floats: W1[128x192] b1 W2[128x128] b2 W3 b3 W4 b4 w5[128] b5) and 40 floats of
+ * metadata (input centre xyz, input scale, 32 frequencies, target clamp, margin, band, reserved), so
+ * that a trained network can be stored and re-created without retraining. */
+GBFWN_API int gbfwn_surrogate_get(gbfwn_surrogate s, float* params, float* meta);
+GBFWN_API int gbfwn_surrogate_create(int device, const float* params, const float* meta, gbfwn_surrogate* out);
+
+/* Network prediction at n points (device pointers). */
+GBFWN_API int gbfwn_surrogate_eval_dev(gbfwn_surrogate s, const float* d_pts, int64_t n, float* d_out, void* stream);
+
+/* Loss and parameter gradients (host, 74,369 floats, same layout as the parameters) of the mean
+ * squared error against clamped targets on n <= 16384 points (device pointers); no update.  For
+ * checking the backward kernels against a CPU reference. */
+GBFWN_API int gbfwn_surrogate_gradients_dev(gbfwn_surrogate s, const float* d_pts, const float* d_targets, int32_t n,
+                                            float* grads, float* loss);
+
+/* Banded calcFromGridWithDistances: opts must have a finite maxDistSq (the band squared) and
+ * nullOutsideMinMax set.  s = NULL culls bricks with the exact unsigned distance at brick centres
+ * instead of the network (same result, no learned part).  Writes every voxel of d_out. */
+GBFWN_API int gbfwn_from_grid_with_distances_banded_dev(gbfwn_handle h, gbfwn_surrogate s, const int32_t dims[3],
+                                                        const float xf[12], const gbfwn_dist_opts* opts, float* d_out,
+                                                        gbfwn_banded_stats* stats, void* stream);
+
 /* Diagnostic (no counterpart in the reference): D[m x n] (+)= A[m x k] * B[n x k]^T on the tcgen05 tensor
  * cores, bf16 inputs (row-major, k contiguous), FP32 output (row-major); m % 128 == 0, n in {128, 192},
  * k % 64 == 0; with split_k > 1 the output is accumulated atomically (zero it first).  Device pointers,

@@ -51,6 +51,25 @@ class DistanceToMeshOptions:
                          self.windingNumberBeta)
 
 
+class _SurrogateOpts(ctypes.Structure):
+    _fields_ = [("samples", ctypes.c_int64), ("validation", ctypes.c_int64), ("steps", ctypes.c_int32),
+                ("batch", ctypes.c_int32), ("learningRate", ctypes.c_float), ("band", ctypes.c_float),
+                ("beta", ctypes.c_float), ("seed", ctypes.c_uint64)]
+
+
+class _SurrogateStats(ctypes.Structure):
+    _fields_ = [("trainLoss", ctypes.c_float), ("validationMaxError", ctypes.c_float), ("margin", ctypes.c_float),
+                ("sampleSeconds", ctypes.c_float), ("trainSeconds", ctypes.c_float), ("steps", ctypes.c_int32)]
+
+
+class _BandedStats(ctypes.Structure):
+    _fields_ = [("bricks", ctypes.c_int32), ("keptBricks", ctypes.c_int32), ("cullMs", ctypes.c_float),
+                ("exactMs", ctypes.c_float)]
+
+
+SURROGATE_PARAMS = 74369
+SURROGATE_META = 40
+
 PROGRESS = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_float, ctypes.c_void_p)
 SLAB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
                         ctypes.c_void_p)
@@ -88,6 +107,16 @@ _SIGS = [
     ("gbfwn_self_intersections_memory", ctypes.c_size_t, [_i64, _i64]),
     ("gbfwn_debug_fail_next_allocs", None, [ctypes.c_int]),
     ("gbfwn_debug_gemm_bf16", ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    ("gbfwn_surrogate_default_opts", None, [ctypes.POINTER(_SurrogateOpts)]),
+    ("gbfwn_surrogate_train", ctypes.c_int,
+     [_vp, _vp, _vp, ctypes.POINTER(_SurrogateOpts), ctypes.POINTER(_vp), ctypes.POINTER(_SurrogateStats)]),
+    ("gbfwn_surrogate_destroy", ctypes.c_int, [_vp]),
+    ("gbfwn_surrogate_get", ctypes.c_int, [_vp, _vp, _vp]),
+    ("gbfwn_surrogate_create", ctypes.c_int, [ctypes.c_int, _vp, _vp, ctypes.POINTER(_vp)]),
+    ("gbfwn_surrogate_eval_dev", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp]),
+    ("gbfwn_surrogate_gradients_dev", ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),
+    ("gbfwn_from_grid_with_distances_banded_dev", ctypes.c_int,
+     [_vp, _vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, ctypes.POINTER(_BandedStats), _vp]),
 ]
 EXPORTED = [s[0] for s in _SIGS]
 
@@ -286,6 +315,18 @@ class FastWindingNumber:
         _check(self._L.gbfwn_from_grid_with_distances_dev(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o),
                                                            ctypes.c_void_p(d_out_ptr), _stream(stream)))
 
+    def calcFromGridWithDistancesBanded_dev(self, dims, xf, d_out_ptr: int, options: "DistanceToMeshOptions",
+                                            surrogate: Optional["Surrogate"] = None, stream=None) -> dict:
+        """Banded signed distance (finite maxDistSq, nullOutsideMinMax) with brick culling by the
+        surrogate, or by exact brick-centre distances when surrogate is None."""
+        d = np.asarray(dims, np.int32)
+        o = options._c()
+        st = _BandedStats()
+        _check(self._L.gbfwn_from_grid_with_distances_banded_dev(
+            self._h, surrogate.handle if surrogate is not None else None, _p(d), _p(_xf12(xf)), ctypes.byref(o),
+            ctypes.c_void_p(d_out_ptr), ctypes.byref(st), _stream(stream)))
+        return {"bricks": st.bricks, "keptBricks": st.keptBricks, "cullMs": st.cullMs, "exactMs": st.exactMs}
+
     def calcFromGridWithDistances_noalloc(self, dims, xf, d_out_ptr: int, options=None, stream=None):
         """Allocation-free variant of calcFromGridWithDistances_dev (see gbfwn_from_grid_with_distances_noalloc)."""
         d = np.asarray(dims, np.int32)
@@ -310,3 +351,67 @@ def memory_estimates(nv: int, nt: int, dims=None, npts: int = 0) -> dict:
     return {"mesh": int(L.gbfwn_mesh_memory(nv, nt)), "from_grid": int(L.gbfwn_from_grid_memory(nv, nt, _p(d))),
             "from_vector": int(L.gbfwn_from_vector_memory(nv, nt, npts)),
             "self_intersections": int(L.gbfwn_self_intersections_memory(nv, nt))}
+
+
+class Surrogate:
+    """Per-mesh signed-distance network used to cull bricks outside a distance band
+    (gbfwn_surrogate_* in include/gbfwn.h)."""
+
+    def __init__(self, handle: ctypes.c_void_p, stats: Optional[dict] = None):
+        self._h = handle
+        self._L = lib()
+        self.stats = stats or {}
+
+    @classmethod
+    def train(cls, fwn: "FastWindingNumber", dims, xf, band: float, **kw) -> "Surrogate":
+        L = lib()
+        o = _SurrogateOpts()
+        L.gbfwn_surrogate_default_opts(ctypes.byref(o))
+        o.band = band
+        for k, v in kw.items():
+            setattr(o, k, v)
+        h = ctypes.c_void_p()
+        st = _SurrogateStats()
+        d = np.asarray(dims, np.int32)
+        _check(L.gbfwn_surrogate_train(fwn.handle, _p(d), _p(_xf12(xf)), ctypes.byref(o), ctypes.byref(h), ctypes.byref(st)))
+        return cls(h, {f: getattr(st, f) for f, _ in _SurrogateStats._fields_})
+
+    @classmethod
+    def create(cls, params: np.ndarray, meta: np.ndarray, device: int = 0) -> "Surrogate":
+        p = np.ascontiguousarray(params, np.float32)
+        m = np.ascontiguousarray(meta, np.float32)
+        h = ctypes.c_void_p()
+        _check(lib().gbfwn_surrogate_create(device, _p(p), _p(m), ctypes.byref(h)))
+        return cls(h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def parameters(self):
+        p = np.empty(SURROGATE_PARAMS, np.float32)
+        m = np.empty(SURROGATE_META, np.float32)
+        _check(self._L.gbfwn_surrogate_get(self._h, _p(p), _p(m)))
+        return p, m
+
+    def eval_dev(self, d_pts_ptr: int, n: int, d_out_ptr: int, stream=None):
+        _check(self._L.gbfwn_surrogate_eval_dev(self._h, ctypes.c_void_p(d_pts_ptr), n, ctypes.c_void_p(d_out_ptr),
+                                                _stream(stream)))
+
+    def gradients_dev(self, d_pts_ptr: int, d_targets_ptr: int, n: int):
+        g = np.empty(SURROGATE_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        _check(self._L.gbfwn_surrogate_gradients_dev(self._h, ctypes.c_void_p(d_pts_ptr), ctypes.c_void_p(d_targets_ptr), n,
+                                                     _p(g), _p(loss)))
+        return g, float(loss[0])
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gbfwn_surrogate_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

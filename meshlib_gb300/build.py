@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden", "--expt-relaxed-constexpr"]
 # build.cu must round every float operation separately (bit-identical boxes and dipoles)
 PER_FILE = {"build.cu": ["-fmad=false"], "treebuild.cu": ["-fmad=false"]}
-SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "mlp_gemm.cu", "surrogate.cu"]
+SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "mlp_gemm.cu", "mlp_net.cu", "surrogate.cu"]
 
 
 def nvcc() -> str:
@@ -58,7 +58,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-Xlinker", "--no-undefined"]
         run(cmd)
     return LIB
 

@@ -14,13 +14,14 @@
 
 #include "../../include/gbfwn.h"
 #include "common.cuh"
+#include "handle.cuh"
 
 using namespace gbfwn;
 
 namespace gbfwn {
 }
 
-namespace {
+namespace gbfwn {
 
 thread_local std::string g_lastError;
 thread_local int g_failAllocs = 0;
@@ -44,84 +45,11 @@ cudaError_t devMalloc(void** p, size_t bytes) {
     return cudaMalloc(p, bytes ? bytes : 16);
 }
 
-struct ListAllocator : Allocator {
-    std::vector<void*> ptrs;
-    cudaError_t alloc(void** p, size_t bytes) override {
-        cudaError_t e = devMalloc(p, bytes);
-        if (e == cudaSuccess) ptrs.push_back(*p);
-        return e;
-    }
-    void freeAll() {
-        for (void* p : ptrs) cudaFree(p);
-        ptrs.clear();
-    }
-};
+}  // namespace gbfwn
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
+namespace {
 bool progress(gbfwn_progress_cb cb, void* user, float p) { return !cb || cb(p, user) != 0; }
-
 }  // namespace
-
-struct gbfwn_mesh_s {
-    int device = 0;
-    cudaStream_t stream = nullptr, copyStream = nullptr;
-    ListAllocator treeMem;
-    DeviceTree tree;
-    float* dVerts = nullptr;
-    int32_t* dTris = nullptr;
-    int64_t nv = 0, nt = 0;
-    unsigned* scratch = nullptr;  // [0] ticket counter, [1] status bits
-    int precise = 1;
-    // device staging reused across host-API calls
-    void* outBuf = nullptr;
-    size_t outCap = 0;
-    void* inBuf = nullptr;
-    size_t inCap = 0;
-    std::vector<cudaEvent_t> events;
-    std::mutex mu;  // calls on one handle are serialised (the reference is not re-entrant per object)
-
-    cudaError_t ensure(void** buf, size_t* cap, size_t bytes) {
-        if (*cap >= bytes) return cudaSuccess;
-        if (*buf) cudaFree(*buf);
-        *buf = nullptr;
-        *cap = 0;
-        cudaError_t e = devMalloc(buf, bytes);
-        if (e == cudaSuccess) *cap = bytes;
-        return e;
-    }
-    cudaError_t ensureEvents(size_t n) {
-        while (events.size() < n) {
-            cudaEvent_t ev;
-            cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-            if (e) return e;
-            events.push_back(ev);
-        }
-        return cudaSuccess;
-    }
-    int checkStatus() {
-        unsigned st[2] = {0, 0};
-        cudaError_t e = cudaMemcpyAsync(st, scratch, sizeof(st), cudaMemcpyDeviceToHost, stream);
-        if (!e) e = cudaStreamSynchronize(stream);
-        if (e) return cudaFail(e, "status read");
-        if (st[1] & kStatusStackOverflow)
-            return fail(GBFWN_TRAVERSAL_OVERFLOW, "traversal stack overflow (tree deeper than 32 levels)");
-        if (st[1] & kStatusTimeout) return fail(GBFWN_TIMEOUT, "device-side wait timed out");
-        return GBFWN_OK;
-    }
-    cudaError_t resetStatus(cudaStream_t s) { return cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned), s); }
-};
 
 namespace {
 

@@ -74,6 +74,10 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
                           unsigned* scratch, cudaStream_t s);
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                           float* out, unsigned* scratch, cudaStream_t s);
+// Signed distance on a list of 8x8x8-voxel bricks of the grid (brick b = bx + by * ceil(nx/8) +
+// bz * ceil(nx/8) * ceil(ny/8)); voxels outside the bricks are not written.
+cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
+                                float* out, const int32_t* bricks, int32_t nBricks, unsigned* scratch, cudaStream_t s);
 cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,
                             float* out, unsigned* scratch, cudaStream_t s);
 cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, const DistOpts& o, int precise, float* out,
@@ -105,6 +109,10 @@ cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTri
                             Allocator& P, Allocator& T, cudaStream_t s, std::string& err);
 
 int numSMs();
+
+// Exclusive prefix sum of n int32 values (treebuild.cu); `sums` holds ceil(n / 1024) + 1 words of
+// scratch, `total` receives the sum of all values.
+cudaError_t exclusiveScanI32(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, int32_t* total, cudaStream_t s);
 
 // Number of warp tiles a grid of nx x ny x nz voxels is cut into; the work-queue ticket counter is
 // 32 bits, so a single launch covers at most 2^32 - 1 tiles.

@@ -30,6 +30,10 @@ struct GemmEpilogue {
 
 // D = A[M x K] * B[N x K]^T with A, B K-major bf16 (lda, ldb multiples of 8 elements, 16-byte
 // aligned rows), M % 128 == 0, N in {128, 192}, K % 64 == 0.
+// Sets the kernels' shared-memory opt-in on the current device (done automatically on first use;
+// call it before capturing GEMMs into a CUDA graph).
+cudaError_t prepareGemm();
+
 cudaError_t launchGemmBf16(const __nv_bfloat16* A, int64_t lda, const __nv_bfloat16* B, int64_t ldb, int M, int N, int K,
                            int splitK, const GemmEpilogue& ep, cudaStream_t s);
 

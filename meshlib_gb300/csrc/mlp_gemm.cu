@@ -15,6 +15,8 @@
 
 namespace gbfwn {
 
+cudaError_t prepareGemm();
+
 namespace {
 
 constexpr int kBM = 128, kBK = 64;
@@ -124,18 +126,37 @@ __global__ void __launch_bounds__(128) gemmKernel(const __nv_bfloat16* __restric
     if (warp == 0) umma::tmemFree(tmem, kTmemCols);
 }
 
+template <int N> constexpr size_t gemmSmem() { return 2 * (kBM * 128 + N * 128) + 1024; }
+
+// the dynamic shared-memory opt-in is set once per device, outside any stream capture
+bool g_gemmReady[64] = {};
+
 template <int N>
 cudaError_t launchGemmN(const __nv_bfloat16* A, int64_t lda, const __nv_bfloat16* B, int64_t ldb, int M, int K, int splitK,
                         const GemmEpilogue& ep, cudaStream_t s) {
-    const size_t smem = 2 * (kBM * 128 + N * 128) + 1024;
-    cudaError_t e = cudaFuncSetAttribute(gemmKernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e) return e;
+    constexpr size_t smem = gemmSmem<N>();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !g_gemmReady[dev]) {
+        cudaError_t e = prepareGemm();
+        if (e) return e;
+    }
     dim3 grid(unsigned(M / kBM), unsigned(splitK));
     gemmKernel<N><<<grid, 128, smem, s>>>(A, lda, B, ldb, K, ep);
     return cudaGetLastError();
 }
 
 }  // namespace
+
+cudaError_t prepareGemm() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if ((e = cudaFuncSetAttribute(gemmKernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(gemmSmem<128>())))) return e;
+    if ((e = cudaFuncSetAttribute(gemmKernel<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(gemmSmem<192>())))) return e;
+    if (dev >= 0 && dev < 64) g_gemmReady[dev] = true;
+    return cudaSuccess;
+}
 
 cudaError_t launchGemmBf16(const __nv_bfloat16* A, int64_t lda, const __nv_bfloat16* B, int64_t ldb, int M, int N, int K,
                            int splitK, const GemmEpilogue& ep, cudaStream_t s) {

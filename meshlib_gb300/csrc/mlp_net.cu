@@ -1,0 +1,650 @@
+// Surrogate signed-distance network: Fourier features -> 4 x (128, SiLU) -> 1, BF16 weights and
+// activations on the tensor cores with FP32 accumulation (mlp_gemm.cu), trained on the GPU on
+// samples whose signed distances come from the exact traversal, then used to cull 8x8x8-voxel
+// bricks that lie outside a requested distance band.
+//
+// Network (74,369 parameters): u = (p - centre) * scale (the grid box mapped to [-1, 1]^3);
+// features f[64 a + 2 k] = sin(w_k u_a), f[64 a + 2 k + 1] = cos(w_k u_a), w_k = pi * 2^(k / 5),
+// k < 32, a < 3 (192 features); h1 = silu(W1 f + b1), h_l = silu(W_l h_{l-1} + b_l) for l = 2..4;
+// y = w5 . h4 + b5.  Target: the signed distance clamped to +-clampD; loss = mean squared error.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "common.cuh"
+#include "mlp.cuh"
+#include "surrogate.cuh"
+
+namespace gbfwn {
+
+namespace {
+
+constexpr int kF = 192, kH = 128, kFreq = 32;
+constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kH * kF, kOffW2 = kOffB1 + kH, kOffB2 = kOffW2 + kH * kH, kOffW3 = kOffB2 + kH,
+              kOffB3 = kOffW3 + kH * kH, kOffW4 = kOffB3 + kH, kOffB4 = kOffW4 + kH * kH, kOffW5 = kOffB4 + kH,
+              kOffB5 = kOffW5 + kH;
+static_assert(kOffB5 + 1 == kSurrogateParams, "parameter layout");
+
+inline unsigned nblk(int64_t n, int t) { return unsigned((n + t - 1) / t); }
+
+// ---------------------------------------------------------------- random numbers (hash based)
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float urand(uint32_t seed, uint32_t i, uint32_t k) {
+    return (hash32(seed * 0x9e3779b9u ^ hash32(i * 4u + k)) >> 8) * (1.f / 16777216.f);
+}
+
+// ---------------------------------------------------------------- features
+__global__ void featuresKernel(const float* __restrict__ pts, const int32_t* __restrict__ idx, const int32_t* __restrict__ offPtr,
+                               int64_t idxMod, int n, int nPad, NetMeta meta, __nv_bfloat16* __restrict__ F,
+                               __nv_bfloat16* __restrict__ FT) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nPad) return;
+    float u[3] = {0.f, 0.f, 0.f};
+    const bool live = i < n;
+    if (live) {
+        int64_t j = i;
+        if (idx) j = idx[(int64_t(offPtr ? *offPtr : 0) + i) % idxMod];
+        for (int a = 0; a < 3; ++a) u[a] = (pts[3 * j + a] - meta.center[a]) * meta.scale;
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < kFreq; ++k) {
+            float sv = 0.f, cv = 0.f;
+            if (live) sincosf(meta.freq[k] * u[a], &sv, &cv);
+            const int c = 64 * a + 2 * k;
+            const __nv_bfloat16 bs = __float2bfloat16(sv), bc = __float2bfloat16(cv);
+            F[int64_t(i) * kF + c] = bs;
+            F[int64_t(i) * kF + c + 1] = bc;
+            if (FT) {
+                FT[int64_t(c) * nPad + i] = bs;
+                FT[int64_t(c + 1) * nPad + i] = bc;
+            }
+        }
+}
+
+// ---------------------------------------------------------------- output layer, loss, dZ4
+// One warp per row (4 hidden units per lane).  Training mode (target != null): loss, gradients of
+// w5, b5, b4 and dZ4 = g * w5 * silu'(z4) in bf16 (+ transposed).  Inference mode: y only.
+__global__ void outputKernel(const __nv_bfloat16* __restrict__ H4, const float* __restrict__ Z4, int n, int nPad,
+                             const float* __restrict__ params, const float* __restrict__ target,
+                             const int32_t* __restrict__ idx, const int32_t* __restrict__ offPtr, int64_t idxMod,
+                             float clampD, float* __restrict__ y, float* __restrict__ grads, float* __restrict__ loss,
+                             __nv_bfloat16* __restrict__ dZ4, __nv_bfloat16* __restrict__ dZ4T) {
+    __shared__ float sW5[kH], sB4[kH];
+    __shared__ float sLoss, sB5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j = threadIdx.x; j < kH; j += blockDim.x) {
+        sW5[j] = 0.f;
+        sB4[j] = 0.f;
+    }
+    if (threadIdx.x == 0) {
+        sLoss = 0.f;
+        sB5 = 0.f;
+    }
+    __syncthreads();
+    const float* w5 = params + kOffW5;
+    const float b5 = params[kOffB5];
+    float aw5[4] = {0, 0, 0, 0}, ab4[4] = {0, 0, 0, 0}, aloss = 0.f, ab5 = 0.f;
+    const float invN = 1.f / float(n);
+    for (int row = blockIdx.x * (blockDim.x >> 5) + warp; row < nPad; row += gridDim.x * (blockDim.x >> 5)) {
+        float h[4], acc = 0.f;
+        for (int q = 0; q < 4; ++q) {
+            const int j = lane + 32 * q;
+            h[q] = __bfloat162float(H4[int64_t(row) * kH + j]);
+            acc += h[q] * w5[j];
+        }
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        const float yv = acc + b5;
+        if (!target) {
+            if (lane == 0 && row < n) y[row] = yv;
+            continue;
+        }
+        float g = 0.f;
+        if (row < n) {
+            const int64_t j = idx ? idx[(int64_t(offPtr ? *offPtr : 0) + row) % idxMod] : row;
+            const float t = fminf(fmaxf(target[j], -clampD), clampD);
+            const float r = yv - t;
+            aloss += (lane == 0) ? r * r * invN : 0.f;
+            g = 2.f * r * invN;
+            ab5 += (lane == 0) ? g : 0.f;
+        }
+        for (int q = 0; q < 4; ++q) {
+            const int j = lane + 32 * q;
+            aw5[q] += g * h[q];
+            const float z = Z4[int64_t(row) * kH + j];
+            const float s = 1.f / (1.f + __expf(-z));
+            const float dz = g * w5[j] * s * (1.f + z * (1.f - s));
+            ab4[q] += dz;
+            const __nv_bfloat16 db = __float2bfloat16(dz);
+            dZ4[int64_t(row) * kH + j] = db;
+            dZ4T[int64_t(j) * nPad + row] = db;
+        }
+    }
+    if (!target) return;
+    for (int q = 0; q < 4; ++q) {
+        atomicAdd(&sW5[lane + 32 * q], aw5[q]);
+        atomicAdd(&sB4[lane + 32 * q], ab4[q]);
+    }
+    if (lane == 0) {
+        atomicAdd(&sLoss, aloss);
+        atomicAdd(&sB5, ab5);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < kH; j += blockDim.x) {
+        atomicAdd(&grads[kOffW5 + j], sW5[j]);
+        atomicAdd(&grads[kOffB4 + j], sB4[j]);
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&grads[kOffB5], sB5);
+        atomicAdd(loss, sLoss);
+    }
+}
+
+// ---------------------------------------------------------------- Adam + weight packing
+// Cosine learning-rate schedule from lr0 to lr0/100 over `total` steps; the step counter lives on
+// the device so that a captured step can be replayed.
+__global__ void adamKernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                           int n, const int32_t* __restrict__ stepPtr, int total, float lr0, float b1, float b2, float eps) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int step = *stepPtr + 1;
+    const float frac = fminf(1.f, float(step) / float(max(total, 1)));
+    const float lr = lr0 * (0.01f + 0.99f * 0.5f * (1.f + cospif(frac)));
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / (1.f - powf(b1, float(step)));
+    const float vh = vi / (1.f - powf(b2, float(step)));
+    p[i] -= lr * mh / (sqrtf(vh) + eps);
+}
+
+__global__ void stepCounterKernel(int32_t* step, int32_t* off, int batch, int batchesPerEpoch) {
+    const int s = *step + 1;
+    *step = s;
+    *off = (s % batchesPerEpoch) * batch;
+}
+
+// bf16 copies of W1..W4 (row-major [out x in]) and transposes of W2..W4 ([in x out])
+__global__ void packKernel(const float* __restrict__ params, __nv_bfloat16* __restrict__ W1, __nv_bfloat16* __restrict__ W234,
+                           __nv_bfloat16* __restrict__ WT234) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kH * kF) W1[i] = __float2bfloat16(params[kOffW1 + i]);
+    if (i < 3 * kH * kH) {
+        const int l = i / (kH * kH), r = (i / kH) % kH, c = i % kH;
+        const int off = (l == 0 ? kOffW2 : l == 1 ? kOffW3 : kOffW4);
+        const float w = params[off + r * kH + c];
+        W234[i] = __float2bfloat16(w);
+        WT234[l * kH * kH + c * kH + r] = __float2bfloat16(w);
+    }
+}
+
+// ---------------------------------------------------------------- sampling
+// Uniform samples: a jittered lattice over the box, consecutive samples neighbours (4x4x2 blocks of
+// lattice cells) so that the exact traversal's warp packets stay coherent.
+__global__ void uniformSamplesKernel(float* __restrict__ pts, int n, int m, float3 lo, float3 cell, uint32_t seed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int blk = i >> 5, ln = i & 31;
+    const int bx = (m + 3) / 4, by = (m + 3) / 4;
+    const int cx = (blk % bx) * 4 + (ln & 3), cy = ((blk / bx) % by) * 4 + ((ln >> 2) & 3), cz = (blk / (bx * by)) * 2 + (ln >> 4);
+    pts[3 * int64_t(i) + 0] = lo.x + (float(cx % m) + urand(seed, i, 0)) * cell.x;
+    pts[3 * int64_t(i) + 1] = lo.y + (float(cy % m) + urand(seed, i, 1)) * cell.y;
+    pts[3 * int64_t(i) + 2] = lo.z + (float(cz % m) + urand(seed, i, 2)) * cell.z;
+}
+
+// Near-surface samples: leaf slots in order (spatially coherent), a uniform point of the triangle,
+// offset along its normal by a normal deviate of standard deviation sigma.
+__global__ void surfaceSamplesKernel(float* __restrict__ pts, int n, const float4* __restrict__ tri, int nLeaves, float sigma,
+                                     float3 lo, float3 hi, uint32_t seed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || nLeaves == 0) return;
+    const int slot = int((int64_t(i) * nLeaves) / n);
+    const float4 A = tri[3 * int64_t(slot)], B = tri[3 * int64_t(slot) + 1], C = tri[3 * int64_t(slot) + 2];
+    float r1 = urand(seed, i, 0), r2 = urand(seed, i, 1);
+    if (r1 + r2 > 1.f) {
+        r1 = 1.f - r1;
+        r2 = 1.f - r2;
+    }
+    const float3 ab = make_float3(B.x - A.x, B.y - A.y, B.z - A.z), ac = make_float3(C.x - A.x, C.y - A.y, C.z - A.z);
+    float3 nrm = make_float3(ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x);
+    const float nl = sqrtf(nrm.x * nrm.x + nrm.y * nrm.y + nrm.z * nrm.z);
+    if (nl > 0.f) {
+        nrm.x /= nl;
+        nrm.y /= nl;
+        nrm.z /= nl;
+    }
+    // Box-Muller
+    const float u1 = fmaxf(urand(seed, i, 2), 1e-7f), u2 = urand(seed, i, 3);
+    const float off = sigma * sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+    // kept inside the box the network serves (it is never evaluated outside it)
+    pts[3 * int64_t(i) + 0] = fminf(fmaxf(A.x + r1 * ab.x + r2 * ac.x + off * nrm.x, lo.x), hi.x);
+    pts[3 * int64_t(i) + 1] = fminf(fmaxf(A.y + r1 * ab.y + r2 * ac.y + off * nrm.y, lo.y), hi.y);
+    pts[3 * int64_t(i) + 2] = fminf(fmaxf(A.z + r1 * ab.z + r2 * ac.z + off * nrm.z, lo.z), hi.z);
+}
+
+__global__ void absErrMaxKernel(const float* __restrict__ pred, const float* __restrict__ target, int n, float clampD,
+                                unsigned* __restrict__ maxBits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float e = 0.f;
+    if (i < n) e = fabsf(pred[i] - fminf(fmaxf(target[i], -clampD), clampD));
+    for (int o = 16; o; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxBits, __float_as_uint(e));  // e >= 0: bits are ordered
+}
+
+// ---------------------------------------------------------------- bricks
+__global__ void brickCentersKernel(float* __restrict__ pts, int3 bdims, int3 dims, Xf xf) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bdims.x * bdims.y * bdims.z) return;
+    const int bx = b % bdims.x, by = (b / bdims.x) % bdims.y, bz = b / (bdims.x * bdims.y);
+    // centre of the voxels the brick actually holds (edge bricks are partial)
+    const float cx = 0.5f * float(8 * bx + min(8 * bx + 7, dims.x - 1));
+    const float cy = 0.5f * float(8 * by + min(8 * by + 7, dims.y - 1));
+    const float cz = 0.5f * float(8 * bz + min(8 * bz + 7, dims.z - 1));
+    pts[3 * b + 0] = xf.a[0] * cx + xf.a[1] * cy + xf.a[2] * cz + xf.b[0];
+    pts[3 * b + 1] = xf.a[3] * cx + xf.a[4] * cy + xf.a[5] * cz + xf.b[1];
+    pts[3 * b + 2] = xf.a[6] * cx + xf.a[7] * cy + xf.a[8] * cz + xf.b[2];
+}
+
+// keep[b] = 1 unless every voxel of brick b is certainly at distance >= band:
+// |d(v)| >= |d(c)| - |v - c| >= lowerBound(c) - radius.
+__global__ void brickKeepKernel(const float* __restrict__ lowerBound, int nb, float band, float radius, int32_t* __restrict__ keep) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const float lb = lowerBound[b];
+    keep[b] = (lb - radius >= band) ? 0 : 1;
+}
+
+__global__ void compactKernel(const int32_t* __restrict__ keep, const int32_t* __restrict__ pos, int nb, int32_t* __restrict__ list) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nb && keep[b]) list[pos[b]] = b;
+}
+
+__global__ void fillNanKernel(float* __restrict__ p, int64_t n) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < n) p[i] = __int_as_float(0x7fc00000);
+}
+
+// lower bound of |d| at each brick centre from the surrogate: |pred| - margin
+__global__ void surrogateLowerBound(const float* __restrict__ pred, int n, float margin, float* __restrict__ lb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) lb[i] = fabsf(pred[i]) - margin;
+}
+
+// lower bound from the exact unsigned distance computed with maxDistSq = (band + radius)^2: NaN
+// (not finite) means the distance is at least band + radius
+__global__ void exactLowerBound(const float* __restrict__ d, int n, float cap, float* __restrict__ lb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) lb[i] = isfinite(d[i]) ? fabsf(d[i]) : cap;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+struct SurrogateNet::Work {
+    int batch = 0;
+    __nv_bfloat16 *F = nullptr, *FT = nullptr;
+    float* Z[4] = {};
+    __nv_bfloat16 *H[4] = {}, *HT[4] = {}, *dZ[4] = {}, *dZT[4] = {};
+};
+
+SurrogateNet::~SurrogateNet() { release(); }
+
+int SurrogateNet::workRows() const { return work_ ? work_->batch : 0; }
+
+void SurrogateNet::release() {
+    for (void* p : mem_) cudaFree(p);
+    mem_.clear();
+    delete work_;
+    work_ = nullptr;
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+}
+
+cudaError_t SurrogateNet::alloc(void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (!e) mem_.push_back(*p);
+    return e;
+}
+
+cudaError_t SurrogateNet::init(uint64_t seed) {
+    cudaError_t e;
+    if ((e = prepareGemm())) return e;
+    if ((e = alloc((void**)&params_, sizeof(float) * kSurrogateParams))) return e;
+    if ((e = alloc((void**)&grads_, sizeof(float) * kSurrogateParams))) return e;
+    if ((e = alloc((void**)&m_, sizeof(float) * kSurrogateParams))) return e;
+    if ((e = alloc((void**)&v_, sizeof(float) * kSurrogateParams))) return e;
+    if ((e = alloc((void**)&W1_, sizeof(__nv_bfloat16) * kH * kF))) return e;
+    if ((e = alloc((void**)&W234_, sizeof(__nv_bfloat16) * 3 * kH * kH))) return e;
+    if ((e = alloc((void**)&WT234_, sizeof(__nv_bfloat16) * 3 * kH * kH))) return e;
+    if ((e = alloc((void**)&counters_, sizeof(int32_t) * 4))) return e;
+    if ((e = alloc((void**)&scalars_, sizeof(float) * 8))) return e;
+    for (int k = 0; k < kFreq; ++k) meta.freq[k] = float(M_PI * std::pow(2.0, k / 5.0));
+    // He-uniform hidden layers, small output layer, zero biases (deterministic from the seed)
+    std::vector<float> h(kSurrogateParams, 0.f);
+    std::mt19937_64 rng(seed);
+    auto fill = [&](int off, int fanOut, int fanIn, float gain) {
+        const float lim = gain * std::sqrt(3.f / float(fanIn));
+        std::uniform_real_distribution<float> U(-lim, lim);
+        for (int i = 0; i < fanOut * fanIn; ++i) h[off + i] = U(rng);
+    };
+    fill(kOffW1, kH, kF, 1.0f);
+    fill(kOffW2, kH, kH, 1.4142f);
+    fill(kOffW3, kH, kH, 1.4142f);
+    fill(kOffW4, kH, kH, 1.4142f);
+    fill(kOffW5, 1, kH, 0.1f);
+    return setParams(h.data(), nullptr);
+}
+
+cudaError_t SurrogateNet::setParams(const float* hostParams, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyAsync(params_, hostParams, sizeof(float) * kSurrogateParams, cudaMemcpyHostToDevice, s);
+    if (!e) e = cudaMemsetAsync(m_, 0, sizeof(float) * kSurrogateParams, s);
+    if (!e) e = cudaMemsetAsync(v_, 0, sizeof(float) * kSurrogateParams, s);
+    if (!e) e = cudaMemsetAsync(counters_, 0, sizeof(int32_t) * 4, s);
+    if (e) return e;
+    return pack(s);
+}
+
+cudaError_t SurrogateNet::getParams(float* hostParams, cudaStream_t s) const {
+    cudaError_t e = cudaMemcpyAsync(hostParams, params_, sizeof(float) * kSurrogateParams, cudaMemcpyDeviceToHost, s);
+    return e ? e : cudaStreamSynchronize(s);
+}
+
+cudaError_t SurrogateNet::pack(cudaStream_t s) {
+    packKernel<<<nblk(3 * kH * kH, 256), 256, 0, s>>>(params_, W1_, W234_, WT234_);
+    return cudaGetLastError();
+}
+
+cudaError_t SurrogateNet::ensureWork(int batchPad) {
+    if (work_) return cudaSuccess;  // sized once per network; inference walks larger inputs in chunks
+    work_ = new Work;
+    work_->batch = batchPad;
+    cudaError_t e;
+    const size_t B = size_t(batchPad);
+    if ((e = alloc((void**)&work_->F, sizeof(__nv_bfloat16) * B * kF))) return e;
+    if ((e = alloc((void**)&work_->FT, sizeof(__nv_bfloat16) * B * kF))) return e;
+    for (int l = 0; l < 4; ++l) {
+        if ((e = alloc((void**)&work_->Z[l], sizeof(float) * B * kH))) return e;
+        if ((e = alloc((void**)&work_->H[l], sizeof(__nv_bfloat16) * B * kH))) return e;
+        if ((e = alloc((void**)&work_->HT[l], sizeof(__nv_bfloat16) * B * kH))) return e;
+        if ((e = alloc((void**)&work_->dZ[l], sizeof(__nv_bfloat16) * B * kH))) return e;
+        if ((e = alloc((void**)&work_->dZT[l], sizeof(__nv_bfloat16) * B * kH))) return e;
+    }
+    return cudaSuccess;
+}
+
+// One training (or gradient-only) step over `n` rows taken from pts/targets through idx (or the
+// first n rows when idx is null), padded to nPad rows.  Leaves the loss in scalars_[0].
+cudaError_t SurrogateNet::step(const float* pts, const float* targets, const int32_t* idx, int64_t idxMod, int n, int nPad,
+                               bool update, int totalSteps, float lr, cudaStream_t s) {
+    Work& w = *work_;
+    cudaError_t e;
+    const int32_t* off = idx ? counters_ + 1 : nullptr;
+    featuresKernel<<<nblk(nPad, 128), 128, 0, s>>>(pts, idx, off, idxMod, n, nPad, meta, w.F, w.FT);
+    const __nv_bfloat16* Wl[4] = {W1_, W234_, W234_ + kH * kH, W234_ + 2 * kH * kH};
+    const int offB[4] = {kOffB1, kOffB2, kOffB3, kOffB4};
+    for (int l = 0; l < 4; ++l) {
+        GemmEpilogue ep;
+        ep.mode = GemmEpilogue::kForward;
+        ep.bias = params_ + offB[l];
+        ep.Z = w.Z[l];
+        ep.ldz = kH;
+        ep.H = w.H[l];
+        ep.ldh = kH;
+        ep.HT = w.HT[l];
+        ep.ldht = nPad;
+        ep.status = reinterpret_cast<unsigned*>(counters_ + 3);
+        const __nv_bfloat16* A = l == 0 ? w.F : w.H[l - 1];
+        if ((e = launchGemmBf16(A, l == 0 ? kF : kH, Wl[l], l == 0 ? kF : kH, nPad, kH, l == 0 ? kF : kH, 1, ep, s))) return e;
+    }
+    if ((e = cudaMemsetAsync(grads_, 0, sizeof(float) * kSurrogateParams, s))) return e;
+    if ((e = cudaMemsetAsync(scalars_, 0, sizeof(float), s))) return e;
+    outputKernel<<<std::min<unsigned>(nblk(nPad, 8), 1024u), 256, 0, s>>>(w.H[3], w.Z[3], n, nPad, params_, targets, idx, off,
+                                                                          idxMod, meta.clampD, nullptr, grads_, scalars_,
+                                                                          w.dZ[3], w.dZT[3]);
+    const int offW[4] = {kOffW1, kOffW2, kOffW3, kOffW4};
+    const int splitK = std::max(1, std::min(16, nPad / 1024));
+    for (int l = 3; l >= 0; --l) {
+        // weight gradient: dW_l = dZ_l^T * act_{l-1}, K = rows
+        GemmEpilogue gw;
+        gw.mode = GemmEpilogue::kStoreF32;
+        gw.D = grads_ + offW[l];
+        gw.ldd = l == 0 ? kF : kH;
+        gw.status = reinterpret_cast<unsigned*>(counters_ + 3);
+        const __nv_bfloat16* Bop = l == 0 ? w.FT : w.HT[l - 1];
+        if ((e = launchGemmBf16(w.dZT[l], nPad, Bop, nPad, kH, l == 0 ? kF : kH, nPad, splitK, gw, s))) return e;
+        if (l == 0) break;
+        // activation gradient of layer l-1: dZ_{l-1} = (dZ_l * W_l) .* silu'(Z_{l-1})
+        GemmEpilogue gb;
+        gb.mode = GemmEpilogue::kBackward;
+        gb.Z = w.Z[l - 1];
+        gb.ldz = kH;
+        gb.H = w.dZ[l - 1];
+        gb.ldh = kH;
+        gb.HT = w.dZT[l - 1];
+        gb.ldht = nPad;
+        gb.dbias = grads_ + offB[l - 1];
+        gb.status = reinterpret_cast<unsigned*>(counters_ + 3);
+        const __nv_bfloat16* WT = WT234_ + (l - 1) * kH * kH;
+        if ((e = launchGemmBf16(w.dZ[l], kH, WT, kH, nPad, kH, kH, 1, gb, s))) return e;
+    }
+    if (!update) return cudaGetLastError();
+    adamKernel<<<nblk(kSurrogateParams, 256), 256, 0, s>>>(params_, grads_, m_, v_, kSurrogateParams, counters_, totalSteps, lr,
+                                                          0.9f, 0.99f, 1e-8f);
+    if ((e = pack(s))) return e;
+    stepCounterKernel<<<1, 1, 0, s>>>(counters_, counters_ + 1, nPad, int(idxMod / nPad));
+    return cudaGetLastError();
+}
+
+cudaError_t SurrogateNet::infer(const float* pts, int64_t n, float* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    Work& w = *work_;
+    const int chunk = w.batch;
+    cudaError_t e;
+    for (int64_t base = 0; base < n; base += chunk) {
+        const int m = int(std::min<int64_t>(chunk, n - base));
+        const int mPad = (m + 127) / 128 * 128;
+        featuresKernel<<<nblk(mPad, 128), 128, 0, s>>>(pts + 3 * base, nullptr, nullptr, 1, m, mPad, meta, w.F, nullptr);
+        const __nv_bfloat16* Wl[4] = {W1_, W234_, W234_ + kH * kH, W234_ + 2 * kH * kH};
+        const int offB[4] = {kOffB1, kOffB2, kOffB3, kOffB4};
+        for (int l = 0; l < 4; ++l) {
+            GemmEpilogue ep;
+            ep.mode = GemmEpilogue::kForward;
+            ep.bias = params_ + offB[l];
+            ep.H = w.H[l];
+            ep.ldh = kH;
+            ep.status = reinterpret_cast<unsigned*>(counters_ + 3);
+            const __nv_bfloat16* A = l == 0 ? w.F : w.H[l - 1];
+            if ((e = launchGemmBf16(A, l == 0 ? kF : kH, Wl[l], l == 0 ? kF : kH, mPad, kH, l == 0 ? kF : kH, 1, ep, s))) return e;
+        }
+        outputKernel<<<std::min<unsigned>(nblk(mPad, 8), 1024u), 256, 0, s>>>(w.H[3], nullptr, m, mPad, params_, nullptr, nullptr,
+                                                                              nullptr, 1, 0.f, out + base, nullptr, nullptr,
+                                                                              nullptr, nullptr);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t SurrogateNet::train(const QueryTree& t, unsigned* scratch, const TrainOptions& o, TrainStats& st, cudaStream_t s) {
+    cudaError_t e;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int batch = (o.batch + 127) / 128 * 128;
+    int64_t nTrain = std::max<int64_t>(o.samples / batch, 1) * batch;
+    if ((e = ensureWork(batch))) return e;
+    float *pts = nullptr, *dist = nullptr;
+    int32_t* idx = nullptr;
+    const int64_t nAll = nTrain + o.validation;
+    if ((e = alloc((void**)&pts, sizeof(float) * 3 * size_t(nAll)))) return e;
+    if ((e = alloc((void**)&dist, sizeof(float) * size_t(nAll)))) return e;
+    if ((e = alloc((void**)&idx, sizeof(int32_t) * size_t(nTrain)))) return e;
+    // samples: half uniform in the box, half near the surface; the validation set likewise
+    auto gen = [&](float* p, int64_t n, uint32_t seed) -> cudaError_t {
+        const int64_t nu = n / 2, ns = n - nu;
+        const int m = std::max(1, int(std::ceil(std::cbrt(double(nu)))));
+        const float3 cell = make_float3((o.hi[0] - o.lo[0]) / m, (o.hi[1] - o.lo[1]) / m, (o.hi[2] - o.lo[2]) / m);
+        if (nu) uniformSamplesKernel<<<nblk(nu, 256), 256, 0, s>>>(p, int(nu), m, make_float3(o.lo[0], o.lo[1], o.lo[2]), cell, seed);
+        if (ns)
+            surfaceSamplesKernel<<<nblk(ns, 256), 256, 0, s>>>(p + 3 * nu, int(ns), t.tri, t.nLeaves, o.sigma,
+                                                               make_float3(o.lo[0], o.lo[1], o.lo[2]),
+                                                               make_float3(o.hi[0], o.hi[1], o.hi[2]), seed ^ 0x5bd1e995u);
+        return cudaGetLastError();
+    };
+    if ((e = gen(pts, nTrain, uint32_t(o.seed)))) return e;
+    if (o.validation && (e = gen(pts + 3 * nTrain, o.validation, uint32_t(o.seed * 31 + 7)))) return e;
+    const DistOpts exact{0.f, 3.402823466e+38f, 0, 0.5f, o.beta};
+    if ((e = launchVectorSdf(t, pts, nAll, exact, 1, dist, scratch, s))) return e;
+    // batches are slices of a random permutation of the training samples
+    {
+        std::vector<int32_t> perm(static_cast<size_t>(nTrain));
+        for (int64_t i = 0; i < nTrain; ++i) perm[i] = int32_t(i);
+        std::mt19937_64 rng(o.seed * 2654435761ull + 1);
+        std::shuffle(perm.begin(), perm.end(), rng);
+        if ((e = cudaMemcpyAsync(idx, perm.data(), sizeof(int32_t) * perm.size(), cudaMemcpyHostToDevice, s))) return e;
+        if ((e = cudaStreamSynchronize(s))) return e;
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    // capture one optimizer step in a CUDA graph and replay it
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking))) return e;
+    cudaGraph_t g = nullptr;
+    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal))) return e;
+    e = step(pts, dist, idx, nTrain, batch, batch, true, o.steps, o.lr, cs);
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e || e2) {
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(cs);
+        return e ? e : e2;
+    }
+    if (graph_) cudaGraphExecDestroy(graph_);
+    e = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e) return e;
+    std::vector<float> lossHist;
+    for (int it = 0; it < o.steps; ++it) {
+        if ((e = cudaGraphLaunch(graph_, s))) return e;
+        if ((it + 1) % 500 == 0 || it + 1 == o.steps) {
+            float l = 0.f;
+            if ((e = cudaMemcpyAsync(&l, scalars_, sizeof(float), cudaMemcpyDeviceToHost, s))) return e;
+            if ((e = cudaStreamSynchronize(s))) return e;
+            lossHist.push_back(l);
+        }
+    }
+    if ((e = cudaStreamSynchronize(s))) return e;
+    const auto t2 = std::chrono::steady_clock::now();
+    // validation: worst error on held-out samples -> margin
+    float valMax = 0.f;
+    if (o.validation) {
+        float* pred = nullptr;
+        unsigned* mx = nullptr;
+        if ((e = alloc((void**)&pred, sizeof(float) * size_t(o.validation)))) return e;
+        if ((e = alloc((void**)&mx, sizeof(unsigned)))) return e;
+        if ((e = infer(pts + 3 * nTrain, o.validation, pred, s))) return e;
+        if ((e = cudaMemsetAsync(mx, 0, sizeof(unsigned), s))) return e;
+        absErrMaxKernel<<<nblk(o.validation, 256), 256, 0, s>>>(pred, dist + nTrain, int(o.validation), meta.clampD, mx);
+        unsigned bits = 0;
+        if ((e = cudaMemcpyAsync(&bits, mx, sizeof(unsigned), cudaMemcpyDeviceToHost, s))) return e;
+        if ((e = cudaStreamSynchronize(s))) return e;
+        std::memcpy(&valMax, &bits, 4);
+    }
+    meta.margin = o.marginScale * valMax + o.marginFloor;
+    st.trainLoss = lossHist.empty() ? 0.f : lossHist.back();
+    st.valMaxErr = valMax;
+    st.margin = meta.margin;
+    st.sampleSeconds = std::chrono::duration<float>(t1 - t0).count();
+    st.trainSeconds = std::chrono::duration<float>(t2 - t1).count();
+    st.steps = o.steps;
+    unsigned status = 0;
+    cudaMemcpy(&status, counters_ + 3, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    return status ? cudaErrorLaunchTimeout : cudaSuccess;
+}
+
+// Banded signed distance: NaN wherever |d| >= band, exact elsewhere.  Bricks of 8x8x8 voxels are
+// culled when a lower bound of |d| at their centre minus their half diagonal is >= band; the lower
+// bound comes from the surrogate (|pred| - margin) or, with net == null, from the exact unsigned
+// distance capped at band + radius.  The kept bricks go through the exact kernel.
+cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
+                       float* out, unsigned* scratch, BandedStats& st, cudaStream_t s) {
+    const int3 dims = make_int3(g.nx, g.ny, g.nz);
+    const int3 bd = make_int3((g.nx + 7) / 8, (g.ny + 7) / 8, (g.nz + 7) / 8);
+    const int nb = bd.x * bd.y * bd.z;
+    const float band = std::sqrt(o.maxDistSq);
+    // largest distance from a brick's centre to its voxel centres: the image of the corner
+    // offsets (+-3.5, +-3.5, +-3.5) voxels under the linear part (edge bricks are smaller)
+    float radius = 0.f;
+    for (int c = 0; c < 8; ++c) {
+        const float d[3] = {(c & 1) ? 3.5f : -3.5f, (c & 2) ? 3.5f : -3.5f, (c & 4) ? 3.5f : -3.5f};
+        float r2 = 0.f;
+        for (int a = 0; a < 3; ++a) {
+            const float w = xf.a[3 * a] * d[0] + xf.a[3 * a + 1] * d[1] + xf.a[3 * a + 2] * d[2];
+            r2 += w * w;
+        }
+        radius = std::fmax(radius, std::sqrt(r2));
+    }
+    radius *= 1.0001f;
+    cudaError_t e;
+    float *centers = nullptr, *lb = nullptr, *tmp = nullptr;
+    int32_t *keep = nullptr, *pos = nullptr, *list = nullptr, *sums = nullptr, *total = nullptr;
+    std::vector<void*> mem;
+    auto A = [&](void** p, size_t b) {
+        cudaError_t r = cudaMallocAsync(p, b ? b : 16, s);
+        if (!r) mem.push_back(*p);
+        return r;
+    };
+    auto done = [&](cudaError_t r) {
+        for (void* p : mem) cudaFreeAsync(p, s);
+        return r;
+    };
+    if ((e = A((void**)&centers, sizeof(float) * 3 * size_t(nb)))) return done(e);
+    if ((e = A((void**)&lb, sizeof(float) * size_t(nb)))) return done(e);
+    if ((e = A((void**)&tmp, sizeof(float) * size_t(nb)))) return done(e);
+    if ((e = A((void**)&keep, sizeof(int32_t) * size_t(nb)))) return done(e);
+    if ((e = A((void**)&pos, sizeof(int32_t) * size_t(nb)))) return done(e);
+    if ((e = A((void**)&list, sizeof(int32_t) * size_t(nb)))) return done(e);
+    if ((e = A((void**)&sums, sizeof(int32_t) * size_t(nb / 1024 + 2)))) return done(e);
+    if ((e = A((void**)&total, sizeof(int32_t)))) return done(e);
+    cudaEvent_t ev[4];
+    for (auto& x : ev) cudaEventCreate(&x);
+    cudaEventRecord(ev[0], s);
+    brickCentersKernel<<<nblk(nb, 256), 256, 0, s>>>(centers, bd, dims, xf);
+    if (net) {
+        if ((e = net->infer(centers, nb, tmp, s))) return done(e);
+        surrogateLowerBound<<<nblk(nb, 256), 256, 0, s>>>(tmp, nb, net->meta.margin, lb);
+    } else {
+        const float cap = band + radius;
+        const DistOpts co{0.f, cap * cap, 1, o.threshold, o.beta};
+        if ((e = launchVectorSdf(t, centers, nb, co, precise, tmp, scratch, s))) return done(e);
+        exactLowerBound<<<nblk(nb, 256), 256, 0, s>>>(tmp, nb, cap, lb);
+    }
+    brickKeepKernel<<<nblk(nb, 256), 256, 0, s>>>(lb, nb, band, radius, keep);
+    if ((e = exclusiveScanI32(keep, pos, nb, sums, total, s))) return done(e);
+    compactKernel<<<nblk(nb, 256), 256, 0, s>>>(keep, pos, nb, list);
+    int32_t kept = 0;
+    if ((e = cudaMemcpyAsync(&kept, total, sizeof(int32_t), cudaMemcpyDeviceToHost, s))) return done(e);
+    cudaEventRecord(ev[1], s);
+    fillNanKernel<<<nblk(int64_t(g.nx) * g.ny * g.nz, 256), 256, 0, s>>>(out, int64_t(g.nx) * g.ny * g.nz);
+    if ((e = cudaStreamSynchronize(s))) return done(e);
+    cudaEventRecord(ev[2], s);
+    if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, list, kept, scratch, s))) return done(e);
+    cudaEventRecord(ev[3], s);
+    if ((e = cudaStreamSynchronize(s))) return done(e);
+    cudaEventElapsedTime(&st.cullMs, ev[0], ev[1]);
+    cudaEventElapsedTime(&st.exactMs, ev[2], ev[3]);
+    for (auto& x : ev) cudaEventDestroy(x);
+    st.bricks = nb;
+    st.keptBricks = kept;
+    return done(cudaGetLastError());
+}
+
+}  // namespace gbfwn

@@ -365,6 +365,10 @@ constexpr int kTX = 4, kTY = 4, kTZ = 2;  // voxel tile of one warp
 struct TileGrid {
     int32_t tilesX, tilesY, tilesZ;
     uint32_t numTiles;
+    // optional list of 8x8x8-voxel bricks to cover instead of the whole range: 16 warp tiles
+    // (2 x 2 x 4 tiles of 4x4x2) per brick
+    const int32_t* bricks;
+    int32_t bricksX, bricksY;
 };
 
 __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
@@ -383,11 +387,22 @@ __global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange
     for (;;) {
         const unsigned tile = nextTicket(scratch, lane);
         if (tile >= tg.numTiles) break;
-        const int tx = int(tile % unsigned(tg.tilesX));
-        const unsigned rest = tile / unsigned(tg.tilesX);
-        const int ty = int(rest % unsigned(tg.tilesY));
-        const int tz = int(rest / unsigned(tg.tilesY));
-        const int x = tx * kTX + lx, y = ty * kTY + ly, z = g.z0 + tz * kTZ + lz;
+        int x, y, z;
+        if (tg.bricks) {
+            const int b = tg.bricks[tile >> 4], sub = int(tile & 15u);
+            const int bx = b % tg.bricksX, by = (b / tg.bricksX) % tg.bricksY, bz = b / (tg.bricksX * tg.bricksY);
+            x = bx * 8 + (sub & 1) * kTX + lx;
+            y = by * 8 + ((sub >> 1) & 1) * kTY + ly;
+            z = g.z0 + bz * 8 + (sub >> 2) * kTZ + lz;
+        } else {
+            const int tx = int(tile % unsigned(tg.tilesX));
+            const unsigned rest = tile / unsigned(tg.tilesX);
+            const int ty = int(rest % unsigned(tg.tilesY));
+            const int tz = int(rest / unsigned(tg.tilesY));
+            x = tx * kTX + lx;
+            y = ty * kTY + ly;
+            z = g.z0 + tz * kTZ + lz;
+        }
         const bool active = x < g.nx && y < g.ny && z < g.z1;
         const float3 q = xfPoint(xf, x, y, z);
         float res;
@@ -510,7 +525,21 @@ static TileGrid tileGridFor(const GridRange& g) {
     tg.tilesY = (g.ny + kTY - 1) / kTY;
     tg.tilesZ = (g.z1 - g.z0 + kTZ - 1) / kTZ;
     tg.numTiles = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.tilesZ);
+    tg.bricks = nullptr;
+    tg.bricksX = tg.bricksY = 0;
     return tg;
+}
+
+cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
+                                float* out, const int32_t* bricks, int32_t nBricks, unsigned* scratch, cudaStream_t s) {
+    TileGrid tg = tileGridFor(g);
+    tg.bricks = bricks;
+    tg.bricksX = (g.nx + 7) / 8;
+    tg.bricksY = (g.ny + 7) / 8;
+    tg.numTiles = uint32_t(nBricks) * 16u;
+    if (precise)
+        return launchPersistent(gridKernel<true, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+    return launchPersistent(gridKernel<false, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,

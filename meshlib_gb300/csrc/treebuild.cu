@@ -537,7 +537,9 @@ __global__ void __launch_bounds__(256) finishSmall(const Elem* __restrict__ el, 
 
 inline unsigned blocks(int64_t n, int t) { return unsigned((n + t - 1) / t); }
 
-cudaError_t exclusiveScan(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, int32_t* total, cudaStream_t s) {
+}  // namespace
+
+cudaError_t exclusiveScanI32(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, int32_t* total, cudaStream_t s) {
     const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
     if (n == 0) return cudaMemsetAsync(total, 0, sizeof(int32_t), s);
     scanBlocks<<<unsigned(nb), 256, 0, s>>>(in, out, n, sums);
@@ -546,6 +548,10 @@ cudaError_t exclusiveScan(const int32_t* in, int32_t* out, int64_t n, int32_t* s
     return cudaGetLastError();
 }
 
+namespace {
+cudaError_t exclusiveScan(const int32_t* in, int32_t* out, int64_t n, int32_t* sums, int32_t* total, cudaStream_t s) {
+    return exclusiveScanI32(in, out, n, sums, total, s);
+}
 }  // namespace
 
 // Builds the reference tree on the device.  Outputs: nodes (2n-1 reference nodes, allocated through

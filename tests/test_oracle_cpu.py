@@ -133,3 +133,26 @@ def test_traversal_counts():
     o = O.Oracle(v, f)
     c = o.traversal_counts(O.grid_points(dims, xf))
     assert all(int(x) > 0 for x in c)
+
+
+def test_mlp_oracle_gradients_finite_differences(monkeypatch):
+    """The surrogate's CPU oracle: analytic gradients equal central finite differences (bf16
+    rounding switched off so the loss is smooth)."""
+    import math
+
+    from oracle import mlp_oracle as MO
+    monkeypatch.setattr(MO, "bf16", lambda x: np.asarray(x, np.float64))
+    rng = np.random.default_rng(0)
+    p = np.concatenate([rng.normal(0, 0.1, int(np.prod(s))) for _, s in MO.SIZES])
+    m = np.zeros(40)
+    m[3] = 1
+    m[4:36] = [math.pi * 2 ** (k / 5) for k in range(32)]
+    m[36] = 10
+    pts = rng.uniform(-1, 1, (64, 3)).astype(np.float32)
+    t = rng.normal(0, 0.3, 64)
+    _, g = MO.loss_and_grads(p, m, pts, t)
+    for idx in [5, 24600, 41100, 57700, 74200, 74368, 30000, 24577]:
+        e = np.zeros_like(p)
+        e[idx] = 1e-6
+        fd = (MO.loss_and_grads(p + e, m, pts, t)[0] - MO.loss_and_grads(p - e, m, pts, t)[0]) / 2e-6
+        assert abs(g[idx] - fd) <= 1e-6 + 1e-5 * abs(fd), (idx, g[idx], fd)
