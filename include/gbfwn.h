@@ -244,6 +244,34 @@ GBFWN_API int gbfwn_from_grid_with_distances_banded_dev(gbfwn_handle h, gbfwn_su
                                                         const float xf[12], const gbfwn_dist_opts* opts, float* d_out,
                                                         gbfwn_banded_stats* stats, void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Batched signed-distance grids (no counterpart in the reference, which handles one mesh per
+ * call): many meshes, each with its own grid, options and device output, computed by ONE
+ * persistent kernel fed from a single work queue.  Grids are queued most expensive first (voxels x
+ * log2 triangles) so that uneven batches balance.  Six kernel variants (voxel-tile shape x block
+ * size) can be timed on the batch and the fastest kept; a batch can be replayed from a CUDA graph. */
+typedef struct gbfwn_batch_s* gbfwn_batch;
+
+typedef struct gbfwn_batch_item {
+    gbfwn_handle mesh;      /* all meshes of a batch on one device; the first mesh's precise setting applies */
+    int32_t dims[3];
+    float xf[12];
+    gbfwn_dist_opts opts;
+    float* d_out;           /* dims[0] * dims[1] * dims[2] floats, device memory */
+} gbfwn_batch_item;
+
+GBFWN_API int gbfwn_batch_create(const gbfwn_batch_item* items, int32_t n, gbfwn_batch* out);
+GBFWN_API int gbfwn_batch_destroy(gbfwn_batch b);
+GBFWN_API int32_t gbfwn_batch_num_configs(void);
+GBFWN_API const char* gbfwn_batch_config_name(int32_t config);
+GBFWN_API int gbfwn_batch_set_config(gbfwn_batch b, int32_t config);
+/* Times every variant on the batch (three runs each, best of the last two) and keeps the fastest;
+ * times_ms (may be NULL) receives gbfwn_batch_num_configs() values. */
+GBFWN_API int gbfwn_batch_autotune(gbfwn_batch b, int32_t* best, float* times_ms);
+/* Enqueues the batch on `stream` (plain launch, or the CUDA graph captured on first use). */
+GBFWN_API int gbfwn_batch_run_dev(gbfwn_batch b, void* stream);
+GBFWN_API int gbfwn_batch_graph_launch(gbfwn_batch b, void* stream);
+
 /* Diagnostic (no counterpart in the reference): D[m x n] (+)= A[m x k] * B[n x k]^T on the tcgen05 tensor
  * cores, bf16 inputs (row-major, k contiguous), FP32 output (row-major); m % 128 == 0, n in {128, 192},
  * k % 64 == 0; with split_k > 1 the output is accumulated atomically (zero it first).  Device pointers,

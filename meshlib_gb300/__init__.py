@@ -67,6 +67,11 @@ class _BandedStats(ctypes.Structure):
                 ("exactMs", ctypes.c_float)]
 
 
+class _BatchItem(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.c_void_p), ("dims", ctypes.c_int32 * 3), ("xf", ctypes.c_float * 12), ("opts", _DistOpts),
+                ("d_out", ctypes.c_void_p)]
+
+
 SURROGATE_PARAMS = 74369
 SURROGATE_META = 40
 
@@ -107,6 +112,14 @@ _SIGS = [
     ("gbfwn_self_intersections_memory", ctypes.c_size_t, [_i64, _i64]),
     ("gbfwn_debug_fail_next_allocs", None, [ctypes.c_int]),
     ("gbfwn_debug_gemm_bf16", ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    ("gbfwn_batch_create", ctypes.c_int, [ctypes.POINTER(_BatchItem), _i32, ctypes.POINTER(_vp)]),
+    ("gbfwn_batch_destroy", ctypes.c_int, [_vp]),
+    ("gbfwn_batch_num_configs", _i32, []),
+    ("gbfwn_batch_config_name", ctypes.c_char_p, [_i32]),
+    ("gbfwn_batch_set_config", ctypes.c_int, [_vp, _i32]),
+    ("gbfwn_batch_autotune", ctypes.c_int, [_vp, ctypes.POINTER(_i32), _vp]),
+    ("gbfwn_batch_run_dev", ctypes.c_int, [_vp, _vp]),
+    ("gbfwn_batch_graph_launch", ctypes.c_int, [_vp, _vp]),
     ("gbfwn_surrogate_default_opts", None, [ctypes.POINTER(_SurrogateOpts)]),
     ("gbfwn_surrogate_train", ctypes.c_int,
      [_vp, _vp, _vp, ctypes.POINTER(_SurrogateOpts), ctypes.POINTER(_vp), ctypes.POINTER(_SurrogateStats)]),
@@ -408,6 +421,99 @@ class Surrogate:
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             self._L.gbfwn_surrogate_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _autotune_cache_path() -> str:
+    return os.environ.get("MESHLIB_GB300_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "meshlib_gb300", "autotune.json"))
+
+
+class Batch:
+    """Many meshes with their own grids in one persistent launch (gbfwn_batch_* in include/gbfwn.h).
+
+    ``items``: sequence of (FastWindingNumber, dims, xf, DistanceToMeshOptions or None, device output
+    pointer).  The tuned variant is remembered in a small JSON cache keyed by GPU, batch size and
+    triangle / voxel totals (bucketed by powers of two)."""
+
+    def __init__(self, items):
+        self._L = lib()
+        arr = (_BatchItem * len(items))()
+        tris = vox = 0
+        for k, (fwn, dims, xf, opts, out_ptr) in enumerate(items):
+            it = arr[k]
+            it.mesh = fwn.handle.value
+            for j in range(3):
+                it.dims[j] = int(dims[j])
+            x = _xf12(xf)
+            for j in range(12):
+                it.xf[j] = float(x[j])
+            it.opts = (opts or DistanceToMeshOptions())._c()
+            it.d_out = int(out_ptr)
+            tris += fwn.num_faces()
+            vox += int(dims[0]) * int(dims[1]) * int(dims[2])
+        self._items = arr
+        self._h = ctypes.c_void_p()
+        _check(self._L.gbfwn_batch_create(arr, len(items), ctypes.byref(self._h)))
+        self.key = f"n{len(items)}_t{max(tris, 1).bit_length()}_v{max(vox, 1).bit_length()}"
+
+    @staticmethod
+    def configs():
+        L = lib()
+        return [L.gbfwn_batch_config_name(i).decode() for i in range(L.gbfwn_batch_num_configs())]
+
+    def set_config(self, c: int):
+        _check(self._L.gbfwn_batch_set_config(self._h, c))
+
+    def autotune(self, use_cache: bool = True) -> dict:
+        import json
+        try:
+            import torch
+            gpu = torch.cuda.get_device_name()
+        except Exception:
+            gpu = "gpu"
+        key = f"{gpu}|{self.key}"
+        path = _autotune_cache_path()
+        cache = {}
+        if use_cache and os.path.exists(path):
+            try:
+                with open(path) as fh:
+                    cache = json.load(fh)
+            except Exception:
+                cache = {}
+        if use_cache and key in cache:
+            self.set_config(int(cache[key]["config"]))
+            return dict(cache[key], cached=True)
+        n = self._L.gbfwn_batch_num_configs()
+        times = (ctypes.c_float * n)()
+        best = ctypes.c_int32()
+        _check(self._L.gbfwn_batch_autotune(self._h, ctypes.byref(best), times))
+        rec = {"config": int(best.value), "name": self.configs()[best.value], "times_ms": [float(t) for t in times]}
+        if use_cache:
+            try:
+                os.makedirs(os.path.dirname(path), exist_ok=True)
+                cache[key] = rec
+                with open(path, "w") as fh:
+                    json.dump(cache, fh, indent=1)
+            except OSError:
+                pass
+        return dict(rec, cached=False)
+
+    def run_dev(self, stream=None):
+        _check(self._L.gbfwn_batch_run_dev(self._h, _stream(stream)))
+
+    def graph_launch(self, stream=None):
+        _check(self._L.gbfwn_batch_graph_launch(self._h, _stream(stream)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gbfwn_batch_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

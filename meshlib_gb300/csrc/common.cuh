@@ -74,6 +74,22 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
                           unsigned* scratch, cudaStream_t s);
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                           float* out, unsigned* scratch, cudaStream_t s);
+// One mesh + grid of a batched launch (query.cu batchKernel): its tickets are
+// [tileBase, tileBase + tiles of its grid under the launch's tile shape).
+struct BatchItem {
+    QueryTree t;
+    GridRange g;  // whole grid: z0 = 0, z1 = nz, zOut = 0
+    Xf xf;
+    DistOpts o;
+    float* out;
+    uint32_t tileBase;
+};
+constexpr int kBatchConfigs = 6;  // tile shape x block size variants
+const char* batchConfigName(int config);
+uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz);
+cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,
+                           cudaStream_t s);
+
 // Signed distance on a list of 8x8x8-voxel bricks of the grid (brick b = bx + by * ceil(nx/8) +
 // bz * ceil(nx/8) * ceil(ny/8)); voxels outside the bricks are not written.
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,

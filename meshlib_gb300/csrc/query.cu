@@ -587,4 +587,98 @@ cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise,
     return launchPersistent(selfIntKernel<false>, tiles, scratch, s, t, beta, bits, wn, scratch);
 }
 
+// ------------------------------------------------------------------ batched meshes
+// Many meshes, each with its own grid, in one persistent launch: the tiles of all grids form one
+// ticket sequence (item i owns tickets [tileBase_i, tileBase_{i+1})); a warp takes a ticket, finds
+// its item by binary search, and runs the same packet traversals on that item's tree.  Items are
+// ordered by estimated cost, most expensive first, so the long grids start early and the short
+// ones fill the tail.  Tile shape (TX x TY x TZ = 32 voxels) and block size are template
+// parameters chosen by the autotuner.
+namespace {
+
+template <bool PRECISE, int TX, int TY, int TZ, int THREADS>
+__global__ void __launch_bounds__(THREADS) batchKernel(const BatchItem* __restrict__ items, int nItems, uint32_t totalTiles,
+                                                       unsigned* scratch) {
+    static_assert(TX * TY * TZ == 32, "one voxel per lane");
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / (TX * TY);
+    for (;;) {
+        const unsigned tile = nextTicket(scratch, lane);
+        if (tile >= totalTiles) break;
+        int lo = 0, hi = nItems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].tileBase <= tile) lo = mid; else hi = mid - 1;
+        }
+        const BatchItem& it = items[lo];
+        const unsigned local = tile - it.tileBase;
+        const int tilesX = (it.g.nx + TX - 1) / TX, tilesY = (it.g.ny + TY - 1) / TY;
+        const int tx = int(local % unsigned(tilesX));
+        const unsigned rest = local / unsigned(tilesX);
+        const int ty = int(rest % unsigned(tilesY)), tz = int(rest / unsigned(tilesY));
+        const int x = tx * TX + lx, y = ty * TY + ly, z = tz * TZ + lz;
+        const bool active = x < it.g.nx && y < it.g.ny && z < it.g.nz;
+        const QueryTree t = it.t;
+        const DistOpts o = it.o;
+        const float3 q = xfPoint(it.xf, x, y, z);
+        const float dsq = cpPacket<PRECISE>(t, q, active, o.maxDistSq, o.minDistSq, scratch + 1);
+        const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
+        const float w = fwnPacket<PRECISE>(t, q, active && valid, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
+        const float d = __fsqrt_rn(dsq);
+        const float res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+        if (active) it.out[(size_t(z) * it.g.ny + y) * it.g.nx + x] = res;
+    }
+}
+
+template <bool PRECISE, int TX, int TY, int TZ, int THREADS>
+cudaError_t launchBatchT(const BatchItem* items, int nItems, uint32_t totalTiles, unsigned* scratch, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned), s);
+    if (e || totalTiles == 0) return e;
+    auto* k = batchKernel<PRECISE, TX, TY, TZ, THREADS>;
+    static int sms = 0;
+    if (!sms) sms = numSMs();
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, THREADS, 0);
+    int blocks = sms * (perSm < 1 ? 1 : perSm);
+    const uint64_t maxBlocks = (uint64_t(totalTiles) + THREADS / 32 - 1) / (THREADS / 32);
+    if (uint64_t(blocks) > maxBlocks) blocks = int(maxBlocks);
+    k<<<blocks, THREADS, 0, s>>>(items, nItems, totalTiles, scratch);
+    return cudaGetLastError();
+}
+
+template <bool PRECISE>
+cudaError_t launchBatchP(const BatchItem* items, int nItems, uint32_t totalTiles, int config, unsigned* scratch,
+                         cudaStream_t s) {
+    switch (config) {
+        case 0: return launchBatchT<PRECISE, 4, 4, 2, 256>(items, nItems, totalTiles, scratch, s);
+        case 1: return launchBatchT<PRECISE, 4, 4, 2, 128>(items, nItems, totalTiles, scratch, s);
+        case 2: return launchBatchT<PRECISE, 8, 4, 1, 256>(items, nItems, totalTiles, scratch, s);
+        case 3: return launchBatchT<PRECISE, 8, 4, 1, 128>(items, nItems, totalTiles, scratch, s);
+        case 4: return launchBatchT<PRECISE, 2, 4, 4, 256>(items, nItems, totalTiles, scratch, s);
+        case 5: return launchBatchT<PRECISE, 2, 4, 4, 128>(items, nItems, totalTiles, scratch, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+const char* batchConfigName(int config) {
+    static const char* names[kBatchConfigs] = {"tile 4x4x2, 256 threads", "tile 4x4x2, 128 threads",
+                                               "tile 8x4x1, 256 threads", "tile 8x4x1, 128 threads",
+                                               "tile 2x4x4, 256 threads", "tile 2x4x4, 128 threads"};
+    return (config >= 0 && config < kBatchConfigs) ? names[config] : "";
+}
+
+uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz) {
+    static const int shape[kBatchConfigs][3] = {{4, 4, 2}, {4, 4, 2}, {8, 4, 1}, {8, 4, 1}, {2, 4, 4}, {2, 4, 4}};
+    const int* t = shape[(config >= 0 && config < kBatchConfigs) ? config : 0];
+    return uint64_t((nx + t[0] - 1) / t[0]) * uint64_t((ny + t[1] - 1) / t[1]) * uint64_t((nz + t[2] - 1) / t[2]);
+}
+
+cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,
+                           cudaStream_t s) {
+    if (precise) return launchBatchP<true>(items, nItems, totalTiles, config, scratch, s);
+    return launchBatchP<false>(items, nItems, totalTiles, config, scratch, s);
+}
+
 }  // namespace gbfwn
