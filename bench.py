@@ -153,6 +153,40 @@ def bytes_per_voxel(c):
     return 4 + 32 * c["cp_nodes"] + 32 * c["fwn_nodes"] + 48 * (c["cp_leaves"] + c["fwn_leaves"])
 
 
+def precision_vs_fp64(v, f, dims, xf, grid_out, shell, shell_d, n_grid=200_000, n_shell=200_000):
+    """Max / RMS error of the GPU results (precise mode) against the FP64 oracle on seeded subsets:
+    signed distances of the timed 512^3 grid and of the shell points (error / bbox diagonal), sign
+    mismatches outside a 1e-3 window around the 0.5 threshold."""
+    import oracle as O
+    from meshlib_gb300 import meshgen as mg
+    o = O.Oracle(v, f)
+    diag = mg.diag(v)
+    rng = np.random.default_rng(777)
+    out = {}
+    idx = rng.integers(0, int(np.prod(dims)), n_grid)
+    z, rem = np.divmod(idx, dims[0] * dims[1])
+    y, x = np.divmod(rem, dims[0])
+    A = np.asarray(xf[:9], np.float32).reshape(3, 3)
+    b = np.asarray(xf[9:], np.float32)
+    p = np.stack([x, y, z], 1).astype(np.float32)
+    pts = ((p[:, 0:1] * A[:, 0] + p[:, 1:2] * A[:, 1]) + p[:, 2:3] * A[:, 2] + b).astype(np.float32)
+    sets = [("grid", pts, grid_out.cpu().numpy()[idx])]
+    if shell is not None:
+        sidx = rng.integers(0, len(shell), n_shell)
+        sets.append(("shell", shell[sidx], shell_d.cpu().numpy()[sidx]))
+    for name, q, gpu in sets:
+        ref = o.vector_with_distances(q, prec=1)
+        wref = o.from_vector(q, prec=1)
+        err = np.abs(np.abs(gpu.astype(np.float64)) - np.abs(ref)) / diag
+        mism = np.signbit(gpu) != np.signbit(ref)  # signbit keeps the sign of a zero distance
+        near = np.abs(wref - 0.5) < 1e-3
+        out[name] = {"points": len(q), "dist_max_err_over_diag": float(err.max()),
+                     "dist_rms_err_over_diag": float(np.sqrt((err ** 2).mean())),
+                     "sign_mismatches_outside_tau": int((mism & ~near).sum()), "sign_mismatches_within_tau": int((mism & near).sum()),
+                     "tau": 1e-3}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -187,6 +221,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-banded", action="store_true", help="skip the banded / surrogate leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-mesh batched leg")
+    ap.add_argument("--no-points", action="store_true", help="skip the shell-point / self-intersection leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -292,6 +327,36 @@ def main():
                   "surrogate_config": "2M samples (50% uniform in box, 50% near surface), 1M validation, 3000 steps x 16384"}
         del sur
 
+    # ---- points and faces on the same mesh: 4M shell points (|d| < 1e-3, calcFromVector and the
+    # signed distance at points) and calcSelfIntersections after folding 1% of the faces inward
+    points = None
+    shell = shell_d = None
+    if not args.no_points:
+        shell = mg.shell_points(v, f, 4_000_000, width=1e-3, seed=0)
+        dpts = torch.from_numpy(shell).cuda()
+        shell_w = torch.empty(len(shell), dtype=torch.float32, device="cuda")
+        shell_d = torch.empty(len(shell), dtype=torch.float32, device="cuda")
+        vec_ms = timed(lambda: fwn.calcFromVector_dev(dpts.data_ptr(), len(shell), shell_w.data_ptr(), stream=sp), 3)
+        vsd_ms = timed(lambda: fwn.calcWithDistances_dev(dpts.data_ptr(), len(shell), shell_d.data_ptr(), stream=sp), 3)
+        fv, ff = mg.fold_faces(v, f, frac=0.01, depth=0.1, seed=0)
+        folded = M.FastWindingNumber(fv, ff, device=local)
+        bits = torch.zeros((len(ff) + 63) // 64, dtype=torch.int64, device="cuda")
+        si_ms = timed(lambda: folded.calcSelfIntersections_dev(bits.data_ptr(), stream=sp), 3)
+        flagged = int(np.unpackbits(bits.cpu().numpy().view(np.uint8)).sum())
+        ov, of = mg.overlapping_spheres(seed=0, level=7, offset=0.5)
+        overl = M.FastWindingNumber(ov, of, device=local)
+        obits = torch.zeros((len(of) + 63) // 64, dtype=torch.int64, device="cuda")
+        osi_ms = timed(lambda: overl.calcSelfIntersections_dev(obits.data_ptr(), stream=sp), 3)
+        oflag = int(np.unpackbits(obits.cpu().numpy().view(np.uint8)).sum())
+        points = {"shell_points": len(shell), "from_vector_ms": vec_ms, "from_vector_points_per_s": len(shell) / (vec_ms * 1e-3),
+                  "with_distances_ms": vsd_ms, "with_distances_points_per_s": len(shell) / (vsd_ms * 1e-3),
+                  "self_intersections_ms": si_ms, "self_intersections_faces_per_s": len(ff) / (si_ms * 1e-3),
+                  "self_intersecting_faces": flagged, "folded_faces_fraction": 0.01,
+                  "note_fold": "pushing 1% of faces 0.1 inward makes pits whose walls cross nothing, so no face is "
+                               "self-intersecting; the overlapping-spheres case exercises the flagged path",
+                  "overlap_faces": len(of), "overlap_self_intersections_ms": osi_ms, "overlap_flagged_faces": oflag}
+        del folded, bits, overl, obits
+
     # ---- batched: 64 uneven meshes (triangles log-uniform in [5k, 500k], grid sides log-uniform in
     # [32, 192]) in one persistent launch vs 64 sequential single-mesh launches
     batched = None
@@ -345,7 +410,7 @@ def main():
             "e2e": {"value": e2e_val, "unit": "voxels/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                     "d2h_bytes_per_step": int(nvox * 4), "s_per_step": e2e_s,
                     "s_create_per_step": float(np.mean(create_times)) if create_times else None},
-            "clocks": clk.summary(), "nan_fraction": nan_frac, "wall_s_timed": wall, "banded": banded, "batched": batched}
+            "clocks": clk.summary(), "nan_fraction": nan_frac, "wall_s_timed": wall, "banded": banded, "batched": batched, "points": points}
     if rank == 0 and not args.no_cpu:
         rate, thr, desc, counts = cpu_reference_rate(v, f, dims, xf)
         bpv = bytes_per_voxel(counts)
@@ -359,6 +424,7 @@ def main():
                                     "from L1/L2, so actual DRAM traffic (traffic) is ~1.5 GB per launch and the kernel is "
                                     "issue/latency-bound, not HBM-bound"}
         line["cpu_baseline"] = {"value": rate, "unit": "voxels/s", "cores": thr, "kind": "port", "sample": desc}
+        line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -357,6 +357,16 @@ class FastWindingNumber:
         _check(self._L.gbfwn_from_vector_dev(self._h, ctypes.c_void_p(d_pts_ptr), n, beta, skipFace,
                                              ctypes.c_void_p(d_out_ptr), _stream(stream)))
 
+    def calcWithDistances_dev(self, d_pts_ptr: int, n: int, d_out_ptr: int, options=None, stream=None):
+        o = (options or DistanceToMeshOptions())._c()
+        _check(self._L.gbfwn_vector_with_distances_dev(self._h, ctypes.c_void_p(d_pts_ptr), n, ctypes.byref(o),
+                                                       ctypes.c_void_p(d_out_ptr), _stream(stream)))
+
+    def calcSelfIntersections_dev(self, d_bits_ptr: int, d_wn_ptr: int = 0, beta: float = 2.0, stream=None):
+        """d_bits: ceil(faces / 64) 64-bit words; d_wn (optional): one float per face."""
+        _check(self._L.gbfwn_self_intersections_dev(self._h, beta, ctypes.c_void_p(d_bits_ptr),
+                                                    ctypes.c_void_p(d_wn_ptr or None), _stream(stream)))
+
 
 def memory_estimates(nv: int, nt: int, dims=None, npts: int = 0) -> dict:
     L = lib()

@@ -597,7 +597,7 @@ cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise,
 namespace {
 
 template <bool PRECISE, int TX, int TY, int TZ, int THREADS>
-__global__ void __launch_bounds__(THREADS) batchKernel(const BatchItem* __restrict__ items, int nItems, uint32_t totalTiles,
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const BatchItem* __restrict__ items, int nItems, uint32_t totalTiles,
                                                        unsigned* scratch) {
     static_assert(TX * TY * TZ == 32, "one voxel per lane");
     const int lane = threadIdx.x & 31;
@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(THREADS) batchKernel(const BatchItem* __restri
         const int ty = int(rest % unsigned(tilesY)), tz = int(rest / unsigned(tilesY));
         const int x = tx * TX + lx, y = ty * TY + ly, z = tz * TZ + lz;
         const bool active = x < it.g.nx && y < it.g.ny && z < it.g.nz;
-        const QueryTree t = it.t;
+        const QueryTree& t = it.t;  // read through the cache, not copied into registers
         const DistOpts o = it.o;
         const float3 q = xfPoint(it.xf, x, y, z);
         const float dsq = cpPacket<PRECISE>(t, q, active, o.maxDistSq, o.minDistSq, scratch + 1);

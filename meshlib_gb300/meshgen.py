@@ -151,7 +151,9 @@ def noisy_icosphere(seed: int = 0, level: int = 8, amp: float = 0.05, octaves: i
 
 def fold_faces(verts: np.ndarray, faces: np.ndarray, frac: float = 0.01, depth: float = 0.1, seed: int = 0):
     """Pushes the vertices of a seeded ``frac`` of the faces inward along the radial direction by
-    ``depth``: the folded pits make parts of the surface cross each other."""
+    ``depth``.  On a sphere this digs narrow pits whose walls stay inside the solid and cross no
+    other part of the surface, so no face becomes self-intersecting; ``overlapping_spheres`` gives a
+    surface that does cross itself."""
     rng = np.random.default_rng(seed + 7919)
     nf = len(faces)
     chosen = rng.choice(nf, max(1, int(round(frac * nf))), replace=False)
@@ -216,3 +218,13 @@ def batch_meshes(count: int = 64, seed: int = 0, tri_lo: int = 5000, tri_hi: int
         dims, xf = grid_for(v, side)
         out.append((v, f, dims, xf))
     return out
+
+
+def overlapping_spheres(seed: int = 0, level: int = 7, offset: float = 0.5):
+    """Two noisy icospheres, the second shifted by `offset` along x, as one triangle list: a
+    self-intersecting surface whose faces inside the other sphere have centroid winding number
+    about 1.5."""
+    v1, f1 = noisy_icosphere(seed=seed, level=level)
+    v2, f2 = noisy_icosphere(seed=seed + 1, level=level)
+    v2 = v2 + np.array([offset, 0, 0], np.float32)
+    return np.concatenate([v1, v2]), np.concatenate([f1, f2 + len(v1)]).astype(np.int32)

@@ -29,7 +29,7 @@ def fwncls(fwn_lib):
 
 def _sign_ok(d_gpu, d_ref, wn_ref, thr=0.5):
     both = np.isfinite(d_gpu) & np.isfinite(d_ref)
-    mism = both & (np.sign(d_gpu) != np.sign(d_ref)) & (np.abs(d_ref) > 0)
+    mism = both & (np.signbit(d_gpu) != np.signbit(d_ref))  # signbit keeps the sign of a zero distance
     near = np.abs(wn_ref - thr) < TAU
     return int((mism & ~near).sum()), int((mism & near).sum())
 
@@ -200,6 +200,16 @@ def test_self_intersections(fwncls, precise):
     near = (np.abs(wn_ref) < TAU) | (np.abs(wn_ref - 1) < TAU)
     assert ((bits != bits_ref) & ~near).sum() == 0
     assert bits.sum() > 0
+
+
+def test_self_intersections_overlapping_spheres(fwncls):
+    v, f = mg.overlapping_spheres(seed=2, level=4, offset=0.6)
+    o = O.Oracle(v, f)
+    bits_ref, wn_ref = o.self_intersections(prec=1)
+    bits, wn = fwncls(v, f).calcSelfIntersections(with_wn=True)
+    near = (np.abs(wn_ref) < TAU) | (np.abs(wn_ref - 1) < TAU)
+    assert ((bits != bits_ref) & ~near).sum() == 0
+    assert 0.1 * len(f) < bits.sum() < 0.5 * len(f)
 
 
 def test_self_intersections_clean_and_invalid_faces(fwncls, torus):
