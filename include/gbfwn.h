@@ -18,6 +18,9 @@
  *    `MR::Cuda::FastWindingNumber`.  `_dev` calls take DEVICE pointers and only enqueue work on
  *    `stream`: NULL = the handle's own stream; any cudaStream_t, including cudaStreamLegacy
  *    (0x1) and cudaStreamPerThread (0x2), is accepted.
+ *  - A handle owns one work-queue counter and staging buffers: calls on the same handle must not
+ *    overlap on the GPU (keep them on one stream, or serialise them); different handles are
+ *    independent.
  *  - Progress callbacks receive a fraction in [0, 1] and return nonzero to continue, zero to
  *    cancel (MRMesh/MRProgressCallback.h); a cancelled call returns GBFWN_CANCELLED.
  *  - Errors: a nonzero status; `gbfwn_last_error()` gives the message of the last failure on the

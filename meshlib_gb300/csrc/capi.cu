@@ -182,6 +182,7 @@ GBFWN_API int gbfwn_destroy(gbfwn_handle h) {
         h->treeMem.freeAll();
         if (h->outBuf) cudaFree(h->outBuf);
         if (h->inBuf) cudaFree(h->inBuf);
+        if (h->sortBuf) cudaFree(h->sortBuf);
         for (auto ev : h->events) cudaEventDestroy(ev);
         if (h->stream) cudaStreamDestroy(h->stream);
         if (h->copyStream) cudaStreamDestroy(h->copyStream);
@@ -208,12 +209,32 @@ GBFWN_API int gbfwn_get_tree(gbfwn_handle h, void* nodes, float* dipoles) {
 }
 
 // ------------------------------------------------------------------------- device-pointer calls
+namespace {
+// Spatially coherent processing order for n >= 8192 arbitrary points (Morton order inside the mesh
+// box); null for small inputs, which are processed as given.
+cudaError_t pointOrder(gbfwn_mesh_s* h, const float* d_pts, int64_t n, cudaStream_t s, const int32_t** order) {
+    *order = nullptr;
+    if (n < 8192 || h->tree.nLeaves == 0) return cudaSuccess;
+    const size_t words = size_t(n) + size_t(mortonOrderScratch(n));
+    cudaError_t e = h->ensure(&h->sortBuf, &h->sortCap, words * sizeof(int32_t));
+    if (e) return e;
+    int32_t* buf = static_cast<int32_t*>(h->sortBuf);
+    const float lo[3] = {h->tree.q.rootBox0.x, h->tree.q.rootBox0.y, h->tree.q.rootBox0.z};
+    const float hi[3] = {h->tree.q.rootBox1.x, h->tree.q.rootBox1.y, h->tree.q.rootBox1.z};
+    e = mortonOrder(d_pts, n, lo, hi, buf, buf + n, s);
+    if (!e) *order = buf;
+    return e;
+}
+}  // namespace
+
 GBFWN_API int gbfwn_from_vector_dev(gbfwn_handle h, const float* d_pts, int64_t n, float beta, int32_t skipFace,
                                     float* d_out, void* stream) {
     if (!h || n < 0 || (n > 0 && (!d_pts || !d_out))) return fail(GBFWN_INVALID, "gbfwn_from_vector_dev: bad arguments");
     DeviceGuard g(h->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
-    cudaError_t e = launchVectorFwn(h->tree.q, d_pts, n, beta, skipFace, h->precise, d_out, h->scratch, s);
+    const int32_t* order = nullptr;
+    cudaError_t e = pointOrder(h, d_pts, n, s, &order);
+    if (!e) e = launchVectorFwn(h->tree.q, d_pts, n, beta, skipFace, h->precise, d_out, h->scratch, s, order);
     return e ? cudaFail(e, "gbfwn_from_vector_dev") : GBFWN_OK;
 }
 
@@ -222,7 +243,9 @@ GBFWN_API int gbfwn_vector_with_distances_dev(gbfwn_handle h, const float* d_pts
     if (!h || n < 0 || (n > 0 && (!d_pts || !d_out))) return fail(GBFWN_INVALID, "gbfwn_vector_with_distances_dev: bad arguments");
     DeviceGuard g(h->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
-    cudaError_t e = launchVectorSdf(h->tree.q, d_pts, n, toOpts(opts), h->precise, d_out, h->scratch, s);
+    const int32_t* order = nullptr;
+    cudaError_t e = pointOrder(h, d_pts, n, s, &order);
+    if (!e) e = launchVectorSdf(h->tree.q, d_pts, n, toOpts(opts), h->precise, d_out, h->scratch, s, order);
     return e ? cudaFail(e, "gbfwn_vector_with_distances_dev") : GBFWN_OK;
 }
 
@@ -402,7 +425,9 @@ GBFWN_API int gbfwn_from_vector(gbfwn_handle h, const float* pts, int64_t n, flo
     return runPoints(
         h, pts, n, out,
         [&](const float* dp, float* dout, cudaStream_t s) {
-            return launchVectorFwn(h->tree.q, dp, n, beta, skipFace, h->precise, dout, h->scratch, s);
+            const int32_t* order = nullptr;
+            cudaError_t oe = pointOrder(h, dp, n, s, &order);
+            return oe ? oe : launchVectorFwn(h->tree.q, dp, n, beta, skipFace, h->precise, dout, h->scratch, s, order);
         },
         cb, user, "gbfwn_from_vector");
 }
@@ -416,7 +441,9 @@ GBFWN_API int gbfwn_vector_with_distances(gbfwn_handle h, const float* pts, int6
     return runPoints(
         h, pts, n, out,
         [&](const float* dp, float* dout, cudaStream_t s) {
-            return launchVectorSdf(h->tree.q, dp, n, o, h->precise, dout, h->scratch, s);
+            const int32_t* order = nullptr;
+            cudaError_t oe = pointOrder(h, dp, n, s, &order);
+            return oe ? oe : launchVectorSdf(h->tree.q, dp, n, o, h->precise, dout, h->scratch, s, order);
         },
         cb, user, "gbfwn_vector_with_distances");
 }

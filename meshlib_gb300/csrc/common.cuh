@@ -94,10 +94,17 @@ cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTil
 // bz * ceil(nx/8) * ceil(ny/8)); voxels outside the bricks are not written.
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                                 float* out, const int32_t* bricks, int32_t nBricks, unsigned* scratch, cudaStream_t s);
+// Point queries; `order` (optional) is a permutation of [0, n): points are processed in that order
+// (mortonOrder gives a spatially coherent one) and results land at their original indices.
 cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,
-                            float* out, unsigned* scratch, cudaStream_t s);
+                            float* out, unsigned* scratch, cudaStream_t s, const int32_t* order = nullptr);
 cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, const DistOpts& o, int precise, float* out,
-                            unsigned* scratch, cudaStream_t s);
+                            unsigned* scratch, cudaStream_t s, const int32_t* order = nullptr);
+// Morton order of n points inside the box [lo, hi] (sort.cu); `scratch` holds mortonOrderScratch(n)
+// int32 words.
+int64_t mortonOrderScratch(int64_t n);
+cudaError_t mortonOrder(const float* pts, int64_t n, const float lo[3], const float hi[3], int32_t* order, int32_t* scratch,
+                        cudaStream_t s);
 cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise, uint64_t* bits, float* wn,
                                     unsigned* scratch, cudaStream_t s);
 

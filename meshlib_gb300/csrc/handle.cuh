@@ -61,6 +61,8 @@ struct gbfwn_mesh_s {
     size_t outCap = 0;
     void* inBuf = nullptr;
     size_t inCap = 0;
+    void* sortBuf = nullptr;  // Morton order + radix-sort scratch of point queries
+    size_t sortCap = 0;
     std::vector<cudaEvent_t> events;
     std::mutex mu;  // calls on one handle are serialised (the reference is not re-entrant per object)
 

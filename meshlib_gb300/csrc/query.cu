@@ -421,7 +421,8 @@ __global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange
 
 template <bool PRECISE, bool DIST>
 __global__ void __launch_bounds__(kThreads, 4) vectorKernel(QueryTree t, const float* __restrict__ pts, int64_t n, DistOpts o,
-                                                         int32_t skipFace, float* __restrict__ out, unsigned* scratch) {
+                                                         int32_t skipFace, float* __restrict__ out, unsigned* scratch,
+                                                         const int32_t* __restrict__ order) {
     const int lane = threadIdx.x & 31;
     const float betaSq = __fmul_rn(o.beta, o.beta);
     const int skipSlot = (skipFace >= 0 && skipFace < t.nFaces) ? t.faceSlot[skipFace] : -1;
@@ -429,8 +430,9 @@ __global__ void __launch_bounds__(kThreads, 4) vectorKernel(QueryTree t, const f
     for (;;) {
         const unsigned tile = nextTicket(scratch, lane);
         if (tile >= numTiles) break;
-        const int64_t i = int64_t(tile) * 32 + lane;
-        const bool active = i < n;
+        const int64_t r = int64_t(tile) * 32 + lane;  // rank in processing order
+        const bool active = r < n;
+        const int64_t i = (order && active) ? int64_t(order[r]) : r;
         float3 q = make_float3(0.f, 0.f, 0.f);
         if (active) q = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
         float res;
@@ -560,18 +562,19 @@ cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, 
 }
 
 cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,
-                            float* out, unsigned* scratch, cudaStream_t s) {
+                            float* out, unsigned* scratch, cudaStream_t s, const int32_t* order) {
     DistOpts o{0.f, FLT_MAX, 0, 0.5f, beta};
     const uint64_t tiles = (uint64_t(n) + 31) / 32;
-    if (precise) return launchPersistent(vectorKernel<true, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch);
-    return launchPersistent(vectorKernel<false, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch);
+    if (precise)
+        return launchPersistent(vectorKernel<true, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order);
+    return launchPersistent(vectorKernel<false, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order);
 }
 
 cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, const DistOpts& o, int precise, float* out,
-                            unsigned* scratch, cudaStream_t s) {
+                            unsigned* scratch, cudaStream_t s, const int32_t* order) {
     const uint64_t tiles = (uint64_t(n) + 31) / 32;
-    if (precise) return launchPersistent(vectorKernel<true, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch);
-    return launchPersistent(vectorKernel<false, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch);
+    if (precise) return launchPersistent(vectorKernel<true, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch, order);
+    return launchPersistent(vectorKernel<false, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch, order);
 }
 
 cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise, uint64_t* bits, float* wn,

@@ -310,3 +310,16 @@ def test_c1_config_parity(fwncls):
     assert err.max() <= 1e-5 * diag
     bad, near = _sign_ok(d, ref, wref)
     assert bad == 0
+
+
+def test_from_vector_large_ordered(fwncls, small_sphere):
+    """>= 8192 points are processed in Morton order and scattered back: same values as the oracle."""
+    v, f = small_sphere
+    rng = np.random.default_rng(9)
+    pts = rng.uniform(-1.3, 1.3, (30000, 3)).astype(np.float32)
+    g = fwncls(v, f, precise=False)
+    o = O.Oracle(v, f)
+    assert np.abs(g.calcFromVector(pts) - o.from_vector(pts)).max() <= WN_TOL
+    d = g.calcWithDistances(pts)
+    ref = o.vector_with_distances(pts, prec=1)
+    assert np.abs(np.abs(d) - np.abs(ref)).max() <= 1e-5 * mg.diag(v)
