@@ -187,6 +187,44 @@ def precision_vs_fp64(v, f, dims, xf, grid_out, shell, shell_d, n_grid=200_000, 
     return out
 
 
+def mrcuda_leg(v, f, dims, xf, ours, ours_ms, banded, timed, stream):
+    """The reference's signedDistanceKernel (MRCuda/MRCudaFastWindingNumber.cu:205-243, one thread
+    per voxel, 32 threads per block, -use_fast_math) on this GPU: unbanded (maxDistSq = inf) and with
+    the reference's banded request, plus how far its results are from ours."""
+    import torch
+
+    from oracle import mrcuda
+    if not mrcuda.kernels_present():
+        return {"unavailable": "reference kernels not built (needs the reference sources at build time)"}
+    import oracle as O
+    from meshlib_gb300 import meshgen as mg
+    t0 = time.perf_counter()
+    o = O.Oracle(v, f)
+    rk = mrcuda.RefKernels(v, f, o.nodes(), o.dipoles(0))
+    prep_s = time.perf_counter() - t0
+    nvox = int(np.prod(dims))
+    out_r = torch.empty(nvox, dtype=torch.float32, device="cuda")
+    plain_ms = timed(lambda: rk.signed_distance(dims, xf, out=out_r, stream=stream), 1)
+    diag = mg.diag(v)
+    both = torch.isfinite(out_r) & torch.isfinite(ours)
+    diff = (out_r.abs() - ours.abs()).abs()
+    res = {"kernel": "MR::Cuda::signedDistanceKernel (reference source, sm_103a, -O3 -DNDEBUG -use_fast_math)",
+           "tree": "reference CPU-built tree + FP32 dipoles (from the oracle, bit-identical to the reference's)",
+           "plain_ms": plain_ms, "plain_voxels_per_s": nvox / (plain_ms * 1e-3),
+           "ours_plain_speedup": plain_ms / ours_ms,
+           "max_abs_dist_diff_over_diag": float(diff[both].max().item()) / diag,
+           "sign_mismatches": int((torch.signbit(out_r) != torch.signbit(ours))[both].sum().item()),
+           "timing": "1 warm-up + 1 timed launch, L2 flushed before it", "host_prep_s": prep_s}
+    if banded is not None:
+        band = banded["band"]
+        bms = timed(lambda: rk.signed_distance(dims, xf, maxDistSq=band * band, out=out_r, stream=stream), 2)
+        res.update({"banded_ms": bms, "banded_voxels_per_s": nvox / (bms * 1e-3),
+                    "ours_plain_banded_speedup": bms / banded["plain_banded_ms"],
+                    "ours_surrogate_banded_speedup": bms / banded["surrogate_banded_ms"]})
+    del out_r
+    return res
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -222,6 +260,7 @@ def main():
     ap.add_argument("--no-banded", action="store_true", help="skip the banded / surrogate leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-mesh batched leg")
     ap.add_argument("--no-points", action="store_true", help="skip the shell-point / self-intersection leg")
+    ap.add_argument("--no-refgpu", action="store_true", help="skip timing the reference's own GPU kernels")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -327,6 +366,12 @@ def main():
                   "surrogate_config": "2M samples (50% uniform in box, 50% near surface), 1M validation, 3000 steps x 16384"}
         del sur
 
+    # ---- the reference's own GPU kernels (MRCuda signedDistanceKernel, built from the reference
+    # sources, fed the reference's CPU-built tree and dipoles) on the same GPU and grid
+    refgpu = None
+    if not args.no_refgpu and rank == 0:
+        refgpu = mrcuda_leg(v, f, dims, xf, out, ms_step, banded, timed, sp)
+
     # ---- points and faces on the same mesh: 4M shell points (|d| < 1e-3, calcFromVector and the
     # signed distance at points) and calcSelfIntersections after folding 1% of the faces inward
     points = None
@@ -410,7 +455,8 @@ def main():
             "e2e": {"value": e2e_val, "unit": "voxels/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                     "d2h_bytes_per_step": int(nvox * 4), "s_per_step": e2e_s,
                     "s_create_per_step": float(np.mean(create_times)) if create_times else None},
-            "clocks": clk.summary(), "nan_fraction": nan_frac, "wall_s_timed": wall, "banded": banded, "batched": batched, "points": points}
+            "clocks": clk.summary(), "nan_fraction": nan_frac, "wall_s_timed": wall, "banded": banded, "batched": batched, "points": points,
+            "reference_gpu": refgpu}
     if rank == 0 and not args.no_cpu:
         rate, thr, desc, counts = cpu_reference_rate(v, f, dims, xf)
         bpv = bytes_per_voxel(counts)

@@ -23,11 +23,14 @@ class Options(ctypes.Structure):
 
 
 def build(force: bool = False) -> str:
-    """Compiles the oracle with the host compiler (no FMA contraction, so FP32 follows the reference)."""
+    """Compiles the oracle with the host compiler (no FMA contraction, so FP32 follows the reference)
+    and the launcher of the reference's GPU kernels (oracle/mrcuda_runner.cpp)."""
     src = os.path.join(_HERE, "fwn_oracle.cpp")
     if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
                                "-o", _SO, src])
+    from . import mrcuda
+    mrcuda.build_runner(force)
     return _SO
 
 
