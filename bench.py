@@ -225,6 +225,30 @@ def mrcuda_leg(v, f, dims, xf, ours, ours_ms, banded, timed, stream):
     return res
 
 
+def mrcuda_projection_leg(v, f, dpp, ours_rec, ours_ms, timed, stream):
+    """The reference's GPU projector (MRCuda/MRCudaPointsToMeshProjector.cu:6-111, 640 threads per
+    block, FP32) on the same points, and how far its distances are from ours."""
+    import torch
+
+    from oracle import mrcuda
+    if not mrcuda.kernels_present():
+        return {"mrcuda_projection": "unavailable (reference kernels not built)"}
+    import oracle as O
+    from meshlib_gb300 import meshgen as mg
+    o = O.Oracle(v, f)
+    rk = mrcuda.RefKernels(v, f, o.nodes(), o.dipoles(0))
+    out = torch.empty_like(ours_rec)
+    ms = timed(lambda: rk.project(dpp, stream=stream, out=out), 1)
+    a = out.view(torch.float32).view(-1, 8)
+    b = ours_rec.view(torch.float32).view(-1, 8)
+    dd = (a[:, 7].double().sqrt() - b[:, 7].double().sqrt()).abs().max().item() / mg.diag(v)
+    same = (a[:, 0].view(torch.int32) == b[:, 0].view(torch.int32)).double().mean().item()
+    del out
+    return {"mrcuda_projection_ms": ms, "mrcuda_projection_points_per_s": dpp.numel() // 3 / (ms * 1e-3),
+            "projection_speedup_vs_mrcuda": ms / ours_ms, "projection_max_dist_diff_over_diag_vs_mrcuda": dd,
+            "projection_same_face_fraction_vs_mrcuda": same}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -401,6 +425,21 @@ def main():
                                "self-intersecting; the overlapping-spheres case exercises the flagged path",
                   "overlap_faces": len(of), "overlap_self_intersections_ms": osi_ms, "overlap_flagged_faces": oflag}
         del folded, bits, overl, obits
+        # points-to-mesh projection of the same 4M shell points plus 1M points uniform in the grid box
+        rng = np.random.default_rng(11)
+        lo_b, hi_b = v.min(0), v.max(0)
+        ppts = np.concatenate([shell, rng.uniform(lo_b - 0.1 * (hi_b - lo_b), hi_b + 0.1 * (hi_b - lo_b),
+                                                  (1_000_000, 3)).astype(np.float32)])
+        dpp = torch.from_numpy(ppts).cuda()
+        prec = torch.empty(32 * len(ppts), dtype=torch.uint8, device="cuda")
+        proj = M.PointsToMeshProjector.from_mesh(fwn)
+        proj_ms = timed(lambda: proj.findProjections_dev(dpp.data_ptr(), len(ppts), prec.data_ptr(), stream=sp), 3)
+        points.update({"projection_points": len(ppts), "projection_ms": proj_ms,
+                       "projection_points_per_s": len(ppts) / (proj_ms * 1e-3),
+                       "projection_note": "4M shell points + 1M uniform in the padded box, maxDist = inf"})
+        if rank == 0 and not args.no_refgpu:
+            points.update(mrcuda_projection_leg(v, f, dpp, prec, proj_ms, timed, sp))
+        del dpp, prec
 
     # ---- batched: 64 uneven meshes (triangles log-uniform in [5k, 500k], grid sides log-uniform in
     # [32, 192]) in one persistent launch vs 64 sequential single-mesh launches

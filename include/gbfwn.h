@@ -162,6 +162,36 @@ GBFWN_API int gbfwn_vector_with_distances(gbfwn_handle h, const float* pts, int6
 GBFWN_API int gbfwn_vector_with_distances_dev(gbfwn_handle h, const float* d_pts, int64_t n,
                                               const gbfwn_dist_opts* opts, float* d_out, void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Points-to-mesh projection, MR::IPointsToMeshProjector::findProjections
+ * (MRMesh/MRPointsToMeshProjector.h:11-30; CPU MRMesh/MRPointsToMeshProjector.cpp:17-32 over
+ * MRMesh/MRMeshProject.cpp:13-104; GPU MRCuda/MRCudaPointsToMeshProjector.cpp:53-126).
+ * One record per point, the memory layout of MR::MeshProjectionResult (MRMesh/MRMeshProject.h:17-31):
+ * the closest point on the mesh, its face (-1 when nothing lies closer than sqrt(upDistLimitSq)),
+ * its barycentric coordinates in that face's vertex order (point = (1-a-b) v0 + a v1 + b v2) and
+ * the squared distance.  `edge` is always -1: the caller's half-edge topology supplies
+ * edgeWithLeft(face), as the reference's GPU class does on the host (.cpp:117-123). */
+typedef struct gbfwn_projection {
+    int32_t face;
+    float point[3];
+    int32_t edge;
+    float bary[2];
+    float distSq;
+} gbfwn_projection;
+
+/* Projects n points (3 floats each).  objXf (12 floats, may be NULL) maps the points, refXf (may be
+ * NULL) maps the mesh; a rigid refXf is folded into the point map and a non-rigid one is applied to
+ * the mesh on the fly (MRMesh/MRMeshProject.cpp:105-121).  The search stops early for a point once a
+ * triangle within sqrt(loDistLimitSq) is found. */
+GBFWN_API int gbfwn_find_projections(gbfwn_handle h, const float* pts, int64_t n, const float* objXf, const float* refXf,
+                                     float upDistLimitSq, float loDistLimitSq, gbfwn_projection* out,
+                                     gbfwn_progress_cb cb, void* user);
+GBFWN_API int gbfwn_find_projections_dev(gbfwn_handle h, const float* d_pts, int64_t n, const float* objXf,
+                                         const float* refXf, float upDistLimitSq, float loDistLimitSq,
+                                         gbfwn_projection* d_out, void* stream);
+/* IPointsToMeshProjector::projectionsHeapBytes: device bytes a call on n points needs beyond the mesh. */
+GBFWN_API size_t gbfwn_projections_heap_bytes(int64_t n);
+
 /* IFastWindingNumberByParts::calcFromGridByParts / calcFromGridWithDistancesByParts
  * (MRMesh/MRFastWindingNumber.h:96-106; MRCuda/MRCudaFastWindingNumber.cpp:285-431): the grid is
  * produced in z-slabs of whole XY layers, consecutive slabs overlapping by `layerOverlap` layers,

@@ -130,6 +130,9 @@ _SIGS = [
     ("gbfwn_surrogate_gradients_dev", ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),
     ("gbfwn_from_grid_with_distances_banded_dev", ctypes.c_int,
      [_vp, _vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, ctypes.POINTER(_BandedStats), _vp]),
+    ("gbfwn_find_projections", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, PROGRESS, _vp]),
+    ("gbfwn_find_projections_dev", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, _vp]),
+    ("gbfwn_projections_heap_bytes", ctypes.c_size_t, [_i64]),
 ]
 EXPORTED = [s[0] for s in _SIGS]
 
@@ -366,6 +369,68 @@ class FastWindingNumber:
         """d_bits: ceil(faces / 64) 64-bit words; d_wn (optional): one float per face."""
         _check(self._L.gbfwn_self_intersections_dev(self._h, beta, ctypes.c_void_p(d_bits_ptr),
                                                     ctypes.c_void_p(d_wn_ptr or None), _stream(stream)))
+
+
+# MR::MeshProjectionResult (MRMesh/MRMeshProject.h:17-31) as returned per point by findProjections:
+# proj = PointOnFace {face, point}, mtp = MeshTriPoint {e, bary a, b} (e = -1: the caller's topology
+# gives edgeWithLeft(face)), distSq.
+PROJECTION_DTYPE = np.dtype([("face", np.int32), ("point", np.float32, 3), ("edge", np.int32), ("bary", np.float32, 2),
+                             ("distSq", np.float32)])
+assert PROJECTION_DTYPE.itemsize == 32
+
+
+class PointsToMeshProjector:
+    """GB300 implementation of ``MR::IPointsToMeshProjector`` (MRMesh/MRPointsToMeshProjector.h:11-30;
+    the reference's GPU class is MRCuda/MRCudaPointsToMeshProjector.{h,cpp,cu}).
+
+    ``updateMeshData(verts, faces)`` builds (or replaces) the device tree; ``findProjections`` returns
+    one ``PROJECTION_DTYPE`` record per point.  Transforms are 12 floats (3x3 rows, then translation)
+    or None, with the reference's meaning: ``objXf`` maps the points, ``refXf`` maps the mesh."""
+
+    def __init__(self, device: int = 0, precise: bool = True):
+        self.device = device
+        self.precise = precise
+        self._fwn: Optional[FastWindingNumber] = None
+
+    def updateMeshData(self, verts: Optional[np.ndarray], faces: Optional[np.ndarray] = None):
+        if self._fwn is not None:
+            self._fwn.close()
+            self._fwn = None
+        if verts is not None:
+            self._fwn = FastWindingNumber(verts, faces, device=self.device, precise=self.precise)
+
+    @classmethod
+    def from_mesh(cls, fwn: "FastWindingNumber") -> "PointsToMeshProjector":
+        """Shares the tree of an existing FastWindingNumber handle (the caller keeps it alive)."""
+        self = cls(precise=True)
+        self._fwn = fwn
+        return self
+
+    def findProjections(self, points: np.ndarray, objXf=None, refXf=None, upDistLimitSq: float = FLT_MAX,
+                        loDistLimitSq: float = 0.0, cb=None) -> np.ndarray:
+        if self._fwn is None:
+            raise FwnError(INVALID, "findProjections: no mesh (call updateMeshData first)")
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        out = np.empty(len(pts), PROJECTION_DTYPE)
+        ox = None if objXf is None else _xf12(objXf)
+        rx = None if refXf is None else _xf12(refXf)
+        c, _keep = _progress(cb)
+        L = self._fwn._L
+        _check(L.gbfwn_find_projections(self._fwn.handle, _p(pts), len(pts), _p(ox), _p(rx), upDistLimitSq, loDistLimitSq,
+                                        _p(out), c, None))
+        return out
+
+    def findProjections_dev(self, d_pts_ptr: int, n: int, d_out_ptr: int, objXf=None, refXf=None,
+                            upDistLimitSq: float = FLT_MAX, loDistLimitSq: float = 0.0, stream=None):
+        """Device pointers: n x 3 floats in, n x 32-byte records out (16-byte aligned)."""
+        ox = None if objXf is None else _xf12(objXf)
+        rx = None if refXf is None else _xf12(refXf)
+        _check(self._fwn._L.gbfwn_find_projections_dev(self._fwn.handle, ctypes.c_void_p(d_pts_ptr), n, _p(ox), _p(rx),
+                                                        upDistLimitSq, loDistLimitSq, ctypes.c_void_p(d_out_ptr),
+                                                        _stream(stream)))
+
+    def projectionsHeapBytes(self, numProjections: int) -> int:
+        return int(lib().gbfwn_projections_heap_bytes(numProjections))
 
 
 def memory_estimates(nv: int, nt: int, dims=None, npts: int = 0) -> dict:

@@ -15,10 +15,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbfwn.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden", "--expt-relaxed-constexpr"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden,-ffp-contract=off", "--expt-relaxed-constexpr"]
 # build.cu must round every float operation separately (bit-identical boxes and dipoles)
 PER_FILE = {"build.cu": ["-fmad=false"], "treebuild.cu": ["-fmad=false"]}
-SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "mlp_gemm.cu", "mlp_net.cu", "surrogate.cu", "batch.cu", "sort.cu"]
+SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "mlp_gemm.cu", "mlp_net.cu", "surrogate.cu", "batch.cu", "sort.cu",
+           "projector.cu"]
 
 
 def nvcc() -> str:

@@ -100,6 +100,11 @@ cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, flo
                             float* out, unsigned* scratch, cudaStream_t s, const int32_t* order = nullptr);
 cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, const DistOpts& o, int precise, float* out,
                             unsigned* scratch, cudaStream_t s, const int32_t* order = nullptr);
+// Closest point on the mesh for n points (MR::IPointsToMeshProjector::findProjections): each point is
+// mapped by pointXf (optional), the mesh by treeXf (optional; the non-rigid case).  out holds 2 float4
+// per point, the layout of MR::MeshProjectionResult: {face, x, y, z} {edge = -1, a, b, distSq}.
+cudaError_t launchProject(const QueryTree& t, const float* pts, int64_t n, const Xf* pointXf, const Xf* treeXf, float upSq,
+                          float loSq, int precise, float4* out, unsigned* scratch, cudaStream_t s, const int32_t* order = nullptr);
 // Morton order of n points inside the box [lo, hi] (sort.cu); `scratch` holds mortonOrderScratch(n)
 // int32 words.
 int64_t mortonOrderScratch(int64_t n);

@@ -284,10 +284,11 @@ __global__ void surrogateLowerBound(const float* __restrict__ pred, int n, float
 }
 
 // lower bound from the exact unsigned distance computed with maxDistSq = (band + radius)^2: NaN
-// (not finite) means the distance is at least band + radius
-__global__ void exactLowerBound(const float* __restrict__ d, int n, float cap, float* __restrict__ lb) {
+// (not finite) means the distance is at least band + radius, so the brick is out whatever the
+// rounding of (band + radius) - radius (+inf, not band + radius)
+__global__ void exactLowerBound(const float* __restrict__ d, int n, float* __restrict__ lb) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) lb[i] = isfinite(d[i]) ? fabsf(d[i]) : cap;
+    if (i < n) lb[i] = isfinite(d[i]) ? fabsf(d[i]) : INFINITY;
 }
 
 }  // namespace
@@ -625,7 +626,7 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
         const float cap = band + radius;
         const DistOpts co{0.f, cap * cap, 1, o.threshold, o.beta};
         if ((e = launchVectorSdf(t, centers, nb, co, precise, tmp, scratch, s))) return done(e);
-        exactLowerBound<<<nblk(nb, 256), 256, 0, s>>>(tmp, nb, cap, lb);
+        exactLowerBound<<<nblk(nb, 256), 256, 0, s>>>(tmp, nb, lb);
     }
     brickKeepKernel<<<nblk(nb, 256), 256, 0, s>>>(lb, nb, band, radius, keep);
     if ((e = exclusiveScanI32(keep, pos, nb, sums, total, s))) return done(e);

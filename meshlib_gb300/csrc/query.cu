@@ -226,6 +226,51 @@ __device__ __forceinline__ float obbDistSq(const float4& a, const float4& b, con
     return fmaf(dt, dt, fmaf(du, du, dn * dn));
 }
 
+// Affine map of a mesh-space point (rows of A, left-to-right dots, then + b: MRMesh/MRMatrix3.h:127-130).
+__device__ __forceinline__ float3 xfApply(const Xf& xf, float x, float y, float z) {
+    return make_float3(__fadd_rn(dot3rn(xf.a[0], xf.a[1], xf.a[2], x, y, z), xf.b[0]),
+                       __fadd_rn(dot3rn(xf.a[3], xf.a[4], xf.a[5], x, y, z), xf.b[1]),
+                       __fadd_rn(dot3rn(xf.a[6], xf.a[7], xf.a[8], x, y, z), xf.b[2]));
+}
+
+// Squared distance from p to the axis-aligned box around the image of a mesh-space box (centre c,
+// half extents h along the orthonormal axes d0, d1, d2) under the affine map xf: a lower bound of
+// the distance to anything inside that box once mapped.  The half extents get a relative margin
+// for the rounding of the mapped triangle vertices.
+__device__ __forceinline__ float mappedBoxDistSq(const Xf& xf, const float3& c, const float3& d0, const float3& d1,
+                                                 const float3& d2, const float3& h, const float3& p) {
+    float r = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a0 = xf.a[3 * k], a1 = xf.a[3 * k + 1], a2 = xf.a[3 * k + 2];
+        const float ck = fmaf(a0, c.x, fmaf(a1, c.y, fmaf(a2, c.z, xf.b[k])));
+        float hk = fabsf(fmaf(a0, d0.x, fmaf(a1, d0.y, a2 * d0.z))) * h.x + fabsf(fmaf(a0, d1.x, fmaf(a1, d1.y, a2 * d1.z))) * h.y +
+                   fabsf(fmaf(a0, d2.x, fmaf(a1, d2.y, a2 * d2.z))) * h.z;
+        hk += 4e-6f * (fabsf(ck) + hk + fabsf(xf.b[k])) + 1e-30f;
+        const float pk = k == 0 ? p.x : k == 1 ? p.y : p.z;
+        const float dk = fmaxf(fabsf(pk - ck) - hk, 0.f);
+        r = fmaf(dk, dk, r);
+    }
+    return r;
+}
+
+// obbDistSq for a tree seen through the affine map xf
+__device__ __forceinline__ float obbDistSqXf(const Xf& xf, const float4& a, const float4& b, const float4& c, const float4& e,
+                                            const float3& p) {
+    const float3 t = make_float3(a.x, a.y, a.z), u = make_float3(b.x, b.y, b.z), n = make_float3(c.x, c.y, c.z);
+    const float3 ctr = make_float3(fmaf(a.w, t.x, fmaf(b.w, u.x, c.w * n.x)), fmaf(a.w, t.y, fmaf(b.w, u.y, c.w * n.y)),
+                                   fmaf(a.w, t.z, fmaf(b.w, u.z, c.w * n.z)));
+    return mappedBoxDistSq(xf, ctr, t, u, n, make_float3(e.x, e.y, e.z), p);
+}
+
+// root box (axis-aligned, min/max) seen through xf
+__device__ __forceinline__ float rootBoxDistSqXf(const Xf& xf, const float4& mn, const float4& mx, const float3& p) {
+    const float3 c = make_float3(0.5f * (mn.x + mx.x), 0.5f * (mn.y + mx.y), 0.5f * (mn.z + mx.z));
+    const float3 h = make_float3(0.5f * (mx.x - mn.x), 0.5f * (mx.y - mn.y), 0.5f * (mx.z - mn.z));
+    const float3 h2 = make_float3(h.x + 1e-6f * (fabsf(c.x) + h.x), h.y + 1e-6f * (fabsf(c.y) + h.y), h.z + 1e-6f * (fabsf(c.z) + h.z));
+    return mappedBoxDistSq(xf, c, make_float3(1.f, 0.f, 0.f), make_float3(0.f, 1.f, 0.f), make_float3(0.f, 0.f, 1.f), h2, p);
+}
+
 template <typename T> struct V3T {
     T x, y, z;
 };
@@ -283,15 +328,29 @@ __device__ __forceinline__ float triDistSq(const float3& p, const float4& A, con
     return ds;
 }
 
-template <bool PRECISE>
+__device__ __forceinline__ float4 xf4(const Xf* xf, const float4& v) {
+    const float3 r = xfApply(*xf, v.x, v.y, v.z);
+    return make_float4(r.x, r.y, r.z, v.w);
+}
+
+// TRACK: remember the leaf slot of the best triangle in *best; TREEXF: the mesh is seen through
+// the affine map *txf (its triangle vertices are mapped before the distance, as the reference does
+// for a non-rigid tree transform, MRMesh/MRMeshProject.cpp:57-63).
+template <bool PRECISE, bool TRACK = false, bool TREEXF = false>
 __device__ __forceinline__ void leafDist(const QueryTree& t, int slot, const float3& q, bool go, float& resSq, bool& done,
-                                         float loSq) {
+                                         float loSq, int* best = nullptr, const Xf* txf = nullptr) {
     const float4* tr = t.tri + 3 * int64_t(slot);
-    const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+    float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
     if (go) {
+        if (TREEXF) {
+            A = xf4(txf, A);
+            B = xf4(txf, B);
+            C = xf4(txf, C);
+        }
         const float ds = triDistSq<PRECISE>(q, A, B, C);
         if (ds < resSq) {
             resSq = ds;
+            if (TRACK) *best = slot;
             if (ds <= loSq) done = true;
         }
     }
@@ -299,18 +358,20 @@ __device__ __forceinline__ void leafDist(const QueryTree& t, int slot, const flo
 
 // Closest squared distance from q to the mesh, starting from the bound upSq (the reference's
 // maxDistSq) and stopping once <= loSq; returns upSq when nothing is closer.
-template <bool PRECISE>
-__device__ float cpPacket(const QueryTree& t, const float3& q, bool active, float upSq, float loSq, unsigned* status) {
+template <bool PRECISE, bool TRACK = false, bool TREEXF = false>
+__device__ float cpPacket(const QueryTree& t, const float3& q, bool active, float upSq, float loSq, unsigned* status,
+                          int* best = nullptr, const Xf* txf = nullptr) {
     const int lane = threadIdx.x & 31;
     float resSq = upSq;
     bool done = !active;
     if (__ballot_sync(FULL, active) == 0 || t.nLeaves == 0) return resSq;
-    const bool inRoot = active && boxDistSq(t.rootBox0, t.rootBox1, q) < resSq;
+    const float rootD = TREEXF ? rootBoxDistSqXf(*txf, t.rootBox0, t.rootBox1, q) : boxDistSq(t.rootBox0, t.rootBox1, q);
+    const bool inRoot = active && rootD < resSq;
     const unsigned m0 = __ballot_sync(FULL, inRoot);
     if (!m0) return resSq;
     const int rootLink = __float_as_int(t.rootBox0.w);
     if (rootLink < 0) {
-        leafDist<PRECISE>(t, ~rootLink, q, inRoot, resSq, done, loSq);
+        leafDist<PRECISE, TRACK, TREEXF>(t, ~rootLink, q, inRoot, resSq, done, loSq, best, txf);
         return resSq;
     }
     WarpStack st;
@@ -326,12 +387,12 @@ __device__ float cpPacket(const QueryTree& t, const float3& q, bool active, floa
         int ll, rl;
         {
             const float4 a = ld4(rec), b = ld4(rec + 1), c = ld4(rec + 2), e = ld4(rec + 3);
-            dl = mine ? obbDistSq(a, b, c, e, q) : FLT_MAX;
+            dl = mine ? (TREEXF ? obbDistSqXf(*txf, a, b, c, e, q) : obbDistSq(a, b, c, e, q)) : FLT_MAX;
             ll = __float_as_int(e.w);
         }
         {
             const float4 a = ld4(rec + 4), b = ld4(rec + 5), c = ld4(rec + 6), e = ld4(rec + 7);
-            dr = mine ? obbDistSq(a, b, c, e, q) : FLT_MAX;
+            dr = mine ? (TREEXF ? obbDistSqXf(*txf, a, b, c, e, q) : obbDistSq(a, b, c, e, q)) : FLT_MAX;
             rl = __float_as_int(e.w);
         }
         const bool gl = mine && dl < resSq, gr = mine && dr < resSq;
@@ -347,8 +408,9 @@ __device__ float cpPacket(const QueryTree& t, const float3& q, bool active, floa
         const unsigned nearM = leftFirst ? ml : mr, farM = leftFirst ? mr : ml;
         const float nearD = leftFirst ? dl : dr, farD = leftFirst ? dr : dl;
         const bool nearGo = leftFirst ? gl : gr, farGo = leftFirst ? gr : gl;
-        if (nearM && nearLink < 0) leafDist<PRECISE>(t, ~nearLink, q, nearGo && !done, resSq, done, loSq);
-        if (farM && farLink < 0) leafDist<PRECISE>(t, ~farLink, q, farGo && !done && farD < resSq, resSq, done, loSq);
+        if (nearM && nearLink < 0) leafDist<PRECISE, TRACK, TREEXF>(t, ~nearLink, q, nearGo && !done, resSq, done, loSq, best, txf);
+        if (farM && farLink < 0)
+            leafDist<PRECISE, TRACK, TREEXF>(t, ~farLink, q, farGo && !done && farD < resSq, resSq, done, loSq, best, txf);
         if (farM && farLink >= 0 && !st.push(lane, farLink, farM)) overflow = true;
         if (nearM && nearLink >= 0 && !st.push(lane, nearLink, nearM)) overflow = true;
         (void)nearD;
@@ -446,6 +508,108 @@ __global__ void __launch_bounds__(kThreads, 4) vectorKernel(QueryTree t, const f
             res = fwnPacket<PRECISE>(t, q, active, betaSq, skipSlot, scratch + 1);
         }
         if (active) out[i] = res;
+    }
+}
+
+// Closest point with barycentric coordinates, FP64 (MRMesh/MRClosestPointInTriangle.h:28-91, in
+// double as MRMesh/MRMeshProject.cpp:66-72 calls it): proj = (1 - ba - bb) a + ba b + bb c.
+__device__ __noinline__ void closestPointBaryFp64(const float3 p, const float4 A, const float4 B, const float4 C, float3* proj,
+                                                  float* ba, float* bb) {
+    using V = V3T<double>;
+    const V pd{p.x, p.y, p.z}, a{A.x, A.y, A.z}, b{B.x, B.y, B.z}, c{C.x, C.y, C.z};
+    const V ab = vsub(b, a), ac = vsub(c, a), ap = vsub(pd, a);
+    V r;
+    double u = 0, w = 0;
+    const double d1 = vdot(ab, ap), d2 = vdot(ac, ap);
+    const V bp = vsub(pd, b);
+    const double d3 = vdot(ab, bp), d4 = vdot(ac, bp);
+    const V cp = vsub(pd, c);
+    const double d5 = vdot(ab, cp), d6 = vdot(ac, cp);
+    const double vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+    if (d1 <= 0 && d2 <= 0) {
+        r = a;
+    } else if (d3 >= 0 && d4 <= d3) {
+        r = b;
+        u = 1;
+    } else if (d6 >= 0 && d5 <= d6) {
+        r = c;
+        w = 1;
+    } else if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+        u = d1 / (d1 - d3);
+        r = vmad(a, u, ab);
+    } else if (vb <= 0 && d6 <= 0 && d2 >= 0) {
+        w = d2 / (d2 - d6);
+        r = vmad(a, w, ac);
+    } else if (va <= 0) {
+        if (d4 < d3) {
+            r = b;
+            u = 1;
+        } else if (d5 < d6) {
+            r = c;
+            w = 1;
+        } else {
+            const double v = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+            r = vmad(b, v, vsub(c, b));
+            u = 1 - v;
+            w = v;
+        }
+    } else {
+        const double denom = 1 / (va + vb + vc);
+        u = vb * denom;
+        w = vc * denom;
+        r = vmad(vmad(a, u, ab), w, ac);
+    }
+    *proj = make_float3(float(r.x), float(r.y), float(r.z));
+    *ba = float(u);
+    *bb = float(w);
+}
+
+// Points-to-mesh projection (MRMesh/MRPointsToMeshProjector.cpp:17-32 over MRMeshProject.cpp:13-104;
+// the GPU counterpart is MRCuda/MRCudaPointsToMeshProjector.cu:6-111).  Each point is mapped by pxf
+// (when given), the packet search finds the nearest triangle (FP32, FP64 near the surface in
+// precise mode), and the winner's projection, barycentrics and distance are recomputed in FP64 and
+// rounded as the reference CPU does.  Output per point, the layout of MR::MeshProjectionResult:
+// {face, proj.xyz} {edge = -1, bary a, bary b, distSq}; face = -1 when nothing lies closer than up.
+template <bool PRECISE, bool TREEXF>
+__global__ void __launch_bounds__(kThreads, 4) projectKernel(QueryTree t, const float* __restrict__ pts, int64_t n, Xf pxf,
+                                                          int hasPxf, Xf txf, float up, float lo, float4* __restrict__ out,
+                                                          unsigned* scratch, const int32_t* __restrict__ order) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t numTiles = (uint64_t(n) + 31) / 32;
+    for (;;) {
+        const unsigned tile = nextTicket(scratch, lane);
+        if (tile >= numTiles) break;
+        const int64_t r = int64_t(tile) * 32 + lane;
+        const bool active = r < n;
+        const int64_t i = (order && active) ? int64_t(order[r]) : r;
+        float3 q = make_float3(0.f, 0.f, 0.f);
+        if (active) {
+            q = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+            if (hasPxf) q = xfApply(pxf, q.x, q.y, q.z);
+        }
+        int best = -1;
+        const float dsq = cpPacket<PRECISE, true, TREEXF>(t, q, active, up, lo, scratch + 1, &best, &txf);
+        if (!active) best = -2;
+        float4 o0 = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f), o1 = make_float4(__int_as_float(-1), 0.f, 0.f, dsq);
+        if (best >= 0) {
+            const float4* tr = t.tri + 3 * int64_t(best);
+            float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+            if (TREEXF) {
+                A = xf4(&txf, A);
+                B = xf4(&txf, B);
+                C = xf4(&txf, C);
+            }
+            float3 pr;
+            float ba, bb;
+            closestPointBaryFp64(q, A, B, C, &pr, &ba, &bb);
+            const float dx = pr.x - q.x, dy = pr.y - q.y, dz = pr.z - q.z;
+            o0 = make_float4(A.w, pr.x, pr.y, pr.z);
+            o1 = make_float4(__int_as_float(-1), ba, bb, dot3rn(dx, dy, dz, dx, dy, dz));
+        }
+        if (active) {
+            out[2 * i] = o0;
+            out[2 * i + 1] = o1;
+        }
     }
 }
 
@@ -575,6 +739,22 @@ cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, con
     const uint64_t tiles = (uint64_t(n) + 31) / 32;
     if (precise) return launchPersistent(vectorKernel<true, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch, order);
     return launchPersistent(vectorKernel<false, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch, order);
+}
+
+cudaError_t launchProject(const QueryTree& t, const float* pts, int64_t n, const Xf* pointXf, const Xf* treeXf, float upSq,
+                          float loSq, int precise, float4* out, unsigned* scratch, cudaStream_t s, const int32_t* order) {
+    const uint64_t tiles = (uint64_t(n) + 31) / 32;
+    const Xf id{{1, 0, 0, 0, 1, 0, 0, 0, 1}, {0, 0, 0}};
+    const Xf px = pointXf ? *pointXf : id, tx = treeXf ? *treeXf : id;
+    const int hp = pointXf ? 1 : 0;
+    if (treeXf) {
+        if (precise)
+            return launchPersistent(projectKernel<true, true>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
+        return launchPersistent(projectKernel<false, true>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
+    }
+    if (precise)
+        return launchPersistent(projectKernel<true, false>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
+    return launchPersistent(projectKernel<false, false>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
 }
 
 cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise, uint64_t* bits, float* wn,

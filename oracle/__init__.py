@@ -61,6 +61,9 @@ def lib():
         L.orc_dist_sq.argtypes = [vp, vp, ctypes.c_int64, fp, fp, ip, vp]
         L.orc_traversal_counts.argtypes = [vp, vp, ctypes.c_int64, ctypes.POINTER(Options), vp]
         L.orc_exact_wn.argtypes = [vp, vp, ctypes.c_int64, ip, vp]
+        L.orc_find_projections.argtypes = [vp, vp, ctypes.c_int64, vp, vp, fp, fp, ip, vp]
+        L.orc_is_rigid.restype = ip
+        L.orc_is_rigid.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -160,6 +163,21 @@ class Oracle:
         self.L.orc_traversal_counts(self.h, _ptr(pts), len(pts), ctypes.byref(o), _ptr(out))
         return out
 
+    def find_projections(self, pts, objXf=None, refXf=None, upDistLimitSq=3.4028234663852886e38, loDistLimitSq=0.0,
+                         threads=None) -> np.ndarray:
+        """PointsToMeshProjector::findProjections (reference CPU arithmetic: FP64 leaf projection):
+        structured records (face, point[3], edge=-1, bary[2], distSq), the MeshProjectionResult layout."""
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+        dt = np.dtype([("face", np.int32), ("point", np.float32, 3), ("edge", np.int32), ("bary", np.float32, 2),
+                       ("distSq", np.float32)])
+        out = np.empty(len(pts), dt)
+        ox = None if objXf is None else np.ascontiguousarray(objXf, np.float32).reshape(12)
+        rx = None if refXf is None else np.ascontiguousarray(refXf, np.float32).reshape(12)
+        self.L.orc_find_projections(self.h, _ptr(pts), len(pts), _ptr(ox) if ox is not None else None,
+                                    _ptr(rx) if rx is not None else None, upDistLimitSq, loDistLimitSq,
+                                    threads or default_threads(), _ptr(out))
+        return out
+
     def exact_wn(self, pts, threads=None):
         pts = np.ascontiguousarray(pts, np.float32)
         out = np.empty(len(pts), np.float64)
@@ -177,6 +195,12 @@ def solid_angle_d(p, tri) -> float:
     p = np.ascontiguousarray(p, np.float64)
     tri = np.ascontiguousarray(tri, np.float64)
     return float(lib().orc_solid_angle_d(_ptr(p), _ptr(tri)))
+
+
+def is_rigid(xf) -> bool:
+    """MRMatrix3Decompose.h isRigid of the 3x3 part of a 12-float transform."""
+    x = np.ascontiguousarray(xf, np.float32).reshape(12)
+    return bool(lib().orc_is_rigid(_ptr(x)))
 
 
 def grid_points(dims, xf) -> np.ndarray:

@@ -404,6 +404,171 @@ static T findProjectionDistSq(const Mesh& m, const std::vector<Node>& nodes, con
     return resSq;
 }
 
+// ---------------------------------------------------------------- points-to-mesh projection
+// Affine map in float (MRAffineXf.h): rows of A, then b; x -> A x + b with left-to-right dots.
+struct AffF {
+    float A[3][3];
+    float b[3];
+};
+static AffF affFrom(const float* x) {
+    AffF r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.A[i][j] = x[3 * i + j];
+    for (int i = 0; i < 3; ++i) r.b[i] = x[9 + i];
+    return r;
+}
+static V3<float> apply(const AffF& x, V3<float> p) {
+    return {(x.A[0][0] * p.x + x.A[0][1] * p.y + x.A[0][2] * p.z) + x.b[0],
+            (x.A[1][0] * p.x + x.A[1][1] * p.y + x.A[1][2] * p.z) + x.b[1],
+            (x.A[2][0] * p.x + x.A[2][1] * p.y + x.A[2][2] * p.z) + x.b[2]};
+}
+// MRMatrix3Decompose.h:27-39 isRigid over MRMatrix3.h:272-294 qr (Gram-Schmidt on the columns)
+static bool affIsRigid(const AffF& x) {
+    V3<float> a0{x.A[0][0], x.A[1][0], x.A[2][0]}, a1{x.A[0][1], x.A[1][1], x.A[2][1]}, a2{x.A[0][2], x.A[1][2], x.A[2][2]};
+    const float r00 = length(a0);
+    const V3<float> e0 = r00 > 0 ? (1 / r00) * a0 : V3<float>{};
+    const float r01 = dot(e0, a1), r02 = dot(e0, a2);
+    a1 = a1 - r01 * e0;
+    const float r11 = length(a1);
+    const V3<float> e1 = r11 > 0 ? (1 / r11) * a1 : V3<float>{};
+    const float r12 = dot(e1, a2);
+    a2 = a2 - (r02 * e0 + r12 * e1);
+    const float r22 = length(a2);
+    const float eps = 10 * std::numeric_limits<float>::epsilon();
+    return std::abs(r00 - 1) <= eps && std::abs(r11 - 1) <= eps && std::abs(r22 - 1) <= eps;
+}
+// MRMatrix3.h:227-247 + MRAffineXf.h:51-57
+static AffF affInverse(const AffF& x) {
+    const auto& m = x.A;
+    const float det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                      m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    AffF r{};
+    if (det != 0) {
+        const float c[3][3] = {
+            {m[1][1] * m[2][2] - m[1][2] * m[2][1], m[0][2] * m[2][1] - m[0][1] * m[2][2], m[0][1] * m[1][2] - m[0][2] * m[1][1]},
+            {m[1][2] * m[2][0] - m[1][0] * m[2][2], m[0][0] * m[2][2] - m[0][2] * m[2][0], m[0][2] * m[1][0] - m[0][0] * m[1][2]},
+            {m[1][0] * m[2][1] - m[1][1] * m[2][0], m[0][1] * m[2][0] - m[0][0] * m[2][1], m[0][0] * m[1][1] - m[0][1] * m[1][0]}};
+        const float inv = 1 / det;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) r.A[i][j] = inv * c[i][j];
+    }
+    for (int i = 0; i < 3; ++i) r.b[i] = -(r.A[i][0] * x.b[0] + r.A[i][1] * x.b[1] + r.A[i][2] * x.b[2]);
+    return r;
+}
+// MRAffineXf.h:61-62: (u * v)(x) = u(v(x))
+static AffF affCompose(const AffF& u, const AffF& v) {
+    AffF r;
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) r.A[i][j] = u.A[i][0] * v.A[0][j] + u.A[i][1] * v.A[1][j] + u.A[i][2] * v.A[2][j];
+        r.b[i] = (u.A[i][0] * v.b[0] + u.A[i][1] * v.b[1] + u.A[i][2] * v.b[2]) + u.b[i];
+    }
+    return r;
+}
+// MRBox.h:336-344 transformed(box, xf): the box of the mapped corners
+static Box3f transformedBox(const Box3f& box, const AffF& xf) {
+    Box3f r;
+    for (int k = 0; k < 8; ++k)
+        r.include(apply(xf, V3<float>{(k & 1) ? box.max.x : box.min.x, (k & 2) ? box.max.y : box.min.y,
+                                       (k & 4) ? box.max.z : box.min.z}));
+    return r;
+}
+
+// MRClosestPointInTriangle.h:28-91 with the barycentric result: proj = (1 - a - b) A + a B + b C
+static void closestPointBary(const V3<double>& p, const V3<double>& a, const V3<double>& b, const V3<double>& c, V3<double>& proj,
+                             double& ba, double& bb) {
+    const V3<double> ab = b - a, ac = c - a, ap = p - a;
+    ba = bb = 0;
+    const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0 && d2 <= 0) { proj = a; return; }
+    const V3<double> bp = p - b;
+    const double d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0 && d4 <= d3) { proj = b; ba = 1; return; }
+    const V3<double> cp = p - c;
+    const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0 && d5 <= d6) { proj = c; bb = 1; return; }
+    const double vc = d1 * d4 - d3 * d2;
+    if (vc <= 0 && d1 >= 0 && d3 <= 0) { ba = d1 / (d1 - d3); proj = a + ba * ab; return; }
+    const double vb = d5 * d2 - d1 * d6;
+    if (vb <= 0 && d6 <= 0 && d2 >= 0) { bb = d2 / (d2 - d6); proj = a + bb * ac; return; }
+    const double va = d3 * d6 - d5 * d4;
+    if (va <= 0) {
+        if (d4 < d3) { proj = b; ba = 1; return; }
+        if (d5 < d6) { proj = c; bb = 1; return; }
+        const double v = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        proj = b + v * (c - b);
+        ba = 1 - v;
+        bb = v;
+        return;
+    }
+    const double denom = 1 / (va + vb + vc);
+    ba = vb * denom;
+    bb = vc * denom;
+    proj = a + ba * ab + bb * ac;
+}
+
+struct ProjRec {  // MR::MeshProjectionResult layout
+    int32_t face;
+    float px, py, pz;
+    int32_t edge;
+    float a, b;
+    float distSq;
+};
+static_assert(sizeof(ProjRec) == 32, "MeshProjectionResult layout");
+
+// MRMeshProject.cpp:13-104 findProjectionSubtree with an optional tree map (no region, no predicates)
+static ProjRec findProjectionRef(const Mesh& m, const std::vector<Node>& nodes, const V3<float>& pt, float upDistLimitSq,
+                                 const AffF* xf, float loDistLimitSq) {
+    ProjRec res{-1, 0, 0, 0, -1, 0, 0, upDistLimitSq};
+    if (nodes.empty()) return res;
+    struct SubTask {
+        int n;
+        float distSq;
+    };
+    SubTask st[64];
+    int sp = 0;
+    auto boxD = [&](int n) {
+        const Box3f b = xf ? transformedBox(nodes[n].box, *xf) : nodes[n].box;
+        return boxDistSq<float>(b, pt);
+    };
+    auto add = [&](const SubTask& s) {
+        if (s.distSq < res.distSq) st[sp++] = s;
+    };
+    add(SubTask{0, boxD(0)});
+    while (sp > 0) {
+        const SubTask s = st[--sp];
+        const Node& node = nodes[s.n];
+        if (s.distSq >= res.distSq) continue;
+        if (node.r < 0) {
+            V3<float> a, b, c;
+            m.tri(node.l, a, b, c);
+            if (xf) {
+                a = apply(*xf, a);
+                b = apply(*xf, b);
+                c = apply(*xf, c);
+            }
+            V3<double> projD;
+            double ba, bb;
+            closestPointBary(cvt<double>(pt), cvt<double>(a), cvt<double>(b), cvt<double>(c), projD, ba, bb);
+            const V3<float> proj = cvt<float>(projD);
+            const float distSq = lengthSq(proj - pt);
+            if (distSq < res.distSq) {
+                res = ProjRec{node.l, proj.x, proj.y, proj.z, -1, float(ba), float(bb), distSq};
+                if (res.distSq <= loDistLimitSq) break;
+            }
+            continue;
+        }
+        const SubTask s1{node.l, boxD(node.l)}, s2{node.r, boxD(node.r)};
+        if (s1.distSq < s2.distSq) {
+            add(s2);
+            add(s1);
+        } else {
+            add(s1);
+            add(s2);
+        }
+    }
+    return res;
+}
+
 struct Options {
     float minDistSq, maxDistSq;
     int nullOutsideMinMax;
@@ -644,5 +809,37 @@ void orc_exact_wn(void* h, const float* pts, int64_t n, int threads, double* out
         out[i] = s / (4 * 3.14159265358979323846);
     });
 }
+
+// PointsToMeshProjector::findProjections (MRPointsToMeshProjector.cpp:17-32) with the transform
+// simplification of createProjectionTransforms (MRMeshProject.cpp:105-121); objXf / refXf may be null.
+void orc_find_projections(void* h, const float* pts, int64_t n, const float* objXf, const float* refXf, float up, float lo,
+                          int threads, void* outv) {
+    auto* o = static_cast<Oracle*>(h);
+    auto* out = static_cast<ProjRec*>(outv);
+    AffF pointXf{}, treeXf{};
+    const AffF* pp = nullptr;
+    const AffF* tp = nullptr;
+    if (refXf && !affIsRigid(affFrom(refXf))) {
+        treeXf = affFrom(refXf);
+        tp = &treeXf;
+    }
+    if (tp || !refXf) {
+        if (objXf) {
+            pointXf = affFrom(objXf);
+            pp = &pointXf;
+        }
+    } else {
+        pointXf = affInverse(affFrom(refXf));
+        if (objXf) pointXf = affCompose(pointXf, affFrom(objXf));
+        pp = &pointXf;
+    }
+    parallelFor(size_t(n), threads, [&](size_t i) {
+        V3<float> q{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        if (pp) q = apply(*pp, q);
+        out[i] = findProjectionRef(o->mesh, o->nodes, q, up, tp, lo);
+    });
+}
+
+int orc_is_rigid(const float* xf) { return affIsRigid(affFrom(xf)) ? 1 : 0; }
 
 }  // extern "C"

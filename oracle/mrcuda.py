@@ -22,6 +22,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _SO = os.path.join(_HERE, "libmrcuda_runner.so")
 _CUBIN = os.path.join(_HERE, "_ref", "mrcuda_fwn.cubin")
 _PTX = os.path.join(_HERE, "_ref", "mrcuda_fwn.ptx")
+_PCUBIN = os.path.join(_HERE, "_ref", "mrcuda_proj.cubin")
+_PPTX = os.path.join(_HERE, "_ref", "mrcuda_proj.ptx")
 _lib = None
 
 
@@ -55,12 +57,37 @@ def _load(device: int):
         L.mrc_from_grid.argtypes = [vp, vp, ip, vp, vp, vp, vp, vp, fp, u64, u64, vp]
         L.mrc_from_vector.argtypes = [vp, vp, vp, vp, vp, vp, fp, ip, u64, vp]
         L.mrc_from_mesh.argtypes = [vp, vp, vp, vp, vp, fp, u64, u64, vp]
+        L.mrc_load_projector.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        L.mrc_project.argtypes = [vp, vp, vp, vp, vp, vp, vp, fp, fp, u64, vp]
         _lib = L
     r = _lib.mrc_load(_CUBIN.encode() if os.path.exists(_CUBIN) else b"", _PTX.encode() if os.path.exists(_PTX) else b"",
                       device)
     if r:
         raise RuntimeError("reference kernels: " + _lib.mrc_last_error().decode())
     return _lib
+
+
+def _fold(objXf, refXf, is_rigid):
+    """(point map, tree map) as MRCudaPointsToMeshProjector.cpp:75-102 derives them, in float64 -> float32
+    (the reference composes in float; the tests compare with tolerances)."""
+    def m(x):
+        x = np.asarray(x, np.float64).reshape(12)
+        A = np.eye(4)
+        A[:3, :3] = x[:9].reshape(3, 3)
+        A[:3, 3] = x[9:]
+        return A
+
+    def back(A):
+        return np.concatenate([A[:3, :3].reshape(-1), A[:3, 3]]).astype(np.float32)
+
+    if refXf is not None and not is_rigid(refXf):
+        return (None if objXf is None else np.asarray(objXf, np.float32)), np.asarray(refXf, np.float32)
+    if refXf is None:
+        return (None if objXf is None else np.asarray(objXf, np.float32)), None
+    A = np.linalg.inv(m(refXf))
+    if objXf is not None:
+        A = A @ m(objXf)
+    return back(A), None
 
 
 def _identity(xf) -> bool:
@@ -132,6 +159,30 @@ class RefKernels:
         s = stream if stream is not None else self.torch.cuda.current_stream(self.dev).cuda_stream
         self._check(self.L.mrc_from_vector(self._p(q), self._p(self.dipoles), self._p(self.nodes), self._p(self.points),
                                            self._p(self.faces), self._p(out), beta, skip_face, n, ctypes.c_void_p(s)))
+        return out
+
+    def project(self, pts, objXf=None, refXf=None, upDistLimitSq=3.4028234663852886e38, loDistLimitSq=0.0, stream=None,
+                out=None):
+        """The reference's GPU projector (MRCuda/MRCudaPointsToMeshProjector.cu:6-111) with its host
+        class's transform handling (.cpp:75-102): a rigid refXf is folded into the point map, a
+        non-rigid one is applied to the tree.  Returns a uint8 tensor of n x 32-byte records
+        (face, point xyz, edge = -1, bary a b, distSq)."""
+        from . import is_rigid
+        if not (os.path.exists(_PCUBIN) or os.path.exists(_PPTX)):
+            raise RuntimeError("reference projector kernel not built")
+        if self.L.mrc_load_projector(_PCUBIN.encode() if os.path.exists(_PCUBIN) else b"",
+                                     _PPTX.encode() if os.path.exists(_PPTX) else b""):
+            raise RuntimeError("reference projector: " + self.L.mrc_last_error().decode())
+        xf_pt, xf_tree = _fold(objXf, refXf, is_rigid)
+        q = pts if hasattr(pts, "data_ptr") else self.torch.from_numpy(np.ascontiguousarray(pts, np.float32).reshape(-1)).to(self.dev)
+        n = q.numel() // 3
+        out = out if out is not None else self.torch.empty(32 * n, dtype=self.torch.uint8, device=self.dev)
+        s = stream if stream is not None else self.torch.cuda.current_stream(self.dev).cuda_stream
+        a = None if xf_pt is None else np.ascontiguousarray(xf_pt, np.float32)
+        b = None if xf_tree is None else np.ascontiguousarray(xf_tree, np.float32)
+        self._check(self.L.mrc_project(self._p(q), self._p(self.nodes), self._p(self.points), self._p(self.faces), self._p(out),
+                                       a.ctypes.data if a is not None else None, b.ctypes.data if b is not None else None,
+                                       upDistLimitSq, loDistLimitSq, n, ctypes.c_void_p(s)))
         return out
 
     def from_mesh(self, beta=2.0, stream=None):

@@ -63,8 +63,8 @@ struct Driver {
     PModuleGetFunction getFunction = nullptr;
     PLaunch launch = nullptr;
     PErrorString errorString = nullptr;
-    CUmodule module = nullptr;
-    CUfunction sdf = nullptr, grid = nullptr, vec = nullptr, mesh = nullptr;
+    CUmodule module = nullptr, projModule = nullptr;
+    CUfunction sdf = nullptr, grid = nullptr, vec = nullptr, mesh = nullptr, proj = nullptr;
 };
 
 Driver g;
@@ -82,6 +82,23 @@ const char* kMesh =
     "_ZN2MR4Cuda31fastWindingNumberFromMeshKernelEPKNS0_6DipoleEPKNS0_5Node3EPK6float3PKNS0_16FaceToThreeVertsEPffmm";
 const char* kVec =
     "_ZN2MR4Cuda33fastWindingNumberFromVectorKernelEPK6float3PKNS0_6DipoleEPKNS0_5Node3ES3_PKNS0_16FaceToThreeVertsEPffim";
+
+// MRCuda/MRCudaPointsToMeshProjector.cu:6-111 (launched with 640 threads per block, .cu:113-120)
+const char* kProj =
+    "_ZN2MR4Cuda6kernelEPK6float3PKNS0_5Node3ES3_PKNS0_16FaceToThreeVertsEPNS0_20MeshProjectionResultENS0_7Matrix4ESC_ffm";
+
+Matrix4 matrix(const float* xf) {  // NULL -> Matrix4{} (identity flag set)
+    Matrix4 m{};
+    if (xf) {
+        std::memcpy(m.m, xf, sizeof(m.m));
+        m.isIdentity = false;
+    } else {
+        const float id[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+        std::memcpy(m.m, id, sizeof(id));
+        m.isIdentity = true;
+    }
+    return m;
+}
 
 int fail(const char* what, CUresult r) {
     const char* s = nullptr;
@@ -208,6 +225,37 @@ int mrc_from_mesh(const void* dipoles, const void* nodes, const void* points, co
     void* args[] = {&dipoles, &nodes, &points, &faces, &out, &beta, &cs, &co};
     const CUresult r = g.launch(g.mesh, blocks(chunkSize), 1, 1, 32, 1, 1, 0, CUstream(stream), args, nullptr);
     return r ? fail("fastWindingNumberFromMeshKernel launch", r) : 0;
+}
+
+// Loads the projection kernel (after mrc_load, which sets up the driver and the context).
+int mrc_load_projector(const char* cubin, const char* ptx) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g.projModule) return 0;
+    if (!g.module) {
+        std::snprintf(g_err, sizeof(g_err), "mrc_load must succeed first");
+        return -1;
+    }
+    CUmodule m = nullptr;
+    CUresult r = cubin && *cubin ? g.moduleLoad(&m, cubin) : CUDA_ERROR_FILE_NOT_FOUND;
+    if (r && ptx && *ptx) r = g.moduleLoad(&m, ptx);
+    if (r) return fail("cuModuleLoad (reference projector)", r);
+    if ((r = g.getFunction(&g.proj, m, kProj))) return fail("projector kernel", r);
+    g.projModule = m;
+    return 0;
+}
+
+// The reference's projection kernel: xf maps the points, refXf the tree (NULL = identity), as its host
+// class passes them after folding a rigid refXf into xf (MRCudaPointsToMeshProjector.cpp:75-102).
+// out: n records of 32 bytes (MeshProjectionResult).
+int mrc_project(const void* queries, const void* nodes, const void* points, const void* faces, void* out, const float* xf,
+                const float* refXf, float upDistLimitSq, float loDistLimitSq, uint64_t n, void* stream) {
+    if (!g.proj) return -1;
+    if (n == 0) return 0;
+    Matrix4 a = matrix(xf), b = matrix(refXf);
+    size_t sz = n;
+    void* args[] = {&queries, &nodes, &points, &faces, &out, &a, &b, &upDistLimitSq, &loDistLimitSq, &sz};
+    const CUresult r = g.launch(g.proj, unsigned((n + 639) / 640), 1, 1, 640, 1, 1, 0, CUstream(stream), args, nullptr);
+    return r ? fail("projector kernel launch", r) : 0;
 }
 
 }  // extern "C"

@@ -156,3 +156,61 @@ def test_mlp_oracle_gradients_finite_differences(monkeypatch):
         e[idx] = 1e-6
         fd = (MO.loss_and_grads(p + e, m, pts, t)[0] - MO.loss_and_grads(p - e, m, pts, t)[0]) / 2e-6
         assert abs(g[idx] - fd) <= 1e-6 + 1e-5 * abs(fd), (idx, g[idx], fd)
+
+
+def _brute_dist2(v, f, p):
+    """FP64 squared distance from p to every face (the reference's closestPointInTriangle)."""
+    out = np.empty(len(f))
+    pd = np.ascontiguousarray(p, np.float64)
+    for k, t in enumerate(f):
+        q = np.empty(3)
+        O.lib().orc_closest_point_d(pd.ctypes.data, np.ascontiguousarray(v[t].astype(np.float64)).ctypes.data, q.ctypes.data)
+        out[k] = float(((q - pd) ** 2).sum())
+    return out
+
+
+def test_projection_known_answers():
+    """One triangle: a point above the interior projects straight down with its barycentrics; a point
+    beyond a vertex lands on it (bary (1, 0) for the second vertex)."""
+    o = O.Oracle(TRI, np.array([[0, 1, 2]], np.int32))
+    r = o.find_projections(np.array([[0.25, 0.25, 2.0], [3.0, -1.0, 0.0]], np.float32))
+    assert r["face"].tolist() == [0, 0] and r["edge"].tolist() == [-1, -1]
+    assert np.allclose(r["point"][0], [0.25, 0.25, 0]) and np.allclose(r["bary"][0], [0.25, 0.25])
+    assert r["distSq"][0] == np.float32(4.0)
+    assert np.array_equal(r["point"][1], [1, 0, 0]) and np.array_equal(r["bary"][1], [1, 0])
+    assert r["distSq"][1] == np.float32(5.0)
+    # nothing closer than the upper limit: face -1 and distSq = the limit
+    r = o.find_projections(np.array([[0.25, 0.25, 2.0]], np.float32), upDistLimitSq=1.0)
+    assert r["face"][0] == -1 and r["distSq"][0] == np.float32(1.0)
+
+
+def test_projection_brute_force_and_transforms():
+    v, f = mg.noisy_icosphere(seed=1, level=2)
+    o = O.Oracle(v, f)
+    rng = np.random.default_rng(3)
+    pts = rng.uniform(-1.5, 1.5, (40, 3)).astype(np.float32)
+    r = o.find_projections(pts)
+    for i, p in enumerate(pts):
+        d = _brute_dist2(v, f, p)
+        assert abs(float(r["distSq"][i]) - d.min()) <= 1e-5 * d.min() + 1e-9
+        assert abs(d[r["face"][i]] - d.min()) <= 1e-9 * max(1.0, d.min())
+        a, b = r["bary"][i]
+        tri = v[f[r["face"][i]]].astype(np.float64)
+        assert np.allclose((1 - a - b) * tri[0] + a * tri[1] + b * tri[2], r["point"][i], atol=1e-5)
+    # a rigid mesh map folds into the points: projecting through refXf = projecting the mapped-back points
+    c, s = math.cos(0.7), math.sin(0.7)
+    rot = np.array([c, -s, 0, s, c, 0, 0, 0, 1, 0.3, -0.2, 0.5], np.float32)
+    assert O.is_rigid(rot)
+    r_rot = o.find_projections(pts, refXf=rot)
+    A, b = rot[:9].reshape(3, 3).astype(np.float64), rot[9:].astype(np.float64)
+    back = ((pts.astype(np.float64) - b) @ A).astype(np.float32)  # A^-1 = A^T
+    r_back = o.find_projections(back)
+    assert np.allclose(r_rot["distSq"], r_back["distSq"], rtol=1e-4, atol=1e-7)
+    # a non-rigid mesh map is applied to the mesh: same as projecting onto the mapped mesh
+    sc = np.array([1.3, 0.2, 0, 0, 0.8, 0, 0, 0, 1.1, 0.1, 0, 0], np.float32)
+    assert not O.is_rigid(sc)
+    r_sc = o.find_projections(pts, refXf=sc)
+    vm = (v.astype(np.float64) @ sc[:9].reshape(3, 3).T.astype(np.float64) + sc[9:]).astype(np.float32)
+    r_m = O.Oracle(vm, f).find_projections(pts)
+    assert np.allclose(r_sc["distSq"], r_m["distSq"], rtol=1e-4, atol=1e-7)
+    assert (r_sc["face"] == r_m["face"]).mean() > 0.9
