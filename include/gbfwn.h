@@ -97,6 +97,18 @@ GBFWN_API int gbfwn_create_dev(const float* d_verts, int64_t nv, const int32_t* 
 /* Frees the device data of the handle. */
 GBFWN_API int gbfwn_destroy(gbfwn_handle h);
 
+/* Moved vertices, same triangles: MR::AABBTree::refit (MRMesh/MRAABBTree.cpp:62-94) as
+ * MR::Mesh::updateCaches calls it (MRMesh/MRMesh.cpp:571-583), then the dipoles recomputed
+ * (updateCaches drops them; MRMesh/MRDipole.cpp:23-71 rebuilds them on the next query).  `verts`
+ * holds all nv vertices at their new positions; `changedVerts` (ceil(nv/64) little-endian 64-bit
+ * words, MeshLib's VertBitSet blocks; NULL = every vertex) marks the moved ones: the boxes of the
+ * faces around them and of every node above those are recomputed, the tree topology is kept (so
+ * queries may be slower than after a rebuild, as in the reference) and every query afterwards sees
+ * the new positions.  Synchronous; must not overlap with other calls on the handle.  The `_dev`
+ * variant takes device pointers (d_verts may be the handle's own vertex array). */
+GBFWN_API int gbfwn_refit(gbfwn_handle h, const float* verts, const uint64_t* changedVerts);
+GBFWN_API int gbfwn_refit_dev(gbfwn_handle h, const float* d_verts, const uint64_t* d_changedVerts, void* stream);
+
 /* Number of triangles (faces, valid or not) and of tree nodes (2 * valid - 1). */
 GBFWN_API int64_t gbfwn_num_faces(gbfwn_handle h);
 GBFWN_API int64_t gbfwn_num_nodes(gbfwn_handle h);

@@ -141,4 +141,42 @@ private:
     Result created_;
 };
 
+// GPU closest points on one mesh with the shape of MR::IPointsToMeshProjector
+// (MRMesh/MRPointsToMeshProjector.h:11-30).  It keeps the mesh's device tree between calls like
+// MR::Cuda::PointsToMeshProjector; results are gbfwn_projection records, the memory layout of
+// MR::MeshProjectionResult, with edge = -1 for the caller's topology to fill (edgeWithLeft(face)).
+class PointsToMeshProjector {
+public:
+    explicit PointsToMeshProjector(int device = 0) : device_(device) {}
+
+    // verts: nv x 3 floats; tris: nt x 3 vertex ids.  verts == nullptr forgets the mesh.
+    Result updateMeshData(const float* verts, int64_t nv, const int32_t* tris, int64_t nt) {
+        h_.reset();
+        if (!verts) return Result{};
+        gbfwn_handle h = nullptr;
+        Result r = Result::fromStatus(gbfwn_create(verts, nv, tris, nt, device_, &h));
+        h_.reset(h);
+        return r;
+    }
+
+    // objXf maps the points, refXf the mesh (12 floats each: 3x3 rows then translation; nullptr = none)
+    Result findProjections(std::vector<gbfwn_projection>& result, const std::vector<float>& points /* 3 per point */,
+                           const float* objXf = nullptr, const float* refXf = nullptr,
+                           float upDistLimitSq = 3.402823466e+38f, float loDistLimitSq = 0.f) {
+        if (!h_) return Result::fromStatus(GBFWN_INVALID);
+        result.resize(points.size() / 3);
+        return Result::fromStatus(gbfwn_find_projections(h_.get(), points.data(), int64_t(result.size()), objXf, refXf,
+                                                         upDistLimitSq, loDistLimitSq, result.data(), nullptr, nullptr));
+    }
+
+    size_t projectionsHeapBytes(size_t numProjections) const { return gbfwn_projections_heap_bytes(int64_t(numProjections)); }
+
+private:
+    struct Del {
+        void operator()(gbfwn_handle h) const { gbfwn_destroy(h); }
+    };
+    int device_;
+    std::unique_ptr<gbfwn_mesh_s, Del> h_;
+};
+
 }  // namespace gbfwn

@@ -130,6 +130,8 @@ _SIGS = [
     ("gbfwn_surrogate_gradients_dev", ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),
     ("gbfwn_from_grid_with_distances_banded_dev", ctypes.c_int,
      [_vp, _vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, ctypes.POINTER(_BandedStats), _vp]),
+    ("gbfwn_refit", ctypes.c_int, [_vp, _vp, _vp]),
+    ("gbfwn_refit_dev", ctypes.c_int, [_vp, _vp, _vp, _vp]),
     ("gbfwn_find_projections", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, PROGRESS, _vp]),
     ("gbfwn_find_projections_dev", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, _vp]),
     ("gbfwn_projections_heap_bytes", ctypes.c_size_t, [_i64]),
@@ -229,6 +231,25 @@ class FastWindingNumber:
 
     def set_precise(self, precise: bool):
         self._L.gbfwn_set_precise(self._h, 1 if precise else 0)
+
+    def refit(self, verts: np.ndarray, changedVerts: Optional[np.ndarray] = None):
+        """MR::AABBTree::refit + dipoles for moved vertices (same triangles).  ``changedVerts``: bool
+        array over vertices (None = all moved)."""
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        bits = None
+        if changedVerts is not None:
+            c = np.asarray(changedVerts, bool).reshape(-1)
+            words = (len(c) + 63) // 64
+            bits = np.zeros(words * 64, bool)
+            bits[:len(c)] = c
+            bits = np.packbits(bits, bitorder="little").view(np.uint64).copy()
+        _check(self._L.gbfwn_refit(self._h, _p(v), _p(bits)))
+        if self.verts is not None:
+            self.verts = v
+
+    def refit_dev(self, d_verts_ptr: int, d_changed_ptr: int = 0, stream=None):
+        _check(self._L.gbfwn_refit_dev(self._h, ctypes.c_void_p(d_verts_ptr), ctypes.c_void_p(d_changed_ptr or None),
+                                       _stream(stream)))
 
     def num_faces(self) -> int:
         return int(self._L.gbfwn_num_faces(self._h))

@@ -213,6 +213,93 @@ __global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const 
     dst[3] = make_float4(e[0], e[1], e[2], __int_as_float(link));
 }
 
+// ------------------------------------------------------------------------------------ refit
+// MRMesh/MRAABBTree.cpp:62-94 AABBTree::refit: leaves whose face touches a changed vertex get the
+// face box again (MRMesh/MRAABBTree.cpp:15-29 computeFaceBox, one ulp wider each way); every
+// internal node above a changed node becomes the union of its children.  Internal boxes are
+// recomputed here for all nodes: a node with no changed descendant already is that union, so the
+// result is the reference's node for node.
+__global__ void refitLeafKernel(RefNode* __restrict__ nodes, int64_t nNodes, const float* __restrict__ verts,
+                                const int32_t* __restrict__ tris, const uint64_t* __restrict__ changed, int64_t nv,
+                                int* __restrict__ arrive) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    arrive[i] = 0;
+    const RefNode nd = nodes[i];
+    if (nd.r >= 0) return;
+    const int32_t* t = tris + 3 * int64_t(nd.l);
+    if (changed) {
+        bool any = false;
+        for (int k = 0; k < 3; ++k) {
+            const int64_t v = t[k];
+            if (v >= 0 && v < nv && ((changed[v >> 6] >> (v & 63)) & 1ull)) any = true;
+        }
+        if (!any) return;
+    }
+    float mn[3], mx[3];
+    for (int d = 0; d < 3; ++d) {
+        float lo = FLT_MAX, hi = -FLT_MAX;
+        for (int k = 0; k < 3; ++k) {
+            const float x = verts[3 * int64_t(t[k]) + d];
+            if (x < lo) lo = x;
+            if (x > hi) hi = x;
+        }
+        mn[d] = nextafterf(lo, -FLT_MAX);
+        mx[d] = nextafterf(hi, FLT_MAX);
+    }
+    nodes[i] = RefNode{mn[0], mn[1], mn[2], mx[0], mx[1], mx[2], nd.l, nd.r};
+}
+
+// internal boxes bottom-up: the second child to arrive at a parent writes the union (MRBox.h:132-139)
+__global__ void refitUpKernel(RefNode* nodes, int64_t nNodes, const int32_t* __restrict__ parent, int* arrive) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    if (nodes[i].r >= 0) return;
+    int32_t p = parent[i];
+    while (p >= 0) {
+        __threadfence();
+        if (atomicAdd(&arrive[p], 1) == 0) return;
+        __threadfence();
+        volatile RefNode* vn = nodes;
+        const int32_t l = vn[p].l, r = vn[p].r;
+        float a[6], b[6];
+        a[0] = vn[l].minx; a[1] = vn[l].miny; a[2] = vn[l].minz; a[3] = vn[l].maxx; a[4] = vn[l].maxy; a[5] = vn[l].maxz;
+        b[0] = vn[r].minx; b[1] = vn[r].miny; b[2] = vn[r].minz; b[3] = vn[r].maxx; b[4] = vn[r].maxy; b[5] = vn[r].maxz;
+        for (int k = 0; k < 3; ++k) {
+            if (b[k] < a[k]) a[k] = b[k];
+            if (b[3 + k] > a[3 + k]) a[3 + k] = b[3 + k];
+        }
+        nodes[p] = RefNode{a[0], a[1], a[2], a[3], a[4], a[5], l, r};
+        p = parent[p];
+    }
+}
+
+// internal rank, leaf slot and leaf range of every node from the pre-order layout alone:
+// leafBefore = leaves before node i (exclusive scan of the leaf flags); a subtree's last leaf is
+// reached by following right children.
+__global__ void leafFlagKernel(const RefNode* __restrict__ nodes, int64_t nNodes, int32_t* __restrict__ flag) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < nNodes) flag[i] = nodes[i].r < 0 ? 1 : 0;
+}
+
+__global__ void ranksKernel(const RefNode* __restrict__ nodes, int64_t nNodes, const int32_t* __restrict__ leafBefore,
+                            int32_t* __restrict__ irs, int2* __restrict__ range) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    const int32_t first = leafBefore[i];
+    if (nodes[i].r < 0) {
+        irs[i] = -1;
+        irs[nNodes + i] = first;
+        range[i] = make_int2(first, 1);
+        return;
+    }
+    int32_t last = nodes[i].r;
+    while (nodes[last].r >= 0) last = nodes[last].r;
+    irs[i] = int32_t(i) - first;
+    irs[nNodes + i] = -1;
+    range[i] = make_int2(first, leafBefore[last] - first + 1);
+}
+
 __global__ void fillInt(int32_t* p, int64_t n, int32_t v) {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i < n) p[i] = v;
@@ -234,16 +321,17 @@ static cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, c
     const int64_t nNodes = out.nLeaves > 0 ? 2 * out.nLeaves - 1 : 0;
     cudaError_t e;
     int32_t *parent = nullptr, *arrive = nullptr;
-    if ((e = P.alloc((void**)&out.faceSlot, sizeof(int32_t) * size_t(std::max<int64_t>(out.nFaces, 1))))) return e;
+    // a refit passes the handle's existing arrays: only missing ones are allocated
+    if (!out.faceSlot && (e = P.alloc((void**)&out.faceSlot, sizeof(int32_t) * size_t(std::max<int64_t>(out.nFaces, 1))))) return e;
     fillInt<<<blocksFor(std::max<int64_t>(out.nFaces, 1), 256), 256, 0, s>>>(out.faceSlot, out.nFaces, -1);
     if (nNodes == 0) return cudaGetLastError();
-    if ((e = P.alloc((void**)&out.dip8, sizeof(float) * 8 * size_t(nNodes)))) return e;
+    if (!out.dip8 && (e = P.alloc((void**)&out.dip8, sizeof(float) * 8 * size_t(nNodes)))) return e;
     if ((e = T.alloc((void**)&parent, sizeof(int32_t) * size_t(nNodes)))) return e;
     if ((e = T.alloc((void**)&arrive, sizeof(int32_t) * size_t(nNodes)))) return e;
     const int64_t nInt = std::max<int64_t>(out.nInternal, 1);
-    if ((e = P.alloc((void**)&out.cp, sizeof(float4) * 8 * size_t(nInt)))) return e;
-    if ((e = P.alloc((void**)&out.dip, sizeof(float4) * 4 * size_t(nInt)))) return e;
-    if ((e = P.alloc((void**)&out.tri, sizeof(float4) * 3 * size_t(out.nLeaves)))) return e;
+    if (!out.cp && (e = P.alloc((void**)&out.cp, sizeof(float4) * 8 * size_t(nInt)))) return e;
+    if (!out.dip && (e = P.alloc((void**)&out.dip, sizeof(float4) * 4 * size_t(nInt)))) return e;
+    if (!out.tri && (e = P.alloc((void**)&out.tri, sizeof(float4) * 3 * size_t(out.nLeaves)))) return e;
     const unsigned B = blocksFor(nNodes, 256);
     leafDipolesKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, dVerts, dTris, out.dip8, arrive);
     parentsKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, parent);
@@ -255,17 +343,10 @@ static cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, c
     return cudaGetLastError();
 }
 
-cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, DeviceTree& out,
-                            Allocator& P, Allocator& T, cudaStream_t s, std::string& err) {
+// Query-tree pointers and the root data that travel in the kernels' parameter block.
+static cudaError_t setQueryRoot(DeviceTree& out, cudaStream_t s) {
     cudaError_t e;
-    int64_t nLeaves = 0;
-    int32_t* irs = nullptr;
-    int2* range = nullptr;
-    if ((e = gpuBuildTopology(dVerts, nv, dTris, nt, nLeaves, out.nodes, irs, range, P, T, s, err))) return e;
-    out.nFaces = nt;
-    out.nLeaves = nLeaves;
-    out.nInternal = nLeaves > 0 ? nLeaves - 1 : 0;
-    if ((e = finishDeviceTree(dVerts, dTris, irs, range, out, P, T, s))) return e;
+    const int64_t nLeaves = out.nLeaves;
     QueryTree& q = out.q;
     q.cp = out.cp;
     q.dip = out.dip;
@@ -288,6 +369,48 @@ cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTri
         q.rootBox1 = make_float4(r.maxx, r.maxy, r.maxz, 0.f);
     }
     return cudaStreamSynchronize(s);
+}
+
+cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, DeviceTree& out,
+                            Allocator& P, Allocator& T, cudaStream_t s, std::string& err) {
+    cudaError_t e;
+    int64_t nLeaves = 0;
+    int32_t* irs = nullptr;
+    int2* range = nullptr;
+    if ((e = gpuBuildTopology(dVerts, nv, dTris, nt, nLeaves, out.nodes, irs, range, P, T, s, err))) return e;
+    out.nFaces = nt;
+    out.nLeaves = nLeaves;
+    out.nInternal = nLeaves > 0 ? nLeaves - 1 : 0;
+    if ((e = finishDeviceTree(dVerts, dTris, irs, range, out, P, T, s))) return e;
+    return setQueryRoot(out, s);
+}
+
+cudaError_t refitDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, const uint64_t* dChanged, DeviceTree& out,
+                            Allocator& P, Allocator& T, cudaStream_t s) {
+    const int64_t nNodes = out.nLeaves > 0 ? 2 * out.nLeaves - 1 : 0;
+    if (nNodes == 0) return cudaSuccess;
+    cudaError_t e;
+    int32_t *parent = nullptr, *arrive = nullptr, *flag = nullptr, *before = nullptr, *sums = nullptr, *total = nullptr,
+            *irs = nullptr;
+    int2* range = nullptr;
+    if ((e = T.alloc((void**)&parent, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&arrive, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&flag, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&before, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&sums, sizeof(int32_t) * size_t(nNodes / 1024 + 2)))) return e;
+    if ((e = T.alloc((void**)&total, sizeof(int32_t)))) return e;
+    if ((e = T.alloc((void**)&irs, sizeof(int32_t) * 2 * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&range, sizeof(int2) * size_t(nNodes)))) return e;
+    const unsigned B = blocksFor(nNodes, 256);
+    parentsKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, parent);
+    refitLeafKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, dVerts, dTris, dChanged, nv, arrive);
+    refitUpKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, parent, arrive);
+    leafFlagKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, flag);
+    if ((e = exclusiveScanI32(flag, before, nNodes, sums, total, s))) return e;
+    ranksKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, before, irs, range);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = finishDeviceTree(dVerts, dTris, irs, range, out, P, T, s))) return e;
+    return setQueryRoot(out, s);
 }
 
 }  // namespace gbfwn

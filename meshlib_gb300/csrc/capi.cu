@@ -102,6 +102,14 @@ int newHandle(int device, gbfwn_mesh_s** out) {
     return GBFWN_OK;
 }
 
+int refitCommon(gbfwn_mesh_s* h, const uint64_t* dChanged, cudaStream_t s, const char* what) {
+    ListAllocator tmp;  // refit work arrays
+    cudaError_t e = refitDeviceTree(h->dVerts, h->nv, h->dTris, dChanged, h->tree, h->treeMem, tmp, s);
+    cudaStreamSynchronize(s);
+    tmp.freeAll();
+    return e ? cudaFail(e, what) : GBFWN_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -189,6 +197,34 @@ GBFWN_API int gbfwn_destroy(gbfwn_handle h) {
     }
     delete h;
     return GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_refit(gbfwn_handle h, const float* verts, const uint64_t* changedVerts) {
+    if (!h || (h->nv > 0 && !verts)) return fail(GBFWN_INVALID, "gbfwn_refit: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    cudaError_t e = h->nv ? cudaMemcpyAsync(h->dVerts, verts, sizeof(float) * 3 * size_t(h->nv), cudaMemcpyHostToDevice, h->stream)
+                          : cudaSuccess;
+    uint64_t* dBits = nullptr;
+    const size_t words = size_t((h->nv + 63) / 64);
+    if (!e && changedVerts && words) {
+        e = devMalloc((void**)&dBits, words * sizeof(uint64_t));
+        if (!e) e = cudaMemcpyAsync(dBits, changedVerts, words * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream);
+    }
+    const int st = e ? cudaFail(e, "gbfwn_refit") : refitCommon(h, changedVerts ? dBits : nullptr, h->stream, "gbfwn_refit");
+    if (dBits) cudaFree(dBits);
+    return st;
+}
+
+GBFWN_API int gbfwn_refit_dev(gbfwn_handle h, const float* d_verts, const uint64_t* d_changedVerts, void* stream) {
+    if (!h || (h->nv > 0 && !d_verts)) return fail(GBFWN_INVALID, "gbfwn_refit_dev: bad arguments");
+    std::lock_guard<std::mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    const cudaError_t e = (h->nv && d_verts != h->dVerts)
+                              ? cudaMemcpyAsync(h->dVerts, d_verts, sizeof(float) * 3 * size_t(h->nv), cudaMemcpyDeviceToDevice, s)
+                              : cudaSuccess;
+    return e ? cudaFail(e, "gbfwn_refit_dev") : refitCommon(h, d_changedVerts, s, "gbfwn_refit_dev");
 }
 
 GBFWN_API int64_t gbfwn_num_faces(gbfwn_handle h) { return h ? h->nt : 0; }

@@ -136,6 +136,12 @@ struct Allocator {
 cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, DeviceTree& out,
                             Allocator& P, Allocator& T, cudaStream_t s, std::string& err);
 
+// AABBTree::refit + dipole recomputation for moved vertices (build.cu): the tree keeps its
+// topology; dVerts holds all vertices at their new positions; dChanged (nv bits in 64-bit words,
+// nullable = all) marks the moved ones.  Reuses the tree's arrays; work arrays come from T.
+cudaError_t refitDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTris, const uint64_t* dChanged, DeviceTree& out,
+                            Allocator& P, Allocator& T, cudaStream_t s);
+
 int numSMs();
 
 // Exclusive prefix sum of n int32 values (treebuild.cu); `sums` holds ceil(n / 1024) + 1 words of

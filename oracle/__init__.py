@@ -62,6 +62,7 @@ def lib():
         L.orc_traversal_counts.argtypes = [vp, vp, ctypes.c_int64, ctypes.POINTER(Options), vp]
         L.orc_exact_wn.argtypes = [vp, vp, ctypes.c_int64, ip, vp]
         L.orc_find_projections.argtypes = [vp, vp, ctypes.c_int64, vp, vp, fp, fp, ip, vp]
+        L.orc_refit.argtypes = [vp, vp, vp]
         L.orc_is_rigid.restype = ip
         L.orc_is_rigid.argtypes = [vp]
         _lib = L
@@ -177,6 +178,18 @@ class Oracle:
                                     _ptr(rx) if rx is not None else None, upDistLimitSq, loDistLimitSq,
                                     threads or default_threads(), _ptr(out))
         return out
+
+    def refit(self, verts, changed=None):
+        """AABBTree::refit + dipoles for moved vertices; changed: bool array over vertices or None (all)."""
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        assert v.shape == self.verts.shape
+        bits = None
+        if changed is not None:
+            c = np.asarray(changed, bool).reshape(-1)
+            b = np.zeros(((len(c) + 63) // 64) * 64, bool)
+            b[:len(c)] = c
+            bits = np.packbits(b, bitorder="little").view(np.uint64).copy()
+        self.L.orc_refit(self.h, _ptr(v), _ptr(bits) if bits is not None else None)
 
     def exact_wn(self, pts, threads=None):
         pts = np.ascontiguousarray(pts, np.float32)

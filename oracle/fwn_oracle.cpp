@@ -842,4 +842,32 @@ void orc_find_projections(void* h, const float* pts, int64_t n, const float* obj
 
 int orc_is_rigid(const float* xf) { return affIsRigid(affFrom(xf)) ? 1 : 0; }
 
+// AABBTree::refit (MRAABBTree.cpp:62-94) after the vertices moved, then the dipoles again (Mesh::updateCaches
+// drops them, MRMesh.cpp:571-583).  changed: nv bits in 64-bit words, or null for all vertices.
+void orc_refit(void* h, const float* verts, const uint64_t* changed) {
+    auto* o = static_cast<Oracle*>(h);
+    std::copy(verts, verts + o->verts.size(), o->verts.begin());
+    auto moved = [&](int v) { return !changed || ((changed[v >> 6] >> (v & 63)) & 1ull); };
+    std::vector<char> changedNode(o->nodes.size(), 0);
+    for (size_t nid = 0; nid < o->nodes.size(); ++nid) {
+        Node& node = o->nodes[nid];
+        if (node.r >= 0) continue;
+        const int f = node.l;
+        const int32_t* t = o->mesh.tris + 3 * size_t(f);
+        if (!(moved(t[0]) || moved(t[1]) || moved(t[2]))) continue;
+        changedNode[nid] = 1;
+        node.box = computeFaceBox(o->mesh, f);
+    }
+    for (int64_t nid = int64_t(o->nodes.size()) - 1; nid >= 0; --nid) {  // NodeId 0 is valid: the root is included
+        Node& node = o->nodes[nid];
+        if (node.r < 0) continue;
+        if (!changedNode[node.l] && !changedNode[node.r]) continue;
+        changedNode[nid] = 1;
+        node.box = o->nodes[node.l].box;
+        node.box.include(o->nodes[node.r].box);
+    }
+    calcDipoles<float>(o->mesh, o->nodes, o->dipF);
+    calcDipoles<double>(o->mesh, o->nodes, o->dipD);
+}
+
 }  // extern "C"

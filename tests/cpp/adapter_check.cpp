@@ -68,7 +68,25 @@ int main() {
     // cancellation through the progress callback
     std::vector<float> tmp;
     auto c = fwn.calcFromGrid(tmp, dims, xf, 2.f, [](float p) { return p < 0.5f; });
-    std::printf("OK sum_sd=%.6f sum_wn=%.6f neg=%d parts_equal=%d selfint=%d cancel_status=%d\n", sumSd, sumWn, neg, same,
-                nbits, c.status());
+    // closest points through the projector adapter: the grid's voxel centres
+    gbfwn::PointsToMeshProjector proj;
+    if (auto pr = proj.updateMeshData(verts.data(), int64_t(verts.size() / 3), tris.data(), int64_t(tris.size() / 3)); !pr) {
+        std::printf("ERROR projector %s\n", pr.error().c_str());
+        return 1;
+    }
+    std::vector<float> pts;
+    for (int z = 0; z < dims[2]; ++z)
+        for (int y = 0; y < dims[1]; ++y)
+            for (int x = 0; x < dims[0]; ++x)
+                pts.insert(pts.end(), {xf[0] * x + xf[9], xf[4] * y + xf[10], xf[8] * z + xf[11]});
+    std::vector<gbfwn_projection> pj;
+    if (auto pr = proj.findProjections(pj, pts); !pr) {
+        std::printf("ERROR project %s\n", pr.error().c_str());
+        return 1;
+    }
+    double maxDiff = 0;
+    for (size_t i = 0; i < pj.size(); ++i) maxDiff = std::fmax(maxDiff, std::fabs(std::sqrt(double(pj[i].distSq)) - std::fabs(sd[i])));
+    std::printf("OK sum_sd=%.6f sum_wn=%.6f neg=%d parts_equal=%d selfint=%d cancel_status=%d proj_max_diff=%.3g\n", sumSd, sumWn,
+                neg, same, nbits, c.status(), maxDiff);
     return 0;
 }

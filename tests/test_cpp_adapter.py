@@ -47,3 +47,5 @@ def test_adapter_matches_python(tmp_path):
     assert kv["parts_equal"] == "1"
     assert int(kv["selfint"]) == 0
     assert int(kv["cancel_status"]) == M.CANCELLED
+    # projector adapter: closest-point distances equal |signed distance| at the same points
+    assert float(kv["proj_max_diff"]) < 1e-5

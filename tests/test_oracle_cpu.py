@@ -214,3 +214,30 @@ def test_projection_brute_force_and_transforms():
     r_m = O.Oracle(vm, f).find_projections(pts)
     assert np.allclose(r_sc["distSq"], r_m["distSq"], rtol=1e-4, atol=1e-7)
     assert (r_sc["face"] == r_m["face"]).mean() > 0.9
+
+
+def test_refit_keeps_topology_and_bounds():
+    """AABBTree::refit (MRAABBTree.cpp:62-94): same topology, every leaf box holds its moved face
+    (one ulp wider), every internal box is the union of its children, distances equal a rebuild's."""
+    v, f = mg.noisy_icosphere(seed=4, level=3)
+    o = O.Oracle(v, f)
+    before = o.nodes().copy()
+    rng = np.random.default_rng(2)
+    moved = rng.random(len(v)) < 0.3
+    v2 = v.copy()
+    v2[moved] += rng.normal(scale=0.05, size=(int(moved.sum()), 3)).astype(np.float32)
+    o.refit(v2, moved)
+    after = o.nodes()
+    assert np.array_equal(after["l"], before["l"]) and np.array_equal(after["r"], before["r"])
+    leaf = after["r"] < 0
+    tri = v2[f[after["l"][leaf]]]
+    assert (after["min"][leaf] < tri.min(1)).all() and (after["max"][leaf] > tri.max(1)).all()
+    inner = np.flatnonzero(~leaf)
+    l, r = after["l"][inner], after["r"][inner]
+    assert np.array_equal(after["min"][inner], np.minimum(after["min"][l], after["min"][r]))
+    assert np.array_equal(after["max"][inner], np.maximum(after["max"][l], after["max"][r]))
+    # untouched faces keep their boxes
+    touched = moved[f[after["l"][leaf]]].any(1)
+    assert np.array_equal(after["min"][leaf][~touched], before["min"][leaf][~touched])
+    pts = rng.uniform(-1.4, 1.4, (200, 3)).astype(np.float32)
+    assert np.allclose(o.dist_sq(pts), O.Oracle(v2, f).dist_sq(pts), rtol=1e-6, atol=1e-9)
