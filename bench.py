@@ -148,6 +148,17 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 KERNEL_DRAM_BYTES_512 = 1_044_935_936 + 507_725_312
 
 
+# FMA-pipe utilisation of the signed-distance grid kernel from the committed ncu capture
+# (profiles/gridKernel_sdf_256cubed_icosphere1.3M.md: sm__pipe_fma_cycles_active)
+KERNEL_FMA_PIPE_ACTIVE = 0.267
+
+
+def flop_per_voxel(c):
+    # FP32 operations of the reference traversal per voxel: box test 9, closest point in triangle
+    # 40, dipole term 12 + sqrt + div, solid angle 45 + atan2 (one count per special function)
+    return 9 * c["cp_nodes"] + 40 * c["cp_leaves"] + 14 * c["fwn_nodes"] + 46 * c["fwn_leaves"]
+
+
 def bytes_per_voxel(c):
     # 4 (output) + 32 per AABB node + 32 per dipole + 48 per leaf triangle (3 ids + 3 vertices)
     return 4 + 32 * c["cp_nodes"] + 32 * c["fwn_nodes"] + 48 * (c["cp_leaves"] + c["fwn_leaves"])
@@ -508,6 +519,20 @@ def main():
                                     "(bytes_per_voxel); the warp-packet traversal reads each record once per 32 voxels "
                                     "from L1/L2, so actual DRAM traffic (traffic) is ~1.5 GB per launch and the kernel is "
                                     "issue/latency-bound, not HBM-bound"}
+        try:
+            fp32_peak = M.fp32_peak_tflops(local)
+        except Exception as ex:  # measurement support only; the line stays valid without it
+            fp32_peak = None
+            print(f"fp32 peak: {ex}", file=sys.stderr)
+        fpv = flop_per_voxel(counts)
+        ref_tf = fpv * nvox / (ms_step * 1e-3) / 1e12
+        line["fp32"] = {"peak_tflops": fp32_peak, "peak_source": "own FMA microbenchmark (gbfwn_debug_fp32_peak)",
+                        "flop_per_voxel_reference_traversal": fpv, "reference_equiv_tflops": ref_tf,
+                        "reference_equiv_frac": (ref_tf / fp32_peak) if fp32_peak else None,
+                        "fma_pipe_active_ncu": KERNEL_FMA_PIPE_ACTIVE,
+                        "note": "reference-equivalent FLOP/s counts the reference traversal's box tests, projections, "
+                                "dipoles and solid angles per voxel; the packet traversal does far fewer, and ncu shows the "
+                                "FMA pipe 27% busy: the kernel is bound by instruction issue and dependent loads"}
         line["cpu_baseline"] = {"value": rate, "unit": "voxels/s", "cores": thr, "kind": "port", "sample": desc}
         line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d)
     if rank == 0:

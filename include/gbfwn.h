@@ -224,6 +224,10 @@ GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t di
 GBFWN_API size_t gbfwn_from_vector_memory(int64_t nv, int64_t nt, int64_t npts);
 GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt);
 
+/* No counterpart in the reference: measured FP32 FMA throughput of `device` in TFLOP/s (best of
+ * `reps` launches), the denominator of the traversal kernels' FP32-op fraction in the benchmark. */
+GBFWN_API int gbfwn_debug_fp32_peak(int device, int reps, double* tflops);
+
 /* ---------------------------------------------------------------------------------------------
  * Learned band culling (no counterpart in the reference).  A small per-mesh network predicts the
  * signed distance; bricks of 8x8x8 voxels whose predicted |d|, less a validated error margin and

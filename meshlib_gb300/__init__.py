@@ -135,6 +135,7 @@ _SIGS = [
     ("gbfwn_find_projections", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, PROGRESS, _vp]),
     ("gbfwn_find_projections_dev", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, _vp]),
     ("gbfwn_projections_heap_bytes", ctypes.c_size_t, [_i64]),
+    ("gbfwn_debug_fp32_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
 ]
 EXPORTED = [s[0] for s in _SIGS]
 
@@ -452,6 +453,13 @@ class PointsToMeshProjector:
 
     def projectionsHeapBytes(self, numProjections: int) -> int:
         return int(lib().gbfwn_projections_heap_bytes(numProjections))
+
+
+def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
+    """Measured FP32 FMA throughput of the GPU (TFLOP/s)."""
+    t = ctypes.c_double()
+    _check(lib().gbfwn_debug_fp32_peak(device, reps, ctypes.byref(t)))
+    return float(t.value)
 
 
 def memory_estimates(nv: int, nt: int, dims=None, npts: int = 0) -> dict:

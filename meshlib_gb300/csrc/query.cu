@@ -431,7 +431,12 @@ struct TileGrid {
     // (2 x 2 x 4 tiles of 4x4x2) per brick
     const int32_t* bricks;
     int32_t bricksX, bricksY;
+    // work items: columns of up to kSeg tiles along z (4 per brick: its 2 x 2 columns)
+    int32_t segsZ;
+    uint32_t numItems;
 };
+
+constexpr int kSeg = 8;  // tiles along z walked by one warp in turn
 
 __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
     unsigned t = 0;
@@ -439,6 +444,11 @@ __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
     return __shfl_sync(FULL, t, 0);
 }
 
+// A warp takes a column of tiles along z and walks it upwards; each lane starts its closest-point
+// search from the triangle that was closest to its voxel two layers below (the same lane of the
+// previous tile).  That triangle's distance is an upper bound the search would reach anyway, so the
+// minimum is unchanged, but it prunes from the first step (a third fewer node visits with an exact
+// bound, in a CPU model of the walk).
 template <bool PRECISE, bool DIST>
 __global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
                                                        float* __restrict__ out, unsigned* scratch) {
@@ -447,37 +457,52 @@ __global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange
     const float betaSq = __fmul_rn(o.beta, o.beta);
     const size_t sxy = size_t(g.nx) * g.ny;
     for (;;) {
-        const unsigned tile = nextTicket(scratch, lane);
-        if (tile >= tg.numTiles) break;
-        int x, y, z;
+        const unsigned item = nextTicket(scratch, lane);
+        if (item >= tg.numItems) break;
+        int x0, y0, zBase, nSeg;
         if (tg.bricks) {
-            const int b = tg.bricks[tile >> 4], sub = int(tile & 15u);
+            const int b = tg.bricks[item >> 2], col = int(item & 3u);
             const int bx = b % tg.bricksX, by = (b / tg.bricksX) % tg.bricksY, bz = b / (tg.bricksX * tg.bricksY);
-            x = bx * 8 + (sub & 1) * kTX + lx;
-            y = by * 8 + ((sub >> 1) & 1) * kTY + ly;
-            z = g.z0 + bz * 8 + (sub >> 2) * kTZ + lz;
+            x0 = bx * 8 + (col & 1) * kTX;
+            y0 = by * 8 + (col >> 1) * kTY;
+            zBase = g.z0 + bz * 8;
+            nSeg = 4;
         } else {
-            const int tx = int(tile % unsigned(tg.tilesX));
-            const unsigned rest = tile / unsigned(tg.tilesX);
+            const int tx = int(item % unsigned(tg.tilesX));
+            const unsigned rest = item / unsigned(tg.tilesX);
             const int ty = int(rest % unsigned(tg.tilesY));
-            const int tz = int(rest / unsigned(tg.tilesY));
-            x = tx * kTX + lx;
-            y = ty * kTY + ly;
-            z = g.z0 + tz * kTZ + lz;
+            const int sz = int(rest / unsigned(tg.tilesY));
+            x0 = tx * kTX;
+            y0 = ty * kTY;
+            zBase = g.z0 + sz * kSeg * kTZ;
+            nSeg = min(kSeg, tg.tilesZ - sz * kSeg);
         }
-        const bool active = x < g.nx && y < g.ny && z < g.z1;
-        const float3 q = xfPoint(xf, x, y, z);
-        float res;
-        if (DIST) {
-            const float dsq = cpPacket<PRECISE>(t, q, active, o.maxDistSq, o.minDistSq, scratch + 1);
-            const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
-            const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
-            const float d = __fsqrt_rn(dsq);
-            res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
-        } else {
-            res = fwnPacket<PRECISE>(t, q, active, betaSq, -1, scratch + 1);
+        const int x = x0 + lx, y = y0 + ly;
+        int seed = -1;  // leaf slot closest to this lane's previous voxel
+        for (int j = 0; j < nSeg; ++j) {
+            const int z = zBase + j * kTZ + lz;
+            const bool active = x < g.nx && y < g.ny && z < g.z1;
+            const float3 q = xfPoint(xf, x, y, z);
+            float res;
+            if (DIST) {
+                float up = o.maxDistSq;
+                if (active && seed >= 0) {
+                    const float4* tr = t.tri + 3 * int64_t(seed);
+                    const float ds = triDistSq<PRECISE>(q, ld4(tr), ld4(tr + 1), ld4(tr + 2));
+                    if (ds < up) up = ds;
+                }
+                int best = active ? seed : -1;
+                const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
+                seed = best;
+                const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
+                const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
+                const float d = __fsqrt_rn(dsq);
+                res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+            } else {
+                res = fwnPacket<PRECISE>(t, q, active, betaSq, -1, scratch + 1);
+            }
+            if (active) out[size_t(z - g.zOut) * sxy + size_t(y) * g.nx + x] = res;
         }
-        if (active) out[size_t(z - g.zOut) * sxy + size_t(y) * g.nx + x] = res;
     }
 }
 
@@ -693,6 +718,8 @@ static TileGrid tileGridFor(const GridRange& g) {
     tg.numTiles = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.tilesZ);
     tg.bricks = nullptr;
     tg.bricksX = tg.bricksY = 0;
+    tg.segsZ = (tg.tilesZ + kSeg - 1) / kSeg;
+    tg.numItems = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.segsZ);
     return tg;
 }
 
@@ -703,9 +730,10 @@ cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf
     tg.bricksX = (g.nx + 7) / 8;
     tg.bricksY = (g.ny + 7) / 8;
     tg.numTiles = uint32_t(nBricks) * 16u;
+    tg.numItems = uint32_t(nBricks) * 4u;
     if (precise)
-        return launchPersistent(gridKernel<true, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
-    return launchPersistent(gridKernel<false, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+        return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+    return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
@@ -713,16 +741,16 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
     const TileGrid tg = tileGridFor(g);
     DistOpts o{0.f, FLT_MAX, 0, 0.5f, beta};
     if (precise)
-        return launchPersistent(gridKernel<true, false>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
-    return launchPersistent(gridKernel<false, false>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+        return launchPersistent(gridKernel<true, false>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+    return launchPersistent(gridKernel<false, false>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
                           unsigned* scratch, cudaStream_t s) {
     const TileGrid tg = tileGridFor(g);
     if (precise)
-        return launchPersistent(gridKernel<true, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
-    return launchPersistent(gridKernel<false, true>, tg.numTiles, scratch, s, t, g, tg, xf, o, out, scratch);
+        return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+    return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
 cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,
