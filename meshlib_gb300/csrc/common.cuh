@@ -75,7 +75,7 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                           float* out, unsigned* scratch, cudaStream_t s);
 // One mesh + grid of a batched launch (query.cu batchKernel): its tickets are
-// [tileBase, tileBase + tiles of its grid under the launch's tile shape).
+// [tileBase, tileBase + batchTiles(...)): columns of up to kBatchSeg tiles of the launch's shape.
 struct BatchItem {
     QueryTree t;
     GridRange g;  // whole grid: z0 = 0, z1 = nz, zOut = 0
@@ -85,6 +85,7 @@ struct BatchItem {
     uint32_t tileBase;
 };
 constexpr int kBatchConfigs = 6;  // tile shape x block size variants
+constexpr int kBatchSeg = 4;      // tiles along z per work item (a column walked by one warp)
 const char* batchConfigName(int config);
 uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz);
 cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,

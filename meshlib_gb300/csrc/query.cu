@@ -431,12 +431,10 @@ struct TileGrid {
     // (2 x 2 x 4 tiles of 4x4x2) per brick
     const int32_t* bricks;
     int32_t bricksX, bricksY;
-    // work items: columns of up to kSeg tiles along z (4 per brick: its 2 x 2 columns)
-    int32_t segsZ;
+    // work items: columns of up to segLen tiles along z (4 per brick: its 2 x 2 columns)
+    int32_t segLen, segsZ;
     uint32_t numItems;
 };
-
-constexpr int kSeg = 8;  // tiles along z walked by one warp in turn
 
 __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
     unsigned t = 0;
@@ -474,8 +472,8 @@ __global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange
             const int sz = int(rest / unsigned(tg.tilesY));
             x0 = tx * kTX;
             y0 = ty * kTY;
-            zBase = g.z0 + sz * kSeg * kTZ;
-            nSeg = min(kSeg, tg.tilesZ - sz * kSeg);
+            zBase = g.z0 + sz * tg.segLen * kTZ;
+            nSeg = min(tg.segLen, tg.tilesZ - sz * tg.segLen);
         }
         const int x = x0 + lx, y = y0 + ly;
         int seed = -1;  // leaf slot closest to this lane's previous voxel
@@ -718,8 +716,14 @@ static TileGrid tileGridFor(const GridRange& g) {
     tg.numTiles = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.tilesZ);
     tg.bricks = nullptr;
     tg.bricksX = tg.bricksY = 0;
-    tg.segsZ = (tg.tilesZ + kSeg - 1) / kSeg;
-    tg.numItems = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.segsZ);
+    // Longer columns reuse more seeds; shorter ones leave more items for the tail of the persistent
+    // grid.  Measured at 256^3 / 512^3 on 1.3 M triangles: keep >= 25 items per resident warp.
+    const uint64_t cols = uint64_t(tg.tilesX) * tg.tilesY;
+    const uint64_t warps = uint64_t(numSMs()) * 4 * (kThreads / 32);
+    tg.segLen = 16;
+    while (tg.segLen > 1 && cols * uint64_t((tg.tilesZ + tg.segLen - 1) / tg.segLen) < 25 * warps) tg.segLen /= 2;
+    tg.segsZ = (tg.tilesZ + tg.segLen - 1) / tg.segLen;
+    tg.numItems = uint32_t(cols * tg.segsZ);
     return tg;
 }
 
@@ -814,30 +818,46 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const Bat
     const int lane = threadIdx.x & 31;
     const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / (TX * TY);
     for (;;) {
-        const unsigned tile = nextTicket(scratch, lane);
-        if (tile >= totalTiles) break;
+        const unsigned ticket = nextTicket(scratch, lane);
+        if (ticket >= totalTiles) break;
         int lo = 0, hi = nItems - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (items[mid].tileBase <= tile) lo = mid; else hi = mid - 1;
+            if (items[mid].tileBase <= ticket) lo = mid; else hi = mid - 1;
         }
         const BatchItem& it = items[lo];
-        const unsigned local = tile - it.tileBase;
+        // a ticket is a column of up to kBatchSeg tiles along z, walked upwards with each lane's
+        // closest-point search seeded by its previous voxel's triangle (as gridKernel does)
+        const unsigned local = ticket - it.tileBase;
         const int tilesX = (it.g.nx + TX - 1) / TX, tilesY = (it.g.ny + TY - 1) / TY;
         const int tx = int(local % unsigned(tilesX));
         const unsigned rest = local / unsigned(tilesX);
-        const int ty = int(rest % unsigned(tilesY)), tz = int(rest / unsigned(tilesY));
-        const int x = tx * TX + lx, y = ty * TY + ly, z = tz * TZ + lz;
-        const bool active = x < it.g.nx && y < it.g.ny && z < it.g.nz;
+        const int ty = int(rest % unsigned(tilesY)), seg = int(rest / unsigned(tilesY));
+        const int x = tx * TX + lx, y = ty * TY + ly;
         const QueryTree& t = it.t;  // read through the cache, not copied into registers
         const DistOpts o = it.o;
-        const float3 q = xfPoint(it.xf, x, y, z);
-        const float dsq = cpPacket<PRECISE>(t, q, active, o.maxDistSq, o.minDistSq, scratch + 1);
-        const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
-        const float w = fwnPacket<PRECISE>(t, q, active && valid, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
-        const float d = __fsqrt_rn(dsq);
-        const float res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
-        if (active) it.out[(size_t(z) * it.g.ny + y) * it.g.nx + x] = res;
+        int seed = -1;
+        for (int j = 0; j < kBatchSeg; ++j) {
+            const int z0 = (seg * kBatchSeg + j) * TZ;
+            if (z0 >= it.g.nz) break;
+            const int z = z0 + lz;
+            const bool active = x < it.g.nx && y < it.g.ny && z < it.g.nz;
+            const float3 q = xfPoint(it.xf, x, y, z);
+            float up = o.maxDistSq;
+            if (active && seed >= 0) {
+                const float4* tr = t.tri + 3 * int64_t(seed);
+                const float ds = triDistSq<PRECISE>(q, ld4(tr), ld4(tr + 1), ld4(tr + 2));
+                if (ds < up) up = ds;
+            }
+            int best = active ? seed : -1;
+            const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
+            seed = best;
+            const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
+            const float w = fwnPacket<PRECISE>(t, q, active && valid, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
+            const float d = __fsqrt_rn(dsq);
+            const float res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+            if (active) it.out[(size_t(z) * it.g.ny + y) * it.g.nx + x] = res;
+        }
     }
 }
 
@@ -883,7 +903,8 @@ const char* batchConfigName(int config) {
 uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz) {
     static const int shape[kBatchConfigs][3] = {{4, 4, 2}, {4, 4, 2}, {8, 4, 1}, {8, 4, 1}, {2, 4, 4}, {2, 4, 4}};
     const int* t = shape[(config >= 0 && config < kBatchConfigs) ? config : 0];
-    return uint64_t((nx + t[0] - 1) / t[0]) * uint64_t((ny + t[1] - 1) / t[1]) * uint64_t((nz + t[2] - 1) / t[2]);
+    const uint64_t tilesZ = uint64_t((nz + t[2] - 1) / t[2]);
+    return uint64_t((nx + t[0] - 1) / t[0]) * uint64_t((ny + t[1] - 1) / t[1]) * ((tilesZ + kBatchSeg - 1) / kBatchSeg);
 }
 
 cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,
