@@ -152,6 +152,16 @@ GBFWN_API int gbfwn_from_grid_with_distances(gbfwn_handle h, const int32_t dims[
 GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
                                                  const gbfwn_dist_opts* opts, float* d_out, void* stream);
 
+/* One z-slab of a grid: layers [z0, z1) of the dims grid (voxel centres exactly as in the whole-grid
+ * call), written to d_out as (z1 - z0) whole XY layers.  The unit a multi-GPU caller shards a grid by
+ * (the slab of MRMesh/MRFastWindingNumber.h:96-106 by-parts calls, MRMesh/MRChunkIterator.h:44-47);
+ * slabs computed separately and stacked equal the whole grid bit for bit. */
+GBFWN_API int gbfwn_from_grid_slab_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta, int32_t z0,
+                                       int32_t z1, float* d_out, void* stream);
+GBFWN_API int gbfwn_from_grid_with_distances_slab_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                      const gbfwn_dist_opts* opts, int32_t z0, int32_t z1, float* d_out,
+                                                      void* stream);
+
 /* No counterpart in the reference.  Allocation-free variant of gbfwn_from_grid_with_distances_dev for
  * callers that may not call cudaMalloc/cudaFree when they need a grid -- a host application that
  * owns the device-memory budget and gives plugins preallocated buffers only, or a latency-bound loop

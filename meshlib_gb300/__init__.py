@@ -130,6 +130,9 @@ _SIGS = [
     ("gbfwn_surrogate_gradients_dev", ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),
     ("gbfwn_from_grid_with_distances_banded_dev", ctypes.c_int,
      [_vp, _vp, _vp, _vp, ctypes.POINTER(_DistOpts), _vp, ctypes.POINTER(_BandedStats), _vp]),
+    ("gbfwn_from_grid_slab_dev", ctypes.c_int, [_vp, _vp, _vp, _f, _i32, _i32, _vp, _vp]),
+    ("gbfwn_from_grid_with_distances_slab_dev", ctypes.c_int,
+     [_vp, _vp, _vp, ctypes.POINTER(_DistOpts), _i32, _i32, _vp, _vp]),
     ("gbfwn_refit", ctypes.c_int, [_vp, _vp, _vp]),
     ("gbfwn_refit_dev", ctypes.c_int, [_vp, _vp, _vp, _vp]),
     ("gbfwn_find_projections", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, PROGRESS, _vp]),
@@ -371,6 +374,18 @@ class FastWindingNumber:
         o = (options or DistanceToMeshOptions())._c()
         _check(self._L.gbfwn_from_grid_with_distances_noalloc(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o),
                                                                ctypes.c_void_p(d_out_ptr), _stream(stream)))
+
+    def calcFromGridSlab_dev(self, dims, xf, z0: int, z1: int, d_out_ptr: int, beta: float = 2.0, stream=None):
+        """Layers [z0, z1) of the grid into d_out (the multi-GPU shard unit)."""
+        d = np.asarray(dims, np.int32)
+        _check(self._L.gbfwn_from_grid_slab_dev(self._h, _p(d), _p(_xf12(xf)), beta, int(z0), int(z1),
+                                                ctypes.c_void_p(d_out_ptr), _stream(stream)))
+
+    def calcFromGridWithDistancesSlab_dev(self, dims, xf, z0: int, z1: int, d_out_ptr: int, options=None, stream=None):
+        d = np.asarray(dims, np.int32)
+        o = (options or DistanceToMeshOptions())._c()
+        _check(self._L.gbfwn_from_grid_with_distances_slab_dev(self._h, _p(d), _p(_xf12(xf)), ctypes.byref(o), int(z0),
+                                                               int(z1), ctypes.c_void_p(d_out_ptr), _stream(stream)))
 
     def calcFromGrid_dev(self, dims, xf, d_out_ptr: int, beta: float = 2.0, stream=None):
         d = np.asarray(dims, np.int32)

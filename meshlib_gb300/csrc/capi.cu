@@ -315,6 +315,31 @@ GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t d
     return e ? cudaFail(e, "gbfwn_from_grid_with_distances_dev") : GBFWN_OK;
 }
 
+GBFWN_API int gbfwn_from_grid_slab_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12], float beta, int32_t z0,
+                                       int32_t z1, float* d_out, void* stream) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !d_out || z0 < 0 || z1 > dims[2] || z0 >= z1)
+        return fail(GBFWN_INVALID, "gbfwn_from_grid_slab_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    GridRange r{dims[0], dims[1], dims[2], z0, z1, z0};
+    cudaError_t e = launchGridFwn(h->tree.q, r, X, beta, h->precise, d_out, h->scratch, s);
+    return e ? cudaFail(e, "gbfwn_from_grid_slab_dev") : GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_from_grid_with_distances_slab_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                      const gbfwn_dist_opts* opts, int32_t z0, int32_t z1, float* d_out,
+                                                      void* stream) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !d_out || z0 < 0 || z1 > dims[2] || z0 >= z1)
+        return fail(GBFWN_INVALID, "gbfwn_from_grid_with_distances_slab_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    GridRange r{dims[0], dims[1], dims[2], z0, z1, z0};
+    cudaError_t e = launchGridSdf(h->tree.q, r, X, toOpts(opts), h->precise, d_out, h->scratch, s);
+    return e ? cudaFail(e, "gbfwn_from_grid_with_distances_slab_dev") : GBFWN_OK;
+}
+
 }  // extern "C"
 
 // ------------------------------------------------------------------------- host-memory calls
