@@ -155,14 +155,18 @@ __global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, co
 // normal of its triangles), t and u completing an orthonormal basis; extents = the range of the
 // projections of all the node's triangle vertices, widened by a relative margin that covers the
 // FP32 rounding of the projections here and at query time, so the box distance stays a lower
-// bound of the distance to every triangle inside.  One warp per node; the node's leaves are the
-// contiguous slots range[i] = (first, count).
-__global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const int2* __restrict__ range,
-                          const float4* __restrict__ tri, const int32_t* __restrict__ parent,
-                          const int32_t* __restrict__ irank, const int32_t* __restrict__ slot, float4* __restrict__ cp) {
-    const int64_t i = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= nNodes || i == 0) return;
+// bound of the distance to every triangle inside.  The node's leaves are the contiguous slots
+// range[i] = (first, count).  Nodes of up to kObbChunk leaves: one warp each (obbKernel); larger
+// ones (the top levels, about 2n / kObbChunk nodes): one warp per chunk of kObbChunk leaves,
+// combined with order-independent atomic min / max (obbChunkKernel), then written by
+// obbBigKernel -- so no warp walks more than kObbChunk triangles.
+constexpr int kObbChunk = 4096;
+
+struct Frame {
+    float t[3], u[3], n[3];
+};
+
+__device__ __forceinline__ Frame nodeFrame(const float* __restrict__ dip8, int64_t i) {
     const float* d = dip8 + 8 * i;
     float nx = d[4], ny = d[5], nz = d[6];
     const float len = sqrtf(nx * nx + ny * ny + nz * nz);
@@ -177,13 +181,25 @@ __global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const 
     float tx = ax - an * nx, ty = ay - an * ny, tz = -an * nz;
     const float tl = sqrtf(tx * tx + ty * ty + tz * tz);
     tx /= tl; ty /= tl; tz /= tl;
-    const float ux = ny * tz - nz * ty, uy = nz * tx - nx * tz, uz = nx * ty - ny * tx;
-    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    const int2 r = range[i];
-    for (int sidx = r.x + lane; sidx < r.x + r.y; sidx += 32) {
+    Frame f;
+    f.t[0] = tx; f.t[1] = ty; f.t[2] = tz;
+    f.u[0] = ny * tz - nz * ty; f.u[1] = nz * tx - nx * tz; f.u[2] = nx * ty - ny * tx;
+    f.n[0] = nx; f.n[1] = ny; f.n[2] = nz;
+    return f;
+}
+
+// lo / hi of the projections of the triangles in slots [a, b) (this lane's share), reduced over the warp
+__device__ __forceinline__ void projRange(const Frame& f, const float4* __restrict__ tri, int a, int b, int lane, float lo[3],
+                                          float hi[3]) {
+    for (int j = 0; j < 3; ++j) {
+        lo[j] = FLT_MAX;
+        hi[j] = -FLT_MAX;
+    }
+    for (int sidx = a + lane; sidx < b; sidx += 32) {
         for (int k = 0; k < 3; ++k) {
             const float4 v = tri[3 * int64_t(sidx) + k];
-            const float p[3] = {tx * v.x + ty * v.y + tz * v.z, ux * v.x + uy * v.y + uz * v.z, nx * v.x + ny * v.y + nz * v.z};
+            const float p[3] = {f.t[0] * v.x + f.t[1] * v.y + f.t[2] * v.z, f.u[0] * v.x + f.u[1] * v.y + f.u[2] * v.z,
+                                f.n[0] * v.x + f.n[1] * v.y + f.n[2] * v.z};
             for (int j = 0; j < 3; ++j) {
                 lo[j] = fminf(lo[j], p[j]);
                 hi[j] = fmaxf(hi[j], p[j]);
@@ -195,7 +211,11 @@ __global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const 
             lo[j] = fminf(lo[j], __shfl_xor_sync(0xffffffffu, lo[j], off));
             hi[j] = fmaxf(hi[j], __shfl_xor_sync(0xffffffffu, hi[j], off));
         }
-    if (lane) return;
+}
+
+__device__ __forceinline__ void writeObb(int64_t i, const Frame& f, const float lo[3], const float hi[3],
+                                         const int32_t* __restrict__ parent, const int32_t* __restrict__ irank,
+                                         const int32_t* __restrict__ slot, float4* __restrict__ cp) {
     float c[3], e[3];
     for (int j = 0; j < 3; ++j) {
         c[j] = 0.5f * (lo[j] + hi[j]);
@@ -207,10 +227,90 @@ __global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const 
     const int32_t k = irank[i];
     const int32_t link = k >= 0 ? k : ~slot[i];
     float4* dst = cp + 8 * int64_t(irank[p]) + 4 * side;
-    dst[0] = make_float4(tx, ty, tz, c[0]);
-    dst[1] = make_float4(ux, uy, uz, c[1]);
-    dst[2] = make_float4(nx, ny, nz, c[2]);
+    dst[0] = make_float4(f.t[0], f.t[1], f.t[2], c[0]);
+    dst[1] = make_float4(f.u[0], f.u[1], f.u[2], c[1]);
+    dst[2] = make_float4(f.n[0], f.n[1], f.n[2], c[2]);
     dst[3] = make_float4(e[0], e[1], e[2], __int_as_float(link));
+}
+
+__global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const int2* __restrict__ range,
+                          const float4* __restrict__ tri, const int32_t* __restrict__ parent,
+                          const int32_t* __restrict__ irank, const int32_t* __restrict__ slot, float4* __restrict__ cp) {
+    const int64_t i = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= nNodes || i == 0) return;
+    const int2 r = range[i];
+    if (r.y > kObbChunk) return;  // obbChunkKernel / obbBigKernel
+    const Frame f = nodeFrame(dip8, i);
+    float lo[3], hi[3];
+    projRange(f, tri, r.x, r.x + r.y, lane, lo, hi);
+    if (lane == 0) writeObb(i, f, lo, hi, parent, irank, slot, cp);
+}
+
+// float <-> int with the same order (for atomicMin / atomicMax on signed ints)
+__device__ __forceinline__ int orderedKey(float x) {
+    const int b = __float_as_int(x);
+    return b >= 0 ? b : b ^ 0x7fffffff;
+}
+__device__ __forceinline__ float orderedVal(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+
+// chunks of the big nodes: chunkStart[i] = first chunk of node i (exclusive scan of its chunk count),
+// big[i] = its index among the big nodes; acc = 6 ordered keys (lo xyz, hi xyz) per big node
+__global__ void obbChunkCount(const int2* __restrict__ range, int64_t nNodes, int32_t* __restrict__ nChunks,
+                              int32_t* __restrict__ isBig) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes) return;
+    const int cnt = range[i].y;
+    const bool big = i > 0 && cnt > kObbChunk;
+    nChunks[i] = big ? (cnt + kObbChunk - 1) / kObbChunk : 0;
+    isBig[i] = big ? 1 : 0;
+}
+
+__global__ void obbAccInit(int* __restrict__ acc, const int32_t* __restrict__ nBig, int64_t maxBig) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= 6 * min(int64_t(*nBig), maxBig)) return;
+    acc[i] = (i % 6) < 3 ? orderedKey(FLT_MAX) : orderedKey(-FLT_MAX);
+}
+
+__global__ void obbChunkKernel(int64_t nNodes, const float* __restrict__ dip8, const int2* __restrict__ range,
+                               const float4* __restrict__ tri, const int32_t* __restrict__ chunkStart,
+                               const int32_t* __restrict__ totalChunks, const int32_t* __restrict__ bigIdx,
+                               int64_t maxBig, int* __restrict__ acc) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nWarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    const int total = *totalChunks;
+    for (int64_t w = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5; w < total; w += nWarps) {
+        int64_t lo_ = 0, hi_ = nNodes - 1;  // last node whose first chunk is <= w
+        while (lo_ < hi_) {
+            const int64_t mid = (lo_ + hi_ + 1) >> 1;
+            if (chunkStart[mid] <= w) lo_ = mid; else hi_ = mid - 1;
+        }
+        const int64_t i = lo_;
+        const int2 r = range[i];
+        const int a = r.x + int(w - chunkStart[i]) * kObbChunk, b = min(a + kObbChunk, r.x + r.y);
+        const Frame f = nodeFrame(dip8, i);
+        float lo[3], hi[3];
+        projRange(f, tri, a, b, lane, lo, hi);
+        if (lane == 0 && bigIdx[i] < maxBig) {
+            int* d = acc + 6 * int64_t(bigIdx[i]);
+            for (int j = 0; j < 3; ++j) {
+                atomicMin(d + j, orderedKey(lo[j]));
+                atomicMax(d + 3 + j, orderedKey(hi[j]));
+            }
+        }
+    }
+}
+
+__global__ void obbBigKernel(int64_t nNodes, const float* __restrict__ dip8, const int32_t* __restrict__ isBig,
+                             const int32_t* __restrict__ bigIdx, int64_t maxBig, const int* __restrict__ acc,
+                             const int32_t* __restrict__ parent, const int32_t* __restrict__ irank,
+                             const int32_t* __restrict__ slot, float4* __restrict__ cp) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nNodes || !isBig[i] || bigIdx[i] >= maxBig) return;
+    const int* d = acc + 6 * int64_t(bigIdx[i]);
+    const float lo[3] = {orderedVal(d[0]), orderedVal(d[1]), orderedVal(d[2])};
+    const float hi[3] = {orderedVal(d[3]), orderedVal(d[4]), orderedVal(d[5])};
+    writeObb(i, nodeFrame(dip8, i), lo, hi, parent, irank, slot, cp);
 }
 
 // ------------------------------------------------------------------------------------ refit
@@ -340,6 +440,25 @@ static cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, c
     packKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, out.dip8, irs, irs + nNodes, dVerts, dTris, out.cp, out.dip, out.tri,
                                  out.faceSlot);
     obbKernel<<<blocksFor(nNodes * 32, 256), 256, 0, s>>>(nNodes, out.dip8, range, out.tri, parent, irs, irs + nNodes, out.cp);
+    // big nodes: chunk counts -> first chunk per node, big-node index -> accumulators
+    int32_t *nChunks = nullptr, *chunkStart = nullptr, *isBig = nullptr, *bigIdx = nullptr, *sums = nullptr, *totals = nullptr;
+    int* acc = nullptr;
+    // a median-split tree has fewer than 2n / kObbChunk nodes above kObbChunk leaves
+    const int64_t maxBig = 2 * (out.nLeaves / kObbChunk) + 2;
+    if ((e = T.alloc((void**)&nChunks, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&chunkStart, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&isBig, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&bigIdx, sizeof(int32_t) * size_t(nNodes)))) return e;
+    if ((e = T.alloc((void**)&sums, sizeof(int32_t) * size_t(nNodes / 1024 + 2)))) return e;
+    if ((e = T.alloc((void**)&totals, 2 * sizeof(int32_t)))) return e;
+    if ((e = T.alloc((void**)&acc, sizeof(int) * 6 * size_t(maxBig)))) return e;
+    obbChunkCount<<<B, 256, 0, s>>>(range, nNodes, nChunks, isBig);
+    if ((e = exclusiveScanI32(nChunks, chunkStart, nNodes, sums, totals, s))) return e;
+    if ((e = exclusiveScanI32(isBig, bigIdx, nNodes, sums, totals + 1, s))) return e;
+    obbAccInit<<<blocksFor(6 * maxBig, 256), 256, 0, s>>>(acc, totals + 1, maxBig);
+    obbChunkKernel<<<unsigned(numSMs()) * 8, 256, 0, s>>>(nNodes, out.dip8, range, out.tri, chunkStart, totals, bigIdx, maxBig,
+                                                           acc);
+    obbBigKernel<<<B, 256, 0, s>>>(nNodes, out.dip8, isBig, bigIdx, maxBig, acc, parent, irs, irs + nNodes, out.cp);
     return cudaGetLastError();
 }
 
