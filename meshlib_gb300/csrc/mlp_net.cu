@@ -19,6 +19,7 @@
 #include "common.cuh"
 #include "mlp.cuh"
 #include "surrogate.cuh"
+#include "umma.cuh"
 
 namespace gbfwn {
 
@@ -291,6 +292,146 @@ __global__ void exactLowerBound(const float* __restrict__ d, int n, float* __res
     if (i < n) lb[i] = isfinite(d[i]) ? fabsf(d[i]) : INFINITY;
 }
 
+// ---------------------------------------------------------------- fused inference
+// The whole network for 128 points per step in one persistent CTA per SM (256 threads): the bf16
+// weights (W1 as three 64-wide K blocks, W2..W4 as two each: 144 KB) are staged once into shared
+// memory with the 128-byte swizzle; per tile the threads write the Fourier features straight into
+// the swizzled activation tile (axis a = K block a), one thread issues the layer's tcgen05 MMAs
+// (M = N = 128, K = 16 each) into a 128-column TMEM accumulator and commits them to an mbarrier,
+// and the epilogue (warp w: TMEM lanes 32 (w % 4).., columns 64 (w / 4)..) adds the bias, applies
+// SiLU, rounds to bf16 and writes the next layer's input tile in place -- the activations never
+// leave the SM.  Rounding points are the training path's (features, h1..h4 in bf16; FP32
+// accumulation); the output layer sums bf16(h4) * w5 in FP32.  A timed-out wait sets status bit 1.
+constexpr int kInferThreads = 256;
+constexpr int kTileBytes = 128 * 128;  // one 128-row x 64-column bf16 K block
+constexpr size_t kInferSmem = 1024 + size_t(kTileBytes) * (3 + 6 + 3);
+
+__device__ __forceinline__ uint32_t packBf16(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void stageWeights(uint8_t* tile, const __nv_bfloat16* src, int ld) {
+    for (int idx = threadIdx.x; idx < 128 * 8; idx += blockDim.x) {
+        const int r = idx >> 3, c = idx & 7;
+        const uint4 v = *reinterpret_cast<const uint4*>(src + int64_t(r) * ld + c * 8);
+        *reinterpret_cast<uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4)) = v;
+    }
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1) inferKernel(const float* __restrict__ pts, int n, NetMeta meta,
+                                                                 const __nv_bfloat16* __restrict__ W1,
+                                                                 const __nv_bfloat16* __restrict__ W234,
+                                                                 const float* __restrict__ params, float* __restrict__ out,
+                                                                 unsigned* status) {
+    extern __shared__ __align__(1024) uint8_t smemRaw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
+    uint8_t* wt = smem;                     // 9 weight tiles: W1 blocks 0..2, then W2, W3, W4 blocks 0..1
+    uint8_t* at = smem + 9 * kTileBytes;    // 3 activation tiles
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmemBase;
+    __shared__ float partial[2][128];
+    __shared__ int failed;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    for (int b = 0; b < 3; ++b) stageWeights(wt + b * kTileBytes, W1 + 64 * b, kF);
+    for (int l = 0; l < 3; ++l)
+        for (int b = 0; b < 2; ++b) stageWeights(wt + (3 + 2 * l + b) * kTileBytes, W234 + int64_t(l) * kH * kH + 64 * b, kH);
+    if (warp == 0) umma::tmemAlloc(&tmemBase, 128);
+    if (t == 0) {
+        umma::mbarInit(&bar, 1);
+        failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    umma::fenceBeforeSync();
+    __syncthreads();
+    umma::fenceAfterSync();
+    const uint32_t tmem = tmemBase;
+    constexpr uint32_t idesc = umma::idescBf16(128, 128);
+    const int q = warp & 3, half = warp >> 2;  // TMEM lane quarter, column half
+    const int erow = 32 * q + lane;            // this thread's row in the epilogue
+    const float b5 = params[kOffB5];
+    uint32_t phase = 0;
+    const int numTiles = (n + 127) / 128;
+    for (int tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
+        // features: thread (row, half) writes frequencies 16 half .. 16 half + 15 of every axis
+        {
+            const int row = t & 127, fh = t >> 7;
+            const int64_t i = int64_t(tile) * 128 + row;
+            const bool live = i < n;
+            float u[3] = {0.f, 0.f, 0.f};
+            if (live)
+                for (int a = 0; a < 3; ++a) u[a] = (pts[3 * i + a] - meta.center[a]) * meta.scale;
+            for (int a = 0; a < 3; ++a)
+                for (int c = 4 * fh; c < 4 * fh + 4; ++c) {  // chunk c = frequencies 4c .. 4c + 3
+                    uint32_t w[4];
+                    for (int j = 0; j < 4; ++j) {
+                        float sv = 0.f, cv = 0.f;
+                        if (live) sincosf(meta.freq[4 * c + j] * u[a], &sv, &cv);
+                        w[j] = packBf16(sv, cv);
+                    }
+                    *reinterpret_cast<uint4*>(at + a * kTileBytes + row * 128 + ((c ^ (row & 7)) << 4)) =
+                        make_uint4(w[0], w[1], w[2], w[3]);
+                }
+        }
+        for (int layer = 0; layer < 4; ++layer) {
+            umma::fenceProxyAsync();
+            umma::fenceBeforeSync();
+            __syncthreads();
+            if (t == 0) {
+                umma::fenceAfterSync();
+                const int nk = layer == 0 ? 3 : 2;
+                const uint8_t* wb = wt + (layer == 0 ? 0 : 3 + 2 * (layer - 1)) * kTileBytes;
+                for (int b = 0; b < nk; ++b) {
+                    const uint32_t sa = umma::smemAddr(at + b * kTileBytes), sb = umma::smemAddr(wb + b * kTileBytes);
+                    for (int kk = 0; kk < 4; ++kk)
+                        umma::mmaBf16(tmem, umma::descK128(sa + 32 * kk), umma::descK128(sb + 32 * kk), idesc,
+                                      (b > 0 || kk > 0) ? 1u : 0u);
+                }
+                umma::commit(&bar);
+            }
+            if (!umma::mbarWait(&bar, phase)) atomicOr(&failed, 1);
+            phase ^= 1u;
+            __syncthreads();
+            if (failed) break;
+            umma::fenceAfterSync();
+            const float* bias = params + (layer == 0 ? kOffB1 : layer == 1 ? kOffB2 : layer == 2 ? kOffB3 : kOffB4);
+            float acc5 = 0.f;
+            for (int c0 = 0; c0 < 64; c0 += 16) {
+                const int col0 = 64 * half + c0;
+                float v[16];
+                umma::tmemLoad16(tmem + (uint32_t(32 * q) << 16) + uint32_t(col0), v);
+                uint32_t w[8];
+                for (int j = 0; j < 16; j += 2) {
+                    const float z0 = v[j] + bias[col0 + j], z1 = v[j + 1] + bias[col0 + j + 1];
+                    const float h0 = z0 / (1.f + __expf(-z0)), h1 = z1 / (1.f + __expf(-z1));
+                    w[j / 2] = packBf16(h0, h1);
+                    if (layer == 3) {
+                        const __nv_bfloat162 hb = *reinterpret_cast<const __nv_bfloat162*>(&w[j / 2]);
+                        acc5 += __low2float(hb) * params[kOffW5 + col0 + j] + __high2float(hb) * params[kOffW5 + col0 + j + 1];
+                    }
+                }
+                if (layer < 3) {  // next layer's input: column block `half`, chunks c0 / 8 and c0 / 8 + 1
+                    uint8_t* dst = at + half * kTileBytes + erow * 128;
+                    const int ca = c0 / 8, cb = c0 / 8 + 1;
+                    *reinterpret_cast<uint4*>(dst + ((ca ^ (erow & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
+                    *reinterpret_cast<uint4*>(dst + ((cb ^ (erow & 7)) << 4)) = make_uint4(w[4], w[5], w[6], w[7]);
+                }
+            }
+            if (layer == 3) partial[half][erow] = acc5;
+        }
+        if (failed) break;
+        __syncthreads();
+        if (t < 128) {
+            const int64_t i = int64_t(tile) * 128 + t;
+            if (i < n) out[i] = partial[0][t] + partial[1][t] + b5;
+        }
+    }
+    if (failed && t == 0 && status) atomicOr(status, 2u);
+    umma::fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0) umma::tmemFree(tmem, 128);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------------------
@@ -310,6 +451,7 @@ void SurrogateNet::release() {
     mem_.clear();
     delete work_;
     work_ = nullptr;
+
     if (graph_) cudaGraphExecDestroy(graph_);
     graph_ = nullptr;
 }
@@ -323,6 +465,7 @@ cudaError_t SurrogateNet::alloc(void** p, size_t bytes) {
 cudaError_t SurrogateNet::init(uint64_t seed) {
     cudaError_t e;
     if ((e = prepareGemm())) return e;
+    if ((e = cudaFuncSetAttribute(inferKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem)))) return e;
     if ((e = alloc((void**)&params_, sizeof(float) * kSurrogateParams))) return e;
     if ((e = alloc((void**)&grads_, sizeof(float) * kSurrogateParams))) return e;
     if ((e = alloc((void**)&m_, sizeof(float) * kSurrogateParams))) return e;
@@ -451,29 +594,11 @@ cudaError_t SurrogateNet::step(const float* pts, const float* targets, const int
 
 cudaError_t SurrogateNet::infer(const float* pts, int64_t n, float* out, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    Work& w = *work_;
-    const int chunk = w.batch;
-    cudaError_t e;
-    for (int64_t base = 0; base < n; base += chunk) {
-        const int m = int(std::min<int64_t>(chunk, n - base));
-        const int mPad = (m + 127) / 128 * 128;
-        featuresKernel<<<nblk(mPad, 128), 128, 0, s>>>(pts + 3 * base, nullptr, nullptr, 1, m, mPad, meta, w.F, nullptr);
-        const __nv_bfloat16* Wl[4] = {W1_, W234_, W234_ + kH * kH, W234_ + 2 * kH * kH};
-        const int offB[4] = {kOffB1, kOffB2, kOffB3, kOffB4};
-        for (int l = 0; l < 4; ++l) {
-            GemmEpilogue ep;
-            ep.mode = GemmEpilogue::kForward;
-            ep.bias = params_ + offB[l];
-            ep.H = w.H[l];
-            ep.ldh = kH;
-            ep.status = reinterpret_cast<unsigned*>(counters_ + 3);
-            const __nv_bfloat16* A = l == 0 ? w.F : w.H[l - 1];
-            if ((e = launchGemmBf16(A, l == 0 ? kF : kH, Wl[l], l == 0 ? kF : kH, mPad, kH, l == 0 ? kF : kH, 1, ep, s))) return e;
-        }
-        outputKernel<<<std::min<unsigned>(nblk(mPad, 8), 1024u), 256, 0, s>>>(w.H[3], nullptr, m, mPad, params_, nullptr, nullptr,
-                                                                              nullptr, 1, 0.f, out + base, nullptr, nullptr,
-                                                                              nullptr, nullptr);
-    }
+    if (n > int64_t(INT32_MAX) - 128) return cudaErrorInvalidValue;
+    const int tiles = int((n + 127) / 128);
+    const int grid = std::max(1, std::min(tiles, numSMs()));
+    inferKernel<<<grid, kInferThreads, kInferSmem, s>>>(pts, int(n), meta, W1_, W234_, params_, out,
+                                                        reinterpret_cast<unsigned*>(counters_ + 3));
     return cudaGetLastError();
 }
 
