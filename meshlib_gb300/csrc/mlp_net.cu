@@ -1,5 +1,6 @@
 // Surrogate signed-distance network: Fourier features -> 4 x (128, SiLU) -> 1, BF16 weights and
-// activations on the tensor cores with FP32 accumulation (mlp_gemm.cu), trained on the GPU on
+// activations on the tensor cores with FP32 accumulation (training: the GEMMs of mlp_gemm.cu;
+// inference: the fused inferKernel below), trained on the GPU on
 // samples whose signed distances come from the exact traversal, then used to cull 8x8x8-voxel
 // bricks that lie outside a requested distance band.
 //
@@ -273,9 +274,18 @@ __global__ void compactKernel(const int32_t* __restrict__ keep, const int32_t* _
     if (b < nb && keep[b]) list[pos[b]] = b;
 }
 
+// NaN everywhere (voxels of culled bricks stay NaN); 16-byte stores when p is 16-byte aligned
 __global__ void fillNanKernel(float* __restrict__ p, int64_t n) {
-    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-    if (i < n) p[i] = __int_as_float(0x7fc00000);
+    const float nan = __int_as_float(0x7fc00000);
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    const int64_t i0 = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+        float4* p4 = reinterpret_cast<float4*>(p);
+        for (int64_t i = i0; i < n / 4; i += stride) p4[i] = make_float4(nan, nan, nan, nan);
+        for (int64_t i = 4 * (n / 4) + i0; i < n; i += stride) p[i] = nan;
+    } else {
+        for (int64_t i = i0; i < n; i += stride) p[i] = nan;
+    }
 }
 
 // lower bound of |d| at each brick centre from the surrogate: |pred| - margin
@@ -759,7 +769,7 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     int32_t kept = 0;
     if ((e = cudaMemcpyAsync(&kept, total, sizeof(int32_t), cudaMemcpyDeviceToHost, s))) return done(e);
     cudaEventRecord(ev[1], s);
-    fillNanKernel<<<nblk(int64_t(g.nx) * g.ny * g.nz, 256), 256, 0, s>>>(out, int64_t(g.nx) * g.ny * g.nz);
+    fillNanKernel<<<unsigned(numSMs()) * 8, 256, 0, s>>>(out, int64_t(g.nx) * g.ny * g.nz);
     if ((e = cudaStreamSynchronize(s))) return done(e);
     cudaEventRecord(ev[2], s);
     if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, list, kept, scratch, s))) return done(e);
