@@ -143,8 +143,9 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 
 
 # DRAM bytes (read + write) of one launch of the signed-distance grid kernel at 512^3 on this
-# workload, from an ncu capture of the same command (dram__bytes_read.sum 1,044,935,936 +
-# dram__bytes_write.sum 507,725,312); the kernel reads the mesh records about once from HBM.
+# workload, from an ncu capture of the same command (profiles/gridKernel_sdf_512cubed_dram.md:
+# dram__bytes_read.sum 676,597,504 + dram__bytes_write.sum 523,374,848); the kernel reads the mesh
+# records about 1.3 times from HBM.
 KERNEL_DRAM_BYTES_512 = 676_597_504 + 523_374_848
 
 
@@ -503,7 +504,7 @@ def main():
             "config": {"workload": f"calcFromGridWithDistances {grid}^3, noisy icosphere {len(f):,} tris, beta=2, "
                                    "maxDistSq=inf (plain)", "grid": grid, "triangles": int(len(f)),
                        "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas x{world}"},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": args.steps,  # one gridKernel launch per timed step (its counter reset is a memset)
             "e2e": {"value": e2e_val, "unit": "voxels/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                     "d2h_bytes_per_step": int(nvox * 4), "s_per_step": e2e_s,
                     "s_create_per_step": float(np.mean(create_times)) if create_times else None},
