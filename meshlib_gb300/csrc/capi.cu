@@ -354,12 +354,13 @@ int runGrid(gbfwn_mesh_s* h, const int32_t dims[3], LaunchFn launch, float* host
     const size_t layer = size_t(dims[0]) * dims[1];
     const int nz = dims[2];
     if (!progress(cb, user, 0.f)) return fail(GBFWN_CANCELLED, "operation canceled");
-    // slab height: about 16 M voxels per slab, at least 1 layer; without a progress callback the
+    // slab height: about 16 M voxels per slab in by-parts mode (the callback's memory), 64 M with a
+    // progress callback (progress / cancellation granularity), at least 1 layer; without either the
     // whole grid is one launch (the device->host copy runs at C2C speed, ~3 ms for 537 MB on GB300,
     // while splitting the launch costs more: every launch drains its persistent grid and restarts the
     // seeded column walk)
     int slabLayers = int(std::max<size_t>(1, (size_t(16) << 20) / layer));
-    if (!slab && !cb) slabLayers = nz;
+    if (!slab) slabLayers = cb ? int(std::max<size_t>(1, (size_t(64) << 20) / layer)) : nz;
     if (maxLayers > 0) slabLayers = std::min(slabLayers, int(maxLayers));
     if (overlap < 0) overlap = 0;
     if (slab && slabLayers <= overlap) slabLayers = overlap + 1;

@@ -439,7 +439,7 @@ struct SubSeg {
 
 constexpr size_t kFinishSmem = sizeof(Elem) * 2 * kSmall + sizeof(SubSeg) * kSmall + sizeof(int16_t) * kSmall + 16;
 
-__global__ void __launch_bounds__(256) finishSmall(const Elem* __restrict__ el, const Seg* __restrict__ small,
+__global__ void __launch_bounds__(1024) finishSmall(const Elem* __restrict__ el, const Seg* __restrict__ small,
                                                    RefNode* nodes, int32_t* irs, int2* range, int64_t nNodes) {
     extern __shared__ __align__(16) unsigned char smem[];
     Elem(*buf)[kSmall] = reinterpret_cast<Elem(*)[kSmall]>(smem);
@@ -660,7 +660,7 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
     }
     if (nsmallHost > 0) {
         if ((e = cudaFuncSetAttribute(finishSmall, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFinishSmem)))) return e;
-        finishSmall<<<unsigned(nsmallHost), 256, kFinishSmem, s>>>(el, small, nodes, irs, range, nNodes);
+        finishSmall<<<unsigned(nsmallHost), 1024, kFinishSmem, s>>>(el, small, nodes, irs, range, nNodes);
     }
     return cudaGetLastError();
 }
