@@ -335,6 +335,11 @@ GBFWN_API int gbfwn_batch_graph_launch(gbfwn_batch b, void* stream);
  * cores, bf16 inputs (row-major, k contiguous), FP32 output (row-major); m % 128 == 0, n in {128, 192},
  * k % 64 == 0; with split_k > 1 the output is accumulated atomically (zero it first).  Device pointers,
  * enqueued on `stream`.  Used by the tests of the surrogate network's GEMM. */
+/* No counterpart in the reference: exercises the tensor-core kernels' timeout path -- one warp
+ * allocates TMEM, waits at most maxPolls polls on an mbarrier that nothing arrives on, records the
+ * timeout and frees its TMEM.  Returns GBFWN_TIMEOUT (the expected outcome) or an error; the device
+ * stays usable.  Synchronous on `stream`. */
+GBFWN_API int gbfwn_debug_wait_timeout(uint32_t maxPolls, void* stream);
 GBFWN_API int gbfwn_debug_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32_t m, int32_t n, int32_t k,
                                     int32_t split_k, void* stream);
 

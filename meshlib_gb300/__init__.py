@@ -111,6 +111,7 @@ _SIGS = [
     ("gbfwn_from_vector_memory", ctypes.c_size_t, [_i64, _i64, _i64]),
     ("gbfwn_self_intersections_memory", ctypes.c_size_t, [_i64, _i64]),
     ("gbfwn_debug_fail_next_allocs", None, [ctypes.c_int]),
+    ("gbfwn_debug_wait_timeout", ctypes.c_int, [ctypes.c_uint32, _vp]),
     ("gbfwn_debug_gemm_bf16", ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     ("gbfwn_batch_create", ctypes.c_int, [ctypes.POINTER(_BatchItem), _i32, ctypes.POINTER(_vp)]),
     ("gbfwn_batch_destroy", ctypes.c_int, [_vp]),

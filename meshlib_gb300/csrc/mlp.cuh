@@ -34,6 +34,10 @@ struct GemmEpilogue {
 // call it before capturing GEMMs into a CUDA graph).
 cudaError_t prepareGemm();
 
+// Runs one warp that waits on an mbarrier nothing arrives on (at most maxPolls polls), sets bit 1 of
+// *status when the wait gives up, and frees its TMEM: the tensor-core kernels' timeout path.
+cudaError_t launchWaitTimeout(uint32_t maxPolls, unsigned* status, cudaStream_t s);
+
 cudaError_t launchGemmBf16(const __nv_bfloat16* A, int64_t lda, const __nv_bfloat16* B, int64_t ldb, int M, int N, int K,
                            int splitK, const GemmEpilogue& ep, cudaStream_t s);
 

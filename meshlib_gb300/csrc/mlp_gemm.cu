@@ -126,6 +126,27 @@ __global__ void __launch_bounds__(128) gemmKernel(const __nv_bfloat16* __restric
     if (warp == 0) umma::tmemFree(tmem, kTmemCols);
 }
 
+// The timeout path of the tensor-core kernels, on purpose: a warp allocates TMEM, waits on an
+// mbarrier that nothing ever arrives on with a bounded number of polls, records the timeout in the
+// status word and still frees its TMEM -- what gemmKernel and inferKernel do when a wait gives up.
+__global__ void __launch_bounds__(32) waitTimeoutKernel(uint32_t maxPolls, unsigned* status) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmemBase;
+    umma::tmemAlloc(&tmemBase, 32);
+    if (threadIdx.x == 0) {
+        umma::mbarInit(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    umma::fenceBeforeSync();
+    __syncthreads();
+    umma::fenceAfterSync();
+    const bool ok = umma::mbarWait(&bar, 0, maxPolls);  // phase 0 never completes
+    if (!ok && threadIdx.x == 0) atomicOr(status, 2u);
+    umma::fenceBeforeSync();
+    __syncthreads();
+    umma::tmemFree(tmemBase, 32);
+}
+
 template <int N> constexpr size_t gemmSmem() { return 2 * (kBM * 128 + N * 128) + 1024; }
 
 // the dynamic shared-memory opt-in is set once per device, outside any stream capture
@@ -147,6 +168,11 @@ cudaError_t launchGemmN(const __nv_bfloat16* A, int64_t lda, const __nv_bfloat16
 }
 
 }  // namespace
+
+cudaError_t launchWaitTimeout(uint32_t maxPolls, unsigned* status, cudaStream_t s) {
+    waitTimeoutKernel<<<1, 32, 0, s>>>(maxPolls, status);
+    return cudaGetLastError();
+}
 
 cudaError_t prepareGemm() {
     int dev = 0;

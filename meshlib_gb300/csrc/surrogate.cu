@@ -218,6 +218,20 @@ GBFWN_API int gbfwn_from_grid_with_distances_banded_dev(gbfwn_handle h, gbfwn_su
     return GBFWN_OK;
 }
 
+GBFWN_API int gbfwn_debug_wait_timeout(uint32_t maxPolls, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned* d = nullptr;
+    cudaError_t e = devMalloc((void**)&d, sizeof(unsigned));
+    if (!e) e = cudaMemsetAsync(d, 0, sizeof(unsigned), s);
+    if (!e) e = launchWaitTimeout(maxPolls, d, s);
+    unsigned st = 0;
+    if (!e) e = cudaMemcpyAsync(&st, d, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    if (d) cudaFree(d);
+    if (e) return cudaFail(e, "gbfwn_debug_wait_timeout");
+    return (st & 2u) ? fail(GBFWN_TIMEOUT, "a bounded device-side wait gave up") : GBFWN_OK;
+}
+
 GBFWN_API int gbfwn_debug_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32_t m, int32_t n, int32_t k,
                                     int32_t split_k, void* stream) {
     if (!d_a || !d_b || !d_d) return GBFWN_INVALID;

@@ -25,3 +25,22 @@ def test_gemm_matches_torch(fwn_lib, m, n, k, split):
     ref = a.float() @ b.float().T
     err = (d - ref).abs().max().item()
     assert err <= 2e-3 * ref.abs().max().item(), err
+
+
+def test_wait_timeout_path_keeps_the_device_usable(fwn_lib):
+    """A bounded mbarrier wait that nothing completes gives up, reports GBFWN_TIMEOUT, frees its TMEM;
+    tensor-core GEMMs still run correctly afterwards on the same context."""
+    import torch
+
+    import meshlib_gb300 as M
+    for _ in range(2):
+        assert M.lib().gbfwn_debug_wait_timeout(1 << 10, None) == M.TIMEOUT
+    assert b"gave up" in M.lib().gbfwn_last_error()
+    a = torch.randn(128, 64, device="cuda").to(torch.bfloat16)
+    b = torch.randn(128, 64, device="cuda").to(torch.bfloat16)
+    d = torch.zeros(128, 128, device="cuda")
+    assert M.lib().gbfwn_debug_gemm_bf16(ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()),
+                                         ctypes.c_void_p(d.data_ptr()), 128, 128, 64, 1, None) == 0
+    torch.cuda.synchronize()
+    ref = a.float() @ b.float().T
+    assert (d - ref).abs().max().item() <= 2e-3 * ref.abs().max().item()
