@@ -165,10 +165,13 @@ def bytes_per_voxel(c):
     return 4 + 32 * c["cp_nodes"] + 32 * c["fwn_nodes"] + 48 * (c["cp_leaves"] + c["fwn_leaves"])
 
 
-def precision_vs_fp64(v, f, dims, xf, grid_out, shell, shell_d, n_grid=200_000, n_shell=200_000):
-    """Max / RMS error of the GPU results (precise mode) against the FP64 oracle on seeded subsets:
-    signed distances of the timed 512^3 grid and of the shell points (error / bbox diagonal), sign
-    mismatches outside a 1e-3 window around the 0.5 threshold."""
+def precision_vs_fp64(v, f, dims, xf, grid_out, shell, shell_d, n_grid=200_000, n_shell=200_000, extra=None, M=None,
+                      device=0):
+    """Max / RMS error of every GPU result (precise mode) against the FP64 oracle on seeded subsets:
+    signed distances of the timed 512^3 grid and of the shell points (error / bbox diagonal, sign
+    mismatches outside a 1e-3 window around the 0.5 threshold), winding numbers at shell points,
+    projection distances at shell points, and self-intersection winding numbers / bits of two
+    overlapping spheres."""
     import oracle as O
     from meshlib_gb300 import meshgen as mg
     o = O.Oracle(v, f)
@@ -196,6 +199,26 @@ def precision_vs_fp64(v, f, dims, xf, grid_out, shell, shell_d, n_grid=200_000, 
                      "dist_rms_err_over_diag": float(np.sqrt((err ** 2).mean())),
                      "sign_mismatches_outside_tau": int((mism & ~near).sum()), "sign_mismatches_within_tau": int((mism & near).sum()),
                      "tau": 1e-3}
+    extra = extra or {}
+    if "shell_fwn" in extra:
+        q, w = extra["shell_fwn"]
+        e = np.abs(w.astype(np.float64) - o.from_vector(q, prec=1))
+        out["shell_winding_numbers"] = {"points": len(q), "max_abs_err": float(e.max()), "rms_abs_err": float(np.sqrt((e ** 2).mean()))}
+    if "shell_proj" in extra:
+        q, recs = extra["shell_proj"]
+        ref = o.find_projections(q)
+        e = np.abs(np.sqrt(recs[:, 7].astype(np.float64)) - np.sqrt(ref["distSq"].astype(np.float64))) / diag
+        out["shell_projections"] = {"points": len(q), "dist_max_err_over_diag": float(e.max()),
+                                    "dist_rms_err_over_diag": float(np.sqrt((e ** 2).mean())),
+                                    "same_face_fraction": float((recs[:, 0].view(np.int32) == ref["face"]).mean())}
+    if M is not None:
+        sv, sf = mg.overlapping_spheres(seed=0, level=5)
+        bits, wn = M.FastWindingNumber(sv, sf, device=device).calcSelfIntersections(with_wn=True)
+        rbits, rwn = O.Oracle(sv, sf).self_intersections(prec=1)
+        e = np.abs(wn.astype(np.float64) - rwn)
+        near = (np.abs(rwn) < 1e-3) | (np.abs(rwn - 1) < 1e-3)
+        out["self_intersections"] = {"faces": len(sf), "wn_max_abs_err": float(e.max()), "wn_rms_abs_err": float(np.sqrt((e ** 2).mean())),
+                                     "bit_mismatches_outside_tau": int(((bits != rbits) & ~near).sum()), "flagged": int(bits.sum())}
     return out
 
 
@@ -430,6 +453,7 @@ def main():
     # signed distance at points) and calcSelfIntersections after folding 1% of the faces inward
     points = None
     shell = shell_d = None
+    prec_extra = {}  # sampled GPU results of the point legs, checked against the FP64 oracle at the end
     if not args.no_points:
         shell = mg.shell_points(v, f, 4_000_000, width=1e-3, seed=0)
         dpts = torch.from_numpy(shell).cuda()
@@ -469,6 +493,12 @@ def main():
                        "projection_note": "4M shell points + 1M uniform in the padded box, maxDist = inf"})
         if rank == 0 and not args.no_refgpu:
             points.update(mrcuda_projection_leg(v, f, dpp, prec, proj_ms, timed, sp))
+        # samples for the precision study: winding numbers and projections at shell points
+        srng = np.random.default_rng(4242)
+        sidx = srng.integers(0, len(shell), 100_000)
+        prec_extra["shell_fwn"] = (shell[sidx], shell_w.cpu().numpy()[sidx])
+        recs = prec.view(torch.float32).view(-1, 8)[torch.from_numpy(sidx).cuda()].cpu().numpy()
+        prec_extra["shell_proj"] = (shell[sidx], recs)
         del dpp, prec
 
     # ---- batched: 64 uneven meshes (triangles log-uniform in [5k, 500k], grid sides log-uniform in
@@ -537,7 +567,7 @@ def main():
                                 "dipoles and solid angles per voxel; the packet traversal does far fewer, and ncu shows the "
                                 "FMA pipe 28% busy: the kernel is bound by instruction issue and dependent loads"}
         line["cpu_baseline"] = {"value": rate, "unit": "voxels/s", "cores": thr, "kind": "port", "sample": desc}
-        line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d)
+        line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d, extra=prec_extra, M=M, device=local)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
