@@ -493,6 +493,21 @@ def main():
                        "projection_note": "4M shell points + 1M uniform in the padded box, maxDist = inf"})
         if rank == 0 and not args.no_refgpu:
             points.update(mrcuda_projection_leg(v, f, dpp, prec, proj_ms, timed, sp))
+        # refit after every vertex moved (AABBTree::refit + dipoles + query records) vs a rebuild
+        vmoved = (v * np.float32(1.01)).astype(np.float32)
+        dvm = torch.from_numpy(vmoved.reshape(-1)).cuda()
+        torch.cuda.synchronize()
+        rg = M.FastWindingNumber(v, f, device=local)
+        rt = []
+        for _ in range(4):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rg.refit_dev(dvm.data_ptr())
+            torch.cuda.synchronize()
+            rt.append(time.perf_counter() - t0)
+        rg.close()
+        points.update({"refit_ms": 1e3 * float(np.mean(rt[1:])), "refit_note": "all 655,362 vertices moved; synchronous call"})
+        del dvm
         # samples for the precision study: winding numbers and projections at shell points
         srng = np.random.default_rng(4242)
         sidx = srng.integers(0, len(shell), 100_000)
