@@ -260,7 +260,7 @@ def mrcuda_leg(v, f, dims, xf, ours, ours_ms, banded, timed, stream):
     return res
 
 
-def mrcuda_projection_leg(v, f, dpp, ours_rec, ours_ms, timed, stream):
+def mrcuda_projection_leg(v, f, dpp, ours_rec, ours_ms, timed, stream, extra=None):
     """The reference's GPU projector (MRCuda/MRCudaPointsToMeshProjector.cu:6-111, 640 threads per
     block, FP32) on the same points, and how far its distances are from ours."""
     import torch
@@ -279,9 +279,22 @@ def mrcuda_projection_leg(v, f, dpp, ours_rec, ours_ms, timed, stream):
     dd = (a[:, 7].double().sqrt() - b[:, 7].double().sqrt()).abs().max().item() / mg.diag(v)
     same = (a[:, 0].view(torch.int32) == b[:, 0].view(torch.int32)).double().mean().item()
     del out
-    return {"mrcuda_projection_ms": ms, "mrcuda_projection_points_per_s": dpp.numel() // 3 / (ms * 1e-3),
-            "projection_speedup_vs_mrcuda": ms / ours_ms, "projection_max_dist_diff_over_diag_vs_mrcuda": dd,
-            "projection_same_face_fraction_vs_mrcuda": same}
+    res = {"mrcuda_projection_ms": ms, "mrcuda_projection_points_per_s": dpp.numel() // 3 / (ms * 1e-3),
+           "projection_speedup_vs_mrcuda": ms / ours_ms, "projection_max_dist_diff_over_diag_vs_mrcuda": dd,
+           "projection_same_face_fraction_vs_mrcuda": same}
+    if extra is not None:
+        # the reference's winding-number kernels at the shell points and at the face centroids
+        shell_pts, ours_vec_ms, ours_wn, fv, ff, ours_si_ms = extra
+        ms_v = timed(lambda: rk.from_vector(shell_pts, stream=stream), 1)
+        wv = rk.from_vector(shell_pts, stream=stream)
+        torch.cuda.synchronize()
+        ofo = O.Oracle(fv, ff)
+        rkf = mrcuda.RefKernels(fv, ff, ofo.nodes(), ofo.dipoles(0))
+        ms_s = timed(lambda: rkf.from_mesh(stream=stream), 1)
+        res.update({"mrcuda_from_vector_ms": ms_v, "from_vector_speedup_vs_mrcuda": ms_v / ours_vec_ms,
+                    "from_vector_max_abs_diff_vs_mrcuda": float((wv - ours_wn).abs().max().item()),
+                    "mrcuda_self_intersections_ms": ms_s, "self_intersections_speedup_vs_mrcuda": ms_s / ours_si_ms})
+    return res
 
 
 def run_reference(args):
@@ -492,7 +505,8 @@ def main():
                        "projection_points_per_s": len(ppts) / (proj_ms * 1e-3),
                        "projection_note": "4M shell points + 1M uniform in the padded box, maxDist = inf"})
         if rank == 0 and not args.no_refgpu:
-            points.update(mrcuda_projection_leg(v, f, dpp, prec, proj_ms, timed, sp))
+            points.update(mrcuda_projection_leg(v, f, dpp, prec, proj_ms, timed, sp,
+                                                extra=(dpts, vec_ms, shell_w, fv, ff, si_ms)))
         # refit after every vertex moved (AABBTree::refit + dipoles + query records) vs a rebuild
         vmoved = (v * np.float32(1.01)).astype(np.float32)
         dvm = torch.from_numpy(vmoved.reshape(-1)).cuda()
