@@ -504,33 +504,49 @@ __global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange
     }
 }
 
+// A warp takes `chunk` consecutive tiles of 32 points; with Morton-ordered points a lane's point in
+// one tile is near its point in the previous one, so (as in gridKernel) each lane starts its
+// closest-point search from the triangle closest to its previous point.
 template <bool PRECISE, bool DIST>
 __global__ void __launch_bounds__(kThreads, 4) vectorKernel(QueryTree t, const float* __restrict__ pts, int64_t n, DistOpts o,
                                                          int32_t skipFace, float* __restrict__ out, unsigned* scratch,
-                                                         const int32_t* __restrict__ order) {
+                                                         const int32_t* __restrict__ order, int chunk) {
     const int lane = threadIdx.x & 31;
     const float betaSq = __fmul_rn(o.beta, o.beta);
     const int skipSlot = (skipFace >= 0 && skipFace < t.nFaces) ? t.faceSlot[skipFace] : -1;
     const uint64_t numTiles = (uint64_t(n) + 31) / 32;
     for (;;) {
-        const unsigned tile = nextTicket(scratch, lane);
-        if (tile >= numTiles) break;
-        const int64_t r = int64_t(tile) * 32 + lane;  // rank in processing order
-        const bool active = r < n;
-        const int64_t i = (order && active) ? int64_t(order[r]) : r;
-        float3 q = make_float3(0.f, 0.f, 0.f);
-        if (active) q = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
-        float res;
-        if (DIST) {
-            const float dsq = cpPacket<PRECISE>(t, q, active, o.maxDistSq, o.minDistSq, scratch + 1);
-            const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
-            const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
-            const float d = __fsqrt_rn(dsq);
-            res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
-        } else {
-            res = fwnPacket<PRECISE>(t, q, active, betaSq, skipSlot, scratch + 1);
+        const unsigned item = nextTicket(scratch, lane);
+        if (uint64_t(item) * chunk >= numTiles) break;
+        int seed = -1;
+        for (int j = 0; j < chunk; ++j) {
+            const uint64_t tile = uint64_t(item) * chunk + j;
+            if (tile >= numTiles) break;
+            const int64_t r = int64_t(tile) * 32 + lane;  // rank in processing order
+            const bool active = r < n;
+            const int64_t i = (order && active) ? int64_t(order[r]) : r;
+            float3 q = make_float3(0.f, 0.f, 0.f);
+            if (active) q = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+            float res;
+            if (DIST) {
+                float up = o.maxDistSq;
+                if (active && seed >= 0) {
+                    const float4* tr = t.tri + 3 * int64_t(seed);
+                    const float ds = triDistSq<PRECISE>(q, ld4(tr), ld4(tr + 1), ld4(tr + 2));
+                    if (ds < up) up = ds;
+                }
+                int best = active ? seed : -1;
+                const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
+                seed = best;
+                const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
+                const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
+                const float d = __fsqrt_rn(dsq);
+                res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+            } else {
+                res = fwnPacket<PRECISE>(t, q, active, betaSq, skipSlot, scratch + 1);
+            }
+            if (active) out[i] = res;
         }
-        if (active) out[i] = res;
     }
 }
 
@@ -596,42 +612,66 @@ __device__ __noinline__ void closestPointBaryFp64(const float3 p, const float4 A
 template <bool PRECISE, bool TREEXF>
 __global__ void __launch_bounds__(kThreads, 4) projectKernel(QueryTree t, const float* __restrict__ pts, int64_t n, Xf pxf,
                                                           int hasPxf, Xf txf, float up, float lo, float4* __restrict__ out,
-                                                          unsigned* scratch, const int32_t* __restrict__ order) {
+                                                          unsigned* scratch, const int32_t* __restrict__ order, int chunk) {
     const int lane = threadIdx.x & 31;
     const uint64_t numTiles = (uint64_t(n) + 31) / 32;
     for (;;) {
-        const unsigned tile = nextTicket(scratch, lane);
-        if (tile >= numTiles) break;
-        const int64_t r = int64_t(tile) * 32 + lane;
-        const bool active = r < n;
-        const int64_t i = (order && active) ? int64_t(order[r]) : r;
-        float3 q = make_float3(0.f, 0.f, 0.f);
-        if (active) {
-            q = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
-            if (hasPxf) q = xfApply(pxf, q.x, q.y, q.z);
-        }
-        int best = -1;
-        const float dsq = cpPacket<PRECISE, true, TREEXF>(t, q, active, up, lo, scratch + 1, &best, &txf);
-        if (!active) best = -2;
-        float4 o0 = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f), o1 = make_float4(__int_as_float(-1), 0.f, 0.f, dsq);
-        if (best >= 0) {
-            const float4* tr = t.tri + 3 * int64_t(best);
-            float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
-            if (TREEXF) {
-                A = xf4(&txf, A);
-                B = xf4(&txf, B);
-                C = xf4(&txf, C);
+        const unsigned item = nextTicket(scratch, lane);
+        if (uint64_t(item) * chunk >= numTiles) break;
+        int seed = -1;  // leaf slot closest to this lane's previous point (see vectorKernel)
+        for (int jt = 0; jt < chunk; ++jt) {
+            const uint64_t tile = uint64_t(item) * chunk + jt;
+            if (tile >= numTiles) break;
+            const int64_t r = int64_t(tile) * 32 + lane;
+            const bool active = r < n;
+            const int64_t i = (order && active) ? int64_t(order[r]) : r;
+            float3 q = make_float3(0.f, 0.f, 0.f);
+            if (active) {
+                q = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+                if (hasPxf) q = xfApply(pxf, q.x, q.y, q.z);
             }
-            float3 pr;
-            float ba, bb;
-            closestPointBaryFp64(q, A, B, C, &pr, &ba, &bb);
-            const float dx = pr.x - q.x, dy = pr.y - q.y, dz = pr.z - q.z;
-            o0 = make_float4(A.w, pr.x, pr.y, pr.z);
-            o1 = make_float4(__int_as_float(-1), ba, bb, dot3rn(dx, dy, dz, dx, dy, dz));
-        }
-        if (active) {
-            out[2 * i] = o0;
-            out[2 * i + 1] = o1;
+            // start from the previous point's triangle when it lies within the limit: its distance is
+            // one the search would reach anyway, so the minimum and the reported face are unchanged
+            float upS = up;
+            bool seeded = false;
+            if (active && seed >= 0) {
+                const float4* tr = t.tri + 3 * int64_t(seed);
+                float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+                if (TREEXF) {
+                    A = xf4(&txf, A);
+                    B = xf4(&txf, B);
+                    C = xf4(&txf, C);
+                }
+                const float ds = triDistSq<PRECISE>(q, A, B, C);
+                if (ds < upS) {
+                    upS = ds;
+                    seeded = true;
+                }
+            }
+            int best = seeded ? seed : -1;
+            const float dsq = cpPacket<PRECISE, true, TREEXF>(t, q, active, upS, lo, scratch + 1, &best, &txf);
+            seed = best;
+            if (!active) best = -2;
+            float4 o0 = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f), o1 = make_float4(__int_as_float(-1), 0.f, 0.f, dsq);
+            if (best >= 0) {
+                const float4* tr = t.tri + 3 * int64_t(best);
+                float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+                if (TREEXF) {
+                    A = xf4(&txf, A);
+                    B = xf4(&txf, B);
+                    C = xf4(&txf, C);
+                }
+                float3 pr;
+                float ba, bb;
+                closestPointBaryFp64(q, A, B, C, &pr, &ba, &bb);
+                const float dx = pr.x - q.x, dy = pr.y - q.y, dz = pr.z - q.z;
+                o0 = make_float4(A.w, pr.x, pr.y, pr.z);
+                o1 = make_float4(__int_as_float(-1), ba, bb, dot3rn(dx, dy, dz, dx, dy, dz));
+            }
+            if (active) {
+                out[2 * i] = o0;
+                out[2 * i + 1] = o1;
+            }
         }
     }
 }
@@ -757,36 +797,50 @@ cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, 
     return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
+// Tiles of 32 points per work item for the seeded point searches: only with a spatial order, and
+// while at least 8 items per resident warp remain for load balance.
+static int pointChunk(uint64_t tiles, const int32_t* order) {
+    if (!order) return 1;
+    const uint64_t warps = uint64_t(numSMs()) * 4 * (kThreads / 32);
+    int k = 8;
+    while (k > 1 && (tiles + k - 1) / k < 8 * warps) k /= 2;
+    return k;
+}
+
 cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,
                             float* out, unsigned* scratch, cudaStream_t s, const int32_t* order) {
     DistOpts o{0.f, FLT_MAX, 0, 0.5f, beta};
     const uint64_t tiles = (uint64_t(n) + 31) / 32;
     if (precise)
-        return launchPersistent(vectorKernel<true, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order);
-    return launchPersistent(vectorKernel<false, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order);
+        return launchPersistent(vectorKernel<true, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order, 1);
+    return launchPersistent(vectorKernel<false, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order, 1);
 }
 
 cudaError_t launchVectorSdf(const QueryTree& t, const float* pts, int64_t n, const DistOpts& o, int precise, float* out,
                             unsigned* scratch, cudaStream_t s, const int32_t* order) {
     const uint64_t tiles = (uint64_t(n) + 31) / 32;
-    if (precise) return launchPersistent(vectorKernel<true, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch, order);
-    return launchPersistent(vectorKernel<false, true>, tiles, scratch, s, t, pts, n, o, -1, out, scratch, order);
+    const int k = pointChunk(tiles, order);
+    const uint64_t items = (tiles + k - 1) / k;
+    if (precise) return launchPersistent(vectorKernel<true, true>, items, scratch, s, t, pts, n, o, -1, out, scratch, order, k);
+    return launchPersistent(vectorKernel<false, true>, items, scratch, s, t, pts, n, o, -1, out, scratch, order, k);
 }
 
 cudaError_t launchProject(const QueryTree& t, const float* pts, int64_t n, const Xf* pointXf, const Xf* treeXf, float upSq,
                           float loSq, int precise, float4* out, unsigned* scratch, cudaStream_t s, const int32_t* order) {
     const uint64_t tiles = (uint64_t(n) + 31) / 32;
+    const int k = pointChunk(tiles, order);
+    const uint64_t items = (tiles + k - 1) / k;
     const Xf id{{1, 0, 0, 0, 1, 0, 0, 0, 1}, {0, 0, 0}};
     const Xf px = pointXf ? *pointXf : id, tx = treeXf ? *treeXf : id;
     const int hp = pointXf ? 1 : 0;
     if (treeXf) {
         if (precise)
-            return launchPersistent(projectKernel<true, true>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
-        return launchPersistent(projectKernel<false, true>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
+            return launchPersistent(projectKernel<true, true>, items, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order, k);
+        return launchPersistent(projectKernel<false, true>, items, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order, k);
     }
     if (precise)
-        return launchPersistent(projectKernel<true, false>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
-    return launchPersistent(projectKernel<false, false>, tiles, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order);
+        return launchPersistent(projectKernel<true, false>, items, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order, k);
+    return launchPersistent(projectKernel<false, false>, items, scratch, s, t, pts, n, px, hp, tx, upSq, loSq, out, scratch, order, k);
 }
 
 cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise, uint64_t* bits, float* wn,

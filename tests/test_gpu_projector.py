@@ -59,9 +59,10 @@ def _check(v, f, got, ref, pts_mapped, mesh_v=None):
         d_ours = np.sqrt(_exact_face_dist2(mv, f, pts_mapped[diff], got["face"][diff]))
         assert np.abs(d_ours - np.sqrt(ref["distSq"][diff].astype(np.float64))).max() <= 1e-5 * diag
         # and almost always it is the same mesh point (a vertex or an edge shared by the tied faces);
-        # a different point means a query equidistant from two parts of the surface
+        # a different point means a query equidistant (within the tolerance) from two parts of the
+        # surface, e.g. near the centre of a sphere, where which one a search keeps is arbitrary
         moved = np.abs(got["point"][diff] - ref["point"][diff]).max(1) > 1e-5 * diag
-        assert moved.sum() <= max(2, len(got) // 500), f"{int(moved.sum())} ties with different closest points"
+        assert moved.sum() <= max(2, len(got) // 100), f"{int(moved.sum())} ties with different closest points"
     same = np.flatnonzero(found & (got["face"] == ref["face"]))
     assert np.abs(got["point"][same] - ref["point"][same]).max(initial=0) <= 1e-5 * diag
     tri = mv[f[got["face"][found]]].astype(np.float64)
@@ -164,3 +165,40 @@ def test_projection_vs_mrcuda(M):
     pr.updateMeshData(v, f)
     got = pr.findProjections(pts)
     _check(v, f, got, ref, pts)
+
+
+def test_projection_many_points_seeded(M):
+    """3 M Morton-ordered points: warps walk several consecutive tiles and seed each lane's search
+    with its previous point's triangle; sampled results match the oracle, with and without an upper
+    distance limit (a seed beyond the limit must not leak into the output)."""
+    import torch
+
+    v, f = mg.noisy_icosphere(seed=7, level=5)
+    rng = np.random.default_rng(11)
+    lo, hi = v.min(0), v.max(0)
+    pts = rng.uniform(lo - 0.3 * (hi - lo), hi + 0.3 * (hi - lo), (3_000_000, 3)).astype(np.float32)
+    g = M.FastWindingNumber(v, f)
+    pr = M.PointsToMeshProjector.from_mesh(g)
+    o = O.Oracle(v, f)
+    sidx = rng.integers(0, len(pts), 20000)
+    full = o.find_projections(pts[sidx])
+    up = float(np.quantile(full["distSq"], 0.4))
+    for limit in (None, up):
+        got = pr.findProjections(pts) if limit is None else pr.findProjections(pts, upDistLimitSq=limit)
+        ref = full if limit is None else o.find_projections(pts[sidx], upDistLimitSq=limit)
+        g_s = got[sidx]
+        if limit is not None:
+            clear_in = ref["distSq"] < limit * (1 - 1e-5)
+            clear_out = ref["distSq"] >= limit * (1 + 1e-5)
+            assert (g_s["face"][clear_in] >= 0).all() and (g_s["face"][clear_out] == -1).all()
+            keep = clear_in | clear_out
+            g_s, ref = g_s[keep], ref[keep]
+        _check(v, f, g_s, ref, pts[sidx] if limit is None else pts[sidx][keep])
+    # signed distances at the same points through the seeded vector path
+    d = torch.from_numpy(pts).cuda()
+    out = torch.empty(len(pts), device="cuda")
+    g.calcWithDistances_dev(d.data_ptr(), len(pts), out.data_ptr(), stream=0)
+    torch.cuda.synchronize()
+    dd = out.cpu().numpy()[sidx]
+    ref_d = o.vector_with_distances(pts[sidx], prec=1)
+    assert np.abs(np.abs(dd) - np.abs(ref_d)).max() <= 1e-5 * mg.diag(v)
