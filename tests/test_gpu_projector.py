@@ -168,15 +168,15 @@ def test_projection_vs_mrcuda(M):
 
 
 def test_projection_many_points_seeded(M):
-    """3 M Morton-ordered points: warps walk several consecutive tiles and seed each lane's search
-    with its previous point's triangle; sampled results match the oracle, with and without an upper
-    distance limit (a seed beyond the limit must not leak into the output)."""
+    """10 M Morton-ordered points (enough for two tiles per work item): warps walk consecutive tiles
+    and seed each lane's search with its previous point's triangle; sampled results match the oracle,
+    with and without an upper distance limit (a seed beyond the limit must not leak into the output)."""
     import torch
 
     v, f = mg.noisy_icosphere(seed=7, level=5)
     rng = np.random.default_rng(11)
     lo, hi = v.min(0), v.max(0)
-    pts = rng.uniform(lo - 0.3 * (hi - lo), hi + 0.3 * (hi - lo), (3_000_000, 3)).astype(np.float32)
+    pts = rng.uniform(lo - 0.3 * (hi - lo), hi + 0.3 * (hi - lo), (10_000_000, 3)).astype(np.float32)
     g = M.FastWindingNumber(v, f)
     pr = M.PointsToMeshProjector.from_mesh(g)
     o = O.Oracle(v, f)
