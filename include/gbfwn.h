@@ -331,6 +331,82 @@ GBFWN_API int gbfwn_batch_autotune(gbfwn_batch b, int32_t* best, float* times_ms
 GBFWN_API int gbfwn_batch_run_dev(gbfwn_batch b, void* stream);
 GBFWN_API int gbfwn_batch_graph_launch(gbfwn_batch b, void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Marching cubes: the mesher that consumes the signed-distance grid in MeshLib's offsetting
+ * (mcOffsetMesh, MRVoxels/MROffset.cpp:185-226).  Output = the reference's TriMesh bit for bit
+ * (same points in the same order, same triangles, same faceMap) of
+ *   marchingCubes(SimpleVolume, MarchingCubesParams)       MRVoxels/MRMarchingCubes.h:65-67
+ *   MarchingCubesByParts::addPart ... finalize()           MRVoxels/MRMarchingCubes.h:96-122
+ * for the default linear positioner.  The volume is x-fastest (MRMesh/MRVolumeIndexer.h:131-139).
+ * The mesh stays on the device until copied out. */
+
+/* MR::MarchingCubesParams (MRVoxels/MRMarchingCubes.h:18-61): origin, iso, lessInside, maxVertices;
+ * wantFaceMap = outVoxelPerFaceMap requested.  voxelSize is the volume's (SimpleVolume::voxelSize).
+ * Defaults (gbfwn_mc_default_params): origin 0, voxelSize 1, iso 0, lessInside 0,
+ * maxVertices INT32_MAX, wantFaceMap 0. */
+typedef struct gbfwn_mc_params {
+    float origin[3];
+    float voxelSize[3];
+    float iso;
+    int32_t lessInside;
+    int64_t maxVertices;
+    int32_t wantFaceMap;
+} gbfwn_mc_params;
+
+typedef struct gbfwn_trimesh_s* gbfwn_trimesh;
+
+GBFWN_API void gbfwn_mc_default_params(gbfwn_mc_params* p);
+
+/* marchingCubes(SimpleVolume) with the volume in host memory (synchronous).  partStarts / nParts:
+ * optional first layers of the overlapping parts a MarchingCubesByParts call sequence would add
+ * (the last layer of a part is the first of the next); they only change the rounding of the z
+ * coordinates, as in the reference.  nParts = 0: the whole volume at once.  Errors (the reference's
+ * Expected strings): a part with fewer than two layers, parts beyond the volume, more vertices than
+ * maxVertices ("Vertices number limit exceeded.").  A volume with a non-positive dimension gives an
+ * empty mesh. */
+GBFWN_API int gbfwn_marching_cubes(const float* volume, const int32_t dims[3], const gbfwn_mc_params* params,
+                                   const int32_t* partStarts, int32_t nParts, int device, gbfwn_trimesh* out,
+                                   gbfwn_progress_cb cb, void* user);
+/* The same on a device volume; enqueued on `stream`, returns once the mesh is built. */
+GBFWN_API int gbfwn_marching_cubes_dev(const float* d_volume, const int32_t dims[3], const gbfwn_mc_params* params,
+                                       const int32_t* partStarts, int32_t nParts, int device, gbfwn_trimesh* out,
+                                       void* stream);
+/* The mesher keeps its work arrays (6 bytes per voxel) on the device between calls; this frees them. */
+GBFWN_API int gbfwn_mc_release_workspace(int device);
+GBFWN_API int gbfwn_trimesh_sizes(gbfwn_trimesh m, int64_t* numPoints, int64_t* numTris);
+/* Copies the mesh to host arrays (points: 3 floats per vertex; tris: 3 vertex ids per triangle;
+ * faceMap: voxel id of each triangle's cell, only if requested).  Any pointer may be NULL. */
+GBFWN_API int gbfwn_trimesh_copy(gbfwn_trimesh m, float* points, int32_t* tris, int32_t* faceMap);
+/* Device arrays of the mesh (owned by it). */
+GBFWN_API int gbfwn_trimesh_device(gbfwn_trimesh m, const float** d_points, const int32_t** d_tris,
+                                   const int32_t** d_faceMap);
+GBFWN_API int gbfwn_trimesh_destroy(gbfwn_trimesh m);
+
+/* MR::MarchingCubesByParts (MRVoxels/MRMarchingCubes.h:96-122): parts of whole XY layers added in
+ * z order, each starting at nextZ() (the previous part's last layer repeated); finalize() builds the
+ * mesh ("Provided parts do not cover whole volume" when the parts stop short).  The parts are
+ * gathered into one device volume, so a repeated layer takes the values of the later part. */
+typedef struct gbfwn_mc_parts_s* gbfwn_mc_parts;
+GBFWN_API int gbfwn_mc_parts_create(const int32_t dims[3], const gbfwn_mc_params* params, int device,
+                                    gbfwn_mc_parts* out);
+GBFWN_API int32_t gbfwn_mc_parts_next_z(gbfwn_mc_parts p);
+/* part: host (or, for _dev, device) volume of partDims[0] x partDims[1] x partDims[2] voxels. */
+GBFWN_API int gbfwn_mc_parts_add(gbfwn_mc_parts p, const float* part, const int32_t partDims[3]);
+GBFWN_API int gbfwn_mc_parts_add_dev(gbfwn_mc_parts p, const float* d_part, const int32_t partDims[3], void* stream);
+GBFWN_API int gbfwn_mc_parts_finalize(gbfwn_mc_parts p, gbfwn_trimesh* out);
+GBFWN_API int gbfwn_mc_parts_destroy(gbfwn_mc_parts p);
+
+/* mcOffsetMesh's volume step fused on the device (no counterpart in the reference, which copies
+ * the distance grid to the host slab by slab and meshes it there): the signed-distance grid of
+ * `dims` voxels with centres at origin + (i + 0.5) * voxelSize (the basis of MROffset.cpp:201) is
+ * computed into device memory with `opts` (banded with brick culling when maxDistSq is finite and
+ * nullOutsideMinMax is set; s = the optional surrogate), then meshed with `mc` (mcOffsetMesh passes
+ * origin, iso = offset, lessInside = 1) and optional partStarts; the grid never leaves the device. */
+GBFWN_API int gbfwn_grid_to_mesh(gbfwn_handle h, gbfwn_surrogate s, const int32_t dims[3], const float origin[3],
+                                 const float voxelSize[3], const gbfwn_dist_opts* opts, const gbfwn_mc_params* mc,
+                                 const int32_t* partStarts, int32_t nParts, gbfwn_trimesh* out, gbfwn_progress_cb cb,
+                                 void* user);
+
 /* Diagnostic (no counterpart in the reference): D[m x n] (+)= A[m x k] * B[n x k]^T on the tcgen05 tensor
  * cores, bf16 inputs (row-major, k contiguous), FP32 output (row-major); m % 128 == 0, n in {128, 192},
  * k % 64 == 0; with split_k > 1 the output is accumulated atomically (zero it first).  Device pointers,

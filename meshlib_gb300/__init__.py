@@ -67,6 +67,11 @@ class _BandedStats(ctypes.Structure):
                 ("exactMs", ctypes.c_float)]
 
 
+class _McParams(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("voxelSize", ctypes.c_float * 3), ("iso", ctypes.c_float),
+                ("lessInside", ctypes.c_int32), ("maxVertices", ctypes.c_int64), ("wantFaceMap", ctypes.c_int32)]
+
+
 class _BatchItem(ctypes.Structure):
     _fields_ = [("mesh", ctypes.c_void_p), ("dims", ctypes.c_int32 * 3), ("xf", ctypes.c_float * 12), ("opts", _DistOpts),
                 ("d_out", ctypes.c_void_p)]
@@ -140,6 +145,25 @@ _SIGS = [
     ("gbfwn_find_projections_dev", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, _vp]),
     ("gbfwn_projections_heap_bytes", ctypes.c_size_t, [_i64]),
     ("gbfwn_debug_fp32_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("gbfwn_mc_default_params", None, [ctypes.POINTER(_McParams)]),
+    ("gbfwn_marching_cubes", ctypes.c_int,
+     [_vp, _vp, ctypes.POINTER(_McParams), _vp, _i32, ctypes.c_int, ctypes.POINTER(_vp), PROGRESS, _vp]),
+    ("gbfwn_marching_cubes_dev", ctypes.c_int,
+     [_vp, _vp, ctypes.POINTER(_McParams), _vp, _i32, ctypes.c_int, ctypes.POINTER(_vp), _vp]),
+    ("gbfwn_mc_release_workspace", ctypes.c_int, [ctypes.c_int]),
+    ("gbfwn_trimesh_sizes", ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    ("gbfwn_trimesh_copy", ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    ("gbfwn_trimesh_device", ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    ("gbfwn_trimesh_destroy", ctypes.c_int, [_vp]),
+    ("gbfwn_mc_parts_create", ctypes.c_int, [_vp, ctypes.POINTER(_McParams), ctypes.c_int, ctypes.POINTER(_vp)]),
+    ("gbfwn_mc_parts_next_z", _i32, [_vp]),
+    ("gbfwn_mc_parts_add", ctypes.c_int, [_vp, _vp, _vp]),
+    ("gbfwn_mc_parts_add_dev", ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    ("gbfwn_mc_parts_finalize", ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    ("gbfwn_mc_parts_destroy", ctypes.c_int, [_vp]),
+    ("gbfwn_grid_to_mesh", ctypes.c_int,
+     [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_DistOpts), ctypes.POINTER(_McParams), _vp, _i32, ctypes.POINTER(_vp),
+      PROGRESS, _vp]),
 ]
 EXPORTED = [s[0] for s in _SIGS]
 
@@ -369,6 +393,26 @@ class FastWindingNumber:
             ctypes.c_void_p(d_out_ptr), ctypes.byref(st), _stream(stream)))
         return {"bricks": st.bricks, "keptBricks": st.keptBricks, "cullMs": st.cullMs, "exactMs": st.exactMs}
 
+    def gridToMesh(self, dims, origin, voxelSize, options: Optional["DistanceToMeshOptions"] = None,
+                   mcParams: Optional["MarchingCubesParams"] = None, surrogate: Optional["Surrogate"] = None,
+                   partStarts=None, cb=None) -> "TriMesh":
+        """The volume step of ``mcOffsetMesh`` (MRVoxels/MROffset.cpp:185-226) fused on the device: the
+        signed-distance grid of ``dims`` voxels centred at origin + (i + 0.5) * voxelSize, then marching
+        cubes on it (mcOffsetMesh passes origin, iso = offset, lessInside = True); the grid never
+        leaves the GPU.  voxelSize: a float or three floats."""
+        d = np.asarray(dims, np.int32)
+        o = np.ascontiguousarray(origin, np.float32)
+        vs = np.ascontiguousarray(np.broadcast_to(np.asarray(voxelSize, np.float32), (3,)))
+        opts = (options or DistanceToMeshOptions())._c()
+        mp = mcParams or MarchingCubesParams(origin=tuple(o), voxelSize=tuple(vs))
+        prm = mp._c()
+        ps, nps = _parts(partStarts)
+        fn, _keep = _progress(cb)
+        h = ctypes.c_void_p()
+        _check(self._L.gbfwn_grid_to_mesh(self._h, surrogate.handle if surrogate is not None else None, _p(d), _p(o), _p(vs),
+                                          ctypes.byref(opts), ctypes.byref(prm), _p(ps), nps, ctypes.byref(h), fn, None))
+        return TriMesh(h)
+
     def calcFromGridWithDistances_noalloc(self, dims, xf, d_out_ptr: int, options=None, stream=None):
         """Allocation-free variant of calcFromGridWithDistances_dev (see gbfwn_from_grid_with_distances_noalloc)."""
         d = np.asarray(dims, np.int32)
@@ -470,6 +514,171 @@ class PointsToMeshProjector:
     def projectionsHeapBytes(self, numProjections: int) -> int:
         return int(lib().gbfwn_projections_heap_bytes(numProjections))
 
+
+
+# ------------------------------------------------------------------ marching cubes (the grid's consumer)
+@dataclass
+class MarchingCubesParams:
+    """MR::MarchingCubesParams (MRVoxels/MRMarchingCubes.h:18-61) for the default linear positioner;
+    ``voxelSize`` is the volume's (SimpleVolume::voxelSize), ``outVoxelPerFaceMap`` asks for the
+    face -> voxel map."""
+    origin: tuple = (0.0, 0.0, 0.0)
+    voxelSize: tuple = (1.0, 1.0, 1.0)
+    iso: float = 0.0
+    lessInside: bool = False
+    maxVertices: int = 2**31 - 1
+    outVoxelPerFaceMap: bool = False
+
+    def _c(self) -> _McParams:
+        c = _McParams()
+        for k in range(3):
+            c.origin[k] = float(self.origin[k])
+            c.voxelSize[k] = float(self.voxelSize[k])
+        c.iso = float(self.iso)
+        c.lessInside = int(bool(self.lessInside))
+        c.maxVertices = int(self.maxVertices)
+        c.wantFaceMap = int(bool(self.outVoxelPerFaceMap))
+        return c
+
+
+class TriMesh:
+    """A mesh produced on the device (MR::TriMesh: points + triangles, plus the optional
+    face -> voxel map).  ``points`` / ``tris`` / ``faceMap`` copy it to host arrays; ``device_ptrs``
+    gives the device arrays, valid while this object lives."""
+
+    def __init__(self, handle: ctypes.c_void_p):
+        self._h = handle
+        self._L = lib()
+        npt, ntr = _i64(), _i64()
+        _check(self._L.gbfwn_trimesh_sizes(self._h, ctypes.byref(npt), ctypes.byref(ntr)))
+        self.numPoints, self.numTris = int(npt.value), int(ntr.value)
+        self._host = None
+
+    def _copy(self):
+        if self._host is None:
+            pts = np.empty((self.numPoints, 3), np.float32)
+            tris = np.empty((self.numTris, 3), np.int32)
+            dp, dt, df = _vp(), _vp(), _vp()
+            _check(self._L.gbfwn_trimesh_device(self._h, ctypes.byref(dp), ctypes.byref(dt), ctypes.byref(df)))
+            fmap = np.empty(self.numTris, np.int32) if df.value else None
+            _check(self._L.gbfwn_trimesh_copy(self._h, _p(pts), _p(tris), _p(fmap)))
+            self._host = (pts, tris, fmap)
+        return self._host
+
+    @property
+    def points(self) -> np.ndarray:
+        return self._copy()[0]
+
+    @property
+    def tris(self) -> np.ndarray:
+        return self._copy()[1]
+
+    @property
+    def faceMap(self) -> Optional[np.ndarray]:
+        return self._copy()[2]
+
+    def device_ptrs(self) -> tuple:
+        dp, dt, df = _vp(), _vp(), _vp()
+        _check(self._L.gbfwn_trimesh_device(self._h, ctypes.byref(dp), ctypes.byref(dt), ctypes.byref(df)))
+        return dp.value, dt.value, df.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gbfwn_trimesh_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _parts(partStarts):
+    if partStarts is None:
+        return None, 0
+    a = np.ascontiguousarray(partStarts, np.int32)
+    return a, len(a)
+
+
+def marchingCubes(volume: np.ndarray, params: Optional[MarchingCubesParams] = None, partStarts=None, device: int = 0,
+                  cb: Optional[Callable[[float], bool]] = None) -> TriMesh:
+    """``MR::marchingCubesAsTriMesh(SimpleVolume, params)`` (MRVoxels/MRMarchingCubes.h:66) on the GPU.
+    ``volume``: (nz, ny, nx) float32, x fastest.  ``partStarts``: first layers of the overlapping
+    parts of an equivalent MarchingCubesByParts sequence (only the rounding of z changes)."""
+    v = np.ascontiguousarray(volume, np.float32)
+    if v.ndim != 3:
+        raise ValueError("volume must be (nz, ny, nx)")
+    dims = np.array([v.shape[2], v.shape[1], v.shape[0]], np.int32)
+    prm = (params or MarchingCubesParams())._c()
+    ps, nps = _parts(partStarts)
+    fn, _keep = _progress(cb)
+    h = ctypes.c_void_p()
+    _check(lib().gbfwn_marching_cubes(_p(v), _p(dims), ctypes.byref(prm), _p(ps), nps, device, ctypes.byref(h), fn, None))
+    return TriMesh(h)
+
+
+def marchingCubes_dev(d_volume_ptr: int, dims, params: Optional[MarchingCubesParams] = None, partStarts=None,
+                      device: int = 0, stream=None) -> TriMesh:
+    """The same on a device volume of dims = (nx, ny, nz) floats (x fastest)."""
+    d = np.asarray(dims, np.int32)
+    prm = (params or MarchingCubesParams())._c()
+    ps, nps = _parts(partStarts)
+    h = ctypes.c_void_p()
+    st = ctypes.c_void_p(None if stream is None else int(stream))
+    _check(lib().gbfwn_marching_cubes_dev(ctypes.c_void_p(d_volume_ptr), _p(d), ctypes.byref(prm), _p(ps), nps, device,
+                                          ctypes.byref(h), st))
+    return TriMesh(h)
+
+
+class MarchingCubesByParts:
+    """``MR::MarchingCubesByParts`` (MRVoxels/MRMarchingCubes.h:96-122): ``addPart`` volumes of whole
+    XY layers starting at ``nextZ()`` (the previous part's last layer repeated), then ``finalize``."""
+
+    def __init__(self, dims, params: Optional[MarchingCubesParams] = None, device: int = 0):
+        self._L = lib()
+        d = np.asarray(dims, np.int32)
+        prm = (params or MarchingCubesParams())._c()
+        self._h = ctypes.c_void_p()
+        _check(self._L.gbfwn_mc_parts_create(_p(d), ctypes.byref(prm), device, ctypes.byref(self._h)))
+
+    def nextZ(self) -> int:
+        return int(self._L.gbfwn_mc_parts_next_z(self._h))
+
+    def addPart(self, part: np.ndarray):
+        v = np.ascontiguousarray(part, np.float32)
+        d = np.array([v.shape[2], v.shape[1], v.shape[0]], np.int32)
+        _check(self._L.gbfwn_mc_parts_add(self._h, _p(v), _p(d)))
+
+    def addPart_dev(self, d_part_ptr: int, dims, stream=None):
+        d = np.asarray(dims, np.int32)
+        st = ctypes.c_void_p(None if stream is None else int(stream))
+        _check(self._L.gbfwn_mc_parts_add_dev(self._h, ctypes.c_void_p(d_part_ptr), _p(d), st))
+
+    def finalize(self) -> TriMesh:
+        h = ctypes.c_void_p()
+        _check(self._L.gbfwn_mc_parts_finalize(self._h, ctypes.byref(h)))
+        return TriMesh(h)
+
+    def __del__(self):
+        try:
+            if self._h.value:
+                self._L.gbfwn_mc_parts_destroy(self._h)
+                self._h = ctypes.c_void_p()
+        except Exception:
+            pass
+
+
+def calcOriginAndDimensions(box_min, box_max, voxelSize: float):
+    """MR::calcOriginAndDimensions (MRVoxels/MRCalcDims.h:18-27): origin = box.min - 2 voxels,
+    dims = int((box.max + 2 voxels - origin) / voxelSize) + 1, in float like the reference."""
+    vs = np.float32(voxelSize)
+    exp = np.float32(2) * vs
+    lo = np.asarray(box_min, np.float32)
+    hi = np.asarray(box_max, np.float32)
+    origin = (lo - exp).astype(np.float32)
+    dims = (((hi + exp).astype(np.float32) - origin).astype(np.float32) / vs).astype(np.float32).astype(np.int32) + 1
+    return origin, dims
 
 def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
     """Measured FP32 FMA throughput of the GPU (TFLOP/s)."""

@@ -19,7 +19,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibilit
 # build.cu must round every float operation separately (bit-identical boxes and dipoles)
 PER_FILE = {"build.cu": ["-fmad=false"], "treebuild.cu": ["-fmad=false"]}
 SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "mlp_gemm.cu", "mlp_net.cu", "surrogate.cu", "batch.cu", "sort.cu",
-           "projector.cu", "peak.cu"]
+           "projector.cu", "peak.cu", "mc.cu"]
 
 
 def nvcc() -> str:

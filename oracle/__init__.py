@@ -1,4 +1,4 @@
-"""ctypes front-end of the CPU oracle (oracle/fwn_oracle.cpp).
+"""ctypes front-end of the CPU oracle (oracle/fwn_oracle.cpp, oracle/mc_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
 CPU-baseline leg of bench.py -- never by the product package.
@@ -25,10 +25,10 @@ class Options(ctypes.Structure):
 def build(force: bool = False) -> str:
     """Compiles the oracle with the host compiler (no FMA contraction, so FP32 follows the reference)
     and the launcher of the reference's GPU kernels (oracle/mrcuda_runner.cpp)."""
-    src = os.path.join(_HERE, "fwn_oracle.cpp")
-    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("fwn_oracle.cpp", "mc_oracle.cpp")]
+    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < max(os.path.getmtime(s) for s in srcs):
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
-                               "-o", _SO, src])
+                               "-o", _SO] + srcs)
     from . import mrcuda
     mrcuda.build_runner(force)
     return _SO
@@ -65,6 +65,18 @@ def lib():
         L.orc_refit.argtypes = [vp, vp, vp]
         L.orc_is_rigid.restype = ip
         L.orc_is_rigid.argtypes = [vp]
+        L.orc_mc.restype = vp
+        L.orc_mc.argtypes = [vp, vp, vp, vp, fp, ip, vp, ip, ctypes.c_int64]
+        L.orc_mc_num_points.restype = ctypes.c_int64
+        L.orc_mc_num_points.argtypes = [vp]
+        L.orc_mc_num_tris.restype = ctypes.c_int64
+        L.orc_mc_num_tris.argtypes = [vp]
+        L.orc_mc_error.restype = ctypes.c_char_p
+        L.orc_mc_error.argtypes = [vp]
+        L.orc_mc_get.argtypes = [vp, vp, vp, vp]
+        L.orc_mc_free.argtypes = [vp]
+        L.orc_mc_plan.restype = ctypes.c_char_p
+        L.orc_mc_plan.argtypes = [ip]
         _lib = L
     return _lib
 
@@ -227,3 +239,40 @@ def grid_points(dims, xf) -> np.ndarray:
     for r in range(3):
         out[:, r] = (p[:, 0] * A[r, 0] + p[:, 1] * A[r, 1]) + p[:, 2] * A[r, 2] + b[r]
     return out
+
+
+class McError(RuntimeError):
+    """An error string of the restated mesher (the reference's Expected<TriMesh> error)."""
+
+
+def marching_cubes(vol, origin=(0.0, 0.0, 0.0), voxel_size=(1.0, 1.0, 1.0), iso=0.0, less_inside=False,
+                   part_starts=None, max_vertices=2**31 - 1):
+    """Restated MeshLib VolumeMesher (oracle/mc_oracle.cpp).  vol: (nz, ny, nx) float32 (x fastest).
+    part_starts: first layer of each overlapping part (MarchingCubesByParts), None = whole volume.
+    Returns (points (n, 3) float32, tris (m, 3) int32, faceMap (m,) int32); raises McError."""
+    v = np.ascontiguousarray(vol, np.float32)
+    nz, ny, nx = v.shape
+    dims = np.array([nx, ny, nz], np.int32)
+    o = np.ascontiguousarray(origin, np.float32)
+    vs = np.ascontiguousarray(voxel_size, np.float32)
+    ps = None if part_starts is None else np.ascontiguousarray(part_starts, np.int32)
+    L = lib()
+    r = L.orc_mc(_ptr(v), _ptr(dims), _ptr(o), _ptr(vs), float(iso), int(bool(less_inside)),
+                 _ptr(ps) if ps is not None else None, 0 if ps is None else len(ps), int(max_vertices))
+    try:
+        err = L.orc_mc_error(r).decode()
+        if err:
+            raise McError(err)
+        npt, ntr = L.orc_mc_num_points(r), L.orc_mc_num_tris(r)
+        pts = np.empty((npt, 3), np.float32)
+        tris = np.empty((ntr, 3), np.int32)
+        fmap = np.empty(ntr, np.int32)
+        L.orc_mc_get(r, _ptr(pts), _ptr(tris), _ptr(fmap))
+        return pts, tris, fmap
+    finally:
+        L.orc_mc_free(r)
+
+
+def mc_plan(config: int) -> str:
+    """Triangulation plan of a cube configuration (hex digits, three per triangle)."""
+    return lib().orc_mc_plan(int(config)).decode()

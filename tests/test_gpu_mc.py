@@ -1,0 +1,175 @@
+"""Marching cubes on the GPU against the restated reference mesher (oracle/mc_oracle.cpp), bit for
+bit: the same points (every float equal), the same triangles in the same order, the same face map.
+Covers the reference's cases: NaN voxels (nullOutsideMinMax bands), parts (MarchingCubesByParts),
+both orientations, odd sizes, the vertex limit, and the fused distance-grid -> mesh call."""
+import numpy as np
+import pytest
+
+import oracle as O
+from meshlib_gb300 import meshgen as mg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def M(fwn_lib):
+    import meshlib_gb300
+    return meshlib_gb300
+
+
+def _same(tm, ref):
+    p, t, f = ref
+    assert tm.numPoints == len(p) and tm.numTris == len(t)
+    assert np.array_equal(tm.points.view(np.uint32), p.view(np.uint32))
+    assert np.array_equal(tm.tris, t)
+    if tm.faceMap is not None:
+        assert np.array_equal(tm.faceMap, f)
+
+
+def _sphere(n=101, r=50.0):
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    pos = np.stack([x, y, z], -1).astype(np.float32)
+    return (np.sqrt(((np.float32(n // 2) - pos) ** 2).sum(-1, dtype=np.float32)) - np.float32(r)).astype(np.float32)
+
+
+@pytest.mark.parametrize("less_inside", [False, True])
+def test_sphere_vs_oracle(M, less_inside):
+    vol = _sphere()
+    prm = M.MarchingCubesParams(voxelSize=(0.01,) * 3, iso=0.0, lessInside=less_inside, outVoxelPerFaceMap=True)
+    ref = O.marching_cubes(vol, voxel_size=(0.01,) * 3, iso=0.0, less_inside=less_inside)
+    _same(M.marchingCubes(vol, prm), ref)
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (3, 5, 7), (17, 16, 33), (40, 37, 48)])
+def test_random_fields_odd_sizes(M, shape):
+    rng = np.random.default_rng(sum(shape))
+    vol = rng.normal(size=shape).astype(np.float32)
+    org, vs = (0.25, -3.0, 1.5), (0.3, 0.7, 0.11)
+    prm = M.MarchingCubesParams(origin=org, voxelSize=vs, iso=0.2, outVoxelPerFaceMap=True)
+    _same(M.marchingCubes(vol, prm), O.marching_cubes(vol, origin=org, voxel_size=vs, iso=0.2))
+
+
+def test_every_configuration(M):
+    """A random +-1 volume meets all 256 cube configurations (checked on the oracle's face map)."""
+    rng = np.random.default_rng(5)
+    vol = np.where(rng.random((48, 48, 48)) < 0.5, -1.0, 1.0).astype(np.float32)
+    ref = O.marching_cubes(vol, iso=0.0, less_inside=True)
+    z, y, x = np.unravel_index(ref[2], vol.shape)
+    cfg = np.zeros(len(z), np.int64)
+    for i, bit in enumerate([0, 1, 3, 2, 4, 5, 7, 6]):
+        cfg |= (vol[z + (i >> 2), y + ((i >> 1) & 1), x + (i & 1)] < 0).astype(np.int64) << bit
+    assert len(np.unique(cfg)) == 254  # all but the empty and the full cube
+    _same(M.marchingCubes(vol, M.MarchingCubesParams(iso=0.0, lessInside=True, outVoxelPerFaceMap=True)), ref)
+
+
+def test_nan_voxels(M):
+    rng = np.random.default_rng(9)
+    vol = rng.normal(size=(30, 29, 31)).astype(np.float32)
+    vol[rng.random(vol.shape) < 0.15] = np.nan
+    vol[10:12] = np.nan
+    vol[:, 5, :] = np.nan
+    prm = M.MarchingCubesParams(origin=(1, 2, 3), voxelSize=(0.5, 0.5, 0.25), iso=-0.1, outVoxelPerFaceMap=True)
+    ref = O.marching_cubes(vol, origin=(1, 2, 3), voxel_size=(0.5, 0.5, 0.25), iso=-0.1)
+    assert len(ref[1]) > 0
+    _same(M.marchingCubes(vol, prm), ref)
+    allnan = np.full((4, 4, 4), np.nan, np.float32)
+    tm = M.marchingCubes(allnan, prm)
+    assert tm.numPoints == 0 and tm.numTris == 0
+
+
+def test_parts_and_by_parts_object(M):
+    vol = _sphere(61, 25.0)
+    prm = M.MarchingCubesParams(voxelSize=(0.02,) * 3, iso=0.0, lessInside=True, outVoxelPerFaceMap=True)
+    for starts in (np.arange(60), [0, 7, 30, 31, 50]):
+        ref = O.marching_cubes(vol, voxel_size=(0.02,) * 3, iso=0.0, less_inside=True, part_starts=starts)
+        _same(M.marchingCubes(vol, prm, partStarts=starts), ref)
+    # MarchingCubesByParts: 2-layer parts as in the reference's test, then uneven parts from device memory
+    ref = O.marching_cubes(vol, voxel_size=(0.02,) * 3, iso=0.0, less_inside=True, part_starts=np.arange(60))
+    mc = M.MarchingCubesByParts((61, 61, 61), prm)
+    for z in range(60):
+        assert mc.nextZ() == z
+        mc.addPart(vol[z:z + 2])
+    _same(mc.finalize(), ref)
+    import torch
+    dv = torch.from_numpy(vol).cuda()
+    mc = M.MarchingCubesByParts((61, 61, 61), prm)
+    starts = [0, 7, 30, 31, 50]
+    for a, b in zip(starts, starts[1:] + [60]):
+        mc.addPart_dev(dv[a:b + 1].data_ptr(), (61, 61, b + 1 - a))
+    ref = O.marching_cubes(vol, voxel_size=(0.02,) * 3, iso=0.0, less_inside=True, part_starts=starts)
+    _same(mc.finalize(), ref)
+
+
+def test_errors(M):
+    vol = np.random.default_rng(1).normal(size=(6, 5, 5)).astype(np.float32)
+    with pytest.raises(M.FwnError, match="at least two Z slices"):
+        M.marchingCubes(vol[:1])
+    with pytest.raises(M.FwnError, match="at least two Z slices"):
+        M.marchingCubes(vol, partStarts=[0, 2, 5])
+    n = len(O.marching_cubes(vol)[0])
+    with pytest.raises(M.FwnError, match="Vertices number limit exceeded"):
+        M.marchingCubes(vol, M.MarchingCubesParams(maxVertices=n - 1))
+    assert M.marchingCubes(vol, M.MarchingCubesParams(maxVertices=n)).numPoints == n
+    assert M.marchingCubes(np.zeros((0, 4, 4), np.float32)).numTris == 0
+    mc = M.MarchingCubesByParts((5, 5, 6))
+    with pytest.raises(M.FwnError, match="XY dimensions"):
+        mc.addPart(np.zeros((2, 5, 4), np.float32))
+    with pytest.raises(M.FwnError, match="at least two Z slices"):
+        mc.addPart(np.zeros((1, 5, 5), np.float32))
+    mc.addPart(vol[:3])
+    with pytest.raises(M.FwnError, match="exceeds whole volume"):
+        mc.addPart(vol[:5])
+    with pytest.raises(M.FwnError, match="do not cover"):
+        mc.finalize()
+
+
+@pytest.mark.parametrize("banded", [False, True])
+def test_grid_to_mesh_vs_host_pipeline(M, banded):
+    """mcOffsetMesh's volume step fused on the device == our distance grid copied to the host and
+    meshed by the oracle (the reference's flow), at an offset of 2 voxels."""
+    v, f = mg.noisy_torus(seed=1)
+    g = M.FastWindingNumber(v, f)
+    vsz = 0.02
+    off = 2 * vsz
+    lo, hi = v.min(0) - off, v.max(0) + off
+    origin, dims = M.calcOriginAndDimensions(lo, hi, vsz)
+    opts = M.DistanceToMeshOptions()
+    if banded:
+        opts.minDistSq = max(off - 1.001 * vsz, 0.0) ** 2
+        opts.maxDistSq = (off + 1.001 * vsz) ** 2
+        opts.nullOutsideMinMax = True
+    prm = M.MarchingCubesParams(origin=tuple(origin), voxelSize=(vsz,) * 3, iso=off, lessInside=True,
+                                outVoxelPerFaceMap=True)
+    tm = g.gridToMesh(dims, origin, vsz, opts, prm)
+    basis = np.array([vsz, 0, 0, 0, vsz, 0, 0, 0, vsz, 0, 0, 0], np.float32)
+    basis[9:] = (origin + np.float32(0.5) * np.float32(vsz)).astype(np.float32)
+    grid = g.calcFromGridWithDistances(dims, basis, opts).reshape(dims[2], dims[1], dims[0])
+    ref = O.marching_cubes(grid, origin=origin, voxel_size=(vsz,) * 3, iso=off, less_inside=True)
+    assert len(ref[1]) > 1000
+    _same(tm, ref)
+    if not banded:  # a clean offset surface of a closed mesh is closed
+        t = tm.tris
+        e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
+        assert len(set(map(tuple, e.tolist()))) == len(e)
+
+
+def test_grid_to_mesh_large(M):
+    """256^3 offset grid of the 1.31 M-triangle icosphere: the fused call against the oracle mesher
+    on the same device grid."""
+    import torch
+    v, f = mg.noisy_icosphere(seed=0, level=8)
+    g = M.FastWindingNumber(v, f)
+    ext = (v.max(0) - v.min(0)).max()
+    vsz = float(ext) / 240
+    off = 3 * vsz
+    origin, dims = M.calcOriginAndDimensions(v.min(0) - off, v.max(0) + off, vsz)
+    prm = M.MarchingCubesParams(origin=tuple(origin), voxelSize=(vsz,) * 3, iso=off, lessInside=True)
+    tm = g.gridToMesh(dims, origin, vsz, M.DistanceToMeshOptions(), prm)
+    basis = np.array([vsz, 0, 0, 0, vsz, 0, 0, 0, vsz, 0, 0, 0], np.float32)
+    basis[9:] = (origin + np.float32(0.5) * np.float32(vsz)).astype(np.float32)
+    out = torch.empty(int(np.prod(dims)), device="cuda")
+    g.calcFromGridWithDistances_dev(dims, basis, out.data_ptr())
+    torch.cuda.synchronize()
+    grid = out.cpu().numpy().reshape(dims[2], dims[1], dims[0])
+    ref = O.marching_cubes(grid, origin=origin, voxel_size=(vsz,) * 3, iso=off, less_inside=True)
+    _same(tm, ref)
