@@ -297,6 +297,55 @@ def mrcuda_projection_leg(v, f, dpp, ours_rec, ours_ms, timed, stream, extra=Non
     return res
 
 
+def offset_leg(M, fwn, v, f, dims, xf, grid_dev, timed, stream, sp, with_cpu):
+    """Marching cubes on the headline grid (iso = 2 voxels, lessInside) and the fused offset mesh."""
+    import torch
+    vs = float(xf[0])
+    iso = 2 * vs
+    origin = tuple(float(x) for x in (np.asarray(xf[9:12], np.float32) - np.float32(0.5 * vs)))
+    prm = M.MarchingCubesParams(origin=origin, voxelSize=(vs,) * 3, iso=iso, lessInside=True)
+    keep = {}
+
+    def mc():
+        keep["m"] = M.marchingCubes_dev(grid_dev.data_ptr(), dims, prm, stream=sp)
+
+    mc_ms = timed(mc, 5, warmup=2)
+    tm = keep.pop("m")
+    res = {"mc_grid": [int(x) for x in dims], "mc_iso": iso, "mc_ms": mc_ms, "mc_points": tm.numPoints,
+           "mc_tris": tm.numTris, "mc_voxels_per_s": int(np.prod(dims)) / (mc_ms * 1e-3)}
+    # mcOffsetMesh's volume step: box expanded by the offset, calcOriginAndDimensions, band
+    # [offset - 1.001 voxel, offset + 1.001 voxel] with nullOutsideMinMax (MRVoxels/MROffset.cpp:160-183)
+    org, odims = M.calcOriginAndDimensions(v.min(0) - iso, v.max(0) + iso, vs)
+    opts = M.DistanceToMeshOptions(minDistSq=max(iso - 1.001 * vs, 0.0) ** 2, maxDistSq=(iso + 1.001 * vs) ** 2,
+                                   nullOutsideMinMax=True)
+    oprm = M.MarchingCubesParams(origin=tuple(float(x) for x in org), voxelSize=(vs,) * 3, iso=iso, lessInside=True)
+    ts, tdev = [], []
+    for i in range(4):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        om = fwn.gridToMesh(odims, org, vs, opts, oprm)
+        t1 = time.perf_counter()
+        _ = om.points, om.tris
+        t2 = time.perf_counter()
+        if i:
+            tdev.append(t1 - t0)
+            ts.append(t2 - t0)
+    res.update({"offset_dims": [int(x) for x in odims], "offset_voxels": int(np.prod(odims)), "offset_tris": om.numTris,
+                "offset_fused_ms": 1e3 * float(np.mean(tdev)), "offset_fused_to_host_ms": 1e3 * float(np.mean(ts)),
+                "offset_note": "banded distance grid (brick culling) + marching cubes on the device, mesh copied to host; "
+                               "the grid never leaves the GPU"})
+    if with_cpu:
+        import oracle as O
+        h = grid_dev.cpu().numpy().reshape(dims[2], dims[1], dims[0])
+        t0 = time.perf_counter()
+        ref = O.marching_cubes(h, origin=origin, voxel_size=(vs,) * 3, iso=iso, less_inside=True)
+        cpu_s = time.perf_counter() - t0
+        res.update({"mc_cpu_port_s": cpu_s, "mc_cpu_cores": 1, "mc_speedup_vs_cpu_port": cpu_s / (mc_ms * 1e-3),
+                    "mc_bitexact_vs_oracle": bool(np.array_equal(tm.points.view(np.uint32), ref[0].view(np.uint32))
+                                                  and np.array_equal(tm.tris, ref[1]))})
+    return res
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -333,6 +382,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-mesh batched leg")
     ap.add_argument("--no-points", action="store_true", help="skip the shell-point / self-intersection leg")
     ap.add_argument("--no-refgpu", action="store_true", help="skip timing the reference's own GPU kernels")
+    ap.add_argument("--no-offset", action="store_true", help="skip the marching-cubes / offset-mesh leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -555,6 +605,11 @@ def main():
                    "batched_voxels_per_s": bvox / (min(batch_ms, graph_ms) * 1e-3), "autotune": tune}
         del batch, handles, outs, items
 
+    # ---- the grid's consumer: marching cubes on the device grid (MeshLib's VolumeMesher, bit for bit)
+    # and mcOffsetMesh's volume step fused on the device (banded distance grid -> mesh -> host)
+    offset = None
+    if not args.no_offset:
+        offset = offset_leg(M, fwn, v, f, dims, xf, out, timed, stream, sp, rank == 0 and not args.no_cpu)
 
     peak, peak_kind = _peaks()
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
@@ -568,7 +623,7 @@ def main():
                     "d2h_bytes_per_step": int(nvox * 4), "s_per_step": e2e_s,
                     "s_create_per_step": float(np.mean(create_times)) if create_times else None},
             "clocks": clk.summary(), "nan_fraction": nan_frac, "wall_s_timed": wall, "banded": banded, "batched": batched, "points": points,
-            "reference_gpu": refgpu}
+            "reference_gpu": refgpu, "offset": offset}
     if rank == 0 and not args.no_cpu:
         rate, thr, desc, counts = cpu_reference_rate(v, f, dims, xf)
         bpv = bytes_per_voxel(counts)

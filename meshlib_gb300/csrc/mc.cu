@@ -18,17 +18,21 @@
 //     zeroPoint = origin + (0.5, 0.5, 0.5 + z0) * voxelSize, p = zeroPoint + voxelSize * (x, y, z - z0)
 //     (MRMarchingCubes.cpp:566); the whole volume is one part with z0 = 0.
 //
-// GB300 design: five streaming passes, no hash map.  The reference keeps separation points in
-// per-block hash maps keyed by voxel id; here one byte per voxel (crossing bits, below-iso bit, NaN
-// bit) and two exclusive scans over 16-voxel chunks give every vertex and triangle its global id:
-// the id of the vertex on edge `dir` of voxel u is
-//   vertBase[u / 16] + popc(crossing bits of the chunk's bytes before u) + popc(u's bits below dir),
-// one 16-byte load.  Passes (thread per voxel, grid-stride, 16-lane groups = chunks):
-//   classifyKernel  flags + vertices per chunk          reads the volume once (+ neighbours, L2)
-//   cellKernel      triangles per cell + per chunk      reads 8 flag bytes per cell (L1/L2)
+// GB300 design: streaming passes, no hash map.  The reference keeps separation points in per-block
+// hash maps keyed by voxel id; here one byte per voxel (crossing bits, below-iso bit, NaN bit) and
+// two exclusive scans over 16-voxel chunks give every vertex and triangle its global id: the id of
+// the vertex on edge `dir` of voxel u is
+//   vertBase[chunk(u)] + popc(crossing bits of the chunk's bytes before u) + popc(u's bits below dir),
+// one 16-byte load.  A warp works on 32 voxels of one row at a time (a contiguous run of rows per
+// warp, no division per voxel); the flag arrays have a row pitch of whole 32-byte segments so that
+// chunks are aligned and numbered in voxel order.
+//   classifyKernel  flags + vertices per chunk: the one dense pass over the volume, four row
+//                   segments in flight per warp
+//   cellKernel      triangles per cell + per chunk; segments whose four rows hold no crossing
+//                   (by the chunk vertex counts) are skipped
 //   two scans       chunk bases (exclusiveScanI32)
-//   vertexKernel    crossing positions
-//   triangleKernel  vertex ids, faceMap
+//   vertexKernel    crossing positions, only where the chunk counts are nonzero
+//   triangleKernel  vertex ids and faceMap, only where the chunk counts are nonzero
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -135,9 +139,11 @@ __device__ const uint8_t kPlanTris[256] = {
 struct McDims {
     int32_t dx, dy, dz;
     int64_t sxy;     // dx * dy
-    int64_t n;       // voxels
-    int64_t nLoop;   // n rounded up to whole warps (every lane of a warp iterates together)
-    int64_t nChunks; // ceil(n / 16)
+    int64_t rows;    // dy * dz
+    int32_t xsegs;   // 32-voxel segments per row
+    int32_t pitch;   // bytes per row of the flag arrays (xsegs * 32)
+    int64_t items;   // rows * xsegs warp work items
+    int64_t nChunks; // rows * pitch / 16
 };
 
 struct McGeom {
@@ -146,13 +152,74 @@ struct McGeom {
     float iso;
 };
 
-__device__ __forceinline__ void voxelPos(const McDims& d, int64_t id, int& x, int& y, int& z) {
-    const int64_t zz = id / d.sxy;
-    const int64_t r = id - zz * d.sxy;
-    const int64_t yy = r / d.dx;
-    z = int(zz);
-    y = int(yy);
-    x = int(r - yy * d.dx);
+// A warp work item is 32 consecutive voxels of one row (x fastest): lane = x % 32.  Flag arrays are
+// stored with a row pitch of whole 32-byte segments, so every 16-voxel chunk is 16-byte aligned and
+// chunks are numbered in voxel order (row-major, then x).  Each warp walks a contiguous run of items
+// with an incrementing cursor (no division per item).
+struct WarpItem {
+    int x, y, z;
+    int64_t row;
+    bool in;  // x < dx
+};
+
+// The contiguous run of items [w0, w1) of this warp.
+__device__ __forceinline__ void warpRange(const McDims& d, int64_t& w0, int64_t& w1) {
+    const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t per = (d.items + nw - 1) / nw;
+    w0 = gw * per;
+    w1 = min(w0 + per, d.items);
+}
+
+// Position of item w (divisions: used once per run, or for the few items a sparse pass visits).
+struct Cursor {
+    int64_t row;
+    int seg, y, z;
+    __device__ __forceinline__ void init(const McDims& d, int64_t w) {
+        row = w / d.xsegs;
+        seg = int(w - row * d.xsegs);
+        z = int(row / d.dy);
+        y = int(row - int64_t(z) * d.dy);
+    }
+    __device__ __forceinline__ WarpItem item(const McDims& d, int lane) const {
+        WarpItem it;
+        it.row = row;
+        it.y = y;
+        it.z = z;
+        it.x = seg * 32 + lane;
+        it.in = it.x < d.dx;
+        return it;
+    }
+    __device__ __forceinline__ void advance(const McDims& d) {
+        if (++seg == d.xsegs) {
+            seg = 0;
+            ++row;
+            if (++y == d.dy) {
+                y = 0;
+                ++z;
+            }
+        }
+    }
+};
+
+// Visits the items of this warp whose two 16-voxel chunks are not both empty by `counts`
+// (chunk c of item w is 2w + c): 32 counts per load, a ballot, then only the marked items.
+template <typename F>
+__device__ __forceinline__ void forEachMarkedItem(const McDims& d, int lane, const int32_t* __restrict__ counts, F&& body) {
+    int64_t w0, w1;
+    warpRange(d, w0, w1);
+    for (int64_t g = w0; g < w1; g += 16) {
+        const int64_t ch = 2 * g + lane;
+        const int cnt = ch < 2 * w1 ? counts[ch] : 0;
+        unsigned m = __ballot_sync(FULL, cnt != 0);
+        while (m) {
+            const int k = (__ffs(m) - 1) >> 1;
+            m &= ~(3u << (2 * k));
+            Cursor c;
+            c.init(d, g + k);
+            body(c.item(d, lane));
+        }
+    }
 }
 
 // sum over the 16 lanes of a chunk (lanes 0-15 and 16-31 of a warp are two chunks)
@@ -175,42 +242,55 @@ __device__ __forceinline__ int chunkExclusive(int c, int lane) {
     return p - c;
 }
 
-__global__ void __launch_bounds__(256) classifyKernel(const float* __restrict__ vol, McDims d, float iso,
+constexpr int kClassifyUnroll = 4;  // row segments in flight per warp
+
+__global__ void __launch_bounds__(256, 4) classifyKernel(const float* __restrict__ vol, McDims d, float iso,
                                                       uint8_t* __restrict__ flags, int32_t* __restrict__ chunkVerts,
                                                       unsigned long long* __restrict__ total) {
     const int lane = threadIdx.x & 31;
     unsigned long long mine = 0;
-    for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < d.nLoop; id += int64_t(gridDim.x) * blockDim.x) {
-        unsigned f = 0;
-        if (id < d.n) {
-            int x, y, z;
-            voxelPos(d, id, x, y, z);
-            const float v = vol[id];
-            const bool lower = v < iso, notLower = v >= iso;
-            if (!lower && !notLower) {
-                f = kInvalid;
-            } else {
-                if (lower) f |= kLower;
-                // a crossing needs the neighbour on the other side; a NaN neighbour is on neither
-                if (x + 1 < d.dx) {
-                    const float nv = vol[id + 1];
-                    if (lower ? nv >= iso : nv < iso) f |= 1u;
-                }
-                if (y + 1 < d.dy) {
-                    const float nv = vol[id + d.dx];
-                    if (lower ? nv >= iso : nv < iso) f |= 2u;
-                }
-                if (z + 1 < d.dz) {
-                    const float nv = vol[id + d.sxy];
-                    if (lower ? nv >= iso : nv < iso) f |= 4u;
+    int64_t w0, w1;
+    warpRange(d, w0, w1);
+    Cursor cur;
+    if (w0 < w1) cur.init(d, w0);
+    for (int64_t w = w0; w < w1; w += kClassifyUnroll) {
+        WarpItem it[kClassifyUnroll];
+        float v[kClassifyUnroll], nx[kClassifyUnroll], ny[kClassifyUnroll], nz[kClassifyUnroll];
+        // all loads of the group first: they do not depend on one another
+#pragma unroll
+        for (int k = 0; k < kClassifyUnroll; ++k) {
+            it[k] = cur.item(d, lane);
+            cur.advance(d);
+            const bool ok = w + k < w1 && it[k].in;
+            const int64_t id = it[k].row * d.dx + it[k].x;
+            v[k] = ok ? vol[id] : 0.f;
+            nx[k] = ok && it[k].x + 1 < d.dx ? vol[id + 1] : 0.f;
+            ny[k] = ok && it[k].y + 1 < d.dy ? vol[id + d.dx] : 0.f;
+            nz[k] = ok && it[k].z + 1 < d.dz ? vol[id + d.sxy] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < kClassifyUnroll; ++k) {
+            if (w + k >= w1) break;  // warp-uniform
+            unsigned f = 0;
+            if (it[k].in) {
+                const bool lower = v[k] < iso, notLower = v[k] >= iso;
+                if (!lower && !notLower) {
+                    f = kInvalid;
+                } else {
+                    // a crossing needs the neighbour on the other side; a NaN neighbour is on neither
+                    if (lower) f |= kLower;
+                    if (it[k].x + 1 < d.dx && (lower ? nx[k] >= iso : nx[k] < iso)) f |= 1u;
+                    if (it[k].y + 1 < d.dy && (lower ? ny[k] >= iso : ny[k] < iso)) f |= 2u;
+                    if (it[k].z + 1 < d.dz && (lower ? nz[k] >= iso : nz[k] < iso)) f |= 4u;
                 }
             }
+            const int64_t at = it[k].row * d.pitch + it[k].x;
+            flags[at] = uint8_t(f);
+            const int c = __popc(f & 7u);
+            const int sum = chunkSum(c);
+            if ((lane & 15) == 0) chunkVerts[at >> 4] = sum;
+            mine += c;
         }
-        flags[id] = uint8_t(f);
-        const int c = __popc(f & 7u);
-        const int s = chunkSum(c);
-        if ((lane & 15) == 0 && (id >> 4) < d.nChunks) chunkVerts[id >> 4] = s;
-        mine += c;
     }
     for (int off = 16; off; off >>= 1) mine += __shfl_xor_sync(FULL, mine, off);
     if (lane == 0 && mine) atomicAdd(total, mine);
@@ -222,18 +302,20 @@ struct CellInfo {
     unsigned cross;  // crossing bits of corners 0..6, three per corner
 };
 
+// offset of corner c of a cell in the pitched flag arrays
 __device__ __forceinline__ int64_t cornerOffset(const McDims& d, int c) {
-    return int64_t(c & 1) + ((c >> 1) & 1) * int64_t(d.dx) + ((c >> 2) & 1) * d.sxy;
+    return int64_t(c & 1) + ((c >> 1) & 1) * int64_t(d.pitch) + ((c >> 2) & 1) * int64_t(d.pitch) * d.dy;
 }
 
-// Configuration, neighbour set and triangle count of the cell whose min corner is voxel id
-// (MRMarchingCubes.cpp:880-1054).  Returns 0 when the cell emits nothing.  Corner states are
-// kept as bit masks (bit i = corner i) so that nothing is indexed at run time.
-__device__ __forceinline__ int cellTriangles(const uint8_t* __restrict__ flags, const McDims& d, int64_t id, CellInfo& ci) {
+// Configuration, neighbour set and triangle count of a cell from the flag bytes of its 8 corners
+// (corner i = byte i of c0123 | c4567 << 32) (MRMarchingCubes.cpp:880-1054).  Returns 0 when the cell
+// emits nothing.  Corner states are kept as bit masks (bit i = corner i): nothing is indexed at
+// run time.
+__device__ __forceinline__ int cellCore(unsigned long long corners, CellInfo& ci) {
     unsigned inv = 0, low = 0, cross = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const unsigned f = flags[id + cornerOffset(d, i)];
+        const unsigned f = unsigned(corners >> (8 * i)) & 0xffu;
         inv |= ((f >> 4) & 1u) << i;
         low |= ((f >> 3) & 1u) << i;
         if (i < 7) cross |= (f & 7u) << (3 * i);
@@ -256,11 +338,11 @@ __device__ __forceinline__ int cellTriangles(const uint8_t* __restrict__ flags, 
         }
         low = sub;
     }
+    if (low == 0u || low == 0xffu) return 0;
     int config = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i)
         if ((low >> i) & 1u) config |= 1 << kCornerBit[i];
-    if (config == 0 || config == 0xff) return 0;
     auto vx = [low](int i) { return (low >> i) & 1u; };
     auto has = [cross](int i, unsigned dirs) { return ((cross >> (3 * i)) & dirs) != 0u; };
     // corner i contributes when its edges inside the cell change sign and its voxel has a point on
@@ -289,70 +371,122 @@ __device__ __forceinline__ int cellTriangles(const uint8_t* __restrict__ flags, 
     return nt;
 }
 
-__global__ void __launch_bounds__(256) cellKernel(const uint8_t* __restrict__ flags, McDims d, uint8_t* __restrict__ tcnt,
-                                                  int32_t* __restrict__ chunkTris, unsigned long long* __restrict__ total) {
+// The same for the cell whose min corner sits at `at` in the pitched flag array (8 loads).
+__device__ __forceinline__ int cellTriangles(const uint8_t* __restrict__ flags, const McDims& d, int64_t at, CellInfo& ci) {
+    unsigned long long corners = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) corners |= (unsigned long long)flags[at + cornerOffset(d, i)] << (8 * i);
+    return cellCore(corners, ci);
+}
+
+// Triangle counts per cell.  A warp first checks the vertex counts of the 16-voxel chunks its 32
+// cells touch (two chunks and the next one in each of the four rows): with no crossing there, no
+// cell can emit a triangle (a triangle needs a vertex on one of its cell's corners), and only the
+// chunk counts are written.  Otherwise it reads its 32 flag bytes in each of the four rows
+// (coalesced); the +x corners come from the next lane (lane 31 reads one more byte).
+__global__ void __launch_bounds__(256) cellKernel(const uint8_t* __restrict__ flags, const int32_t* __restrict__ chunkVerts,
+                                                  McDims d, uint8_t* __restrict__ tcnt, int32_t* __restrict__ chunkTris,
+                                                  unsigned long long* __restrict__ total) {
     const int lane = threadIdx.x & 31;
     unsigned long long mine = 0;
-    for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < d.nLoop; id += int64_t(gridDim.x) * blockDim.x) {
-        int nt = 0;
-        if (id < d.n) {
-            int x, y, z;
-            voxelPos(d, id, x, y, z);
-            CellInfo ci;
-            if (x + 1 < d.dx && y + 1 < d.dy && z + 1 < d.dz) nt = cellTriangles(flags, d, id, ci);
+    const int64_t layer = int64_t(d.pitch) * d.dy;
+    int64_t w0, w1;
+    warpRange(d, w0, w1);
+    Cursor cur;
+    if (w0 < w1) cur.init(d, w0);
+    for (int64_t w = w0; w < w1; ++w, cur.advance(d)) {
+        const WarpItem it = cur.item(d, lane);
+        const int64_t at = it.row * d.pitch + it.x;
+        const bool hy = it.y + 1 < d.dy, hz = it.z + 1 < d.dz;
+        int cnt = 0;
+        if (lane < 12) {
+            const int r = lane / 3, k = lane - 3 * r;
+            const bool rowOk = ((r & 1) == 0 || hy) && ((r & 2) == 0 || hz);
+            if (rowOk && (k < 2 || cur.seg + 1 < d.xsegs)) {
+                const int64_t rr = it.row + (r & 1) + ((r & 2) ? d.dy : 0);
+                cnt = chunkVerts[2 * (rr * d.xsegs + cur.seg) + k];
+            }
         }
-        tcnt[id] = uint8_t(nt);
-        const int s = chunkSum(nt);
-        if ((lane & 15) == 0 && (id >> 4) < d.nChunks) chunkTris[id >> 4] = s;
+        if (!__any_sync(FULL, cnt != 0)) {
+            if ((lane & 15) == 0) chunkTris[at >> 4] = 0;
+            continue;
+        }
+        const bool cell = it.x + 1 < d.dx && hy && hz;
+        const unsigned r0 = flags[at];
+        const unsigned r1 = hy ? flags[at + d.pitch] : 0u;
+        const unsigned r2 = hz ? flags[at + layer] : 0u;
+        const unsigned r3 = hy && hz ? flags[at + d.pitch + layer] : 0u;
+        unsigned n0 = __shfl_down_sync(FULL, r0, 1), n1 = __shfl_down_sync(FULL, r1, 1);
+        unsigned n2 = __shfl_down_sync(FULL, r2, 1), n3 = __shfl_down_sync(FULL, r3, 1);
+        if (lane == 31 && cell) {  // x + 1 starts the next segment of the same row
+            n0 = flags[at + 1];
+            n1 = flags[at + d.pitch + 1];
+            n2 = flags[at + layer + 1];
+            n3 = flags[at + d.pitch + layer + 1];
+        }
+        int nt = 0;
+        if (cell && ((r0 | r1 | r2 | r3 | n0 | n1 | n2 | n3) & 7u)) {
+            const unsigned long long corners =
+                (unsigned long long)(r0 | (n0 << 8) | (r1 << 16) | (n1 << 24)) |
+                ((unsigned long long)(r2 | (n2 << 8) | (r3 << 16) | (n3 << 24)) << 32);
+            CellInfo ci;
+            nt = cellCore(corners, ci);
+        }
+        tcnt[at] = uint8_t(nt);
+        const int sum = chunkSum(nt);
+        if ((lane & 15) == 0) chunkTris[at >> 4] = sum;
         mine += nt;
     }
     for (int off = 16; off; off >>= 1) mine += __shfl_xor_sync(FULL, mine, off);
     if (lane == 0 && mine) atomicAdd(total, mine);
 }
 
+// Crossing positions: only the items whose chunks hold vertices.
 __global__ void __launch_bounds__(256) vertexKernel(const float* __restrict__ vol, const uint8_t* __restrict__ flags,
-                                                    const int32_t* __restrict__ vertBase, McDims d, McGeom g,
-                                                    const float* __restrict__ layerZ, float* __restrict__ points) {
+                                                    const int32_t* __restrict__ chunkVerts, const int32_t* __restrict__ vertBase,
+                                                    McDims d, McGeom g, const float* __restrict__ layerZ,
+                                                    float* __restrict__ points) {
     const int lane = threadIdx.x & 31;
-    for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < d.nLoop; id += int64_t(gridDim.x) * blockDim.x) {
-        const unsigned f = id < d.n ? flags[id] : 0u;
+    forEachMarkedItem(d, lane, chunkVerts, [&](const WarpItem& it) {
+        const int64_t at = it.row * d.pitch + it.x;
+        const unsigned f = flags[at];  // 0 past the row end
         const int c = __popc(f & 7u);
         const int ex = chunkExclusive(c, lane);
-        if (!c) continue;
-        int64_t v = int64_t(vertBase[id >> 4]) + ex;
-        int x, y, z;
-        voxelPos(d, id, x, y, z);
+        if (!c) return;
+        int64_t v = int64_t(vertBase[at >> 4]) + ex;
+        const int64_t id = it.row * d.dx + it.x;
         const float v0 = vol[id];
-        const float p0[3] = {__fadd_rn(g.zpx, __fmul_rn(g.vs[0], float(x))), __fadd_rn(g.zpy, __fmul_rn(g.vs[1], float(y))),
-                             layerZ[z]};
+        const float p0[3] = {__fadd_rn(g.zpx, __fmul_rn(g.vs[0], float(it.x))),
+                             __fadd_rn(g.zpy, __fmul_rn(g.vs[1], float(it.y))), layerZ[it.z]};
         const int64_t inc[3] = {1, d.dx, d.sxy};
 #pragma unroll
         for (int n = 0; n < 3; ++n) {
             if (!((f >> n) & 1u)) continue;
             const float v1 = vol[id + inc[n]];
             const float r = __fdiv_rn(__fsub_rn(g.iso, v0), __fsub_rn(v1, v0));
-            const float w = __fsub_rn(1.0f, r);
+            const float wgt = __fsub_rn(1.0f, r);
             float p1[3] = {p0[0], p0[1], p0[2]};
             p1[n] = __fadd_rn(p0[n], g.vs[n]);
             float* o = points + 3 * v;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) o[k] = __fadd_rn(__fmul_rn(w, p0[k]), __fmul_rn(r, p1[k]));
+            for (int k = 0; k < 3; ++k) o[k] = __fadd_rn(__fmul_rn(wgt, p0[k]), __fmul_rn(r, p1[k]));
             ++v;
         }
-    }
+    });
 }
 
-// Global id of the vertex on edge `dir` of voxel u (which has it).
-__device__ __forceinline__ int32_t vertexId(const uint8_t* __restrict__ flags, const int32_t* __restrict__ vertBase, int64_t u,
+// Global id of the vertex on edge `dir` of the voxel at `at` in the pitched flag array (which has it):
+// its chunk's base + the crossings of the chunk's voxels before it + its own below `dir`.
+__device__ __forceinline__ int32_t vertexId(const uint8_t* __restrict__ flags, const int32_t* __restrict__ vertBase, int64_t at,
                                             int dir) {
-    const int64_t chunk = u >> 4;
+    const int64_t chunk = at >> 4;
     const uint4 w = __ldg(reinterpret_cast<const uint4*>(flags) + chunk);
-    const int j = int(u & 15);
+    const int j = int(at & 15);
     const unsigned words[4] = {w.x, w.y, w.z, w.w};
     int p = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const int nb = min(max(j - 4 * q, 0), 4);  // bytes of this word before u
+        const int nb = min(max(j - 4 * q, 0), 4);  // bytes of this word before the voxel
         const unsigned m = nb >= 4 ? 0x07070707u : (0x07070707u & ((1u << (8 * nb)) - 1u));
         p += __popc(words[q] & m);
     }
@@ -361,33 +495,35 @@ __device__ __forceinline__ int32_t vertexId(const uint8_t* __restrict__ flags, c
     return vertBase[chunk] + p;
 }
 
+// Triangles: only the items whose chunks hold triangles (tcnt is only written for those).
 __global__ void __launch_bounds__(256) triangleKernel(const uint8_t* __restrict__ flags, const uint8_t* __restrict__ tcnt,
-                                                      const int32_t* __restrict__ vertBase, const int32_t* __restrict__ triBase,
-                                                      McDims d, int lessInside, int32_t* __restrict__ tris,
-                                                      int32_t* __restrict__ faceMap) {
+                                                      const int32_t* __restrict__ chunkTris, const int32_t* __restrict__ vertBase,
+                                                      const int32_t* __restrict__ triBase, McDims d, int lessInside,
+                                                      int32_t* __restrict__ tris, int32_t* __restrict__ faceMap) {
     const int lane = threadIdx.x & 31;
-    for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < d.nLoop; id += int64_t(gridDim.x) * blockDim.x) {
-        const int t = id < d.n ? tcnt[id] : 0;
+    forEachMarkedItem(d, lane, chunkTris, [&](const WarpItem& it) {
+        const int64_t at = it.row * d.pitch + it.x;
+        const int t = tcnt[at];  // 0 past the row end
         const int ex = chunkExclusive(t, lane);
-        if (!t) continue;
+        if (!t) return;
         CellInfo ci;
-        const int nt = cellTriangles(flags, d, id, ci);
+        const int nt = cellTriangles(flags, d, at, ci);
         const unsigned long long plan = kPlan[ci.config];
-        int64_t base = int64_t(triBase[id >> 4]) + ex;
+        int64_t base = int64_t(triBase[at >> 4]) + ex;
         for (int k = 0; k < nt; ++k, ++base) {
             int32_t ids[3];
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
                 const int e = int((plan >> (4 * (3 * k + m))) & 15u);
-                ids[m] = vertexId(flags, vertBase, id + cornerOffset(d, kEdgeCorner[e]), kEdgeDir[e]);
+                ids[m] = vertexId(flags, vertBase, at + cornerOffset(d, kEdgeCorner[e]), kEdgeDir[e]);
             }
             int32_t* o = tris + 3 * base;
             o[0] = ids[0];
             o[1] = lessInside ? ids[2] : ids[1];
             o[2] = lessInside ? ids[1] : ids[2];
-            if (faceMap) faceMap[base] = int32_t(id);
+            if (faceMap) faceMap[base] = int32_t(it.row * d.dx + it.x);
         }
-    }
+    });
 }
 
 }  // namespace
@@ -496,10 +632,12 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     d.dy = dims[1];
     d.dz = dims[2];
     d.sxy = int64_t(dims[0]) * dims[1];
-    d.n = d.sxy * dims[2];
-    d.nLoop = (d.n + 31) / 32 * 32;
-    d.nChunks = (d.n + 15) / 16;
-    if (p.wantFaceMap && d.n > INT32_MAX) {
+    d.rows = int64_t(dims[1]) * dims[2];
+    d.xsegs = (dims[0] + 31) / 32;
+    d.pitch = d.xsegs * 32;
+    d.items = d.rows * d.xsegs;
+    d.nChunks = d.rows * d.pitch / 16;
+    if (p.wantFaceMap && d.sxy * dims[2] > INT32_MAX) {
         delete m;
         return mcError("voxel ids of the face map exceed 32 bits");
     }
@@ -518,8 +656,9 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     unsigned long long* totals = nullptr;
     float* dLz = nullptr;
     const int64_t nbSums = (d.nChunks + 1023) / 1024 + 1;
-    const size_t sizes[10] = {size_t(d.nLoop) + 16,
-                              size_t(d.nLoop) + 16,
+    const size_t flagBytes = size_t(d.rows) * size_t(d.pitch) + 16;
+    const size_t sizes[10] = {flagBytes,
+                              flagBytes,
                               sizeof(int32_t) * size_t(d.nChunks),
                               sizeof(int32_t) * size_t(d.nChunks),
                               sizeof(int32_t) * size_t(d.nChunks),
@@ -542,11 +681,11 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     }
     if (!e) e = cudaMemsetAsync(totals, 0, sizeof(unsigned long long) * 2, s);
     if (!e) e = cudaMemcpyAsync(dLz, lz.data(), sizeof(float) * lz.size(), cudaMemcpyHostToDevice, s);
-    const int64_t want = (d.nLoop + 255) / 256;
+    const int64_t want = (d.items + 7) / 8;  // 8 warps per block
     const unsigned nb = unsigned(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(numSMs()) * 8)));
     if (!e) {
         classifyKernel<<<nb, 256, 0, s>>>(dVol, d, p.iso, flags, chunkV, totals);
-        cellKernel<<<nb, 256, 0, s>>>(flags, d, tcnt, chunkT, totals + 1);
+        cellKernel<<<nb, 256, 0, s>>>(flags, chunkV, d, tcnt, chunkT, totals + 1);
         e = cudaGetLastError();
     }
     unsigned long long ht[2] = {0, 0};
@@ -572,8 +711,8 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     if (!e) e = devMalloc((void**)&m->dTris, sizeof(int32_t) * 3 * size_t(m->nTris));
     if (!e && p.wantFaceMap) e = devMalloc((void**)&m->dFaceMap, sizeof(int32_t) * size_t(m->nTris));
     if (!e) {
-        vertexKernel<<<nb, 256, 0, s>>>(dVol, flags, baseV, d, g, dLz, m->dPoints);
-        triangleKernel<<<nb, 256, 0, s>>>(flags, tcnt, baseV, baseT, d, p.lessInside ? 1 : 0, m->dTris, m->dFaceMap);
+        vertexKernel<<<nb, 256, 0, s>>>(dVol, flags, chunkV, baseV, d, g, dLz, m->dPoints);
+        triangleKernel<<<nb, 256, 0, s>>>(flags, tcnt, chunkT, baseV, baseT, d, p.lessInside ? 1 : 0, m->dTris, m->dFaceMap);
         e = cudaGetLastError();
     }
     if (!e) e = cudaStreamSynchronize(s);
