@@ -68,6 +68,97 @@ inline int slabThunk(const float* data, const int32_t dims[3], int32_t zOffset, 
 }
 }  // namespace detail
 
+// MR::TriMesh as the mesher returns it: points (3 floats each), triangles (3 vertex ids each) and,
+// when requested, the face -> voxel map (MR::Vector<VoxelId, FaceId>).
+struct TriMesh {
+    std::vector<float> points;
+    std::vector<int32_t> tris;
+    std::vector<int32_t> faceMap;
+};
+
+// MR::MarchingCubesParams (MRVoxels/MRMarchingCubes.h:18-61) for the default linear positioner;
+// voxelSize is the volume's (SimpleVolume::voxelSize).
+struct MarchingCubesParams {
+    float origin[3] = {0.f, 0.f, 0.f};
+    float voxelSize[3] = {1.f, 1.f, 1.f};
+    float iso = 0.f;
+    bool lessInside = false;
+    int64_t maxVertices = 2147483647;
+    bool outVoxelPerFaceMap = false;
+    gbfwn_mc_params c() const {
+        gbfwn_mc_params p;
+        gbfwn_mc_default_params(&p);
+        for (int k = 0; k < 3; ++k) {
+            p.origin[k] = origin[k];
+            p.voxelSize[k] = voxelSize[k];
+        }
+        p.iso = iso;
+        p.lessInside = lessInside ? 1 : 0;
+        p.maxVertices = maxVertices;
+        p.wantFaceMap = outVoxelPerFaceMap ? 1 : 0;
+        return p;
+    }
+};
+
+namespace detail {
+// copies a device mesh into `out` and frees it
+inline Result takeMesh(int st, gbfwn_trimesh m, TriMesh& out) {
+    if (st != GBFWN_OK) return Result::fromStatus(st);
+    int64_t np = 0, nt = 0;
+    gbfwn_trimesh_sizes(m, &np, &nt);
+    const int32_t* dFace = nullptr;
+    gbfwn_trimesh_device(m, nullptr, nullptr, &dFace);
+    out.points.resize(size_t(3 * np));
+    out.tris.resize(size_t(3 * nt));
+    out.faceMap.resize(dFace ? size_t(nt) : 0);
+    st = gbfwn_trimesh_copy(m, out.points.data(), out.tris.data(), dFace ? out.faceMap.data() : nullptr);
+    gbfwn_trimesh_destroy(m);
+    return Result::fromStatus(st);
+}
+}  // namespace detail
+
+// MR::marchingCubesAsTriMesh(SimpleVolume, params) (MRVoxels/MRMarchingCubes.h:66) on the GPU:
+// the same TriMesh, bit for bit.  volume: dims[0] x dims[1] x dims[2] floats, x fastest.
+inline Result marchingCubes(TriMesh& out, const std::vector<float>& volume, const int32_t dims[3],
+                            const MarchingCubesParams& params = {}, const ProgressCallback& cb = {}, int device = 0) {
+    const gbfwn_mc_params p = params.c();
+    gbfwn_trimesh m = nullptr;
+    const int st = gbfwn_marching_cubes(volume.data(), dims, &p, nullptr, 0, device, &m,
+                                        cb ? &detail::progressThunk : nullptr,
+                                        cb ? const_cast<ProgressCallback*>(&cb) : nullptr);
+    return detail::takeMesh(st, m, out);
+}
+
+// MR::MarchingCubesByParts (MRVoxels/MRMarchingCubes.h:96-122): addPart() volumes of whole XY layers
+// starting at nextZ() (the previous part's last layer repeated), then finalize().
+class MarchingCubesByParts {
+public:
+    MarchingCubesByParts(const int32_t dims[3], const MarchingCubesParams& params, int device = 0) {
+        const gbfwn_mc_params p = params.c();
+        gbfwn_mc_parts h = nullptr;
+        created_ = Result::fromStatus(gbfwn_mc_parts_create(dims, &p, device, &h));
+        h_.reset(h);
+    }
+    int nextZ() const { return h_ ? gbfwn_mc_parts_next_z(h_.get()) : 0; }
+    Result addPart(const std::vector<float>& part, const int32_t partDims[3]) {
+        if (!h_) return created_;
+        return Result::fromStatus(gbfwn_mc_parts_add(h_.get(), part.data(), partDims));
+    }
+    Result finalize(TriMesh& out) {
+        if (!h_) return created_;
+        gbfwn_trimesh m = nullptr;
+        const int st = gbfwn_mc_parts_finalize(h_.get(), &m);
+        return detail::takeMesh(st, m, out);
+    }
+
+private:
+    struct Del {
+        void operator()(gbfwn_mc_parts p) const { gbfwn_mc_parts_destroy(p); }
+    };
+    std::unique_ptr<gbfwn_mc_parts_s, Del> h_;
+    Result created_;
+};
+
 // GPU fast winding number of one mesh.  Like MR::Cuda::FastWindingNumber it keeps the device data
 // (mesh, tree, dipoles) for the lifetime of the object; calls on one object are serialised.
 class FastWindingNumber {
@@ -130,6 +221,19 @@ public:
                                                                cb ? &detail::progressThunk : nullptr, cbUser(cb));
         if (!ctx.err) return ctx.err;
         return Result::fromStatus(st);
+    }
+
+    // mcOffsetMesh's volume step fused on the device: the signed-distance grid of dims voxels centred
+    // at origin + (i + 0.5) * voxelSize, meshed by marching cubes without leaving the GPU
+    // (gbfwn_grid_to_mesh).  mcOffsetMesh passes mc.origin = origin, mc.iso = offset, lessInside.
+    Result gridToMesh(TriMesh& out, const int32_t dims[3], const float origin[3], const float voxelSize[3],
+                      const DistanceToMeshOptions& options, const MarchingCubesParams& mc, const ProgressCallback& cb = {}) {
+        const gbfwn_dist_opts o = options.c();
+        const gbfwn_mc_params p = mc.c();
+        gbfwn_trimesh m = nullptr;
+        const int st = gbfwn_grid_to_mesh(h_.get(), nullptr, dims, origin, voxelSize, &o, &p, nullptr, 0, &m,
+                                          cb ? &detail::progressThunk : nullptr, cbUser(cb));
+        return detail::takeMesh(st, m, out);
     }
 
 private:

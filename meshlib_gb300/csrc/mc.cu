@@ -611,6 +611,13 @@ int layerCoords(const int32_t dims[3], const gbfwn_mc_params& p, const int32_t* 
     return GBFWN_OK;
 }
 
+// Blocks of 256 threads: 8 per SM (a one-wave grid sized by occupancy measured no faster), fewer
+// for small volumes.
+unsigned mcBlocks(const McDims& d) {
+    const int64_t want = (d.items + 7) / 8;  // 8 warps per block
+    return unsigned(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(numSMs()) * 8)));
+}
+
 // The mesher on a device volume; the result is complete when this returns.
 int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_params& p, const int32_t* partStarts,
                      int32_t nParts, int device, cudaStream_t s, gbfwn_trimesh* out, const char* what) {
@@ -681,11 +688,9 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     }
     if (!e) e = cudaMemsetAsync(totals, 0, sizeof(unsigned long long) * 2, s);
     if (!e) e = cudaMemcpyAsync(dLz, lz.data(), sizeof(float) * lz.size(), cudaMemcpyHostToDevice, s);
-    const int64_t want = (d.items + 7) / 8;  // 8 warps per block
-    const unsigned nb = unsigned(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(numSMs()) * 8)));
     if (!e) {
-        classifyKernel<<<nb, 256, 0, s>>>(dVol, d, p.iso, flags, chunkV, totals);
-        cellKernel<<<nb, 256, 0, s>>>(flags, chunkV, d, tcnt, chunkT, totals + 1);
+        classifyKernel<<<mcBlocks(d), 256, 0, s>>>(dVol, d, p.iso, flags, chunkV, totals);
+        cellKernel<<<mcBlocks(d), 256, 0, s>>>(flags, chunkV, d, tcnt, chunkT, totals + 1);
         e = cudaGetLastError();
     }
     unsigned long long ht[2] = {0, 0};
@@ -711,8 +716,9 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     if (!e) e = devMalloc((void**)&m->dTris, sizeof(int32_t) * 3 * size_t(m->nTris));
     if (!e && p.wantFaceMap) e = devMalloc((void**)&m->dFaceMap, sizeof(int32_t) * size_t(m->nTris));
     if (!e) {
-        vertexKernel<<<nb, 256, 0, s>>>(dVol, flags, chunkV, baseV, d, g, dLz, m->dPoints);
-        triangleKernel<<<nb, 256, 0, s>>>(flags, tcnt, chunkT, baseV, baseT, d, p.lessInside ? 1 : 0, m->dTris, m->dFaceMap);
+        vertexKernel<<<mcBlocks(d), 256, 0, s>>>(dVol, flags, chunkV, baseV, d, g, dLz, m->dPoints);
+        triangleKernel<<<mcBlocks(d), 256, 0, s>>>(flags, tcnt, chunkT, baseV, baseT, d,
+                                                                  p.lessInside ? 1 : 0, m->dTris, m->dFaceMap);
         e = cudaGetLastError();
     }
     if (!e) e = cudaStreamSynchronize(s);

@@ -86,7 +86,41 @@ int main() {
     }
     double maxDiff = 0;
     for (size_t i = 0; i < pj.size(); ++i) maxDiff = std::fmax(maxDiff, std::fabs(std::sqrt(double(pj[i].distSq)) - std::fabs(sd[i])));
-    std::printf("OK sum_sd=%.6f sum_wn=%.6f neg=%d parts_equal=%d selfint=%d cancel_status=%d proj_max_diff=%.3g\n", sumSd, sumWn,
-                neg, same, nbits, c.status(), maxDiff);
+    // marching cubes on the signed-distance grid, whole and in 2-layer parts, and the fused call
+    gbfwn::MarchingCubesParams mp;
+    for (int k = 0; k < 3; ++k) {
+        mp.voxelSize[k] = xf[4 * k];
+        mp.origin[k] = xf[9 + k] - 0.5f * xf[4 * k];
+    }
+    mp.lessInside = true;
+    mp.outVoxelPerFaceMap = true;
+    gbfwn::TriMesh whole, byParts, fused;
+    if (auto r = gbfwn::marchingCubes(whole, sd, dims, mp); !r) {
+        std::printf("ERROR mc %s\n", r.error().c_str());
+        return 1;
+    }
+    gbfwn::MarchingCubesByParts mcp(dims, mp);
+    const size_t layer = size_t(dims[0]) * dims[1];
+    for (int z = 0; z + 1 < dims[2]; ++z) {
+        std::vector<float> part(sd.begin() + layer * z, sd.begin() + layer * (z + 2));
+        const int32_t pd[3] = {dims[0], dims[1], 2};
+        if (auto r = mcp.addPart(part, pd); !r) {
+            std::printf("ERROR mc part %s\n", r.error().c_str());
+            return 1;
+        }
+    }
+    if (auto r = mcp.finalize(byParts); !r) {
+        std::printf("ERROR mc finalize %s\n", r.error().c_str());
+        return 1;
+    }
+    const float vs[3] = {xf[0], xf[4], xf[8]};
+    if (auto r = fwn.gridToMesh(fused, dims, mp.origin, vs, gbfwn::DistanceToMeshOptions{}, mp); !r) {
+        std::printf("ERROR grid_to_mesh %s\n", r.error().c_str());
+        return 1;
+    }
+    const int mcSame = whole.tris == byParts.tris && whole.faceMap == byParts.faceMap && whole.tris == fused.tris;
+    std::printf("OK sum_sd=%.6f sum_wn=%.6f neg=%d parts_equal=%d selfint=%d cancel_status=%d proj_max_diff=%.3g "
+                "mc_tris=%zu mc_points=%zu mc_same=%d\n",
+                sumSd, sumWn, neg, same, nbits, c.status(), maxDiff, whole.tris.size() / 3, whole.points.size() / 3, mcSame);
     return 0;
 }

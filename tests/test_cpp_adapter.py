@@ -49,3 +49,10 @@ def test_adapter_matches_python(tmp_path):
     assert int(kv["cancel_status"]) == M.CANCELLED
     # projector adapter: closest-point distances equal |signed distance| at the same points
     assert float(kv["proj_max_diff"]) < 1e-5
+    # marching-cubes adapter: the same mesh as the Python front-end; by parts and fused give the same
+    # triangles (points of parts differ only in the rounding of z)
+    assert kv["mc_same"] == "1"
+    prm = M.MarchingCubesParams(origin=tuple(xf[9:12] - 0.5 * xf[[0, 4, 8]]), voxelSize=tuple(xf[[0, 4, 8]]),
+                                lessInside=True)
+    tm = M.marchingCubes(sd.reshape(8, 16, 16), prm)
+    assert int(kv["mc_tris"]) == tm.numTris > 0 and int(kv["mc_points"]) == tm.numPoints
