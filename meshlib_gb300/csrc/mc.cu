@@ -26,13 +26,14 @@
 // one 16-byte load.  A warp works on 32 voxels of one row at a time (a contiguous run of rows per
 // warp, no division per voxel); the flag arrays have a row pitch of whole 32-byte segments so that
 // chunks are aligned and numbered in voxel order.
-//   classifyKernel  flags + vertices per chunk: the one dense pass over the volume, four row
-//                   segments in flight per warp
-//   cellKernel      triangles per cell + per chunk; segments whose four rows hold no crossing
-//                   (by the chunk vertex counts) are skipped
-//   two scans       chunk bases (exclusiveScanI32)
-//   vertexKernel    crossing positions, only where the chunk counts are nonzero
-//   triangleKernel  vertex ids and faceMap, only where the chunk counts are nonzero
+//   classifyKernel     flags + vertices per chunk: the one dense pass over the volume, 4 voxels per
+//                      lane (float4 loads when rows allow), two 128-voxel segments in flight per warp
+//   cellKernel         triangles per cell + per chunk, 4 cells per lane; segments whose four rows
+//                      hold no crossing (by the chunk vertex counts) are skipped
+//   two scans          chunk bases (exclusiveScanI32)
+//   vertexKernel       crossing positions, only where the chunk counts are nonzero
+//   collectCellsKernel the cells that emit triangles, as a list
+//   triangleKernel     one thread per listed cell: vertex ids and faceMap
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -144,6 +145,8 @@ struct McDims {
     int32_t pitch;   // bytes per row of the flag arrays (xsegs * 32)
     int64_t items;   // rows * xsegs warp work items
     int64_t nChunks; // rows * pitch / 16
+    int32_t qsegs;   // 128-voxel segments per row (the classification's work items, 4 voxels per lane)
+    int64_t qitems;  // rows * qsegs
 };
 
 struct McGeom {
@@ -162,22 +165,24 @@ struct WarpItem {
     bool in;  // x < dx
 };
 
-// The contiguous run of items [w0, w1) of this warp.
-__device__ __forceinline__ void warpRange(const McDims& d, int64_t& w0, int64_t& w1) {
+// The contiguous run of items [w0, w1) of this warp out of `items`.
+__device__ __forceinline__ void warpRange(int64_t items, int64_t& w0, int64_t& w1) {
     const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
     const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int64_t per = (d.items + nw - 1) / nw;
+    const int64_t per = (items + nw - 1) / nw;
     w0 = gw * per;
-    w1 = min(w0 + per, d.items);
+    w1 = min(w0 + per, items);
 }
 
 // Position of item w (divisions: used once per run, or for the few items a sparse pass visits).
 struct Cursor {
     int64_t row;
     int seg, y, z;
-    __device__ __forceinline__ void init(const McDims& d, int64_t w) {
-        row = w / d.xsegs;
-        seg = int(w - row * d.xsegs);
+    int segs;  // segments per row
+    __device__ __forceinline__ void init(const McDims& d, int64_t w, int segsPerRow = 0) {
+        segs = segsPerRow ? segsPerRow : d.xsegs;
+        row = w / segs;
+        seg = int(w - row * segs);
         z = int(row / d.dy);
         y = int(row - int64_t(z) * d.dy);
     }
@@ -191,7 +196,7 @@ struct Cursor {
         return it;
     }
     __device__ __forceinline__ void advance(const McDims& d) {
-        if (++seg == d.xsegs) {
+        if (++seg == segs) {
             seg = 0;
             ++row;
             if (++y == d.dy) {
@@ -207,7 +212,7 @@ struct Cursor {
 template <typename F>
 __device__ __forceinline__ void forEachMarkedItem(const McDims& d, int lane, const int32_t* __restrict__ counts, F&& body) {
     int64_t w0, w1;
-    warpRange(d, w0, w1);
+    warpRange(d.items, w0, w1);
     for (int64_t g = w0; g < w1; g += 16) {
         const int64_t ch = 2 * g + lane;
         const int cnt = ch < 2 * w1 ? counts[ch] : 0;
@@ -242,53 +247,81 @@ __device__ __forceinline__ int chunkExclusive(int c, int lane) {
     return p - c;
 }
 
-constexpr int kClassifyUnroll = 4;  // row segments in flight per warp
+// Flag byte of one voxel from its value and its +X/+Y/+Z neighbours' (MRMarchingCubes.cpp:598-646):
+// a crossing needs the neighbour on the other side of iso; a NaN neighbour is on neither side.
+__device__ __forceinline__ unsigned voxelFlags(float v, float nx, float ny, float nz, bool hx, bool hy, bool hz, float iso) {
+    const bool lower = v < iso, notLower = v >= iso;
+    if (!lower && !notLower) return kInvalid;
+    unsigned f = lower ? kLower : 0u;
+    if (hx && (lower ? nx >= iso : nx < iso)) f |= 1u;
+    if (hy && (lower ? ny >= iso : ny < iso)) f |= 2u;
+    if (hz && (lower ? nz >= iso : nz < iso)) f |= 4u;
+    return f;
+}
 
+constexpr int kClassifyUnroll = 2;  // 128-voxel segments in flight per warp
+
+// The dense pass: each lane classifies 4 consecutive voxels of a row (a warp 128) and stores their
+// flags as one 32-bit word; 16-voxel chunk counts are sums over groups of 4 lanes.  VEC: the
+// volume is 16-byte aligned and dx % 4 == 0, so the loads are float4.
+template <bool VEC>
 __global__ void __launch_bounds__(256, 4) classifyKernel(const float* __restrict__ vol, McDims d, float iso,
-                                                      uint8_t* __restrict__ flags, int32_t* __restrict__ chunkVerts,
-                                                      unsigned long long* __restrict__ total) {
+                                                         uint8_t* __restrict__ flags, int32_t* __restrict__ chunkVerts,
+                                                         unsigned long long* __restrict__ total) {
     const int lane = threadIdx.x & 31;
     unsigned long long mine = 0;
     int64_t w0, w1;
-    warpRange(d, w0, w1);
+    warpRange(d.qitems, w0, w1);
     Cursor cur;
-    if (w0 < w1) cur.init(d, w0);
+    if (w0 < w1) cur.init(d, w0, d.qsegs);
     for (int64_t w = w0; w < w1; w += kClassifyUnroll) {
-        WarpItem it[kClassifyUnroll];
-        float v[kClassifyUnroll], nx[kClassifyUnroll], ny[kClassifyUnroll], nz[kClassifyUnroll];
+        int x[kClassifyUnroll], y[kClassifyUnroll], z[kClassifyUnroll];
+        int64_t row[kClassifyUnroll];
+        float v[kClassifyUnroll][5], ny[kClassifyUnroll][4], nz[kClassifyUnroll][4];
         // all loads of the group first: they do not depend on one another
 #pragma unroll
         for (int k = 0; k < kClassifyUnroll; ++k) {
-            it[k] = cur.item(d, lane);
+            x[k] = cur.seg * 128 + 4 * lane;
+            y[k] = cur.y;
+            z[k] = cur.z;
+            row[k] = cur.row;
             cur.advance(d);
-            const bool ok = w + k < w1 && it[k].in;
-            const int64_t id = it[k].row * d.dx + it[k].x;
-            v[k] = ok ? vol[id] : 0.f;
-            nx[k] = ok && it[k].x + 1 < d.dx ? vol[id + 1] : 0.f;
-            ny[k] = ok && it[k].y + 1 < d.dy ? vol[id + d.dx] : 0.f;
-            nz[k] = ok && it[k].z + 1 < d.dz ? vol[id + d.sxy] : 0.f;
+            const bool ok = w + k < w1;
+            const int64_t id = row[k] * d.dx + x[k];
+            const bool hy = y[k] + 1 < d.dy, hz = z[k] + 1 < d.dz;
+            if (VEC && ok && x[k] < d.dx) {  // x % 4 == 0 and dx % 4 == 0: all four in the row
+                const float4 a = __ldg(reinterpret_cast<const float4*>(vol + id));
+                v[k][0] = a.x; v[k][1] = a.y; v[k][2] = a.z; v[k][3] = a.w;
+                v[k][4] = x[k] + 4 < d.dx ? vol[id + 4] : 0.f;
+                const float4 b = hy ? __ldg(reinterpret_cast<const float4*>(vol + id + d.dx)) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 c = hz ? __ldg(reinterpret_cast<const float4*>(vol + id + d.sxy)) : make_float4(0.f, 0.f, 0.f, 0.f);
+                ny[k][0] = b.x; ny[k][1] = b.y; ny[k][2] = b.z; ny[k][3] = b.w;
+                nz[k][0] = c.x; nz[k][1] = c.y; nz[k][2] = c.z; nz[k][3] = c.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 5; ++j) v[k][j] = ok && x[k] + j < d.dx ? vol[id + j] : 0.f;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    ny[k][j] = ok && hy && x[k] + j < d.dx ? vol[id + d.dx + j] : 0.f;
+                    nz[k][j] = ok && hz && x[k] + j < d.dx ? vol[id + d.sxy + j] : 0.f;
+                }
+            }
         }
 #pragma unroll
         for (int k = 0; k < kClassifyUnroll; ++k) {
             if (w + k >= w1) break;  // warp-uniform
-            unsigned f = 0;
-            if (it[k].in) {
-                const bool lower = v[k] < iso, notLower = v[k] >= iso;
-                if (!lower && !notLower) {
-                    f = kInvalid;
-                } else {
-                    // a crossing needs the neighbour on the other side; a NaN neighbour is on neither
-                    if (lower) f |= kLower;
-                    if (it[k].x + 1 < d.dx && (lower ? nx[k] >= iso : nx[k] < iso)) f |= 1u;
-                    if (it[k].y + 1 < d.dy && (lower ? ny[k] >= iso : ny[k] < iso)) f |= 2u;
-                    if (it[k].z + 1 < d.dz && (lower ? nz[k] >= iso : nz[k] < iso)) f |= 4u;
-                }
-            }
-            const int64_t at = it[k].row * d.pitch + it[k].x;
-            flags[at] = uint8_t(f);
-            const int c = __popc(f & 7u);
-            const int sum = chunkSum(c);
-            if ((lane & 15) == 0) chunkVerts[at >> 4] = sum;
+            const bool hy = y[k] + 1 < d.dy, hz = z[k] + 1 < d.dz;
+            unsigned word = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (x[k] + j < d.dx)
+                    word |= voxelFlags(v[k][j], v[k][j + 1], ny[k][j], nz[k][j], x[k] + j + 1 < d.dx, hy, hz, iso) << (8 * j);
+            const int64_t at = row[k] * d.pitch + x[k];
+            if (x[k] < d.pitch) reinterpret_cast<uint32_t*>(flags)[at >> 2] = word;
+            const int c = __popc(word & 0x07070707u);
+            int sum = c + __shfl_xor_sync(FULL, c, 1);
+            sum += __shfl_xor_sync(FULL, sum, 2);
+            if ((lane & 3) == 0 && x[k] < d.pitch) chunkVerts[at >> 4] = sum;
             mine += c;
         }
     }
@@ -379,11 +412,12 @@ __device__ __forceinline__ int cellTriangles(const uint8_t* __restrict__ flags, 
     return cellCore(corners, ci);
 }
 
-// Triangle counts per cell.  A warp first checks the vertex counts of the 16-voxel chunks its 32
-// cells touch (two chunks and the next one in each of the four rows): with no crossing there, no
-// cell can emit a triangle (a triangle needs a vertex on one of its cell's corners), and only the
-// chunk counts are written.  Otherwise it reads its 32 flag bytes in each of the four rows
-// (coalesced); the +x corners come from the next lane (lane 31 reads one more byte).
+// Triangle counts per cell, 4 cells per lane (a warp: 128 cells of a row).  The warp first checks
+// the vertex counts of the 16-voxel chunks its cells touch (8 chunks and the next one in each of the
+// four rows): with no crossing there, no cell can emit a triangle (a triangle needs a vertex on one
+// of its cell's corners) and only the chunk counts are written.  Otherwise each lane reads its four
+// flag bytes in each of the four rows as one word; the +x corner of its last cell comes from the next
+// lane (lane 31 reads one more byte).
 __global__ void __launch_bounds__(256) cellKernel(const uint8_t* __restrict__ flags, const int32_t* __restrict__ chunkVerts,
                                                   McDims d, uint8_t* __restrict__ tcnt, int32_t* __restrict__ chunkTris,
                                                   unsigned long long* __restrict__ total) {
@@ -391,51 +425,65 @@ __global__ void __launch_bounds__(256) cellKernel(const uint8_t* __restrict__ fl
     unsigned long long mine = 0;
     const int64_t layer = int64_t(d.pitch) * d.dy;
     int64_t w0, w1;
-    warpRange(d, w0, w1);
+    warpRange(d.qitems, w0, w1);
     Cursor cur;
-    if (w0 < w1) cur.init(d, w0);
+    if (w0 < w1) cur.init(d, w0, d.qsegs);
     for (int64_t w = w0; w < w1; ++w, cur.advance(d)) {
-        const WarpItem it = cur.item(d, lane);
-        const int64_t at = it.row * d.pitch + it.x;
-        const bool hy = it.y + 1 < d.dy, hz = it.z + 1 < d.dz;
-        int cnt = 0;
-        if (lane < 12) {
-            const int r = lane / 3, k = lane - 3 * r;
-            const bool rowOk = ((r & 1) == 0 || hy) && ((r & 2) == 0 || hz);
-            if (rowOk && (k < 2 || cur.seg + 1 < d.xsegs)) {
-                const int64_t rr = it.row + (r & 1) + ((r & 2) ? d.dy : 0);
-                cnt = chunkVerts[2 * (rr * d.xsegs + cur.seg) + k];
+        const int x0 = cur.seg * 128, x = x0 + 4 * lane;
+        const int64_t at = cur.row * d.pitch + x;
+        const bool hy = cur.y + 1 < d.dy, hz = cur.z + 1 < d.dz;
+        {
+            const int r = lane >> 3, k = lane & 7;
+            int cnt = 0;
+            if (((r & 1) == 0 || hy) && ((r & 2) == 0 || hz)) {
+                const int64_t rr = cur.row + (r & 1) + ((r & 2) ? d.dy : 0);
+                const int64_t c0 = (rr * d.pitch + x0) >> 4;
+                if (x0 + 16 * k < d.pitch) cnt = chunkVerts[c0 + k];
+                if (k == 7 && x0 + 128 < d.pitch) cnt |= chunkVerts[c0 + 8];
+            }
+            if (!__any_sync(FULL, cnt != 0)) {
+                if ((lane & 3) == 0 && x < d.pitch) chunkTris[at >> 4] = 0;
+                continue;
             }
         }
-        if (!__any_sync(FULL, cnt != 0)) {
-            if ((lane & 15) == 0) chunkTris[at >> 4] = 0;
-            continue;
+        const bool inRow = x < d.pitch;
+        const uint32_t* fw = reinterpret_cast<const uint32_t*>(flags);
+        const unsigned f0 = inRow ? fw[at >> 2] : 0u;
+        const unsigned f1 = inRow && hy ? fw[(at + d.pitch) >> 2] : 0u;
+        const unsigned f2 = inRow && hz ? fw[(at + layer) >> 2] : 0u;
+        const unsigned f3 = inRow && hy && hz ? fw[(at + d.pitch + layer) >> 2] : 0u;
+        unsigned n0 = __shfl_down_sync(FULL, f0, 1) & 0xffu, n1 = __shfl_down_sync(FULL, f1, 1) & 0xffu;
+        unsigned n2 = __shfl_down_sync(FULL, f2, 1) & 0xffu, n3 = __shfl_down_sync(FULL, f3, 1) & 0xffu;
+        if (lane == 31) {  // x + 4 starts the next segment of the same row
+            const bool nx = x + 4 < d.pitch;
+            n0 = nx ? flags[at + 4] : 0u;
+            n1 = nx && hy ? flags[at + d.pitch + 4] : 0u;
+            n2 = nx && hz ? flags[at + layer + 4] : 0u;
+            n3 = nx && hy && hz ? flags[at + d.pitch + layer + 4] : 0u;
         }
-        const bool cell = it.x + 1 < d.dx && hy && hz;
-        const unsigned r0 = flags[at];
-        const unsigned r1 = hy ? flags[at + d.pitch] : 0u;
-        const unsigned r2 = hz ? flags[at + layer] : 0u;
-        const unsigned r3 = hy && hz ? flags[at + d.pitch + layer] : 0u;
-        unsigned n0 = __shfl_down_sync(FULL, r0, 1), n1 = __shfl_down_sync(FULL, r1, 1);
-        unsigned n2 = __shfl_down_sync(FULL, r2, 1), n3 = __shfl_down_sync(FULL, r3, 1);
-        if (lane == 31 && cell) {  // x + 1 starts the next segment of the same row
-            n0 = flags[at + 1];
-            n1 = flags[at + d.pitch + 1];
-            n2 = flags[at + layer + 1];
-            n3 = flags[at + d.pitch + layer + 1];
-        }
-        int nt = 0;
-        if (cell && ((r0 | r1 | r2 | r3 | n0 | n1 | n2 | n3) & 7u)) {
+        // row words extended by the next byte: byte j and j + 1 of row r are cell j's corners
+        const unsigned long long e0 = f0 | ((unsigned long long)n0 << 32), e1 = f1 | ((unsigned long long)n1 << 32);
+        const unsigned long long e2 = f2 | ((unsigned long long)n2 << 32), e3 = f3 | ((unsigned long long)n3 << 32);
+        unsigned word = 0;
+        int c = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (!(x + j + 1 < d.dx && hy && hz)) continue;
+            const unsigned b0 = unsigned(e0 >> (8 * j)) & 0xffffu, b1 = unsigned(e1 >> (8 * j)) & 0xffffu;
+            const unsigned b2 = unsigned(e2 >> (8 * j)) & 0xffffu, b3 = unsigned(e3 >> (8 * j)) & 0xffffu;
+            if (!((b0 | b1 | b2 | b3) & 0x0707u)) continue;  // no crossing on any corner
             const unsigned long long corners =
-                (unsigned long long)(r0 | (n0 << 8) | (r1 << 16) | (n1 << 24)) |
-                ((unsigned long long)(r2 | (n2 << 8) | (r3 << 16) | (n3 << 24)) << 32);
+                (unsigned long long)(b0 | (b1 << 16)) | ((unsigned long long)(b2 | (b3 << 16)) << 32);
             CellInfo ci;
-            nt = cellCore(corners, ci);
+            const int nt = cellCore(corners, ci);
+            word |= unsigned(nt) << (8 * j);
+            c += nt;
         }
-        tcnt[at] = uint8_t(nt);
-        const int sum = chunkSum(nt);
-        if ((lane & 15) == 0) chunkTris[at >> 4] = sum;
-        mine += nt;
+        if (inRow) reinterpret_cast<uint32_t*>(tcnt)[at >> 2] = word;
+        int sum = c + __shfl_xor_sync(FULL, c, 1);
+        sum += __shfl_xor_sync(FULL, sum, 2);
+        if ((lane & 3) == 0 && inRow) chunkTris[at >> 4] = sum;
+        mine += c;
     }
     for (int off = 16; off; off >>= 1) mine += __shfl_xor_sync(FULL, mine, off);
     if (lane == 0 && mine) atomicAdd(total, mine);
@@ -495,21 +543,55 @@ __device__ __forceinline__ int32_t vertexId(const uint8_t* __restrict__ flags, c
     return vertBase[chunk] + p;
 }
 
-// Triangles: only the items whose chunks hold triangles (tcnt is only written for those).
-__global__ void __launch_bounds__(256) triangleKernel(const uint8_t* __restrict__ flags, const uint8_t* __restrict__ tcnt,
-                                                      const int32_t* __restrict__ chunkTris, const int32_t* __restrict__ vertBase,
-                                                      const int32_t* __restrict__ triBase, McDims d, int lessInside,
-                                                      int32_t* __restrict__ tris, int32_t* __restrict__ faceMap) {
+// Positions (in the pitched arrays) of the cells that emit triangles, in any order: a warp counts
+// the nonzero cells of its marked items, reserves that many slots with one atomic, then writes them.
+__global__ void __launch_bounds__(256) collectCellsKernel(const uint8_t* __restrict__ tcnt, const int32_t* __restrict__ chunkTris,
+                                                          McDims d, int64_t* __restrict__ cells,
+                                                          unsigned long long* __restrict__ count) {
     const int lane = threadIdx.x & 31;
+    unsigned n = 0;
+    forEachMarkedItem(d, lane, chunkTris, [&](const WarpItem& it) {
+        n += __popc(__ballot_sync(FULL, tcnt[it.row * d.pitch + it.x] != 0));
+    });
+    unsigned long long base = 0;
+    if (lane == 0 && n) base = atomicAdd(count, (unsigned long long)n);
+    base = __shfl_sync(FULL, base, 0);
     forEachMarkedItem(d, lane, chunkTris, [&](const WarpItem& it) {
         const int64_t at = it.row * d.pitch + it.x;
-        const int t = tcnt[at];  // 0 past the row end
-        const int ex = chunkExclusive(t, lane);
-        if (!t) return;
+        const bool has = tcnt[at] != 0;
+        const unsigned m = __ballot_sync(FULL, has);
+        if (has) cells[base + __popc(m & ((1u << lane) - 1u))] = at;
+        base += __popc(m);
+    });
+}
+
+// sum of the bytes of w before byte j (values < 64, so no carries between bytes)
+__device__ __forceinline__ unsigned bytesBefore(unsigned w, int j) {
+    const unsigned m = j >= 4 ? 0xffffffffu : ((1u << (8 * j)) - 1u);
+    return ((w & m) * 0x01010101u) >> 24;
+}
+
+// Triangles, one thread per listed cell: its first triangle id = the chunk's base + the counts of
+// the chunk's cells before it; then the plan's vertex ids and the face map.
+__global__ void __launch_bounds__(256) triangleKernel(const uint8_t* __restrict__ flags, const uint8_t* __restrict__ tcnt,
+                                                      const int64_t* __restrict__ cells,
+                                                      const unsigned long long* __restrict__ cellCount,
+                                                      const int32_t* __restrict__ vertBase, const int32_t* __restrict__ triBase,
+                                                      McDims d, int lessInside, int32_t* __restrict__ tris,
+                                                      int32_t* __restrict__ faceMap) {
+    const int64_t nCells = int64_t(*cellCount);
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nCells; i += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t at = cells[i];
+        const uint4 w = __ldg(reinterpret_cast<const uint4*>(tcnt) + (at >> 4));
+        const int j = int(at & 15);
+        const unsigned before = bytesBefore(w.x, j) + bytesBefore(w.y, j - 4 < 0 ? 0 : j - 4) +
+                                bytesBefore(w.z, j - 8 < 0 ? 0 : j - 8) + bytesBefore(w.w, j - 12 < 0 ? 0 : j - 12);
+        int64_t base = int64_t(triBase[at >> 4]) + before;
         CellInfo ci;
         const int nt = cellTriangles(flags, d, at, ci);
         const unsigned long long plan = kPlan[ci.config];
-        int64_t base = int64_t(triBase[at >> 4]) + ex;
+        const int64_t row = at / d.pitch;
+        const int32_t voxel = faceMap ? int32_t(row * d.dx + (at - row * d.pitch)) : 0;
         for (int k = 0; k < nt; ++k, ++base) {
             int32_t ids[3];
 #pragma unroll
@@ -521,9 +603,9 @@ __global__ void __launch_bounds__(256) triangleKernel(const uint8_t* __restrict_
             o[0] = ids[0];
             o[1] = lessInside ? ids[2] : ids[1];
             o[2] = lessInside ? ids[1] : ids[2];
-            if (faceMap) faceMap[base] = int32_t(it.row * d.dx + it.x);
+            if (faceMap) faceMap[base] = voxel;
         }
-    });
+    }
 }
 
 }  // namespace
@@ -568,17 +650,21 @@ int mcError(const char* msg) { return fail(GBFWN_INVALID, msg); }
 // gbfwn_mc_release_workspace frees it.
 struct McWorkspace {
     std::mutex mu;
-    char* buf = nullptr;
+    char* buf = nullptr;  // flags, counts, bases, scan scratch, totals, layer z
     size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (cap >= bytes) return cudaSuccess;
-        cudaFree(buf);
-        buf = nullptr;
-        cap = 0;
-        cudaError_t e = devMalloc((void**)&buf, bytes);
-        if (!e) cap = bytes;
+    char* cells = nullptr;  // list of the cells that emit triangles
+    size_t cellCap = 0;
+    static cudaError_t grow(char*& p, size_t& c, size_t bytes) {
+        if (c >= bytes) return cudaSuccess;
+        cudaFree(p);
+        p = nullptr;
+        c = 0;
+        cudaError_t e = devMalloc((void**)&p, bytes);
+        if (!e) c = bytes;
         return e;
     }
+    cudaError_t ensure(size_t bytes) { return grow(buf, cap, bytes); }
+    cudaError_t ensureCells(size_t bytes) { return grow(cells, cellCap, bytes); }
 };
 constexpr int kMaxDevices = 64;
 McWorkspace g_workspaces[kMaxDevices];
@@ -644,6 +730,8 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     d.pitch = d.xsegs * 32;
     d.items = d.rows * d.xsegs;
     d.nChunks = d.rows * d.pitch / 16;
+    d.qsegs = (dims[0] + 127) / 128;
+    d.qitems = d.rows * d.qsegs;
     if (p.wantFaceMap && d.sxy * dims[2] > INT32_MAX) {
         delete m;
         return mcError("voxel ids of the face map exceed 32 bits");
@@ -672,7 +760,7 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
                               sizeof(int32_t) * size_t(d.nChunks),
                               sizeof(int32_t) * size_t(nbSums),
                               sizeof(int32_t) * 4,
-                              sizeof(unsigned long long) * 2,
+                              sizeof(unsigned long long) * 3,
                               sizeof(float) * lz.size()};
     void** ptrs[10] = {(void**)&flags, (void**)&tcnt, (void**)&chunkV, (void**)&chunkT, (void**)&baseV,
                        (void**)&baseT, (void**)&sums, (void**)&misc, (void**)&totals, (void**)&dLz};
@@ -686,11 +774,16 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
             off += (sizes[k] + 255) / 256 * 256;
         }
     }
-    if (!e) e = cudaMemsetAsync(totals, 0, sizeof(unsigned long long) * 2, s);
+    if (!e) e = cudaMemsetAsync(totals, 0, sizeof(unsigned long long) * 3, s);
     if (!e) e = cudaMemcpyAsync(dLz, lz.data(), sizeof(float) * lz.size(), cudaMemcpyHostToDevice, s);
     if (!e) {
-        classifyKernel<<<mcBlocks(d), 256, 0, s>>>(dVol, d, p.iso, flags, chunkV, totals);
-        cellKernel<<<mcBlocks(d), 256, 0, s>>>(flags, chunkV, d, tcnt, chunkT, totals + 1);
+        const bool vec = (d.dx % 4) == 0 && (reinterpret_cast<uintptr_t>(dVol) % 16) == 0;
+        const unsigned nbq = unsigned(std::max<int64_t>(1, std::min<int64_t>((d.qitems + 7) / 8, int64_t(numSMs()) * 8)));
+        if (vec)
+            classifyKernel<true><<<nbq, 256, 0, s>>>(dVol, d, p.iso, flags, chunkV, totals);
+        else
+            classifyKernel<false><<<nbq, 256, 0, s>>>(dVol, d, p.iso, flags, chunkV, totals);
+        cellKernel<<<nbq, 256, 0, s>>>(flags, chunkV, d, tcnt, chunkT, totals + 1);
         e = cudaGetLastError();
     }
     unsigned long long ht[2] = {0, 0};
@@ -715,10 +808,14 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     if (!e) e = devMalloc((void**)&m->dPoints, sizeof(float) * 3 * size_t(m->nPoints));
     if (!e) e = devMalloc((void**)&m->dTris, sizeof(int32_t) * 3 * size_t(m->nTris));
     if (!e && p.wantFaceMap) e = devMalloc((void**)&m->dFaceMap, sizeof(int32_t) * size_t(m->nTris));
+    if (!e) e = ws.ensureCells(sizeof(int64_t) * size_t(std::max<int64_t>(m->nTris, 1)));  // cells <= triangles
     if (!e) {
+        int64_t* cellList = reinterpret_cast<int64_t*>(ws.cells);
         vertexKernel<<<mcBlocks(d), 256, 0, s>>>(dVol, flags, chunkV, baseV, d, g, dLz, m->dPoints);
-        triangleKernel<<<mcBlocks(d), 256, 0, s>>>(flags, tcnt, chunkT, baseV, baseT, d,
-                                                                  p.lessInside ? 1 : 0, m->dTris, m->dFaceMap);
+        collectCellsKernel<<<mcBlocks(d), 256, 0, s>>>(tcnt, chunkT, d, cellList, totals + 2);
+        const unsigned nbt = unsigned(std::max<int64_t>(1, std::min<int64_t>((m->nTris + 255) / 256, int64_t(numSMs()) * 8)));
+        triangleKernel<<<nbt, 256, 0, s>>>(flags, tcnt, cellList, totals + 2, baseV, baseT, d, p.lessInside ? 1 : 0,
+                                          m->dTris, m->dFaceMap);
         e = cudaGetLastError();
     }
     if (!e) e = cudaStreamSynchronize(s);
@@ -796,8 +893,9 @@ GBFWN_API int gbfwn_mc_release_workspace(int device) {
     std::lock_guard<std::mutex> lk(ws.mu);
     DeviceGuard g(device);
     cudaFree(ws.buf);
-    ws.buf = nullptr;
-    ws.cap = 0;
+    cudaFree(ws.cells);
+    ws.buf = ws.cells = nullptr;
+    ws.cap = ws.cellCap = 0;
     return GBFWN_OK;
 }
 

@@ -173,3 +173,29 @@ def test_grid_to_mesh_large(M):
     grid = out.cpu().numpy().reshape(dims[2], dims[1], dims[0])
     ref = O.marching_cubes(grid, origin=origin, voxel_size=(vsz,) * 3, iso=off, less_inside=True)
     _same(tm, ref)
+
+
+def test_cancel_and_allocation_failure(M):
+    """Progress callbacks cancel (MeshLib's unexpectedOperationCanceled); a failed device allocation
+    (host-side injection) is reported as out of memory and leaves the library usable."""
+    vol = _sphere(41, 15.0)
+    prm = M.MarchingCubesParams(iso=0.0, lessInside=True)
+    with pytest.raises(M.FwnError) as ei:
+        M.marchingCubes(vol, prm, cb=lambda p: p < 0.2)
+    assert ei.value.status == M.CANCELLED
+    seen = []
+    tm = M.marchingCubes(vol, prm, cb=lambda p: seen.append(p) or True)
+    assert tm.numTris > 0 and seen[0] == 0.0 and seen[-1] == 1.0
+    M.lib().gbfwn_debug_fail_next_allocs(1)
+    with pytest.raises(M.FwnError) as ei:
+        M.marchingCubes(vol, prm)
+    assert ei.value.status == M.OUT_OF_MEMORY
+    again = M.marchingCubes(vol, prm)
+    assert np.array_equal(again.tris, tm.tris)
+    v, f = mg.noisy_torus(seed=1)
+    g = M.FastWindingNumber(v, f)
+    origin, dims = M.calcOriginAndDimensions(v.min(0) - 0.05, v.max(0) + 0.05, 0.02)
+    with pytest.raises(M.FwnError) as ei:
+        g.gridToMesh(dims, origin, 0.02, cb=lambda p: p < 0.5)
+    assert ei.value.status == M.CANCELLED
+    assert g.gridToMesh(dims, origin, 0.02).numTris > 0
