@@ -199,3 +199,37 @@ def test_cancel_and_allocation_failure(M):
         g.gridToMesh(dims, origin, 0.02, cb=lambda p: p < 0.5)
     assert ei.value.status == M.CANCELLED
     assert g.gridToMesh(dims, origin, 0.02).numTris > 0
+
+
+def test_offset_flow_by_parts(M):
+    """mcOffsetMesh's own flow (MRVoxels/MROffset.cpp:194-226): the banded distance grid produced by
+    parts with one overlapping layer (IFastWindingNumberByParts) feeds MarchingCubesByParts slab by
+    slab.  The GPU mesher by parts == the fused call given the same part starts == the oracle."""
+    v, f = mg.noisy_torus(seed=4)
+    g = M.FastWindingNumber(v, f)
+    vsz = 0.02
+    off = 2 * vsz
+    origin, dims = M.calcOriginAndDimensions(v.min(0) - off, v.max(0) + off, vsz)
+    opts = M.DistanceToMeshOptions(minDistSq=max(off - 1.001 * vsz, 0.0) ** 2, maxDistSq=(off + 1.001 * vsz) ** 2,
+                                   nullOutsideMinMax=True)
+    prm = M.MarchingCubesParams(origin=tuple(origin), voxelSize=(vsz,) * 3, iso=off, lessInside=True,
+                                outVoxelPerFaceMap=True)
+    basis = np.array([vsz, 0, 0, 0, vsz, 0, 0, 0, vsz, 0, 0, 0], np.float32)
+    basis[9:] = (origin + np.float32(0.5) * np.float32(vsz)).astype(np.float32)
+    mc = M.MarchingCubesByParts(dims, prm)
+    starts = []
+
+    def part(arr, sd, zoff):
+        assert zoff == mc.nextZ()
+        starts.append(zoff)
+        mc.addPart(arr.reshape(sd[2], sd[1], sd[0]))
+
+    g.calcFromGridWithDistancesByParts(part, dims, basis, opts, layerOverlap=1, maxLayersPerSlab=7)
+    assert len(starts) > 2
+    tm = mc.finalize()
+    assert tm.numTris > 1000
+    fused = g.gridToMesh(dims, origin, vsz, opts, prm, partStarts=starts)
+    _same(fused, (tm.points, tm.tris, tm.faceMap))
+    grid = g.calcFromGridWithDistances(dims, basis, opts).reshape(dims[2], dims[1], dims[0])
+    _same(tm, O.marching_cubes(grid, origin=origin, voxel_size=(vsz,) * 3, iso=off, less_inside=True,
+                               part_starts=starts))
