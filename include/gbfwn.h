@@ -371,7 +371,11 @@ GBFWN_API int gbfwn_marching_cubes(const float* volume, const int32_t dims[3], c
 GBFWN_API int gbfwn_marching_cubes_dev(const float* d_volume, const int32_t dims[3], const gbfwn_mc_params* params,
                                        const int32_t* partStarts, int32_t nParts, int device, gbfwn_trimesh* out,
                                        void* stream);
-/* The mesher keeps its work arrays (6 bytes per voxel) on the device between calls; this frees them. */
+/* Device bytes a mesher call needs (MRCuda/MRCudaAccessor.cpp:162-194 gives such estimators for the
+ * reference's GPU calls): work arrays (about 3 bytes per voxel) plus the output and the cell list for
+ * `expectedTriangles` triangles; the host-volume call adds 4 bytes per voxel for the volume. */
+GBFWN_API size_t gbfwn_marching_cubes_memory(const int32_t dims[3], int64_t expectedTriangles);
+/* The mesher keeps its work arrays on the device between calls; this frees them. */
 GBFWN_API int gbfwn_mc_release_workspace(int device);
 GBFWN_API int gbfwn_trimesh_sizes(gbfwn_trimesh m, int64_t* numPoints, int64_t* numTris);
 /* Copies the mesh to host arrays (points: 3 floats per vertex; tris: 3 vertex ids per triangle;

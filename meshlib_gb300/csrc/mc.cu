@@ -645,7 +645,7 @@ namespace {
 
 int mcError(const char* msg) { return fail(GBFWN_INVALID, msg); }
 
-// Work arrays of the mesher (6 bytes per voxel), kept per device between calls so that repeated
+// Work arrays of the mesher (about 3 bytes per voxel), kept per device between calls so that repeated
 // meshing does not pay for cudaMalloc / cudaFree of hundreds of MB; it only grows, and
 // gbfwn_mc_release_workspace frees it.
 struct McWorkspace {
@@ -704,6 +704,47 @@ unsigned mcBlocks(const McDims& d) {
     return unsigned(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(numSMs()) * 8)));
 }
 
+McDims mcDims(const int32_t dims[3]) {
+    McDims d;
+    d.dx = dims[0];
+    d.dy = dims[1];
+    d.dz = dims[2];
+    d.sxy = int64_t(dims[0]) * dims[1];
+    d.rows = int64_t(dims[1]) * dims[2];
+    d.xsegs = (dims[0] + 31) / 32;
+    d.pitch = d.xsegs * 32;
+    d.items = d.rows * d.xsegs;
+    d.nChunks = d.rows * d.pitch / 16;
+    d.qsegs = (dims[0] + 127) / 128;
+    d.qitems = d.rows * d.qsegs;
+    return d;
+}
+
+// Bytes of the mesher's work arrays: flags, triangle counts, chunk counts and bases, scan
+// scratch, totals, layer z coordinates.
+void mcSizes(const McDims& d, size_t sizes[10]) {
+    const int64_t nbSums = (d.nChunks + 1023) / 1024 + 1;
+    const size_t flagBytes = size_t(d.rows) * size_t(d.pitch) + 16;
+    const size_t list[10] = {flagBytes,
+                             flagBytes,
+                             sizeof(int32_t) * size_t(d.nChunks),
+                             sizeof(int32_t) * size_t(d.nChunks),
+                             sizeof(int32_t) * size_t(d.nChunks),
+                             sizeof(int32_t) * size_t(d.nChunks),
+                             sizeof(int32_t) * size_t(nbSums),
+                             sizeof(int32_t) * 4,
+                             sizeof(unsigned long long) * 3,
+                             sizeof(float) * size_t(d.dz)};
+    for (int k = 0; k < 10; ++k) sizes[k] = list[k];
+}
+
+size_t mcWorkspaceBytes(const McDims& d) {
+    size_t sizes[10], need = 0;
+    mcSizes(d, sizes);
+    for (size_t b : sizes) need += (b + 255) / 256 * 256;
+    return need;
+}
+
 // The mesher on a device volume; the result is complete when this returns.
 int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_params& p, const int32_t* partStarts,
                      int32_t nParts, int device, cudaStream_t s, gbfwn_trimesh* out, const char* what) {
@@ -720,18 +761,7 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
         delete m;
         return st;
     }
-    McDims d;
-    d.dx = dims[0];
-    d.dy = dims[1];
-    d.dz = dims[2];
-    d.sxy = int64_t(dims[0]) * dims[1];
-    d.rows = int64_t(dims[1]) * dims[2];
-    d.xsegs = (dims[0] + 31) / 32;
-    d.pitch = d.xsegs * 32;
-    d.items = d.rows * d.xsegs;
-    d.nChunks = d.rows * d.pitch / 16;
-    d.qsegs = (dims[0] + 127) / 128;
-    d.qitems = d.rows * d.qsegs;
+    const McDims d = mcDims(dims);
     if (p.wantFaceMap && d.sxy * dims[2] > INT32_MAX) {
         delete m;
         return mcError("voxel ids of the face map exceed 32 bits");
@@ -750,23 +780,11 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     int32_t *chunkV = nullptr, *chunkT = nullptr, *baseV = nullptr, *baseT = nullptr, *sums = nullptr, *misc = nullptr;
     unsigned long long* totals = nullptr;
     float* dLz = nullptr;
-    const int64_t nbSums = (d.nChunks + 1023) / 1024 + 1;
-    const size_t flagBytes = size_t(d.rows) * size_t(d.pitch) + 16;
-    const size_t sizes[10] = {flagBytes,
-                              flagBytes,
-                              sizeof(int32_t) * size_t(d.nChunks),
-                              sizeof(int32_t) * size_t(d.nChunks),
-                              sizeof(int32_t) * size_t(d.nChunks),
-                              sizeof(int32_t) * size_t(d.nChunks),
-                              sizeof(int32_t) * size_t(nbSums),
-                              sizeof(int32_t) * 4,
-                              sizeof(unsigned long long) * 3,
-                              sizeof(float) * lz.size()};
+    size_t sizes[10];
+    mcSizes(d, sizes);
     void** ptrs[10] = {(void**)&flags, (void**)&tcnt, (void**)&chunkV, (void**)&chunkT, (void**)&baseV,
                        (void**)&baseT, (void**)&sums, (void**)&misc, (void**)&totals, (void**)&dLz};
-    size_t need = 0;
-    for (size_t b : sizes) need += (b + 255) / 256 * 256;
-    cudaError_t e = ws.ensure(need);
+    cudaError_t e = ws.ensure(mcWorkspaceBytes(d));
     if (!e) {
         size_t off = 0;
         for (int k = 0; k < 10; ++k) {
@@ -897,6 +915,14 @@ GBFWN_API int gbfwn_mc_release_workspace(int device) {
     ws.buf = ws.cells = nullptr;
     ws.cap = ws.cellCap = 0;
     return GBFWN_OK;
+}
+
+GBFWN_API size_t gbfwn_marching_cubes_memory(const int32_t dims[3], int64_t expectedTriangles) {
+    if (!dims || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return 0;
+    const McDims d = mcDims(dims);
+    const size_t nt = size_t(std::max<int64_t>(expectedTriangles, 0));
+    // work arrays + cell list + output (points ~ triangles / 2, 3 floats; triangles 3 ints + face map)
+    return mcWorkspaceBytes(d) + 8 * nt + 6 * nt + 16 * nt;
 }
 
 GBFWN_API int gbfwn_trimesh_sizes(gbfwn_trimesh m, int64_t* numPoints, int64_t* numTris) {

@@ -116,3 +116,15 @@ def test_calc_origin_and_dimensions():
     o, d = M.calcOriginAndDimensions([-1, -0.5, 0], [1, 0.5, 2], 0.1)
     assert np.allclose(o, [-1.2, -0.7, -0.2]) and o.dtype == np.float32
     assert d.tolist() == [25, 15, 25]
+
+
+def test_mesher_memory_estimate():
+    """The mesher's memory estimator (pure host arithmetic): about 3 bytes per voxel of work arrays,
+    plus the output for the expected triangles; 0 for an empty volume."""
+    import meshlib_gb300 as M
+    L = M.lib()
+    dims = np.array([512, 512, 512], np.int32)
+    w = L.gbfwn_marching_cubes_memory(dims.ctypes.data, 0)
+    assert 3 * 512 ** 3 <= w <= 3.1 * 512 ** 3
+    assert L.gbfwn_marching_cubes_memory(dims.ctypes.data, 1_000_000) == w + 30 * 1_000_000
+    assert L.gbfwn_marching_cubes_memory(np.array([0, 4, 4], np.int32).ctypes.data, 10) == 0
