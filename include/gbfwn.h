@@ -331,6 +331,14 @@ GBFWN_API int gbfwn_batch_autotune(gbfwn_batch b, int32_t* best, float* times_ms
 GBFWN_API int gbfwn_batch_run_dev(gbfwn_batch b, void* stream);
 GBFWN_API int gbfwn_batch_graph_launch(gbfwn_batch b, void* stream);
 
+/* makeSignedByWindingNumber (MRVoxels/MRVDBConversions.cpp:491-571) on a dense device grid: the
+ * winding number of every voxel (centre = xf applied to (x, y, z), as for gbfwn_from_grid) is computed
+ * and each value whose voxel's winding number exceeds `threshold` is negated in place.  MeshLib's VDB
+ * path reaches the same computation through IFastWindingNumberByParts::calcFromGridByParts; this is
+ * for grids that already live in device memory.  Enqueued on `stream` (NULL = the handle's). */
+GBFWN_API int gbfwn_make_signed_by_winding_number_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                      float beta, float threshold, float* d_values, void* stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Marching cubes: the mesher that consumes the signed-distance grid in MeshLib's offsetting
  * (mcOffsetMesh, MRVoxels/MROffset.cpp:185-226).  Output = the reference's TriMesh bit for bit

@@ -145,6 +145,7 @@ _SIGS = [
     ("gbfwn_find_projections_dev", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, _vp]),
     ("gbfwn_projections_heap_bytes", ctypes.c_size_t, [_i64]),
     ("gbfwn_debug_fp32_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("gbfwn_make_signed_by_winding_number_dev", ctypes.c_int, [_vp, _vp, _vp, _f, _f, _vp, _vp]),
     ("gbfwn_mc_default_params", None, [ctypes.POINTER(_McParams)]),
     ("gbfwn_marching_cubes", ctypes.c_int,
      [_vp, _vp, ctypes.POINTER(_McParams), _vp, _i32, ctypes.c_int, ctypes.POINTER(_vp), PROGRESS, _vp]),
@@ -437,6 +438,14 @@ class FastWindingNumber:
         d = np.asarray(dims, np.int32)
         _check(self._L.gbfwn_from_grid_dev(self._h, _p(d), _p(_xf12(xf)), beta, ctypes.c_void_p(d_out_ptr),
                                            _stream(stream)))
+
+    def makeSignedByWindingNumber_dev(self, dims, xf, d_values_ptr: int, beta: float = 2.0, threshold: float = 0.5,
+                                      stream=None):
+        """MeshLib's makeSignedByWindingNumber on a dense device grid: values of voxels whose winding
+        number exceeds `threshold` are negated in place (MRVoxels/MRVDBConversions.cpp:491-571)."""
+        d = np.asarray(dims, np.int32)
+        _check(self._L.gbfwn_make_signed_by_winding_number_dev(self._h, _p(d), _p(_xf12(xf)), beta, threshold,
+                                                               ctypes.c_void_p(d_values_ptr), _stream(stream)))
 
     def calcFromVector_dev(self, d_pts_ptr: int, n: int, d_out_ptr: int, beta: float = 2.0, skipFace: int = -1,
                            stream=None):

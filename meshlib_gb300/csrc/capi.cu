@@ -5,6 +5,7 @@
 // cancellation honoured between slabs.  Unlike the reference, the output is produced in z-slabs on
 // one stream while finished slabs are copied to the host on a second stream, so the device->host
 // copy of slab k overlaps the computation of slabs k+1...
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -49,6 +50,13 @@ cudaError_t devMalloc(void** p, size_t bytes) {
 
 namespace {
 bool progress(gbfwn_progress_cb cb, void* user, float p) { return !cb || cb(p, user) != 0; }
+
+// makeSignedByWindingNumber's update (MRVoxels/MRVDBConversions.cpp:516-530): a voxel whose winding
+// number exceeds the threshold has its value negated
+__global__ void flipByWindingKernel(float* __restrict__ values, const float* __restrict__ wn, int64_t n, float threshold) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        if (wn[i] > threshold) values[i] = -values[i];
+}
 }  // namespace
 
 namespace {
@@ -302,6 +310,30 @@ GBFWN_API int gbfwn_from_grid_dev(gbfwn_handle h, const int32_t dims[3], const f
     GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
     cudaError_t e = launchGridFwn(h->tree.q, r, X, beta, h->precise, d_out, h->scratch, s);
     return e ? cudaFail(e, "gbfwn_from_grid_dev") : GBFWN_OK;
+}
+
+GBFWN_API int gbfwn_make_signed_by_winding_number_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
+                                                      float beta, float threshold, float* d_values, void* stream) {
+    Xf X;
+    if (!h || !validDims(dims) || !toXf(xf, X) || !d_values)
+        return fail(GBFWN_INVALID, "gbfwn_make_signed_by_winding_number_dev: bad arguments");
+    DeviceGuard g(h->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    const int64_t n = int64_t(dims[0]) * dims[1] * dims[2];
+    float* wn = nullptr;
+    cudaError_t e = g_failAllocs > 0 ? (--g_failAllocs, cudaErrorMemoryAllocation)
+                                     : cudaMallocAsync((void**)&wn, sizeof(float) * size_t(n), s);
+    if (e) return cudaFail(e, "gbfwn_make_signed_by_winding_number_dev");
+    GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
+    e = launchGridFwn(h->tree.q, r, X, beta, h->precise, wn, h->scratch, s);
+    if (!e) {
+        flipByWindingKernel<<<unsigned(std::min<int64_t>((n + 255) / 256, int64_t(numSMs()) * 16)), 256, 0, s>>>(d_values, wn, n,
+                                                                                                           threshold);
+        e = cudaGetLastError();
+    }
+    const cudaError_t ef = cudaFreeAsync(wn, s);
+    if (!e) e = ef;
+    return e ? cudaFail(e, "gbfwn_make_signed_by_winding_number_dev") : GBFWN_OK;
 }
 
 GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
