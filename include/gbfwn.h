@@ -375,7 +375,8 @@ GBFWN_API void gbfwn_mc_default_params(gbfwn_mc_params* p);
 GBFWN_API int gbfwn_marching_cubes(const float* volume, const int32_t dims[3], const gbfwn_mc_params* params,
                                    const int32_t* partStarts, int32_t nParts, int device, gbfwn_trimesh* out,
                                    gbfwn_progress_cb cb, void* user);
-/* The same on a device volume; enqueued on `stream`, returns once the mesh is built. */
+/* The same on a device volume; enqueued on `stream` (no handle here: NULL = the legacy default
+ * stream), returns once the mesh is built. */
 GBFWN_API int gbfwn_marching_cubes_dev(const float* d_volume, const int32_t dims[3], const gbfwn_mc_params* params,
                                        const int32_t* partStarts, int32_t nParts, int device, gbfwn_trimesh* out,
                                        void* stream);
