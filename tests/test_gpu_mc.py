@@ -233,3 +233,37 @@ def test_offset_flow_by_parts(M):
     grid = g.calcFromGridWithDistances(dims, basis, opts).reshape(dims[2], dims[1], dims[0])
     _same(tm, O.marching_cubes(grid, origin=origin, voxel_size=(vsz,) * 3, iso=off, less_inside=True,
                                part_starts=starts))
+
+
+def test_more_than_2_31_voxels(M):
+    """1300^3 = 2.2e9 voxels (64-bit voxel and flag indices): a sphere of radius 200 voxels gives a
+    closed, consistently oriented genus-0 mesh (V - E + F = 2) whose volume is the ball's within
+    1e-3; the face map is refused (32-bit voxel ids), as the reference's VoxelId would overflow."""
+    import torch
+    n, r = 1300, 200.0
+    vol = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
+    ax = torch.arange(n, device="cuda", dtype=torch.float32) - (n - 1) / 2
+    yy, xx = torch.meshgrid(ax, ax, indexing="ij")
+    rxy = yy * yy + xx * xx
+    for z0 in range(0, n, 100):
+        zz = ax[z0:z0 + 100].view(-1, 1, 1)
+        vol[z0:z0 + 100] = torch.sqrt(rxy.unsqueeze(0) + zz * zz) - r
+    del yy, xx, rxy
+    prm = M.MarchingCubesParams(iso=0.0, lessInside=True)
+    tm = M.marchingCubes_dev(vol.data_ptr(), (n, n, n), prm)
+    with pytest.raises(M.FwnError, match="32 bits"):
+        M.marchingCubes_dev(vol.data_ptr(), (n, n, n), M.MarchingCubesParams(outVoxelPerFaceMap=True))
+    del vol
+    torch.cuda.empty_cache()
+    p, t = tm.points.astype(np.float64), tm.tris.astype(np.int64)
+    assert tm.numTris > 900_000 and (t >= 0).all() and (t < len(p)).all()
+    e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
+    key = e[:, 0] * len(p) + e[:, 1]
+    rkey = e[:, 1] * len(p) + e[:, 0]
+    ks = np.sort(key)
+    assert (np.diff(ks) > 0).all()  # every directed edge once
+    assert np.isin(rkey, ks).all()  # and its reverse present: closed and consistently oriented
+    assert len(p) - len(e) // 2 + len(t) == 2
+    a, b, c = p[t[:, 0]], p[t[:, 1]], p[t[:, 2]]
+    volume = np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6
+    assert abs(volume / (4 / 3 * np.pi * r ** 3) - 1) < 1e-3
