@@ -256,7 +256,7 @@ def test_more_than_2_31_voxels(M):
     del vol
     torch.cuda.empty_cache()
     p, t = tm.points.astype(np.float64), tm.tris.astype(np.int64)
-    assert tm.numTris > 900_000 and (t >= 0).all() and (t < len(p)).all()
+    assert tm.numTris > 500_000 and (t >= 0).all() and (t < len(p)).all()
     e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
     key = e[:, 0] * len(p) + e[:, 1]
     rkey = e[:, 1] * len(p) + e[:, 0]
