@@ -350,8 +350,9 @@ GBFWN_API int gbfwn_make_signed_by_winding_number_dev(gbfwn_handle h, const int3
 
 /* MR::MarchingCubesParams (MRVoxels/MRMarchingCubes.h:18-61): origin, iso, lessInside, maxVertices;
  * wantFaceMap = outVoxelPerFaceMap requested.  voxelSize is the volume's (SimpleVolume::voxelSize).
- * Defaults (gbfwn_mc_default_params): origin 0, voxelSize 1, iso 0, lessInside 0,
- * maxVertices INT32_MAX, wantFaceMap 0. */
+ * A mesh with more than maxVertices vertices is an error, as in the reference (start from
+ * gbfwn_mc_default_params: a zeroed struct allows no vertex).  Defaults: origin 0, voxelSize 1,
+ * iso 0, lessInside 0, maxVertices INT32_MAX, wantFaceMap 0. */
 typedef struct gbfwn_mc_params {
     float origin[3];
     float voxelSize[3];

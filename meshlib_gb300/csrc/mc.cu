@@ -771,7 +771,8 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     g.zpy = p.origin[1] + 0.5f * p.voxelSize[1];
     for (int k = 0; k < 3; ++k) g.vs[k] = p.voxelSize[k];
     g.iso = p.iso;
-    const int64_t maxVerts = p.maxVertices > 0 ? std::min<int64_t>(p.maxVertices, INT32_MAX) : INT32_MAX;
+    // "if the mesh exceeds this number of vertices, an error returns" (vertex ids are 32-bit either way)
+    const int64_t maxVerts = std::min<int64_t>(p.maxVertices, INT32_MAX);
 
     DeviceGuard guard(device);
     McWorkspace& ws = workspace(device);

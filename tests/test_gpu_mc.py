@@ -110,6 +110,9 @@ def test_errors(M):
     with pytest.raises(M.FwnError, match="Vertices number limit exceeded"):
         M.marchingCubes(vol, M.MarchingCubesParams(maxVertices=n - 1))
     assert M.marchingCubes(vol, M.MarchingCubesParams(maxVertices=n)).numPoints == n
+    with pytest.raises(M.FwnError, match="Vertices number limit exceeded"):
+        M.marchingCubes(vol, M.MarchingCubesParams(maxVertices=0))
+    assert M.marchingCubes(np.ones((3, 3, 3), np.float32), M.MarchingCubesParams(maxVertices=0)).numPoints == 0
     assert M.marchingCubes(np.zeros((0, 4, 4), np.float32)).numTris == 0
     mc = M.MarchingCubesByParts((5, 5, 6))
     with pytest.raises(M.FwnError, match="XY dimensions"):

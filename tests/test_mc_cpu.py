@@ -128,3 +128,11 @@ def test_mesher_memory_estimate():
     assert 3 * 512 ** 3 <= w <= 3.1 * 512 ** 3
     assert L.gbfwn_marching_cubes_memory(dims.ctypes.data, 1_000_000) == w + 30 * 1_000_000
     assert L.gbfwn_marching_cubes_memory(np.array([0, 4, 4], np.int32).ctypes.data, 10) == 0
+
+
+def test_vertex_limit_zero_like_reference():
+    """maxVertices = 0: any vertex exceeds the limit (VolumeMesher::finalize), an empty mesh does not."""
+    vol = np.random.default_rng(2).normal(size=(4, 4, 4)).astype(np.float32)
+    with pytest.raises(O.McError, match="Vertices number limit exceeded"):
+        O.marching_cubes(vol, max_vertices=0)
+    assert len(O.marching_cubes(np.ones((3, 3, 3), np.float32), max_vertices=0)[0]) == 0
