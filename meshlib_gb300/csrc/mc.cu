@@ -421,6 +421,8 @@ __device__ __forceinline__ int cellTriangles(const uint8_t* __restrict__ flags, 
 __global__ void __launch_bounds__(256) cellKernel(const uint8_t* __restrict__ flags, const int32_t* __restrict__ chunkVerts,
                                                   McDims d, uint8_t* __restrict__ tcnt, int32_t* __restrict__ chunkTris,
                                                   unsigned long long* __restrict__ total) {
+    __shared__ unsigned long long sCorners[8][128];  // per warp: corner bytes of its candidate cells
+    __shared__ uint8_t sCounts[8][128];
     const int lane = threadIdx.x & 31;
     unsigned long long mine = 0;
     const int64_t layer = int64_t(d.pitch) * d.dy;
@@ -464,21 +466,54 @@ __global__ void __launch_bounds__(256) cellKernel(const uint8_t* __restrict__ fl
         // row words extended by the next byte: byte j and j + 1 of row r are cell j's corners
         const unsigned long long e0 = f0 | ((unsigned long long)n0 << 32), e1 = f1 | ((unsigned long long)n1 << 32);
         const unsigned long long e2 = f2 | ((unsigned long long)n2 << 32), e3 = f3 | ((unsigned long long)n3 << 32);
-        unsigned word = 0;
-        int c = 0;
+        // candidate cells (a corner with a crossing) of this lane, then spread over the warp: lane l
+        // evaluates candidates l, l + 32, ... of the warp's list in shared memory, so a run of surface
+        // cells held by a few lanes does not serialise their evaluations
+        unsigned cand = 0;
+        unsigned long long corners[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            if (!(x + j + 1 < d.dx && hy && hz)) continue;
             const unsigned b0 = unsigned(e0 >> (8 * j)) & 0xffffu, b1 = unsigned(e1 >> (8 * j)) & 0xffffu;
             const unsigned b2 = unsigned(e2 >> (8 * j)) & 0xffffu, b3 = unsigned(e3 >> (8 * j)) & 0xffffu;
-            if (!((b0 | b1 | b2 | b3) & 0x0707u)) continue;  // no crossing on any corner
-            const unsigned long long corners =
-                (unsigned long long)(b0 | (b1 << 16)) | ((unsigned long long)(b2 | (b3 << 16)) << 32);
-            CellInfo ci;
-            const int nt = cellCore(corners, ci);
-            word |= unsigned(nt) << (8 * j);
-            c += nt;
+            corners[j] = (unsigned long long)(b0 | (b1 << 16)) | ((unsigned long long)(b2 | (b3 << 16)) << 32);
+            if (x + j + 1 < d.dx && hy && hz && ((b0 | b1 | b2 | b3) & 0x0707u)) cand |= 1u << j;
         }
+        const int nc = __popc(cand);
+        int excl = nc;  // exclusive prefix of the candidate counts over the lanes
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(FULL, excl, off);
+            if (lane >= off) excl += t;
+        }
+        const int totalC = __shfl_sync(FULL, excl, 31);
+        excl -= nc;
+        unsigned long long* slots = sCorners[threadIdx.x >> 5];
+        uint8_t* counts = sCounts[threadIdx.x >> 5];
+        {
+            int k = excl;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if ((cand >> j) & 1u) slots[k++] = corners[j];
+        }
+        __syncwarp();
+        for (int g = lane; g < totalC; g += 32) {
+            CellInfo ci;
+            counts[g] = uint8_t(cellCore(slots[g], ci));
+        }
+        __syncwarp();
+        unsigned word = 0;
+        int c = 0;
+        {
+            int k = excl;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if ((cand >> j) & 1u) {
+                    const int nt = counts[k++];
+                    word |= unsigned(nt) << (8 * j);
+                    c += nt;
+                }
+        }
+        __syncwarp();  // the slots are rewritten by the next item
         if (inRow) reinterpret_cast<uint32_t*>(tcnt)[at >> 2] = word;
         int sum = c + __shfl_xor_sync(FULL, c, 1);
         sum += __shfl_xor_sync(FULL, sum, 2);
