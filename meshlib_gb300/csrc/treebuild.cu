@@ -30,7 +30,7 @@ namespace gbfwn {
 
 namespace {
 
-constexpr int kSmall = 1024;  // segments of at most this many leaves are finished in shared memory
+constexpr int kSmall = 512;  // segments of at most this many leaves are finished in shared memory
 constexpr int kScanBlock = 1024;
 
 struct Elem {  // one leaf during construction (40 bytes)
@@ -252,15 +252,20 @@ __global__ void segBoxes(const Elem* __restrict__ el, int32_t n, const Seg* __re
     if (s < 0) return;
     float v[6] = {e.mn[0], e.mn[1], e.mn[2], -e.mx[0], -e.mx[1], -e.mx[2]};  // all as minima
     const int leader = __ffs(same) - 1;
-    for (int j = 0; j < 6; ++j) {  // reduce inside the group of lanes of the same segment
-        unsigned m = same;
-        float r = FLT_MAX;
-        while (m) {
-            const int src = __ffs(m) - 1;
-            r = fminf(r, __shfl_sync(same, v[j], src));
-            m &= m - 1;
+    if (same == 0xffffffffu) {  // the whole warp in one segment (the common case): butterfly
+        for (int j = 0; j < 6; ++j)
+            for (int off = 16; off; off >>= 1) v[j] = fminf(v[j], __shfl_xor_sync(0xffffffffu, v[j], off));
+    } else {
+        for (int j = 0; j < 6; ++j) {  // reduce inside the group of lanes of the same segment
+            unsigned m = same;
+            float r = FLT_MAX;
+            while (m) {
+                const int src = __ffs(m) - 1;
+                r = fminf(r, __shfl_sync(same, v[j], src));
+                m &= m - 1;
+            }
+            v[j] = r;
         }
-        v[j] = r;
     }
     if (lane == leader) {
         for (int j = 0; j < 3; ++j) atomicMin(&box[6 * s + j], floatToOrderedInt(v[j]));
@@ -439,7 +444,7 @@ struct SubSeg {
 
 constexpr size_t kFinishSmem = sizeof(Elem) * 2 * kSmall + sizeof(SubSeg) * kSmall + sizeof(int16_t) * kSmall + 16;
 
-__global__ void __launch_bounds__(1024) finishSmall(const Elem* __restrict__ el, const Seg* __restrict__ small,
+__global__ void __launch_bounds__(kSmall) finishSmall(const Elem* __restrict__ el, const Seg* __restrict__ small,
                                                    RefNode* nodes, int32_t* irs, int2* range, int64_t nNodes) {
     extern __shared__ __align__(16) unsigned char smem[];
     Elem(*buf)[kSmall] = reinterpret_cast<Elem(*)[kSmall]>(smem);
@@ -660,7 +665,7 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
     }
     if (nsmallHost > 0) {
         if ((e = cudaFuncSetAttribute(finishSmall, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFinishSmem)))) return e;
-        finishSmall<<<unsigned(nsmallHost), 1024, kFinishSmem, s>>>(el, small, nodes, irs, range, nNodes);
+        finishSmall<<<unsigned(nsmallHost), kSmall, kFinishSmem, s>>>(el, small, nodes, irs, range, nNodes);
     }
     return cudaGetLastError();
 }
