@@ -1,7 +1,7 @@
 """Seeded synthetic meshes, grids and query sets for the winding-number workloads.
 
 The reference project's own fixtures (``test_data/``) are not available, so every
-workload is generated here from a seed.  Conventions (recorded again in the design doc):
+workload is generated here from a seed.  Conventions:
 
 * noisy torus: major radius R, minor radius r, ``nu x nv`` quads split into two
   triangles each; every vertex moves along its torus normal by
