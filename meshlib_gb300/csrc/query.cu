@@ -422,6 +422,12 @@ __device__ float cpPacket(const QueryTree& t, const float3& q, bool active, floa
 
 // ------------------------------------------------------------------ kernels
 constexpr int kThreads = 256;
+// Resident blocks per SM of the kernels that run the closest-point walk (40 registers, some spilled):
+// more warps hide the dependent record loads better than registers help.  Measured at 512^3 on
+// 1.31 M triangles: 4 blocks (64 registers) 129 ms, 5 (48) 120 ms, 6 (40) 115 ms, 7-8 150 ms (spills).
+// The winding-number-only walks keep 4 (23.4 -> 25.1 ms at 6); so do self-intersections and the
+// batched kernel, which measured slower with more warps.
+constexpr int kDistBlocks = 6;
 constexpr int kTX = 4, kTY = 4, kTZ = 2;  // voxel tile of one warp
 
 struct TileGrid {
@@ -448,7 +454,7 @@ __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
 // minimum is unchanged, but it prunes from the first step (a third fewer node visits with an exact
 // bound, in a CPU model of the walk).
 template <bool PRECISE, bool DIST>
-__global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
+__global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
                                                        float* __restrict__ out, unsigned* scratch) {
     const int lane = threadIdx.x & 31;
     const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
@@ -508,7 +514,7 @@ __global__ void __launch_bounds__(kThreads, 4) gridKernel(QueryTree t, GridRange
 // one tile is near its point in the previous one, so (as in gridKernel) each lane starts its
 // closest-point search from the triangle closest to its previous point.
 template <bool PRECISE, bool DIST>
-__global__ void __launch_bounds__(kThreads, 4) vectorKernel(QueryTree t, const float* __restrict__ pts, int64_t n, DistOpts o,
+__global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) vectorKernel(QueryTree t, const float* __restrict__ pts, int64_t n, DistOpts o,
                                                          int32_t skipFace, float* __restrict__ out, unsigned* scratch,
                                                          const int32_t* __restrict__ order, int chunk) {
     const int lane = threadIdx.x & 31;
@@ -610,7 +616,7 @@ __device__ __noinline__ void closestPointBaryFp64(const float3 p, const float4 A
 // rounded as the reference CPU does.  Output per point, the layout of MR::MeshProjectionResult:
 // {face, proj.xyz} {edge = -1, bary a, bary b, distSq}; face = -1 when nothing lies closer than up.
 template <bool PRECISE, bool TREEXF>
-__global__ void __launch_bounds__(kThreads, 4) projectKernel(QueryTree t, const float* __restrict__ pts, int64_t n, Xf pxf,
+__global__ void __launch_bounds__(kThreads, kDistBlocks) projectKernel(QueryTree t, const float* __restrict__ pts, int64_t n, Xf pxf,
                                                           int hasPxf, Xf txf, float up, float lo, float4* __restrict__ out,
                                                           unsigned* scratch, const int32_t* __restrict__ order, int chunk) {
     const int lane = threadIdx.x & 31;
