@@ -146,12 +146,12 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 # workload, from an ncu capture of the same command (profiles/gridKernel_sdf_512cubed_dram.md:
 # dram__bytes_read.sum 676,597,504 + dram__bytes_write.sum 523,374,848); the kernel reads the mesh
 # records about 1.3 times from HBM.
-KERNEL_DRAM_BYTES_512 = 676_597_504 + 523_374_848
+KERNEL_DRAM_BYTES_512 = 754_624_256 + 611_213_824
 
 
 # FMA-pipe utilisation of the signed-distance grid kernel from the committed ncu capture
 # (profiles/gridKernel_sdf_256cubed_icosphere1.3M.md: sm__pipe_fma_cycles_active)
-KERNEL_FMA_PIPE_ACTIVE = 0.282
+KERNEL_FMA_PIPE_ACTIVE = 0.321
 
 
 def flop_per_voxel(c):
@@ -634,7 +634,7 @@ def main():
                             "dram_gbs_actual": (traffic / (ms_step * 1e-3) / 1e9) if traffic else None,
                             "note": "achieved counts the reference traversal's per-voxel node/dipole/triangle reads "
                                     "(bytes_per_voxel); the warp-packet traversal reads each record once per 32 voxels "
-                                    "from L1/L2, so actual DRAM traffic (traffic) is ~1.2 GB per launch and the kernel is "
+                                    "from L1/L2, so actual DRAM traffic (traffic) is ~1.4 GB per launch and the kernel is "
                                     "issue/latency-bound, not HBM-bound"}
         try:
             fp32_peak = M.fp32_peak_tflops(local)
@@ -649,7 +649,7 @@ def main():
                         "fma_pipe_active_ncu": KERNEL_FMA_PIPE_ACTIVE,
                         "note": "reference-equivalent FLOP/s counts the reference traversal's box tests, projections, "
                                 "dipoles and solid angles per voxel; the packet traversal does far fewer, and ncu shows the "
-                                "FMA pipe 28% busy: the kernel is bound by instruction issue and dependent loads"}
+                                "FMA pipe 32% busy: the kernel is bound by instruction issue and dependent loads"}
         line["cpu_baseline"] = {"value": rate, "unit": "voxels/s", "cores": thr, "kind": "port", "sample": desc}
         line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d, extra=prec_extra, M=M, device=local)
     if rank == 0:
