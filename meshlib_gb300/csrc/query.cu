@@ -888,7 +888,19 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const Bat
             const int mid = (lo + hi + 1) >> 1;
             if (items[mid].tileBase <= ticket) lo = mid; else hi = mid - 1;
         }
-        const BatchItem& it = items[lo];
+        // the item (tree, grid, transform, options: ~210 bytes) is staged in this warp's shared-memory
+        // slot and read from there, instead of living in registers for the whole column walk
+        // (measured 78.1 -> 74.9 ms on the 64-mesh batch)
+        __shared__ BatchItem sItem[THREADS / 32];
+        BatchItem& it = sItem[threadIdx.x >> 5];
+        {
+            static_assert(sizeof(BatchItem) % 4 == 0, "copied as 32-bit words");
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(items + lo);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&it);
+            __syncwarp();  // every lane is done with the previous item
+            for (int k = lane; k < int(sizeof(BatchItem) / 4); k += 32) dst[k] = src[k];
+            __syncwarp();
+        }
         // a ticket is a column of up to kBatchSeg tiles along z, walked upwards with each lane's
         // closest-point search seeded by its previous voxel's triangle (as gridKernel does)
         const unsigned local = ticket - it.tileBase;
