@@ -433,6 +433,11 @@ GBFWN_API int gbfwn_debug_wait_timeout(uint32_t maxPolls, void* stream);
 GBFWN_API int gbfwn_debug_gemm_bf16(const void* d_a, const void* d_b, float* d_d, int32_t m, int32_t n, int32_t k,
                                     int32_t split_k, void* stream);
 
+/* The library keeps device memory for reuse: staging buffers of freed handles (so creating a handle
+ * per call, as MeshLib does, does not map a grid-sized buffer every time) and the mesher's work
+ * arrays.  This returns all of it on `device` to the driver. */
+GBFWN_API int gbfwn_release_cached_memory(int device);
+
 /* Test hook: makes the next `count` device allocations of this thread fail with
  * GBFWN_OUT_OF_MEMORY (host-side fault injection; no device fault is involved). */
 GBFWN_API void gbfwn_debug_fail_next_allocs(int count);

@@ -152,6 +152,7 @@ _SIGS = [
     ("gbfwn_marching_cubes_dev", ctypes.c_int,
      [_vp, _vp, ctypes.POINTER(_McParams), _vp, _i32, ctypes.c_int, ctypes.POINTER(_vp), _vp]),
     ("gbfwn_mc_release_workspace", ctypes.c_int, [ctypes.c_int]),
+    ("gbfwn_release_cached_memory", ctypes.c_int, [ctypes.c_int]),
     ("gbfwn_marching_cubes_memory", ctypes.c_size_t, [_vp, _i64]),
     ("gbfwn_trimesh_sizes", ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     ("gbfwn_trimesh_copy", ctypes.c_int, [_vp, _vp, _vp, _vp]),

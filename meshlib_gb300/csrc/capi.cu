@@ -46,6 +46,48 @@ cudaError_t devMalloc(void** p, size_t bytes) {
     return cudaMalloc(p, bytes ? bytes : 16);
 }
 
+static constexpr int kMaxPoolDevices = 64;
+static std::mutex g_poolMu;
+static cudaMemPool_t g_pools[kMaxPoolDevices] = {};
+
+// The library's own stream-ordered pool on `device`: freed blocks stay reserved for the next
+// allocation, so a handle created per call (the reference's usage) does not map its grid-sized
+// staging buffer afresh every time.  gbfwn_release_cached_memory returns the reserve.
+cudaMemPool_t devicePool(int device) {
+    std::lock_guard<std::mutex> lk(g_poolMu);
+    cudaMemPool_t& pool = g_pools[unsigned(device) % kMaxPoolDevices];
+    if (!pool) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+            pool = nullptr;
+            return nullptr;
+        }
+        uint64_t keep = ~uint64_t(0);
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    return pool;
+}
+
+cudaError_t poolMalloc(void** p, size_t bytes, int device, cudaStream_t s) {
+    if (g_failAllocs > 0) {
+        --g_failAllocs;
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    cudaMemPool_t pool = devicePool(device);
+    if (!pool) return cudaMalloc(p, bytes ? bytes : 16);
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, s);
+    if (!e) e = cudaStreamSynchronize(s);  // usable from any stream once this returns
+    return e;
+}
+
+void poolFree(void* p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+}
+
 }  // namespace gbfwn
 
 namespace {
@@ -128,6 +170,16 @@ GBFWN_API const char* gbfwn_last_error(void) { return g_lastError.c_str(); }
 
 GBFWN_API void gbfwn_debug_fail_next_allocs(int count) { g_failAllocs = count; }
 
+GBFWN_API int gbfwn_release_cached_memory(int device) {
+    DeviceGuard g(device);
+    cudaMemPool_t pool = devicePool(device);
+    if (pool) {
+        cudaDeviceSynchronize();
+        cudaMemPoolTrimTo(pool, 0);
+    }
+    return gbfwn_mc_release_workspace(device);
+}
+
 GBFWN_API void gbfwn_set_precise(gbfwn_handle h, int precise) {
     if (h) h->precise = precise ? 1 : 0;
 }
@@ -196,9 +248,13 @@ GBFWN_API int gbfwn_destroy(gbfwn_handle h) {
         if (h->stream) cudaStreamSynchronize(h->stream);
         if (h->copyStream) cudaStreamSynchronize(h->copyStream);
         h->treeMem.freeAll();
-        if (h->outBuf) cudaFree(h->outBuf);
-        if (h->inBuf) cudaFree(h->inBuf);
-        if (h->sortBuf) cudaFree(h->sortBuf);
+        // staging buffers go back to the pool; the device is idle for them first (as cudaFree
+        // would make it), since a _dev call may have used them on a caller's stream
+        if (h->outBuf || h->inBuf || h->sortBuf) cudaDeviceSynchronize();
+        poolFree(h->outBuf, h->stream);
+        poolFree(h->inBuf, h->stream);
+        poolFree(h->sortBuf, h->stream);
+        if (h->stream) cudaStreamSynchronize(h->stream);
         for (auto ev : h->events) cudaEventDestroy(ev);
         if (h->stream) cudaStreamDestroy(h->stream);
         if (h->copyStream) cudaStreamDestroy(h->copyStream);

@@ -17,6 +17,11 @@ int fail(int status, const std::string& msg);
 int cudaFail(cudaError_t e, const char* what);
 // cudaMalloc honouring the fault-injection hook gbfwn_debug_fail_next_allocs.
 cudaError_t devMalloc(void** p, size_t bytes);
+// The library's stream-ordered memory pool on a device (freed memory is kept for reuse), an
+// allocation from it (honouring the same hook; complete when it returns) and a stream-ordered free.
+cudaMemPool_t devicePool(int device);
+cudaError_t poolMalloc(void** p, size_t bytes, int device, cudaStream_t s);
+void poolFree(void* p, cudaStream_t s);
 
 struct ListAllocator : Allocator {
     std::vector<void*> ptrs;
@@ -66,12 +71,17 @@ struct gbfwn_mesh_s {
     std::vector<cudaEvent_t> events;
     std::mutex mu;  // calls on one handle are serialised (the reference is not re-entrant per object)
 
+    // grows a staging buffer; buffers come from the device's pool, so one freed by an earlier handle
+    // is reused without mapping new memory
     cudaError_t ensure(void** buf, size_t* cap, size_t bytes) {
         if (*cap >= bytes) return cudaSuccess;
-        if (*buf) cudaFree(*buf);
+        if (*buf) {
+            cudaDeviceSynchronize();  // no call may still use it on another stream (as cudaFree ensured)
+            gbfwn::poolFree(*buf, stream);
+        }
         *buf = nullptr;
         *cap = 0;
-        cudaError_t e = gbfwn::devMalloc(buf, bytes);
+        cudaError_t e = gbfwn::poolMalloc(buf, bytes, device, stream);
         if (e == cudaSuccess) *cap = bytes;
         return e;
     }
