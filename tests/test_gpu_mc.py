@@ -270,3 +270,17 @@ def test_more_than_2_31_voxels(M):
     a, b, c = p[t[:, 0]], p[t[:, 1]], p[t[:, 2]]
     volume = np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6
     assert abs(volume / (4 / 3 * np.pi * r ** 3) - 1) < 1e-3
+
+
+def test_release_cached_memory(M):
+    """Handles created one per call reuse the library's pooled staging memory; releasing the cache
+    (pool and mesher workspace) leaves every call working and the results unchanged."""
+    v, f = mg.noisy_torus(seed=2)
+    dims, xf = mg.grid_for(v, 24)
+    first = M.FastWindingNumber(v, f).calcFromGridWithDistances(dims, xf)
+    tm = M.marchingCubes(first.reshape(dims[2], dims[1], dims[0]), M.MarchingCubesParams(lessInside=True))
+    assert M.lib().gbfwn_release_cached_memory(0) == M.OK
+    again = M.FastWindingNumber(v, f).calcFromGridWithDistances(dims, xf)
+    assert np.array_equal(first, again)
+    tm2 = M.marchingCubes(again.reshape(dims[2], dims[1], dims[0]), M.MarchingCubesParams(lessInside=True))
+    assert np.array_equal(tm.tris, tm2.tris)
