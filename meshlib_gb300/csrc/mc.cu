@@ -227,15 +227,6 @@ __device__ __forceinline__ void forEachMarkedItem(const McDims& d, int lane, con
     }
 }
 
-// sum over the 16 lanes of a chunk (lanes 0-15 and 16-31 of a warp are two chunks)
-__device__ __forceinline__ int chunkSum(int c) {
-    c += __shfl_xor_sync(FULL, c, 8);
-    c += __shfl_xor_sync(FULL, c, 4);
-    c += __shfl_xor_sync(FULL, c, 2);
-    c += __shfl_xor_sync(FULL, c, 1);
-    return c;
-}
-
 // exclusive prefix of c over the lanes of the chunk before this one
 __device__ __forceinline__ int chunkExclusive(int c, int lane) {
     int p = c;
