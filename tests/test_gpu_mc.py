@@ -284,3 +284,15 @@ def test_release_cached_memory(M):
     assert np.array_equal(first, again)
     tm2 = M.marchingCubes(again.reshape(dims[2], dims[1], dims[0]), M.MarchingCubesParams(lessInside=True))
     assert np.array_equal(tm.tris, tm2.tris)
+
+
+@pytest.mark.parametrize("vals", [[-1, 1, 1, 1, 1, 1, 1, 1], [np.nan, -1, 1, 1, 1, 1, 1, 1], [-1, -1, 1, 1, 1, 1, 1, 1],
+                                  [1, -1, -1, 1, -1, 1, 1, -1], [np.nan, np.nan, -1, 1, 1, np.nan, 1, -1]])
+def test_single_cells(M, vals):
+    """The hand-worked cells of the oracle tests (and two ambiguous / NaN-heavy ones) on the GPU."""
+    vol = np.empty((2, 2, 2), np.float32)
+    for i, val in enumerate(vals):
+        vol[i >> 2, (i >> 1) & 1, i & 1] = val
+    for li in (False, True):
+        _same(M.marchingCubes(vol, M.MarchingCubesParams(lessInside=li, outVoxelPerFaceMap=True)),
+              O.marching_cubes(vol, less_inside=li))

@@ -136,3 +136,39 @@ def test_vertex_limit_zero_like_reference():
     with pytest.raises(O.McError, match="Vertices number limit exceeded"):
         O.marching_cubes(vol, max_vertices=0)
     assert len(O.marching_cubes(np.ones((3, 3, 3), np.float32), max_vertices=0)[0]) == 0
+
+
+def _one_cell(vals):
+    """2x2x2 volume from corner values indexed x + 2y + 4z."""
+    v = np.empty((2, 2, 2), np.float32)
+    for i, val in enumerate(vals):
+        v[i >> 2, (i >> 1) & 1, i & 1] = val
+    return v
+
+
+def test_hand_worked_single_cell():
+    """Corner 0 below iso, the rest above: configuration 1 (plan edges 0, 8, 3), vertices on corner
+    0's +X, +Y, +Z edges in that order at the midpoints (ratio 0.5), one triangle (X, Z, Y); lessInside
+    reverses it (MRMarchingCubes.cpp:610-646, 1030-1045)."""
+    vol = _one_cell([-1, 1, 1, 1, 1, 1, 1, 1])
+    p, t, f = O.marching_cubes(vol, iso=0.0)
+    assert p.tolist() == [[1.0, 0.5, 0.5], [0.5, 1.0, 0.5], [0.5, 0.5, 1.0]]
+    assert t.tolist() == [[0, 2, 1]] and f.tolist() == [0]
+    p2, t2, _ = O.marching_cubes(vol, iso=0.0, less_inside=True)
+    assert np.array_equal(p2, p) and t2.tolist() == [[0, 1, 2]]
+    # iso between: ratio (iso - v0) / (v1 - v0) from the lower-id end of each edge
+    p3, _, _ = O.marching_cubes(_one_cell([-1, 3, 3, 3, 3, 3, 3, 3]), iso=0.0)
+    assert np.allclose(p3, [[0.75, 0.5, 0.5], [0.5, 0.75, 0.5], [0.5, 0.5, 0.75]])
+
+
+def test_hand_worked_nan_corner():
+    """Corner 0 NaN takes corner 1's side (first valid neighbour: x, then y, z, ...), giving
+    configuration 3; its plan needs a vertex on corner 0's +Z edge, which a NaN end cannot have, so the
+    cell emits nothing (MRMarchingCubes.cpp:913-1032) -- while corner 1's +Y and +Z vertices exist."""
+    vol = _one_cell([np.nan, -1, 1, 1, 1, 1, 1, 1])
+    p, t, f = O.marching_cubes(vol, iso=0.0)
+    assert p.tolist() == [[1.5, 1.0, 0.5], [1.5, 0.5, 1.0]]
+    assert len(t) == 0
+    # with corner 0 valid and below iso the same cell is configuration 3 and meshes fully
+    p2, t2, _ = O.marching_cubes(_one_cell([-1, -1, 1, 1, 1, 1, 1, 1]), iso=0.0)
+    assert len(t2) == 2 and O.mc_plan(3) == "183981"
