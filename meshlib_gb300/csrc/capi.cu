@@ -127,6 +127,8 @@ bool validDims(const int32_t* dims) {
 int createCommon(gbfwn_mesh_s* h, const std::string& where) {
     std::string err;
     ListAllocator tmp;  // build work arrays, freed once the build has finished
+    tmp.device = h->device;
+    tmp.stream = h->stream;
     cudaError_t e = buildDeviceTree(h->dVerts, h->nv, h->dTris, h->nt, h->tree, h->treeMem, tmp, h->stream, err);
     cudaStreamSynchronize(h->stream);
     tmp.freeAll();
@@ -141,6 +143,8 @@ int newHandle(int device, gbfwn_mesh_s** out) {
     cudaError_t e = cudaSetDevice(device);
     if (!e) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (!e) e = cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking);
+    h->treeMem.device = device;
+    h->treeMem.stream = h->stream;
     if (!e) e = h->treeMem.alloc((void**)&h->scratch, 64);
     if (!e) e = cudaMemsetAsync(h->scratch, 0, 64, h->stream);
     if (e) {
@@ -154,6 +158,8 @@ int newHandle(int device, gbfwn_mesh_s** out) {
 
 int refitCommon(gbfwn_mesh_s* h, const uint64_t* dChanged, cudaStream_t s, const char* what) {
     ListAllocator tmp;  // refit work arrays
+    tmp.device = h->device;
+    tmp.stream = s;
     cudaError_t e = refitDeviceTree(h->dVerts, h->nv, h->dTris, dChanged, h->tree, h->treeMem, tmp, s);
     cudaStreamSynchronize(s);
     tmp.freeAll();
@@ -245,12 +251,10 @@ GBFWN_API int gbfwn_destroy(gbfwn_handle h) {
     if (!h) return GBFWN_OK;
     {
         DeviceGuard g(h->device);
-        if (h->stream) cudaStreamSynchronize(h->stream);
-        if (h->copyStream) cudaStreamSynchronize(h->copyStream);
+        // everything goes back to the device's pool; the device is idle first (as cudaFree would
+        // make it), since a _dev call may have used the handle's arrays on a caller's stream
+        cudaDeviceSynchronize();
         h->treeMem.freeAll();
-        // staging buffers go back to the pool; the device is idle for them first (as cudaFree
-        // would make it), since a _dev call may have used them on a caller's stream
-        if (h->outBuf || h->inBuf || h->sortBuf) cudaDeviceSynchronize();
         poolFree(h->outBuf, h->stream);
         poolFree(h->inBuf, h->stream);
         poolFree(h->sortBuf, h->stream);

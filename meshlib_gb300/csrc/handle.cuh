@@ -23,15 +23,25 @@ cudaMemPool_t devicePool(int device);
 cudaError_t poolMalloc(void** p, size_t bytes, int device, cudaStream_t s);
 void poolFree(void* p, cudaStream_t s);
 
+// Allocations freed together.  With a device set, they come from that device's pool (complete, and
+// usable from any stream, when alloc returns) and go back to it on freeAll, stream-ordered on
+// `stream`: the caller makes sure nothing still uses them, as cudaFree's synchronisation used to.
 struct ListAllocator : Allocator {
     std::vector<void*> ptrs;
+    int device = -1;
+    cudaStream_t stream = nullptr;
     cudaError_t alloc(void** p, size_t bytes) override {
-        cudaError_t e = devMalloc(p, bytes);
+        cudaError_t e = device >= 0 ? poolMalloc(p, bytes, device, stream) : devMalloc(p, bytes);
         if (e == cudaSuccess) ptrs.push_back(*p);
         return e;
     }
     void freeAll() {
-        for (void* p : ptrs) cudaFree(p);
+        for (void* p : ptrs) {
+            if (device >= 0)
+                poolFree(p, stream);
+            else
+                cudaFree(p);
+        }
         ptrs.clear();
     }
 };
