@@ -645,9 +645,10 @@ struct gbfwn_trimesh_s {
     int64_t nPoints = 0, nTris = 0;
     ~gbfwn_trimesh_s() {
         gbfwn::DeviceGuard g(device);
-        cudaFree(dPoints);
-        cudaFree(dTris);
-        cudaFree(dFaceMap);
+        if (dPoints || dTris || dFaceMap) cudaDeviceSynchronize();  // as cudaFree would: no use in flight
+        gbfwn::poolFree(dPoints, nullptr);
+        gbfwn::poolFree(dTris, nullptr);
+        gbfwn::poolFree(dFaceMap, nullptr);
     }
 };
 
@@ -661,7 +662,9 @@ struct gbfwn_mc_parts_s {
     cudaStream_t stream = nullptr;
     ~gbfwn_mc_parts_s() {
         gbfwn::DeviceGuard g(device);
-        cudaFree(dVol);
+        if (dVol) cudaDeviceSynchronize();
+        gbfwn::poolFree(dVol, stream);
+        if (stream) cudaStreamSynchronize(stream);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -850,9 +853,10 @@ int runMarchingCubes(const float* dVol, const int32_t dims[3], const gbfwn_mc_pa
     m->nTris = int64_t(ht[1]);
     e = exclusiveScanI32(chunkV, baseV, d.nChunks, sums, misc, s);
     if (!e) e = exclusiveScanI32(chunkT, baseT, d.nChunks, sums, misc + 1, s);
-    if (!e) e = devMalloc((void**)&m->dPoints, sizeof(float) * 3 * size_t(m->nPoints));
-    if (!e) e = devMalloc((void**)&m->dTris, sizeof(int32_t) * 3 * size_t(m->nTris));
-    if (!e && p.wantFaceMap) e = devMalloc((void**)&m->dFaceMap, sizeof(int32_t) * size_t(m->nTris));
+    // outputs from the device's pool (reused across calls; returned when the mesh is destroyed)
+    if (!e) e = poolMalloc((void**)&m->dPoints, sizeof(float) * 3 * size_t(m->nPoints), device, s);
+    if (!e) e = poolMalloc((void**)&m->dTris, sizeof(int32_t) * 3 * size_t(m->nTris), device, s);
+    if (!e && p.wantFaceMap) e = poolMalloc((void**)&m->dFaceMap, sizeof(int32_t) * size_t(m->nTris), device, s);
     if (!e) e = ws.ensureCells(sizeof(int64_t) * size_t(std::max<int64_t>(m->nTris, 1)));  // cells <= triangles
     if (!e) {
         int64_t* cellList = reinterpret_cast<int64_t*>(ws.cells);
@@ -918,12 +922,13 @@ GBFWN_API int gbfwn_marching_cubes(const float* volume, const int32_t dims[3], c
     if (e) return cudaFail(e, "gbfwn_marching_cubes");
     float* dVol = nullptr;
     const size_t n = empty ? 0 : size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]);
-    e = devMalloc((void**)&dVol, sizeof(float) * n);
+    e = poolMalloc((void**)&dVol, sizeof(float) * n, device, s);
     if (!e && n) e = cudaMemcpyAsync(dVol, volume, sizeof(float) * n, cudaMemcpyHostToDevice, s);
     int st = e ? cudaFail(e, "gbfwn_marching_cubes") : GBFWN_OK;
     if (!st && !mcProgress(cb, user, 0.3f)) st = fail(GBFWN_CANCELLED, "Operation was canceled");
     if (!st) st = runMarchingCubes(dVol, dims, *params, partStarts, nParts, device, s, out, "gbfwn_marching_cubes");
-    cudaFree(dVol);
+    poolFree(dVol, s);  // stream-ordered after the copy and the mesher on s
+    cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     if (!st && !mcProgress(cb, user, 1.f)) {
         gbfwn_trimesh_destroy(*out);
@@ -994,7 +999,7 @@ GBFWN_API int gbfwn_mc_parts_create(const int32_t dims[3], const gbfwn_mc_params
     p->params = *params;
     DeviceGuard g(device);
     cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
-    if (!e) e = devMalloc((void**)&p->dVol, sizeof(float) * size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]));
+    if (!e) e = poolMalloc((void**)&p->dVol, sizeof(float) * size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]), device, p->stream);
     if (e) {
         delete p;
         return cudaFail(e, "gbfwn_mc_parts_create");
@@ -1066,7 +1071,8 @@ GBFWN_API int gbfwn_grid_to_mesh(gbfwn_handle h, gbfwn_surrogate sur, const int3
     const bool banded = o.maxDistSq > 0.f && o.maxDistSq < FLT_MAX && o.nullOutsideMinMax;
     DeviceGuard g(h->device);
     float* grid = nullptr;
-    cudaError_t e = devMalloc((void**)&grid, sizeof(float) * size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]));
+    cudaError_t e = poolMalloc((void**)&grid, sizeof(float) * size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]), h->device,
+                               h->stream);
     if (e) return cudaFail(e, "gbfwn_grid_to_mesh");
     int st = GBFWN_OK;
     if ((e = h->resetStatus(h->stream))) st = cudaFail(e, "gbfwn_grid_to_mesh");
@@ -1080,7 +1086,7 @@ GBFWN_API int gbfwn_grid_to_mesh(gbfwn_handle h, gbfwn_surrogate sur, const int3
     if (!st) st = h->checkStatus();  // synchronises; reports a traversal overflow
     if (!st && !mcProgress(cb, user, 0.9f)) st = fail(GBFWN_CANCELLED, "Operation was canceled");
     if (!st) st = runMarchingCubes(grid, dims, *mc, partStarts, nParts, h->device, h->stream, out, "gbfwn_grid_to_mesh");
-    cudaFree(grid);
+    poolFree(grid, h->stream);  // the mesher has synchronised h->stream
     if (!st && !mcProgress(cb, user, 1.f)) {
         gbfwn_trimesh_destroy(*out);
         *out = nullptr;
