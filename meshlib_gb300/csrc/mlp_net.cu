@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "handle.cuh"
 #include "mlp.cuh"
 #include "surrogate.cuh"
 #include "umma.cuh"
@@ -733,8 +734,11 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     float *centers = nullptr, *lb = nullptr, *tmp = nullptr;
     int32_t *keep = nullptr, *pos = nullptr, *list = nullptr, *sums = nullptr, *total = nullptr;
     std::vector<void*> mem;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaMemPool_t pool = devicePool(dev);  // the library's pool keeps the memory for the next call
     auto A = [&](void** p, size_t b) {
-        cudaError_t r = cudaMallocAsync(p, b ? b : 16, s);
+        cudaError_t r = pool ? cudaMallocFromPoolAsync(p, b ? b : 16, pool, s) : cudaMallocAsync(p, b ? b : 16, s);
         if (!r) mem.push_back(*p);
         return r;
     };
