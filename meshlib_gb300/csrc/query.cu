@@ -754,7 +754,7 @@ uint64_t gridTiles(int32_t nx, int32_t ny, int32_t nz) {
     return uint64_t((nx + kTX - 1) / kTX) * uint64_t((ny + kTY - 1) / kTY) * uint64_t((nz + kTZ - 1) / kTZ);
 }
 
-static TileGrid tileGridFor(const GridRange& g) {
+static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
     TileGrid tg;
     tg.tilesX = (g.nx + kTX - 1) / kTX;
     tg.tilesY = (g.ny + kTY - 1) / kTY;
@@ -764,10 +764,12 @@ static TileGrid tileGridFor(const GridRange& g) {
     tg.bricksX = tg.bricksY = 0;
     // Longer columns reuse more seeds; shorter ones leave more items for the tail of the persistent
     // grid.  Measured at 256^3 / 512^3 on 1.3 M triangles: keep >= 25 items per (32-warps-per-SM)
-    // resident warp; at 512^3 that gives 32-tile columns (16: +0.7 %, 64: +1 %).
+    // resident warp, and columns of at most 32 tiles for unbanded signed distances (512^3: 16 tiles
+    // +0.7 %, 64 +1 %) but 16 otherwise (banded requests, where the cost sits in the voxels near the
+    // surface: 32 tiles made a 512^3 band 10 % slower).
     const uint64_t cols = uint64_t(tg.tilesX) * tg.tilesY;
     const uint64_t warps = uint64_t(numSMs()) * 4 * (kThreads / 32);
-    tg.segLen = 32;
+    tg.segLen = maxSegLen;
     while (tg.segLen > 1 && cols * uint64_t((tg.tilesZ + tg.segLen - 1) / tg.segLen) < 25 * warps) tg.segLen /= 2;
     tg.segsZ = (tg.tilesZ + tg.segLen - 1) / tg.segLen;
     tg.numItems = uint32_t(cols * tg.segsZ);
@@ -798,7 +800,7 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
                           unsigned* scratch, cudaStream_t s) {
-    const TileGrid tg = tileGridFor(g);
+    const TileGrid tg = tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16);
     if (precise)
         return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
     return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
