@@ -85,7 +85,18 @@ cudaError_t poolMalloc(void** p, size_t bytes, int device, cudaStream_t s) {
 }
 
 void poolFree(void* p, cudaStream_t s) {
-    if (p) cudaFreeAsync(p, s);
+    if (!p) return;
+    int device = 0;
+    cudaGetDevice(&device);
+    bool pooled;
+    {
+        std::lock_guard<std::mutex> lk(g_poolMu);
+        pooled = g_pools[unsigned(device) % kMaxPoolDevices] != nullptr;
+    }
+    if (pooled)
+        cudaFreeAsync(p, s);
+    else
+        cudaFree(p);  // poolMalloc fell back to cudaMalloc: no pool on this device
 }
 
 }  // namespace gbfwn
