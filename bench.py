@@ -472,6 +472,16 @@ def main():
             tot += a.elapsed_time(b)
         return tot / steps
 
+    # ---- the other grid calls on the same grid: winding numbers only (calcFromGrid, the grid the
+    # reference's makeSignedByWindingNumber needs) and the dense sign pass over |distance|
+    wgrid = torch.empty(nvox, dtype=torch.float32, device="cuda")
+    fwn_grid_ms = timed(lambda: fwn.calcFromGrid_dev(dims, xf, wgrid.data_ptr(), stream=sp), 3)
+    absd = out.abs()
+    sign_ms = timed(lambda: fwn.makeSignedByWindingNumber_dev(dims, xf, absd.data_ptr(), stream=sp), 3)
+    other_grids = {"from_grid_ms": fwn_grid_ms, "from_grid_voxels_per_s": nvox / (fwn_grid_ms * 1e-3),
+                   "sign_pass_ms": sign_ms, "note": "calcFromGrid (beta 2) and makeSignedByWindingNumber on the same grid"}
+    del wgrid, absd
+
     # ---- banded forms (offset band 0.01 * diag): the reference's own banded request per voxel,
     # exact brick culling, and learned (surrogate) brick culling; identical results expected
     banded = None
@@ -623,7 +633,7 @@ def main():
                     "d2h_bytes_per_step": int(nvox * 4), "s_per_step": e2e_s,
                     "s_create_per_step": float(np.mean(create_times)) if create_times else None},
             "clocks": clk.summary(), "nan_fraction": nan_frac, "wall_s_timed": wall, "banded": banded, "batched": batched, "points": points,
-            "reference_gpu": refgpu, "offset": offset}
+            "reference_gpu": refgpu, "offset": offset, "other_grids": other_grids}
     if rank == 0 and not args.no_cpu:
         rate, thr, desc, counts = cpu_reference_rate(v, f, dims, xf)
         bpv = bytes_per_voxel(counts)
