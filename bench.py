@@ -222,10 +222,11 @@ def precision_vs_fp64(v, f, dims, xf, grid_out, shell, shell_d, n_grid=200_000, 
     return out
 
 
-def mrcuda_leg(v, f, dims, xf, ours, ours_ms, banded, timed, stream):
+def mrcuda_leg(v, f, dims, xf, ours, ours_ms, banded, timed, stream, ours_wn=None, ours_wn_ms=None):
     """The reference's signedDistanceKernel (MRCuda/MRCudaFastWindingNumber.cu:205-243, one thread
     per voxel, 32 threads per block, -use_fast_math) on this GPU: unbanded (maxDistSq = inf) and with
-    the reference's banded request, plus how far its results are from ours."""
+    the reference's banded request, plus how far its results are from ours; and its winding-number
+    grid kernel (fastWindingNumberFromGridKernel, .cu:175-203) beside our calcFromGrid."""
     import torch
 
     from oracle import mrcuda
@@ -256,6 +257,12 @@ def mrcuda_leg(v, f, dims, xf, ours, ours_ms, banded, timed, stream):
         res.update({"banded_ms": bms, "banded_voxels_per_s": nvox / (bms * 1e-3),
                     "ours_plain_banded_speedup": bms / banded["plain_banded_ms"],
                     "ours_surrogate_banded_speedup": bms / banded["surrogate_banded_ms"]})
+    if ours_wn is not None:
+        wms = timed(lambda: rk.from_grid(dims, xf, out=out_r, stream=stream), 1)
+        wdiff = (out_r - ours_wn).abs()
+        res.update({"from_grid_ms": wms, "ours_from_grid_speedup": wms / ours_wn_ms,
+                    "from_grid_max_abs_wn_diff": float(wdiff.max().item()),
+                    "from_grid_inside_mismatches": int(((out_r > 0.5) != (ours_wn > 0.5)).sum().item())})
     del out_r
     return res
 
@@ -480,7 +487,7 @@ def main():
     sign_ms = timed(lambda: fwn.makeSignedByWindingNumber_dev(dims, xf, absd.data_ptr(), stream=sp), 3)
     other_grids = {"from_grid_ms": fwn_grid_ms, "from_grid_voxels_per_s": nvox / (fwn_grid_ms * 1e-3),
                    "sign_pass_ms": sign_ms, "note": "calcFromGrid (beta 2) and makeSignedByWindingNumber on the same grid"}
-    del wgrid, absd
+    del absd
 
     # ---- banded forms (offset band 0.01 * diag): the reference's own banded request per voxel,
     # exact brick culling, and learned (surrogate) brick culling; identical results expected
@@ -520,7 +527,8 @@ def main():
     # sources, fed the reference's CPU-built tree and dipoles) on the same GPU and grid
     refgpu = None
     if not args.no_refgpu and rank == 0:
-        refgpu = mrcuda_leg(v, f, dims, xf, out, ms_step, banded, timed, sp)
+        refgpu = mrcuda_leg(v, f, dims, xf, out, ms_step, banded, timed, sp, wgrid, fwn_grid_ms)
+    del wgrid
 
     # ---- points and faces on the same mesh: 4M shell points (|d| < 1e-3, calcFromVector and the
     # signed distance at points) and calcSelfIntersections after folding 1% of the faces inward

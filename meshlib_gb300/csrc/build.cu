@@ -156,8 +156,9 @@ __global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, co
 // projections of all the node's triangle vertices, widened by a relative margin that covers the
 // FP32 rounding of the projections here and at query time, so the box distance stays a lower
 // bound of the distance to every triangle inside.  The node's leaves are the contiguous slots
-// range[i] = (first, count).  Nodes of up to kObbChunk leaves: one warp each (obbKernel); larger
-// ones (the top levels, about 2n / kObbChunk nodes): one warp per chunk of kObbChunk leaves,
+// range[i] = (first, count).  Nodes of up to kObbChunk leaves: obbKernel (a thread for a node of up
+// to 4 leaves, a warp for a larger one); larger ones (the top levels, about 2n / kObbChunk nodes):
+// one warp per chunk of kObbChunk leaves,
 // combined with order-independent atomic min / max (obbChunkKernel), then written by
 // obbBigKernel -- so no warp walks more than kObbChunk triangles.
 constexpr int kObbChunk = 4096;
@@ -233,18 +234,45 @@ __device__ __forceinline__ void writeObb(int64_t i, const Frame& f, const float 
     dst[3] = make_float4(e[0], e[1], e[2], __int_as_float(link));
 }
 
+// Nodes of up to kObbThread leaves (three quarters of all nodes): one thread each; larger ones up to
+// kObbChunk leaves: the warp of the 32 consecutive nodes holding them, one node after the other.
+// min / max are exact, so the boxes are the same however the projections are split.
+constexpr int kObbThread = 4;
+
 __global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const int2* __restrict__ range,
                           const float4* __restrict__ tri, const int32_t* __restrict__ parent,
                           const int32_t* __restrict__ irank, const int32_t* __restrict__ slot, float4* __restrict__ cp) {
-    const int64_t i = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    if (i >= nNodes || i == 0) return;
-    const int2 r = range[i];
-    if (r.y > kObbChunk) return;  // obbChunkKernel / obbBigKernel
-    const Frame f = nodeFrame(dip8, i);
-    float lo[3], hi[3];
-    projRange(f, tri, r.x, r.x + r.y, lane, lo, hi);
-    if (lane == 0) writeObb(i, f, lo, hi, parent, irank, slot, cp);
+    int2 r = make_int2(0, 0);
+    if (i < nNodes && i != 0) r = range[i];
+    if (r.y >= 1 && r.y <= kObbThread) {
+        const Frame f = nodeFrame(dip8, i);
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int sidx = r.x; sidx < r.x + r.y; ++sidx) {
+            for (int k = 0; k < 3; ++k) {
+                const float4 v = tri[3 * int64_t(sidx) + k];
+                const float p[3] = {f.t[0] * v.x + f.t[1] * v.y + f.t[2] * v.z, f.u[0] * v.x + f.u[1] * v.y + f.u[2] * v.z,
+                                    f.n[0] * v.x + f.n[1] * v.y + f.n[2] * v.z};
+                for (int j = 0; j < 3; ++j) {
+                    lo[j] = fminf(lo[j], p[j]);
+                    hi[j] = fmaxf(hi[j], p[j]);
+                }
+            }
+        }
+        writeObb(i, f, lo, hi, parent, irank, slot, cp);
+    }
+    unsigned big = __ballot_sync(0xffffffffu, r.y > kObbThread && r.y <= kObbChunk);
+    while (big) {  // obbChunkKernel / obbBigKernel take the nodes above kObbChunk
+        const int src = __ffs(big) - 1;
+        big &= big - 1;
+        const int64_t j = i - lane + src;
+        const int first = __shfl_sync(0xffffffffu, r.x, src), num = __shfl_sync(0xffffffffu, r.y, src);
+        const Frame f = nodeFrame(dip8, j);
+        float lo[3], hi[3];
+        projRange(f, tri, first, first + num, lane, lo, hi);
+        if (lane == 0) writeObb(j, f, lo, hi, parent, irank, slot, cp);
+    }
 }
 
 // float <-> int with the same order (for atomicMin / atomicMax on signed ints)
@@ -439,7 +467,7 @@ static cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, c
     finalizeKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, out.dip8);
     packKernel<<<B, 256, 0, s>>>(out.nodes, nNodes, out.dip8, irs, irs + nNodes, dVerts, dTris, out.cp, out.dip, out.tri,
                                  out.faceSlot);
-    obbKernel<<<blocksFor(nNodes * 32, 256), 256, 0, s>>>(nNodes, out.dip8, range, out.tri, parent, irs, irs + nNodes, out.cp);
+    obbKernel<<<blocksFor(nNodes, 256), 256, 0, s>>>(nNodes, out.dip8, range, out.tri, parent, irs, irs + nNodes, out.cp);
     // big nodes: chunk counts -> first chunk per node, big-node index -> accumulators
     int32_t *nChunks = nullptr, *chunkStart = nullptr, *isBig = nullptr, *bigIdx = nullptr, *sums = nullptr, *totals = nullptr;
     int* acc = nullptr;

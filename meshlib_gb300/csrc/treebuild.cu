@@ -11,8 +11,10 @@
 //  * large segments (> kSmall leaves, the top ~10 levels): one level at a time over all segments;
 //    node box = segmented min/max reduction; the median is found by an MSB-first radix select on
 //    the 128-bit key (three order-preserving coordinate words, then the id), 8 bits per pass,
-//    stopping as soon as the selected prefix is unique in every segment; then a stable partition
-//    by "key below the median" built on a global exclusive scan;
+//    starting below the leading bytes the node box already fixes and stopping as soon as the
+//    selected prefix is unique in every segment (the host reads that count every 4 passes; passes
+//    after the last needed one return at once); then a stable partition by "key below the median"
+//    built on a global exclusive scan;
 //  * small segments (2..kSmall leaves): one thread block per segment finishes the whole subtree in
 //    shared memory, level by level, ranking every element within its sub-segment by counting.
 //
@@ -229,28 +231,27 @@ __device__ __forceinline__ void writeInternal(const float mn[3], const float mx[
 }
 
 // ---------------------------------------------------------------- large-segment level
-__device__ __forceinline__ int findSeg(const Seg* segs, int nseg, int32_t p) {  // last seg with first <= p
-    int lo = 0, hi = nseg - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (segs[mid].first <= p) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
+// Every element carries its entry in the current level's segment list (segOf, -1 when its segment
+// is not split on this path), so the per-element kernels below need no search.
 
-__global__ void segBoxes(const Elem* __restrict__ el, int32_t n, const Seg* __restrict__ segs, int nseg, int* __restrict__ box) {
+__global__ void __launch_bounds__(256) segBoxes(const Elem* __restrict__ el, int32_t n, const int32_t* __restrict__ segOf,
+                                                int* __restrict__ box) {
+    __shared__ int sSeg[8];
+    __shared__ float sV[8][6];
     const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int s = -1;
     Elem e;
     if (p < n) {
-        s = findSeg(segs, nseg, p);
-        if (!(segs[s].large && p < segs[s].first + segs[s].num)) s = -1;
-        else e = el[p];
+        s = segOf[p];
+        if (s >= 0) e = el[p];
     }
     const unsigned same = __match_any_sync(0xffffffffu, s);
-    if (s < 0) return;
-    float v[6] = {e.mn[0], e.mn[1], e.mn[2], -e.mx[0], -e.mx[1], -e.mx[2]};  // all as minima
+    float v[6] = {FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX};
+    if (s >= 0) {  // all as minima
+        v[0] = e.mn[0]; v[1] = e.mn[1]; v[2] = e.mn[2];
+        v[3] = -e.mx[0]; v[4] = -e.mx[1]; v[5] = -e.mx[2];
+    }
     const int leader = __ffs(same) - 1;
     if (same == 0xffffffffu) {  // the whole warp in one segment (the common case): butterfly
         for (int j = 0; j < 6; ++j)
@@ -267,7 +268,26 @@ __global__ void segBoxes(const Elem* __restrict__ el, int32_t n, const Seg* __re
             v[j] = r;
         }
     }
-    if (lane == leader) {
+    // a block whose 256 elements all lie in one segment (most blocks of the upper levels) reduces its
+    // eight warps in shared memory and updates the segment box once instead of eight times
+    if (lane == 0) sSeg[w] = same == 0xffffffffu ? s : -1;
+    __syncthreads();
+    bool uniform = sSeg[0] >= 0;
+    for (int k = 1; k < 8; ++k) uniform = uniform && sSeg[k] == sSeg[0];
+    if (uniform) {
+        if (lane == 0)
+            for (int j = 0; j < 6; ++j) sV[w][j] = v[j];
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            const int j = threadIdx.x;
+            float r = sV[0][j];
+            for (int k = 1; k < 8; ++k) r = fminf(r, sV[k][j]);
+            if (j < 3) atomicMin(&box[6 * s + j], floatToOrderedInt(r));
+            else atomicMax(&box[6 * s + j], floatToOrderedInt(-r));
+        }
+        return;
+    }
+    if (s >= 0 && lane == leader) {
         for (int j = 0; j < 3; ++j) atomicMin(&box[6 * s + j], floatToOrderedInt(v[j]));
         for (int j = 0; j < 3; ++j) atomicMax(&box[6 * s + 3 + j], floatToOrderedInt(-v[3 + j]));
     }
@@ -287,7 +307,6 @@ __global__ void segInit(const Seg* __restrict__ segs, int nseg, int* __restrict_
     z.done = segs[s].large ? 0 : 1;
     z.dims = 0;
     st[s] = z;
-    for (int j = 0; j < 256; ++j) hist[256 * s + j] = 0;
 }
 
 __global__ void segNodes(const Seg* __restrict__ segs, int nseg, const int* __restrict__ box, SegState* __restrict__ st,
@@ -303,17 +322,24 @@ __global__ void segNodes(const Seg* __restrict__ segs, int nseg, const int* __re
     int d0, d1, d2;
     sortedDims(ext, d0, d1, d2);
     st[s].dims = d0 | (d1 << 2) | (d2 << 4);
+    // every leaf's key word c[d2] = mn + mx lies in [min mn + min mn, max mx + max mx] (rounding is
+    // monotone), so the leading bytes both ends share are the median's too: the select starts below them
+    const uint32_t lo = orderedBits(mn[d2] + mn[d2]), hi = orderedBits(mx[d2] + mx[d2]);
+    const int nb = (lo ^ hi) ? (__clz(lo ^ hi) >> 3) : 4;
+    st[s].prefix[0] = nb == 4 ? lo : (nb == 0 ? 0u : lo & ~(0xffffffffu >> (8 * nb)));
+    st[s].nbytes = nb;
     writeInternal(mn, mx, segs[s].root, segs[s].first, segs[s].num, nodes, irs, range, nNodes);
 }
 
-__global__ void radixHist(const Elem* __restrict__ el, int32_t n, const Seg* __restrict__ segs, int nseg,
-                          const SegState* __restrict__ st, int* __restrict__ hist) {
+__global__ void radixHist(const Elem* __restrict__ el, int32_t n, const int32_t* __restrict__ segOf,
+                          const SegState* __restrict__ st, int* __restrict__ hist, const int* __restrict__ prevPending) {
+    if (prevPending && *prevPending == 0) return;  // every segment finished in an earlier pass
     const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     int key = -1;
-    if (p < n) {
-        const int s = findSeg(segs, nseg, p);
+    const int s = p < n ? segOf[p] : -1;
+    if (s >= 0) {
         const SegState S = st[s];
-        if (segs[s].large && !S.done && p < segs[s].first + segs[s].num) {
+        if (!S.done) {
             uint32_t w[4];
             keyWords(el[p], (S.dims >> 4) & 3, (S.dims >> 2) & 3, S.dims & 3, w);
             if (cmpPrefix(w, S.prefix, S.nbytes) == 0) key = 256 * s + keyByte(w, S.nbytes);
@@ -325,7 +351,8 @@ __global__ void radixHist(const Elem* __restrict__ el, int32_t n, const Seg* __r
 
 // one warp per segment: pick the bucket holding rank k, extend the prefix, clear the histogram
 __global__ void radixSelect(const Seg* __restrict__ segs, int nseg, SegState* __restrict__ st, int* __restrict__ hist,
-                            int* __restrict__ pending) {
+                            int* __restrict__ pending, const int* __restrict__ prevPending) {
+    if (prevPending && *prevPending == 0) return;
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= nseg) return;
@@ -357,6 +384,7 @@ __global__ void radixSelect(const Seg* __restrict__ segs, int nseg, SegState* __
     }
     const unsigned who = __ballot_sync(0xffffffffu, bucket >= 0);
     if (who == 0) {  // cannot happen (k < bucket total by construction); stop this segment safely
+        for (int j = 0; j < 8; ++j) hist[256 * s + 8 * lane + j] = 0;
         if (lane == 0) st[s].done = 1;
         return;
     }
@@ -376,13 +404,13 @@ __global__ void radixSelect(const Seg* __restrict__ segs, int nseg, SegState* __
     }
 }
 
-__global__ void partFlags(const Elem* __restrict__ el, int32_t n, const Seg* __restrict__ segs, int nseg,
+__global__ void partFlags(const Elem* __restrict__ el, int32_t n, const int32_t* __restrict__ segOf,
                           const SegState* __restrict__ st, int32_t* __restrict__ flag) {
     const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const int s = findSeg(segs, nseg, p);
+    const int s = segOf[p];
     int f = 0;
-    if (segs[s].large && p < segs[s].first + segs[s].num) {
+    if (s >= 0) {
         const SegState S = st[s];
         uint32_t w[4];
         keyWords(el[p], (S.dims >> 4) & 3, (S.dims >> 2) & 3, S.dims & 3, w);
@@ -391,18 +419,24 @@ __global__ void partFlags(const Elem* __restrict__ el, int32_t n, const Seg* __r
     flag[p] = f;
 }
 
+// also writes the element's segment at the next level: child c of segment s is entry 2s + c of the
+// next segment list, or -1 when that child is finished elsewhere (kSmall leaves or fewer)
 __global__ void partScatter(const Elem* __restrict__ el, Elem* __restrict__ out, int32_t n, const Seg* __restrict__ segs,
-                            int nseg, const int32_t* __restrict__ flag, const int32_t* __restrict__ scan) {
+                            const int32_t* __restrict__ segOf, int32_t* __restrict__ segOfNext,
+                            const int32_t* __restrict__ flag, const int32_t* __restrict__ scan) {
     const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const int s = findSeg(segs, nseg, p);
-    int32_t dst = p;
-    if (segs[s].large && p < segs[s].first + segs[s].num) {
-        const int32_t first = segs[s].first, k = segs[s].num / 2;
+    const int s = segOf[p];
+    int32_t dst = p, next = -1;
+    if (s >= 0) {
+        const int32_t first = segs[s].first, num = segs[s].num, k = num / 2;
         const int32_t leftBefore = scan[p] - scan[first];
-        dst = flag[p] ? first + leftBefore : first + k + ((p - first) - leftBefore);
+        const bool left = flag[p] != 0;
+        dst = left ? first + leftBefore : first + k + ((p - first) - leftBefore);
+        if ((left ? k : num - k) > kSmall) next = 2 * s + (left ? 0 : 1);
     }
     out[dst] = el[p];
+    segOfNext[dst] = next;
 }
 
 // children of every large segment; small ones are queued for the shared-memory finish, single
@@ -577,7 +611,8 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
     if ((e = A.alloc((void**)&flag, sizeof(int32_t) * size_t(nt)))) return e;
     if ((e = A.alloc((void**)&pos, sizeof(int32_t) * size_t(nt)))) return e;
     if ((e = A.alloc((void**)&sums, sizeof(int32_t) * size_t(nbMax)))) return e;
-    if ((e = A.alloc((void**)&misc, sizeof(int32_t) * 8))) return e;  // [0] error, [1] total, [2] pending, [3] nsmall
+    if ((e = A.alloc((void**)&misc, sizeof(int32_t) * 32))) return e;  // [0] error, [1] total, [3] nsmall, [16..31] pending per pass
+    int32_t* pend = misc + 16;
     if ((e = cudaMemsetAsync(misc, 0, sizeof(int32_t) * 8, s))) return e;
     validFaces<<<blocks(nt, 256), 256, 0, s>>>(dTris, nt, nv, flag, misc);
     if ((e = exclusiveScan(flag, pos, nt, sums, misc + 1, s))) return e;
@@ -615,28 +650,41 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
     if ((e = A.alloc((void**)&box, sizeof(int) * 6 * size_t(maxSegs)))) return e;
     if ((e = A.alloc((void**)&hist, sizeof(int) * 256 * size_t(maxSegs)))) return e;
     int32_t* scan = pos;  // reuse: n <= nt
+    int32_t *segOf = nullptr, *segOf2 = nullptr;  // each element's entry in the current segment list, -1 if none
+    if ((e = A.alloc((void**)&segOf, sizeof(int32_t) * size_t(n)))) return e;
+    if ((e = A.alloc((void**)&segOf2, sizeof(int32_t) * size_t(n)))) return e;
     int nsmallHost = 0;
     const Seg root{0, 0, n, n > kSmall ? 1 : 0};
     if (n > kSmall) {
         if ((e = cudaMemcpyAsync(segA, &root, sizeof(Seg), cudaMemcpyHostToDevice, s))) return e;
+        if ((e = cudaMemsetAsync(segOf, 0, sizeof(int32_t) * size_t(n), s))) return e;
+        // histogram rows are cleared once here; every select pass clears the rows it read, so they
+        // are zero again at the start of each level
+        if ((e = cudaMemsetAsync(hist, 0, sizeof(int) * 256 * size_t(maxSegs), s))) return e;
         int nseg = 1;
         for (int level = 0; level < 40; ++level) {
             segInit<<<blocks(nseg, 128), 128, 0, s>>>(segA, nseg, box, st, hist);
-            segBoxes<<<blocks(n, 256), 256, 0, s>>>(el, n, segA, nseg, box);
+            segBoxes<<<blocks(n, 256), 256, 0, s>>>(el, n, segOf, box);
             segNodes<<<blocks(nseg, 128), 128, 0, s>>>(segA, nseg, box, st, nodes, irs, range, nNodes);
+            // pass p counts its unfinished segments in pend[p]; a pass after one that left none returns
+            // at once, so the host reads the count only every kGroup passes
+            constexpr int kGroup = 4;
+            if ((e = cudaMemsetAsync(pend, 0, sizeof(int32_t) * 16, s))) return e;
             for (int pass = 0; pass < 16; ++pass) {
-                if ((e = cudaMemsetAsync(misc + 2, 0, sizeof(int32_t), s))) return e;
-                radixHist<<<blocks(n, 256), 256, 0, s>>>(el, n, segA, nseg, st, hist);
-                radixSelect<<<blocks(int64_t(nseg) * 32, 256), 256, 0, s>>>(segA, nseg, st, hist, misc + 2);
+                const int* prev = pass ? pend + pass - 1 : nullptr;
+                radixHist<<<blocks(n, 256), 256, 0, s>>>(el, n, segOf, st, hist, prev);
+                radixSelect<<<blocks(int64_t(nseg) * 32, 256), 256, 0, s>>>(segA, nseg, st, hist, pend + pass, prev);
+                if ((pass + 1) % kGroup && pass != 15) continue;
                 int32_t pending = 0;
-                if ((e = cudaMemcpyAsync(&pending, misc + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, s))) return e;
+                if ((e = cudaMemcpyAsync(&pending, pend + pass, sizeof(int32_t), cudaMemcpyDeviceToHost, s))) return e;
                 if ((e = cudaStreamSynchronize(s))) return e;
                 if (pending == 0) break;
             }
-            partFlags<<<blocks(n, 256), 256, 0, s>>>(el, n, segA, nseg, st, flag);
+            partFlags<<<blocks(n, 256), 256, 0, s>>>(el, n, segOf, st, flag);
             if ((e = exclusiveScan(flag, scan, n, sums, misc + 1, s))) return e;
-            partScatter<<<blocks(n, 256), 256, 0, s>>>(el, el2, n, segA, nseg, flag, scan);
+            partScatter<<<blocks(n, 256), 256, 0, s>>>(el, el2, n, segA, segOf, segOf2, flag, scan);
             std::swap(el, el2);
+            std::swap(segOf, segOf2);
             segChildren<<<blocks(nseg, 128), 128, 0, s>>>(segA, nseg, segB, el, small, misc + 3, nodes, irs, range, nNodes);
             std::swap(segA, segB);
             nseg *= 2;
