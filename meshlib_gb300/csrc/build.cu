@@ -69,6 +69,8 @@ __global__ void parentsKernel(const RefNode* __restrict__ nodes, int64_t nNodes,
 // MRMesh/MRDipole.cpp:47-60: internal dipole = left + right (pos and dirArea are still
 // area-weighted sums here).  Each leaf thread climbs; the second child to arrive at a parent
 // computes it.  dl + dr is commutative, so the result is the reference's whatever arrives first.
+// The children's 32-byte rows are read from L2 (ld.global.cg, past this SM's L1, which may hold a
+// row from before the sibling's thread wrote it) as two 16-byte loads.
 __global__ void sumUpKernel(const RefNode* __restrict__ nodes, int64_t nNodes, const int32_t* __restrict__ parent,
                             float* dip8, int* arrive) {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -80,11 +82,12 @@ __global__ void sumUpKernel(const RefNode* __restrict__ nodes, int64_t nNodes, c
         if (atomicAdd(&arrive[p], 1) == 0) return;  // first arrival: the sibling's thread finishes p
         __threadfence();
         const RefNode nd = nodes[p];
-        const volatile float* dl = dip8 + 8 * int64_t(nd.l);
-        const volatile float* dr = dip8 + 8 * int64_t(nd.r);
-        float* d = dip8 + 8 * int64_t(p);
-        for (int k = 0; k < 7; ++k) d[k] = dl[k] + dr[k];
-        d[7] = 0;
+        const float4* dl = reinterpret_cast<const float4*>(dip8 + 8 * int64_t(nd.l));
+        const float4* dr = reinterpret_cast<const float4*>(dip8 + 8 * int64_t(nd.r));
+        const float4 l0 = __ldcg(dl), l1 = __ldcg(dl + 1), r0 = __ldcg(dr), r1 = __ldcg(dr + 1);
+        float4* d = reinterpret_cast<float4*>(dip8 + 8 * int64_t(p));
+        d[0] = make_float4(l0.x + r0.x, l0.y + r0.y, l0.z + r0.z, l0.w + r0.w);
+        d[1] = make_float4(l1.x + r1.x, l1.y + r1.y, l1.z + r1.z, 0.f);
         p = parent[p];
     }
 }
@@ -388,11 +391,12 @@ __global__ void refitUpKernel(RefNode* nodes, int64_t nNodes, const int32_t* __r
         __threadfence();
         if (atomicAdd(&arrive[p], 1) == 0) return;
         __threadfence();
-        volatile RefNode* vn = nodes;
-        const int32_t l = vn[p].l, r = vn[p].r;
-        float a[6], b[6];
-        a[0] = vn[l].minx; a[1] = vn[l].miny; a[2] = vn[l].minz; a[3] = vn[l].maxx; a[4] = vn[l].maxy; a[5] = vn[l].maxz;
-        b[0] = vn[r].minx; b[1] = vn[r].miny; b[2] = vn[r].minz; b[3] = vn[r].maxx; b[4] = vn[r].maxy; b[5] = vn[r].maxz;
+        // the links never change here; the children's boxes are read from L2 as in sumUpKernel
+        const int32_t l = nodes[p].l, r = nodes[p].r;
+        const float4* nl = reinterpret_cast<const float4*>(nodes + l);
+        const float4* nr = reinterpret_cast<const float4*>(nodes + r);
+        const float4 l0 = __ldcg(nl), l1 = __ldcg(nl + 1), r0 = __ldcg(nr), r1 = __ldcg(nr + 1);
+        float a[6] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y}, b[6] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y};
         for (int k = 0; k < 3; ++k) {
             if (b[k] < a[k]) a[k] = b[k];
             if (b[3 + k] > a[3 + k]) a[3 + k] = b[3 + k];

@@ -48,27 +48,44 @@ cudaError_t devMalloc(void** p, size_t bytes) {
 
 static constexpr int kMaxPoolDevices = 64;
 static std::mutex g_poolMu;
-static cudaMemPool_t g_pools[kMaxPoolDevices] = {};
+struct PoolSlot {
+    cudaMemPool_t pool = nullptr;
+    bool failed = false;  // creation failed once: this device allocates with cudaMalloc from then on
+};
+static PoolSlot g_pools[kMaxPoolDevices];
+
+// The pool of `device` if it exists (never creates one); null for devices without a pool.
+static cudaMemPool_t existingPool(int device) {
+    if (device < 0 || device >= kMaxPoolDevices) return nullptr;
+    std::lock_guard<std::mutex> lk(g_poolMu);
+    return g_pools[device].pool;
+}
 
 // The library's own stream-ordered pool on `device`: freed blocks stay reserved for the next
 // allocation, so a handle created per call (the reference's usage) does not map its grid-sized
-// staging buffer afresh every time.  gbfwn_release_cached_memory returns the reserve.
+// staging buffer afresh every time.  gbfwn_release_cached_memory returns the reserve.  A device
+// gets its pool on first use or never, so every block of a device comes from one allocator and
+// poolFree can tell which one from the device alone.
 cudaMemPool_t devicePool(int device) {
+    if (device < 0 || device >= kMaxPoolDevices) return nullptr;
     std::lock_guard<std::mutex> lk(g_poolMu);
-    cudaMemPool_t& pool = g_pools[unsigned(device) % kMaxPoolDevices];
-    if (!pool) {
+    PoolSlot& slot = g_pools[device];
+    if (!slot.pool && !slot.failed) {
         cudaMemPoolProps props = {};
         props.allocType = cudaMemAllocationTypePinned;
         props.location.type = cudaMemLocationTypeDevice;
         props.location.id = device;
+        cudaMemPool_t pool = nullptr;
         if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
-            pool = nullptr;
+            cudaGetLastError();
+            slot.failed = true;
             return nullptr;
         }
         uint64_t keep = ~uint64_t(0);
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        slot.pool = pool;
     }
-    return pool;
+    return slot.pool;
 }
 
 cudaError_t poolMalloc(void** p, size_t bytes, int device, cudaStream_t s) {
@@ -86,14 +103,16 @@ cudaError_t poolMalloc(void** p, size_t bytes, int device, cudaStream_t s) {
 
 void poolFree(void* p, cudaStream_t s) {
     if (!p) return;
-    int device = 0;
-    cudaGetDevice(&device);
-    bool pooled;
-    {
-        std::lock_guard<std::mutex> lk(g_poolMu);
-        pooled = g_pools[unsigned(device) % kMaxPoolDevices] != nullptr;
+    // the device the block lives on (not the caller's current device) decides the allocator
+    int device = -1;
+    cudaPointerAttributes a = {};
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess) {
+        device = a.device;
+    } else {
+        cudaGetLastError();
+        cudaGetDevice(&device);
     }
-    if (pooled)
+    if (existingPool(device))
         cudaFreeAsync(p, s);
     else
         cudaFree(p);  // poolMalloc fell back to cudaMalloc: no pool on this device
@@ -189,7 +208,7 @@ GBFWN_API void gbfwn_debug_fail_next_allocs(int count) { g_failAllocs = count; }
 
 GBFWN_API int gbfwn_release_cached_memory(int device) {
     DeviceGuard g(device);
-    cudaMemPool_t pool = devicePool(device);
+    cudaMemPool_t pool = existingPool(device);
     if (pool) {
         cudaDeviceSynchronize();
         cudaMemPoolTrimTo(pool, 0);
