@@ -775,6 +775,50 @@ def _autotune_cache_path() -> str:
                           os.path.join(os.path.expanduser("~"), ".cache", "meshlib_gb300", "autotune.json"))
 
 
+def _autotune_cache_lookup(path: str, key: str, names) -> Optional[dict]:
+    """The cached record for ``key`` if it names a variant this library still has at the same index;
+    None when the file is missing, unreadable or the entry is stale."""
+    import json
+    try:
+        with open(path) as fh:
+            rec = json.load(fh).get(key)
+        c = int(rec["config"])
+        if 0 <= c < len(names) and rec.get("name") == names[c]:
+            return rec
+    except (OSError, ValueError, TypeError, KeyError, AttributeError):
+        pass
+    return None
+
+
+def _autotune_cache_store(path: str, key: str, rec: dict) -> None:
+    """Adds ``rec`` under ``key``; the file is replaced atomically, so concurrent writers never leave a
+    torn file (the last writer wins)."""
+    import json
+    import tempfile
+    try:
+        cache = {}
+        try:
+            with open(path) as fh:
+                cache = json.load(fh)
+            if not isinstance(cache, dict):
+                cache = {}
+        except (OSError, ValueError):
+            pass
+        cache[key] = rec
+        d = os.path.dirname(path) or "."
+        os.makedirs(d, exist_ok=True)
+        fd, tmp = tempfile.mkstemp(prefix=".autotune.", dir=d)
+        try:
+            with os.fdopen(fd, "w") as fh:
+                json.dump(cache, fh, indent=1)
+            os.replace(tmp, path)
+        except BaseException:
+            os.unlink(tmp)
+            raise
+    except OSError:
+        pass
+
+
 class Batch:
     """Many meshes with their own grids in one persistent launch (gbfwn_batch_* in include/gbfwn.h).
 
@@ -812,7 +856,6 @@ class Batch:
         _check(self._L.gbfwn_batch_set_config(self._h, c))
 
     def autotune(self, use_cache: bool = True) -> dict:
-        import json
         try:
             import torch
             gpu = torch.cuda.get_device_name()
@@ -820,29 +863,18 @@ class Batch:
             gpu = "gpu"
         key = f"{gpu}|{self.key}"
         path = _autotune_cache_path()
-        cache = {}
-        if use_cache and os.path.exists(path):
-            try:
-                with open(path) as fh:
-                    cache = json.load(fh)
-            except Exception:
-                cache = {}
-        if use_cache and key in cache:
-            self.set_config(int(cache[key]["config"]))
-            return dict(cache[key], cached=True)
-        n = self._L.gbfwn_batch_num_configs()
-        times = (ctypes.c_float * n)()
+        names = self.configs()
+        if use_cache:
+            rec = _autotune_cache_lookup(path, key, names)
+            if rec is not None:
+                self.set_config(int(rec["config"]))
+                return dict(rec, cached=True)
+        times = (ctypes.c_float * len(names))()
         best = ctypes.c_int32()
         _check(self._L.gbfwn_batch_autotune(self._h, ctypes.byref(best), times))
-        rec = {"config": int(best.value), "name": self.configs()[best.value], "times_ms": [float(t) for t in times]}
+        rec = {"config": int(best.value), "name": names[best.value], "times_ms": [float(t) for t in times]}
         if use_cache:
-            try:
-                os.makedirs(os.path.dirname(path), exist_ok=True)
-                cache[key] = rec
-                with open(path, "w") as fh:
-                    json.dump(cache, fh, indent=1)
-            except OSError:
-                pass
+            _autotune_cache_store(path, key, rec)
         return dict(rec, cached=False)
 
     def run_dev(self, stream=None):
