@@ -326,6 +326,10 @@ class FastWindingNumber:
         n = int(np.prod(d.astype(np.int64)))
         if out is None:
             out = np.empty(n, np.float32)
+        elif not (isinstance(out, np.ndarray) and out.dtype == np.float32 and out.flags.c_contiguous
+                  and out.flags.writeable and out.size == n):
+            # the library writes n floats through the raw pointer: anything else would corrupt memory
+            raise ValueError(f"out must be a writeable C-contiguous float32 array of {n} elements (dims product)")
         o = (options or DistanceToMeshOptions())._c()
         c, _keep = _progress(cb)
         _check(self._L.gbfwn_from_grid_with_distances(self._h, _p(d), _p(_xf12(gridToMeshXf)), ctypes.byref(o), _p(out),

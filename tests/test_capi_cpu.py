@@ -63,3 +63,21 @@ def test_no_cpu_fallback_when_library_missing(tmp_path, monkeypatch):
     monkeypatch.setattr(M, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(ImportError):
         M.lib()
+
+
+def test_host_output_buffer_is_checked_before_the_library_writes():
+    """A caller-supplied result array must be exactly what the library writes through its pointer."""
+    import types
+
+    import numpy as np
+
+    import meshlib_gb300 as M
+    dims, xf = (4, 3, 2), np.eye(3, 4, dtype=np.float32)
+    dummy = types.SimpleNamespace()  # the check runs before any use of the handle
+    bad = [np.empty(24, np.float64), np.empty(23, np.float32), np.empty(48, np.float32)[::2],
+           np.empty((24, 2), np.float32)[:, 0]]
+    ro = np.empty(24, np.float32)
+    ro.flags.writeable = False
+    for out in bad + [ro, [0.0] * 24]:
+        with pytest.raises(ValueError):
+            M.FastWindingNumber.calcFromGridWithDistances(dummy, dims, xf, out=out)
