@@ -724,18 +724,29 @@ GBFWN_API int gbfwn_from_grid_with_distances_by_parts(gbfwn_handle h, const int3
         nullptr, layerOverlap, maxLayersPerSlab, slab, slabUser, cb, user, "gbfwn_from_grid_with_distances_by_parts");
 }
 
-// Memory estimators: mesh data (verts, tris, reference nodes + dipoles kept for export, wide query
-// records, leaf triangles, face->slot) plus the per-call staging.
+// Memory estimators (the reference's: MRViewer/MRCudaAccessor.cpp:162-194).  Callers compare them
+// with the free device memory before choosing the GPU path, so they cover the peak, which is the
+// tree build.  Kept per handle: vertices, triangles, face -> slot, the reference nodes and dipoles
+// (32 B each per node, for export and refit), the wide query records (128 B closest-point + 64 B
+// winding-number per internal node) and leaf triangles (48 B): 384 B per face.  Build work arrays,
+// all alive until the build ends: two 40-byte leaf records, flags, ranks and ranges per node,
+// segment lists and histograms, parents, arrival counters and oriented-box bookkeeping: under 212 B
+// per face.  32 MiB cover the rounding of the thirty-odd allocations.
 GBFWN_API size_t gbfwn_mesh_memory(int64_t nv, int64_t nt) {
-    const size_t n = size_t(std::max<int64_t>(nt, 0));
-    return size_t(nv) * 12 + n * 12 + (2 * n) * (32 + 32) + n * (64 + 64) + n * 48 + n * 4 + (2 * n) * 16 + 4096;
+    const size_t v = size_t(std::max<int64_t>(nv, 0)), n = size_t(std::max<int64_t>(nt, 0));
+    const size_t kept = v * 12 + n * (12 + 4) + (2 * n) * (32 + 32) + n * (128 + 64) + n * 48;
+    const size_t build = n * 212;
+    return kept + build + (size_t(32) << 20);
 }
 GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t dims[3]) {
     const size_t vox = dims ? size_t(std::max(dims[0], 0)) * size_t(std::max(dims[1], 0)) * size_t(std::max(dims[2], 0)) : 0;
     return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float);
 }
+// staging: points in (12 B) and results out (4 B); from 8,192 points also the Morton order and its
+// sort scratch (6 int32 words per point)
 GBFWN_API size_t gbfwn_from_vector_memory(int64_t nv, int64_t nt, int64_t npts) {
-    return gbfwn_mesh_memory(nv, nt) + size_t(std::max<int64_t>(npts, 0)) * 16;
+    const size_t n = size_t(std::max<int64_t>(npts, 0));
+    return gbfwn_mesh_memory(nv, nt) + n * 16 + (n >= 8192 ? n * 24 + 4096 : 0);
 }
 GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt) {
     return gbfwn_mesh_memory(nv, nt) + size_t(std::max<int64_t>(nt, 0)) * 4 + size_t((nt + 63) / 64) * 8;
