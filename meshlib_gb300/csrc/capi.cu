@@ -2,9 +2,10 @@
 //
 // Host-facing calls behave like MR::Cuda::FastWindingNumber (MRCuda/MRCudaFastWindingNumber.cpp):
 // synchronous, results in host memory, progress reported at phase boundaries and per z-slab,
-// cancellation honoured between slabs.  Unlike the reference, the output is produced in z-slabs on
-// one stream while finished slabs are copied to the host on a second stream, so the device->host
-// copy of slab k overlaps the computation of slabs k+1...
+// cancellation honoured between slabs.  Without a progress callback a grid is one launch followed
+// by one device->host copy; with one (or by parts) it is produced in z-slabs on one stream while
+// finished slabs are copied to the host on a second stream, so the copy of slab k overlaps the
+// computation of slabs k+1...
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
