@@ -143,15 +143,35 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 
 
 # DRAM bytes (read + write) of one launch of the signed-distance grid kernel at 512^3 on this
-# workload, from an ncu capture of the same command (profiles/gridKernel_sdf_512cubed_dram.md:
-# dram__bytes_read.sum 676,597,504 + dram__bytes_write.sum 523,374,848); the kernel reads the mesh
-# records about 1.3 times from HBM.
+# workload: dram__bytes_read.sum 754,624,256 + dram__bytes_write.sum 611,213,824 from one ncu
+# capture of the same kernel (a constant copied from that capture, not measured by this run; the
+# committed profile summary under profiles/ gives the command).  536,870,912 of the written bytes
+# are the output grid.
 KERNEL_DRAM_BYTES_512 = 754_624_256 + 611_213_824
 
 
-# FMA-pipe utilisation of the signed-distance grid kernel from the committed ncu capture
-# (profiles/gridKernel_sdf_256cubed_icosphere1.3M.md: sm__pipe_fma_cycles_active)
+# Counters of the signed-distance grid kernel at 256^3 on this workload from one ncu capture
+# (constants copied from that capture, not measured by this run): FMA-pipe utilisation
+# (sm__pipe_fma_cycles_active), issue-slot utilisation and active lanes per warp instruction.
 KERNEL_FMA_PIPE_ACTIVE = 0.321
+KERNEL_ISSUE_ACTIVE = 0.860
+KERNEL_LANES_PER_INSTR = 21.5
+
+
+def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
+    """Measured FP32 FMA throughput of the GPU (TFLOP/s), from the benchmark-support library that
+    the package build compiles beside the product library."""
+    import ctypes
+
+    from meshlib_gb300 import build as B
+    L = ctypes.CDLL(B.BENCH_LIB)
+    L.bench_fp32_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.bench_fp32_peak.restype = ctypes.c_int
+    t = ctypes.c_double()
+    rc = L.bench_fp32_peak(device, reps, ctypes.byref(t))
+    if rc != 0:
+        raise RuntimeError(f"bench_fp32_peak failed with CUDA error {rc}")
+    return float(t.value)
 
 
 def flop_per_voxel(c):
@@ -647,21 +667,28 @@ def main():
         bpv = bytes_per_voxel(counts)
         achieved = bpv * nvox / (ms_step * 1e-3) / 1e9
         traffic = KERNEL_DRAM_BYTES_512 if grid == GRID else None
+        dram_gbs = (traffic / (ms_step * 1e-3) / 1e9) if traffic else None
         line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                            "traffic": traffic, "peak_source": peak_kind, "bytes_per_voxel": bpv, "work_per_voxel": counts,
-                            "dram_gbs_actual": (traffic / (ms_step * 1e-3) / 1e9) if traffic else None,
+                            "traffic": traffic, "traffic_source": "ncu capture of this kernel at this size (constant, "
+                                                                  "not measured by this run)",
+                            "peak_source": peak_kind, "bytes_per_voxel": bpv, "work_per_voxel": counts,
+                            "dram_gbs_actual": dram_gbs, "dram_frac_actual": (dram_gbs / peak) if dram_gbs else None,
+                            "issue_active_ncu": KERNEL_ISSUE_ACTIVE, "lanes_per_instruction_ncu": KERNEL_LANES_PER_INSTR,
+                            "lane_efficiency_ncu": KERNEL_LANES_PER_INSTR / 32,
                             "note": "achieved counts the reference traversal's per-voxel node/dipole/triangle reads "
-                                    "(bytes_per_voxel); the warp-packet traversal reads each record once per 32 voxels "
-                                    "from L1/L2, so actual DRAM traffic (traffic) is ~1.4 GB per launch and the kernel is "
-                                    "issue/latency-bound, not HBM-bound"}
+                                    "(bytes_per_voxel), so frac > 1 only says the reference walk would need that multiple "
+                                    "of HBM peak; the warp-packet walk reads each record once per 32 voxels from L1/L2. "
+                                    "The bound that holds is instruction issue: dram_frac_actual (measured DRAM bytes "
+                                    "per launch / step time / peak) is well under 1 %, issue_active_ncu is the busy "
+                                    "fraction of the issue slots (ncu, 256^3 capture)"}
         try:
-            fp32_peak = M.fp32_peak_tflops(local)
+            fp32_peak = fp32_peak_tflops(local)
         except Exception as ex:  # measurement support only; the line stays valid without it
             fp32_peak = None
             print(f"fp32 peak: {ex}", file=sys.stderr)
         fpv = flop_per_voxel(counts)
         ref_tf = fpv * nvox / (ms_step * 1e-3) / 1e12
-        line["fp32"] = {"peak_tflops": fp32_peak, "peak_source": "own FMA microbenchmark (gbfwn_debug_fp32_peak)",
+        line["fp32"] = {"peak_tflops": fp32_peak, "peak_source": "own FMA microbenchmark (libgbfwn_bench.so, bench_fp32_peak)",
                         "flop_per_voxel_reference_traversal": fpv, "reference_equiv_tflops": ref_tf,
                         "reference_equiv_frac": (ref_tf / fp32_peak) if fp32_peak else None,
                         "fma_pipe_active_ncu": KERNEL_FMA_PIPE_ACTIVE,

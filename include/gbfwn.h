@@ -21,6 +21,11 @@
  *  - A handle owns one work-queue counter and staging buffers: calls on the same handle must not
  *    overlap on the GPU (keep them on one stream, or serialise them); different handles are
  *    independent.
+ *  - Traversal status: the kernels record a traversal-stack overflow (GBFWN_TRAVERSAL_OVERFLOW) in a
+ *    device status word.  Host-memory calls read it back before returning; `_dev` calls only enqueue
+ *    work and do not.  An overflow cannot happen for the trees this library builds: the median split
+ *    of at most 2^30 faces gives a depth of at most 30, and a depth-first walk that pushes at most
+ *    two children per step then holds at most 31 entries, below the fixed depth of 32.
  *  - Progress callbacks receive a fraction in [0, 1] and return nonzero to continue, zero to
  *    cancel (MRMesh/MRProgressCallback.h); a cancelled call returns GBFWN_CANCELLED.
  *  - Errors: a nonzero status; `gbfwn_last_error()` gives the message of the last failure on the
@@ -94,7 +99,9 @@ GBFWN_API int gbfwn_create(const float* verts, int64_t nv, const int32_t* tris, 
 GBFWN_API int gbfwn_create_dev(const float* d_verts, int64_t nv, const int32_t* d_tris, int64_t nt, int device,
                                gbfwn_handle* out);
 
-/* Frees the device data of the handle. */
+/* Frees the device data of the handle.  A handle that is an item of a live batch (gbfwn_batch_create)
+ * is not freed: the call returns GBFWN_INVALID and the handle stays valid until the batch is
+ * destroyed. */
 GBFWN_API int gbfwn_destroy(gbfwn_handle h);
 
 /* Moved vertices, same triangles: MR::AABBTree::refit (MRMesh/MRAABBTree.cpp:62-94) as
@@ -168,12 +175,14 @@ GBFWN_API int gbfwn_from_grid_with_distances_slab_dev(gbfwn_handle h, const int3
  * that cannot take cudaFree's implicit device synchronisation.  Create the handle beforehand (that
  * allocates); this call then allocates nothing: the output is the caller's device buffer and the
  * kernel's scratch (work-queue counter + status word) is a fixed 256-byte device array that every
- * GPU loading the library keeps until exit.  The first call on a device resolves that array's
- * device address (cudaGetSymbolAddress), so make that first call before any stream capture.  Every
+ * GPU loading the library keeps until exit.  Each call looks up that array's device address
+ * (cudaGetSymbolAddress, a host-side query); the first call on a device may also load the library's
+ * device code there, so make that first call before any stream capture.  Every
  * call shares the array and clears it first, so calls that overlap on the GPU (concurrent streams,
  * threads or handles) race: serialise them.  Limit: at most 2^32-1 warp tiles of 4x4x2 voxels per
  * call (the counter is 32 bits); larger grids are rejected with GBFWN_INVALID.  Enqueues on
- * `stream` (NULL = the handle's stream) and returns without waiting. */
+ * `stream` (NULL = the handle's stream) and returns without waiting; like the other `_dev` calls it
+ * does not read the status word back (see the note on traversal status above). */
 GBFWN_API int gbfwn_from_grid_with_distances_noalloc(gbfwn_handle h, const int32_t dims[3], const float xf[12],
                                                      const gbfwn_dist_opts* opts, float* d_out, void* stream);
 
@@ -233,10 +242,6 @@ GBFWN_API size_t gbfwn_mesh_memory(int64_t nv, int64_t nt);
 GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t dims[3]);
 GBFWN_API size_t gbfwn_from_vector_memory(int64_t nv, int64_t nt, int64_t npts);
 GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt);
-
-/* No counterpart in the reference: measured FP32 FMA throughput of `device` in TFLOP/s (best of
- * `reps` launches), the denominator of the traversal kernels' FP32-op fraction in the benchmark. */
-GBFWN_API int gbfwn_debug_fp32_peak(int device, int reps, double* tflops);
 
 /* ---------------------------------------------------------------------------------------------
  * Learned band culling (no counterpart in the reference).  A small per-mesh network predicts the
@@ -311,6 +316,10 @@ GBFWN_API int gbfwn_from_grid_with_distances_banded_dev(gbfwn_handle h, gbfwn_su
  * size) can be timed on the batch and the fastest kept; a batch can be replayed from a CUDA graph. */
 typedef struct gbfwn_batch_s* gbfwn_batch;
 
+/* A batch keeps device pointers into every item's mesh and output: each item's handle and d_out must
+ * stay alive and unmoved until gbfwn_batch_destroy (also for graph replays and autotuning).  The
+ * library enforces the handle part -- gbfwn_destroy refuses a handle that a live batch references --
+ * while the output buffers are the caller's to keep. */
 typedef struct gbfwn_batch_item {
     gbfwn_handle mesh;      /* all meshes of a batch on one device; the first mesh's precise setting applies */
     int32_t dims[3];

@@ -144,7 +144,6 @@ _SIGS = [
     ("gbfwn_find_projections", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, PROGRESS, _vp]),
     ("gbfwn_find_projections_dev", ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _f, _f, _vp, _vp]),
     ("gbfwn_projections_heap_bytes", ctypes.c_size_t, [_i64]),
-    ("gbfwn_debug_fp32_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gbfwn_make_signed_by_winding_number_dev", ctypes.c_int, [_vp, _vp, _vp, _f, _f, _vp, _vp]),
     ("gbfwn_mc_default_params", None, [ctypes.POINTER(_McParams)]),
     ("gbfwn_marching_cubes", ctypes.c_int,
@@ -247,8 +246,9 @@ class FastWindingNumber:
         return self
 
     def close(self):
+        """Frees the device data; raises (and keeps the handle) while a live Batch uses the mesh."""
         if getattr(self, "_h", None) and self._h.value:
-            self._L.gbfwn_destroy(self._h)
+            _check(self._L.gbfwn_destroy(self._h))
             self._h = ctypes.c_void_p()
 
     def __del__(self):
@@ -695,12 +695,6 @@ def calcOriginAndDimensions(box_min, box_max, voxelSize: float):
     dims = (((hi + exp).astype(np.float32) - origin).astype(np.float32) / vs).astype(np.float32).astype(np.int32) + 1
     return origin, dims
 
-def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
-    """Measured FP32 FMA throughput of the GPU (TFLOP/s)."""
-    t = ctypes.c_double()
-    _check(lib().gbfwn_debug_fp32_peak(device, reps, ctypes.byref(t)))
-    return float(t.value)
-
 
 def memory_estimates(nv: int, nt: int, dims=None, npts: int = 0) -> dict:
     L = lib()
@@ -847,6 +841,7 @@ class Batch:
             tris += fwn.num_faces()
             vox += int(dims[0]) * int(dims[1]) * int(dims[2])
         self._items = arr
+        self._meshes = [it[0] for it in items]  # the batch points into their trees: keep them alive
         self._h = ctypes.c_void_p()
         _check(self._L.gbfwn_batch_create(arr, len(items), ctypes.byref(self._h)))
         self.key = f"n{len(items)}_t{max(tris, 1).bit_length()}_v{max(vox, 1).bit_length()}"

@@ -19,7 +19,10 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibilit
 # build.cu must round every float operation separately (bit-identical boxes and dipoles)
 PER_FILE = {"build.cu": ["-fmad=false"], "treebuild.cu": ["-fmad=false"]}
 SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "mlp_gemm.cu", "mlp_net.cu", "surrogate.cu", "batch.cu", "sort.cu",
-           "projector.cu", "peak.cu", "mc.cu"]
+           "projector.cu", "mc.cu"]
+# measurement support for bench.py (the FP32 FMA peak), kept out of the product library
+BENCH_SOURCES = ["bench/fp32_peak.cu"]
+BENCH_LIB = os.path.join(HERE, "libgbfwn_bench.so")
 
 
 def nvcc() -> str:
@@ -40,11 +43,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "gbfwn.h"))
-    objs, jobs = [], []
-    for src in SOURCES:
+    objs, bench_objs, jobs = [], [], []
+    for src in SOURCES + BENCH_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
-        objs.append(o)
+        o = os.path.join(BUILD, src.replace("/", "_") + ".o")
+        (bench_objs if src in BENCH_SOURCES else objs).append(o)
         if force or _needs(o, [s] + headers + [__file__]):
             cmd = [nvcc()] + ARCH + COMMON + PER_FILE.get(src, []) + ["-c", s, "-o", o]
             jobs.append(cmd)
@@ -61,6 +64,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if jobs or not os.path.exists(LIB):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-Xlinker", "--no-undefined"]
         run(cmd)
+    if jobs or not os.path.exists(BENCH_LIB):
+        run([nvcc()] + ARCH + ["-shared", "-o", BENCH_LIB] + bench_objs + ["-Xlinker", "--no-undefined"])
     return LIB
 
 

@@ -22,7 +22,11 @@ struct gbfwn_batch_s {
     cudaStream_t captureStream = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graphConfig = -1;
+    // every distinct mesh of the batch, each holding one reference: gbfwn_destroy refuses a mesh
+    // that a live batch still points into
+    std::vector<gbfwn_mesh_s*> meshes;
     ~gbfwn_batch_s() {
+        for (auto* m : meshes) m->batchRefs.fetch_sub(1);
         DeviceGuard g(device);
         if (graph) cudaGraphExecDestroy(graph);
         if (captureStream) cudaStreamDestroy(captureStream);
@@ -54,6 +58,13 @@ GBFWN_API int gbfwn_batch_create(const gbfwn_batch_item* items, int32_t n, gbfwn
     b->device = device;
     b->precise = items[0].mesh->precise;
     b->nItems = n;
+    for (int i = 0; i < n; ++i) {
+        gbfwn_mesh_s* m = items[i].mesh;
+        if (std::find(b->meshes.begin(), b->meshes.end(), m) == b->meshes.end()) {
+            m->batchRefs.fetch_add(1);
+            b->meshes.push_back(m);
+        }
+    }
     DeviceGuard g(device);
     cudaError_t e = cudaSuccess;
     for (int c = 0; c < kBatchConfigs && !e; ++c) {

@@ -1,14 +1,11 @@
-// FP32 CUDA-core throughput microbenchmark: the denominator of the traversal kernels' FP32-op
-// fraction.  Every thread runs 8 independent FMA chains (no dependency between them, so the FMA
-// pipes, not latency, set the pace) on a persistent grid of 8 blocks per SM; the result is written
-// only under a condition the data never meets, so the work cannot be removed.
+// FP32 CUDA-core throughput microbenchmark for the benchmark script (built into its own library,
+// libgbfwn_bench.so, not into the product library): the denominator of the traversal kernels'
+// FP32-op fraction.  Every thread runs 8 independent FMA chains (no dependency between them, so the
+// FMA pipes, not latency, set the pace) on a persistent grid of 8 blocks per SM; the result is
+// written only under a condition the data never meets, so the work cannot be removed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-
-#include "../../include/gbfwn.h"
-#include "common.cuh"
-#include "handle.cuh"
 
 namespace {
 
@@ -34,17 +31,17 @@ __global__ void __launch_bounds__(256) fmaKernel(int iters, float seed, float* s
 
 }  // namespace
 
-extern "C" {
-
 // Measured FP32 FMA throughput of `device` in TFLOP/s (2 FLOP per FMA), best of `reps` launches of
-// about 10 ms each.  No counterpart in the reference: measurement support for the benchmark.
-GBFWN_API int gbfwn_debug_fp32_peak(int device, int reps, double* tflops) {
-    if (!tflops || reps <= 0) return gbfwn::fail(GBFWN_INVALID, "gbfwn_debug_fp32_peak: bad arguments");
-    gbfwn::DeviceGuard g(device);
+// about 10 ms each.  Returns a cudaError_t value (0 = success).
+extern "C" __attribute__((visibility("default"))) int bench_fp32_peak(int device, int reps, double* tflops) {
+    if (!tflops || reps <= 0) return int(cudaErrorInvalidValue);
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaError_t e = cudaSetDevice(device);
     int sms = 0;
-    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (!e) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     float* sink = nullptr;
-    if (!e) e = gbfwn::devMalloc((void**)&sink, 256 * sizeof(float));
+    if (!e) e = cudaMalloc((void**)&sink, 256 * sizeof(float));
     cudaEvent_t a = nullptr, b = nullptr;
     if (!e) e = cudaEventCreate(&a);
     if (!e) e = cudaEventCreate(&b);
@@ -65,9 +62,7 @@ GBFWN_API int gbfwn_debug_fp32_peak(int device, int reps, double* tflops) {
     if (a) cudaEventDestroy(a);
     if (b) cudaEventDestroy(b);
     if (sink) cudaFree(sink);
-    if (e) return gbfwn::cudaFail(e, "gbfwn_debug_fp32_peak");
-    *tflops = best;
-    return GBFWN_OK;
+    if (prev >= 0) cudaSetDevice(prev);
+    if (!e) *tflops = best;
+    return int(e);
 }
-
-}  // extern "C"

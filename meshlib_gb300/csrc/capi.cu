@@ -280,6 +280,8 @@ GBFWN_API int gbfwn_create_dev(const float* d_verts, int64_t nv, const int32_t* 
 
 GBFWN_API int gbfwn_destroy(gbfwn_handle h) {
     if (!h) return GBFWN_OK;
+    if (h->batchRefs.load() > 0)
+        return fail(GBFWN_INVALID, "gbfwn_destroy: the mesh is part of a live batch; destroy the batch first");
     {
         DeviceGuard g(h->device);
         // everything goes back to the device's pool; the device is idle first (as cudaFree would
@@ -771,22 +773,14 @@ namespace {
 // 256 bytes per device; words [0] ticket counter, [1] status bits, the rest unused.
 static __device__ __align__(256) unsigned g_noallocScratch[64];
 
-constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noallocMu;
-unsigned* g_noallocAddr[kNoallocMaxDevices] = {};
-
-// Device address of g_noallocScratch on `device` (which must be current).  Resolved once per
-// device: in host code the array's name is only a host-side stand-in, not a device address.
-int noallocScratch(int device, unsigned** out) {
-    if (device < 0 || device >= kNoallocMaxDevices) return fail(GBFWN_INVALID, "gbfwn_from_grid_with_distances_noalloc: device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_noallocMu);
-    if (!g_noallocAddr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
-        if (e != cudaSuccess) return cudaFail(e, "gbfwn_from_grid_with_distances_noalloc: cudaGetSymbolAddress");
-        g_noallocAddr[device] = static_cast<unsigned*>(p);
-    }
-    *out = g_noallocAddr[device];
+// Device address of g_noallocScratch on the current device.  In host code the array's name is only
+// a host-side stand-in, not a device address.  Looked up on every call (a host-side query that
+// enqueues nothing), so a context created afresh after a device reset is seen.
+int noallocScratch(unsigned** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+    if (e != cudaSuccess) return cudaFail(e, "gbfwn_from_grid_with_distances_noalloc: cudaGetSymbolAddress");
+    *out = static_cast<unsigned*>(p);
     return GBFWN_OK;
 }
 
@@ -803,7 +797,7 @@ extern "C" GBFWN_API int gbfwn_from_grid_with_distances_noalloc(gbfwn_handle h, 
                     "counter covers at most 2^32-1 tiles of 4x4x2 voxels)");
     DeviceGuard g(h->device);
     unsigned* scratch = nullptr;
-    if (int st = noallocScratch(h->device, &scratch)) return st;
+    if (int st = noallocScratch(&scratch)) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     // the array keeps the previous call's contents: the ticket counter and the status word must start at zero
     cudaError_t e = cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned), s);

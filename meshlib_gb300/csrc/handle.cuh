@@ -2,6 +2,7 @@
 // shared by the C ABI translation units.
 #pragma once
 
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -80,6 +81,7 @@ struct gbfwn_mesh_s {
     size_t sortCap = 0;
     std::vector<cudaEvent_t> events;
     std::mutex mu;  // calls on one handle are serialised (the reference is not re-entrant per object)
+    std::atomic<int> batchRefs{0};  // live batches whose work items point into this handle's tree
 
     // grows a staging buffer; buffers come from the device's pool, so one freed by an earlier handle
     // is reused without mapping new memory

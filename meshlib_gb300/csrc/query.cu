@@ -720,8 +720,7 @@ __global__ void fillNan(float* p, int64_t n) {
 }
 
 int gridBlocks(const void* kernel) {
-    static int sms = 0;
-    if (!sms) sms = numSMs();
+    const int sms = numSMs();  // of the current device (an attribute query, cheap)
     int perSm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kThreads, 0);
     if (perSm < 1) perSm = 1;
@@ -944,8 +943,7 @@ cudaError_t launchBatchT(const BatchItem* items, int nItems, uint32_t totalTiles
     cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned), s);
     if (e || totalTiles == 0) return e;
     auto* k = batchKernel<PRECISE, TX, TY, TZ, THREADS>;
-    static int sms = 0;
-    if (!sms) sms = numSMs();
+    const int sms = numSMs();
     int perSm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, THREADS, 0);
     int blocks = sms * (perSm < 1 ? 1 : perSm);

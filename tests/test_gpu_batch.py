@@ -51,3 +51,28 @@ def test_batch_matches_single_calls(fwn_lib, tmp_path, monkeypatch):
     for r, o in zip(refs, outs):
         fin = ~torch.isnan(r)
         assert torch.equal(r[fin], o[fin])
+
+
+def test_mesh_of_live_batch_cannot_be_destroyed(fwn_lib):
+    """A batch points into its meshes' trees: destroying one of them while the batch lives is refused
+    (the handle stays usable), and succeeds once the batch is gone."""
+    import torch
+
+    import meshlib_gb300 as M
+    from meshlib_gb300 import meshgen as mg
+    v, f = mg.noisy_icosphere(seed=5, level=3)
+    g = M.FastWindingNumber(v, f)
+    dims, xf = mg.grid_for(v, 12)
+    out = torch.empty(int(np.prod(dims)), device="cuda")
+    out2 = torch.empty_like(out)
+    b = M.Batch([(g, dims, xf, None, out.data_ptr()), (g, dims, xf, None, out2.data_ptr())])
+    with pytest.raises(M.FwnError) as ei:
+        g.close()
+    assert ei.value.status == M.INVALID and "batch" in str(ei.value)
+    b.run_dev()
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), g.calcFromGridWithDistances(dims, xf))
+    assert torch.equal(out, out2)
+    b.close()
+    g.close()
+    assert not g.handle.value

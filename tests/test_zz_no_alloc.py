@@ -40,10 +40,17 @@ def test_no_alloc_matches_device_entry_twice(fwn_lib):
         d = np.asarray(dims, np.int32)
         x12 = np.ascontiguousarray(xf, np.float32)
         copts = (opts or M.DistanceToMeshOptions())._c()
-        for o in outs:  # two calls in a row through the C ABI
-            st = L.gbfwn_from_grid_with_distances_noalloc(g.handle, d.ctypes.data, x12.ctypes.data, ctypes.byref(copts),
-                                                         ctypes.c_void_p(o.data_ptr()), ctypes.c_void_p(s.cuda_stream))
-            assert st == M.OK, L.gbfwn_last_error()
+        # every device allocation the library makes on this thread fails while the hook is armed, so
+        # an allocation slipped into this path would turn the status into GBFWN_OUT_OF_MEMORY
+        L.gbfwn_debug_fail_next_allocs(1 << 30)
+        try:
+            for o in outs:  # two calls in a row through the C ABI
+                st = L.gbfwn_from_grid_with_distances_noalloc(g.handle, d.ctypes.data, x12.ctypes.data,
+                                                             ctypes.byref(copts), ctypes.c_void_p(o.data_ptr()),
+                                                             ctypes.c_void_p(s.cuda_stream))
+                assert st == M.OK, L.gbfwn_last_error()
+        finally:
+            L.gbfwn_debug_fail_next_allocs(0)
         s.synchronize()
         r = ref.cpu().numpy()
         tol = DIST_TOL * mg.diag(v)
