@@ -2,8 +2,8 @@
 // MR::IFastWindingNumber / MR::IFastWindingNumberByParts (MRMesh/MRFastWindingNumber.h:11-107).
 //
 // It depends on nothing but the C++ standard library, so it compiles inside or outside MeshLib;
-// INTEGRATION.md shows the thin MeshLib-side class that derives from MR::IFastWindingNumber and
-// forwards to this one.  Method names, argument meaning and error behaviour follow the reference:
+// the MeshLib-side class MR::GbFastWindingNumber (include/MRGbFastWindingNumber.h) derives from
+// MR::IFastWindingNumberByParts and forwards to this one.  Method names, argument meaning and error behaviour follow the reference:
 // results are written to caller-owned std::vector / bitset words that the callee resizes, and
 // every call returns an Expected-like value whose error is the library's message.
 #pragma once
