@@ -58,6 +58,8 @@ def lib():
         L.orc_from_grid.argtypes = [vp, vp, vp, fp, ip, ip, vp]
         L.orc_from_grid_with_distances.argtypes = [vp, vp, vp, ctypes.POINTER(Options), ip, ip, vp, vp]
         L.orc_vector_with_distances.argtypes = [vp, vp, ctypes.c_int64, ctypes.POINTER(Options), ip, ip, vp]
+        L.orc_grid_voxels.argtypes = [vp, vp, vp, vp, ctypes.c_int64, ctypes.POINTER(Options), ip, ip, ip, vp, vp]
+        L.orc_self_intersections_at.argtypes = [vp, vp, ctypes.c_int64, fp, ip, ip, vp, vp]
         L.orc_dist_sq.argtypes = [vp, vp, ctypes.c_int64, fp, fp, ip, vp]
         L.orc_traversal_counts.argtypes = [vp, vp, ctypes.c_int64, ctypes.POINTER(Options), vp]
         L.orc_exact_wn.argtypes = [vp, vp, ctypes.c_int64, ip, vp]
@@ -155,6 +157,28 @@ class Oracle:
         self.L.orc_from_grid_with_distances(self.h, _ptr(d), _ptr(xf), ctypes.byref(o), prec, threads or default_threads(),
                                             _ptr(out), _ptr(fwn) if fwn is not None else None)
         return (out, fwn) if want_fwn else out
+
+    def grid_voxels(self, dims, xf, ids, opts: Options | None = None, distances=True, prec=0, threads=None):
+        """calcFromGridWithDistances (distances=True) or calcFromGrid (False; beta from opts) at the
+        voxels with linear ids `ids` (x fastest) of the dims grid; returns (values, winding numbers)."""
+        d = np.asarray(dims, np.int32)
+        xf = np.ascontiguousarray(xf, np.float32)
+        ids = np.ascontiguousarray(ids, np.int64)
+        out = np.empty(len(ids), np.float64)
+        fwn = np.empty(len(ids), np.float64)
+        o = opts or make_options()
+        self.L.orc_grid_voxels(self.h, _ptr(d), _ptr(xf), _ptr(ids), len(ids), ctypes.byref(o), 1 if distances else 0, prec,
+                               threads or default_threads(), _ptr(out), _ptr(fwn))
+        return out, fwn
+
+    def self_intersections_at(self, faces, beta=2.0, prec=0, threads=None):
+        """calcSelfIntersections bits and centroid winding numbers at the given faces only."""
+        faces = np.ascontiguousarray(faces, np.int32)
+        bits = np.empty(len(faces), np.uint8)
+        wn = np.empty(len(faces), np.float64)
+        self.L.orc_self_intersections_at(self.h, _ptr(faces), len(faces), beta, prec, threads or default_threads(), _ptr(bits),
+                                         _ptr(wn))
+        return bits.astype(bool), wn
 
     def vector_with_distances(self, pts, opts: Options | None = None, prec=0, threads=None):
         pts = np.ascontiguousarray(pts, np.float32)

@@ -757,6 +757,56 @@ void orc_from_grid_with_distances(void* h, const int* dims, const float* xf, con
     });
 }
 
+// calcFromGridWithDistances / calcFromGrid at n chosen voxels of a dims grid (linear ids, x fastest):
+// the same voxel centres and per-voxel computation as the whole-grid calls above, for sampling a
+// grid too large to evaluate whole on the CPU.  fwn may be null; distances = 0 gives calcFromGrid.
+void orc_grid_voxels(void* h, const int* dims, const float* xf, const int64_t* ids, int64_t n, const Options* op, int distances,
+                     int prec, int threads, double* out, double* fwn) {
+    auto* o = static_cast<Oracle*>(h);
+    const int64_t sxy = int64_t(dims[0]) * dims[1];
+    parallelFor(size_t(n), threads, [&](size_t k) {
+        const int64_t i = ids[k];
+        const int z = int(i / sxy), s = int(i % sxy), y = s / dims[0], x = s % dims[0];
+        double* fo = fwn ? fwn + k : nullptr;
+        if (distances) {
+            if (prec == 0)
+                out[k] = withDistances<float>(o, o->dipF, xfPoint<float>(xf, x, y, z), *op, fo, nullptr);
+            else
+                out[k] = withDistances<double>(o, o->dipD, xfPoint<double>(xf, x, y, z), *op, fo, nullptr);
+        } else {
+            const float beta = op->windingNumberBeta;
+            if (prec == 0)
+                out[k] = calcFWN<float>(o->mesh, o->nodes, o->dipF, xfPoint<float>(xf, x, y, z), beta, -1, nullptr);
+            else
+                out[k] = calcFWN<double>(o->mesh, o->nodes, o->dipD, xfPoint<double>(xf, x, y, z), double(beta), -1, nullptr,
+                                         &o->dipF, xfPoint<float>(xf, x, y, z));
+            if (fo) *fo = out[k];
+        }
+    });
+}
+
+// calcSelfIntersections at n chosen faces: bit and centroid winding number (skipping the face itself)
+// of each, as orc_self_intersections computes them for every face.
+void orc_self_intersections_at(void* h, const int32_t* faces, int64_t n, float beta, int prec, int threads, uint8_t* bits,
+                               double* wn) {
+    auto* o = static_cast<Oracle*>(h);
+    parallelFor(size_t(n), threads, [&](size_t k) {
+        const int f = faces[k];
+        if (!o->mesh.valid(f)) {
+            wn[k] = std::numeric_limits<double>::quiet_NaN();
+            bits[k] = 0;
+            return;
+        }
+        V3<float> a, b, c;
+        o->mesh.tri(f, a, b, c);
+        const V3<float> q = (1 / 3.0f) * (a + b + c);
+        const double w = prec == 0 ? double(calcFWN<float>(o->mesh, o->nodes, o->dipF, q, beta, f, nullptr))
+                                   : calcFWN<double>(o->mesh, o->nodes, o->dipD, cvt<double>(q), double(beta), f, nullptr, &o->dipF, q);
+        wn[k] = w;
+        bits[k] = (w < 0 || w > 1) ? 1 : 0;
+    });
+}
+
 // the same at arbitrary points (the CPU-only FastWindingNumber::calcWithDistances, MRFastWindingNumber.h:62)
 void orc_vector_with_distances(void* h, const float* pts, int64_t n, const Options* op, int prec, int threads, double* out) {
     auto* o = static_cast<Oracle*>(h);
