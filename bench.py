@@ -540,6 +540,8 @@ def main():
                   "surrogate_cull_ms": st_sur.get("cullMs"), "surrogate_exact_pass_ms": st_sur.get("exactMs"),
                   "exact_cull_ms_cull": st_exact.get("cullMs"), "exact_cull_ms_exact_pass": st_exact.get("exactMs"),
                   "surrogate_train_s": train_s, "surrogate_stats": sur.stats,
+                  "surrogate_with_training_ms": 1e3 * train_s + sur_ms,
+                  "break_even_grids_vs_plain_banded": (1e3 * train_s / (plain_b_ms - sur_ms)) if plain_b_ms > sur_ms else None,
                   "surrogate_config": "2M samples (50% uniform in box, 50% near surface), 1M validation, 3000 steps x 16384"}
         del sur
 

@@ -248,7 +248,10 @@ GBFWN_API size_t gbfwn_self_intersections_memory(int64_t nv, int64_t nt);
  * signed distance; bricks of 8x8x8 voxels whose predicted |d|, less a validated error margin and
  * less the brick's half diagonal, is still >= the band are known to be NaN and are skipped; every
  * other voxel goes through the exact traversal, so the result is the reference's banded result
- * (maxDistSq = band^2, nullOutsideMinMax) wherever the margin holds.  Network: Fourier features
+ * (maxDistSq = band^2, nullOutsideMinMax) wherever the margin holds.  The margin bounds how far the
+ * prediction overstates |d|, measured on held-out samples with |d| below a limit that covers every
+ * brick centre able to hold an in-band voxel (the only error that can make a cull wrong); a banded
+ * call whose band plus brick half diagonal exceeds that limit uses the two-sided margin instead.  Network: Fourier features
  * of the point (32 frequencies x 3 axes x sin/cos = 192) -> 4 x 128 SiLU -> 1; BF16 weights and
  * activations on the tcgen05 tensor cores, FP32 accumulation; trained on the GPU on samples whose
  * targets come from the exact traversal (half uniform in the grid box, half near the surface). */
@@ -268,10 +271,12 @@ typedef struct gbfwn_surrogate_opts {
 typedef struct gbfwn_surrogate_stats {
     float trainLoss;           /* last mean squared error (targets clamped to +-6 band) */
     float validationMaxError;  /* max |prediction - clamped target| on the held-out samples */
-    float margin;              /* margin used for culling: 1.25 x validationMaxError + 0.001 band */
+    float margin;              /* culling margin: 1.25 x validationOverestimate + 0.001 band */
     float sampleSeconds;       /* sample generation + exact targets */
     float trainSeconds;        /* optimizer steps */
     int32_t steps;
+    float validationOverestimate; /* max (|prediction| - |d|) over held-out samples with |d| < limit */
+    float limit;               /* band + twice the half diagonal of the training grid's 8x8x8 bricks */
 } gbfwn_surrogate_stats;
 
 typedef struct gbfwn_banded_stats {
@@ -286,9 +291,10 @@ GBFWN_API int gbfwn_surrogate_train(gbfwn_handle h, const int32_t dims[3], const
                                     const gbfwn_surrogate_opts* opts, gbfwn_surrogate* out, gbfwn_surrogate_stats* stats);
 GBFWN_API int gbfwn_surrogate_destroy(gbfwn_surrogate s);
 
-/* Parameters (74,369 floats: W1[128x192] b1 W2[128x128] b2 W3 b3 W4 b4 w5[128] b5) and 40 floats of
- * metadata (input centre xyz, input scale, 32 frequencies, target clamp, margin, band, reserved), so
- * that a trained network can be stored and re-created without retraining. */
+/* Parameters (74,369 floats: W1[128x192] b1 W2[128x128] b2 W3 b3 W4 b4 w5[128] b5) and 48 floats of
+ * metadata (input centre xyz, input scale, 32 frequencies, target clamp, culling margin, band, limit,
+ * two-sided margin, 7 reserved), so that a trained network can be stored and re-created without
+ * retraining. */
 GBFWN_API int gbfwn_surrogate_get(gbfwn_surrogate s, float* params, float* meta);
 GBFWN_API int gbfwn_surrogate_create(int device, const float* params, const float* meta, gbfwn_surrogate* out);
 

@@ -59,7 +59,8 @@ class _SurrogateOpts(ctypes.Structure):
 
 class _SurrogateStats(ctypes.Structure):
     _fields_ = [("trainLoss", ctypes.c_float), ("validationMaxError", ctypes.c_float), ("margin", ctypes.c_float),
-                ("sampleSeconds", ctypes.c_float), ("trainSeconds", ctypes.c_float), ("steps", ctypes.c_int32)]
+                ("sampleSeconds", ctypes.c_float), ("trainSeconds", ctypes.c_float), ("steps", ctypes.c_int32),
+                ("validationOverestimate", ctypes.c_float), ("limit", ctypes.c_float)]
 
 
 class _BandedStats(ctypes.Structure):
@@ -78,7 +79,7 @@ class _BatchItem(ctypes.Structure):
 
 
 SURROGATE_PARAMS = 74369
-SURROGATE_META = 40
+SURROGATE_META = 48
 
 PROGRESS = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_float, ctypes.c_void_p)
 SLAB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,

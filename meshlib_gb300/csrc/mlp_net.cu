@@ -247,6 +247,19 @@ __global__ void absErrMaxKernel(const float* __restrict__ pred, const float* __r
     if ((threadIdx.x & 31) == 0) atomicMax(maxBits, __float_as_uint(e));  // e >= 0: bits are ordered
 }
 
+// largest overstatement of the distance, |pred| - |d|, over samples with |d| < limit
+__global__ void overestimateMaxKernel(const float* __restrict__ pred, const float* __restrict__ target, int n, float limit,
+                                      unsigned* __restrict__ maxBits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float e = 0.f;
+    if (i < n) {
+        const float d = fabsf(target[i]);
+        if (d < limit) e = fmaxf(fabsf(pred[i]) - d, 0.f);
+    }
+    for (int o = 16; o; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxBits, __float_as_uint(e));
+}
+
 // ---------------------------------------------------------------- bricks
 __global__ void brickCentersKernel(float* __restrict__ pts, int3 bdims, int3 dims, Xf xf) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -680,24 +693,32 @@ cudaError_t SurrogateNet::train(const QueryTree& t, unsigned* scratch, const Tra
     }
     if ((e = cudaStreamSynchronize(s))) return e;
     const auto t2 = std::chrono::steady_clock::now();
-    // validation: worst error on held-out samples -> margin
-    float valMax = 0.f;
+    // validation on held-out samples: the worst error overall (two-sided, against the clamped
+    // target) and the worst overstatement of |d| where |d| < limit -> the two margins
+    float valMax = 0.f, valOver = 0.f;
+    const float limit = o.limit > 0.f ? std::min(o.limit, meta.clampD) : meta.clampD;
     if (o.validation) {
         float* pred = nullptr;
         unsigned* mx = nullptr;
         if ((e = alloc((void**)&pred, sizeof(float) * size_t(o.validation)))) return e;
-        if ((e = alloc((void**)&mx, sizeof(unsigned)))) return e;
+        if ((e = alloc((void**)&mx, 2 * sizeof(unsigned)))) return e;
         if ((e = infer(pts + 3 * nTrain, o.validation, pred, s))) return e;
-        if ((e = cudaMemsetAsync(mx, 0, sizeof(unsigned), s))) return e;
+        if ((e = cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned), s))) return e;
         absErrMaxKernel<<<nblk(o.validation, 256), 256, 0, s>>>(pred, dist + nTrain, int(o.validation), meta.clampD, mx);
-        unsigned bits = 0;
-        if ((e = cudaMemcpyAsync(&bits, mx, sizeof(unsigned), cudaMemcpyDeviceToHost, s))) return e;
+        overestimateMaxKernel<<<nblk(o.validation, 256), 256, 0, s>>>(pred, dist + nTrain, int(o.validation), limit, mx + 1);
+        unsigned bits[2] = {0, 0};
+        if ((e = cudaMemcpyAsync(bits, mx, sizeof(bits), cudaMemcpyDeviceToHost, s))) return e;
         if ((e = cudaStreamSynchronize(s))) return e;
-        std::memcpy(&valMax, &bits, 4);
+        std::memcpy(&valMax, &bits[0], 4);
+        std::memcpy(&valOver, &bits[1], 4);
     }
-    meta.margin = o.marginScale * valMax + o.marginFloor;
+    meta.marginAll = o.marginScale * valMax + o.marginFloor;
+    meta.margin = o.marginScale * valOver + o.marginFloor;
+    meta.limit = limit;
     st.trainLoss = lossHist.empty() ? 0.f : lossHist.back();
     st.valMaxErr = valMax;
+    st.valOverestimate = valOver;
+    st.limit = limit;
     st.margin = meta.margin;
     st.sampleSeconds = std::chrono::duration<float>(t1 - t0).count();
     st.trainSeconds = std::chrono::duration<float>(t2 - t1).count();
@@ -760,7 +781,11 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     brickCentersKernel<<<nblk(nb, 256), 256, 0, s>>>(centers, bd, dims, xf);
     if (net) {
         if ((e = net->infer(centers, nb, tmp, s))) return done(e);
-        surrogateLowerBound<<<nblk(nb, 256), 256, 0, s>>>(tmp, nb, net->meta.margin, lb);
+        // the one-sided margin is validated for |d| < limit, which covers every brick centre that can
+        // hold an in-band voxel (|d(c)| < band + radius) only when band + radius <= limit; otherwise
+        // the two-sided margin over all samples applies
+        const float m = (band + radius <= net->meta.limit) ? net->meta.margin : std::max(net->meta.margin, net->meta.marginAll);
+        surrogateLowerBound<<<nblk(nb, 256), 256, 0, s>>>(tmp, nb, m, lb);
     } else {
         const float cap = band + radius;
         const DistOpts co{0.f, cap * cap, 1, o.threshold, o.beta};

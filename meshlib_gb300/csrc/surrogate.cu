@@ -22,7 +22,8 @@ struct gbfwn_surrogate_s {
 
 namespace {
 
-constexpr int kMetaFloats = 40;  // centre xyz, scale, 32 frequencies, clampD, margin, band, reserved
+// centre xyz, scale, 32 frequencies, clampD, margin, band, limit, marginAll, 7 reserved
+constexpr int kMetaFloats = 48;
 
 void metaOut(const gbfwn_surrogate_s* s, float* m) {
     std::memset(m, 0, sizeof(float) * kMetaFloats);
@@ -32,6 +33,8 @@ void metaOut(const gbfwn_surrogate_s* s, float* m) {
     m[36] = s->net.meta.clampD;
     m[37] = s->net.meta.margin;
     m[38] = s->band;
+    m[39] = s->net.meta.limit;
+    m[40] = s->net.meta.marginAll;
 }
 
 void metaIn(gbfwn_surrogate_s* s, const float* m) {
@@ -41,6 +44,8 @@ void metaIn(gbfwn_surrogate_s* s, const float* m) {
     s->net.meta.clampD = m[36];
     s->net.meta.margin = m[37];
     s->band = m[38];
+    s->net.meta.limit = m[39];
+    s->net.meta.marginAll = m[40];
 }
 
 bool xfOk(const float* xf, Xf& X) {
@@ -113,6 +118,21 @@ GBFWN_API int gbfwn_surrogate_train(gbfwn_handle h, const int32_t dims[3], const
     t.beta = opts->beta;
     t.seed = opts->seed;
     t.marginFloor = 1e-3f * opts->band;
+    // the one-sided margin is validated out to band + twice the half diagonal of this grid's 8x8x8
+    // bricks, which covers the brick centres a banded call on this grid (or a finer one) can keep
+    {
+        float r = 0.f;
+        for (int c = 0; c < 8; ++c) {
+            const float d[3] = {(c & 1) ? 3.5f : -3.5f, (c & 2) ? 3.5f : -3.5f, (c & 4) ? 3.5f : -3.5f};
+            float r2 = 0.f;
+            for (int a = 0; a < 3; ++a) {
+                const float w = X.a[3 * a] * d[0] + X.a[3 * a + 1] * d[1] + X.a[3 * a + 2] * d[2];
+                r2 += w * w;
+            }
+            r = std::fmax(r, std::sqrt(r2));
+        }
+        t.limit = opts->band + 2.f * 1.0001f * r;
+    }
     TrainStats st;
     e = s->net.train(h->tree.q, h->scratch, t, st, h->stream);
     if (e) {
@@ -127,6 +147,8 @@ GBFWN_API int gbfwn_surrogate_train(gbfwn_handle h, const int32_t dims[3], const
         stats->sampleSeconds = st.sampleSeconds;
         stats->trainSeconds = st.trainSeconds;
         stats->steps = st.steps;
+        stats->validationOverestimate = st.valOverestimate;
+        stats->limit = st.limit;
     }
     *out = s;
     return GBFWN_OK;

@@ -18,7 +18,12 @@ struct NetMeta {
     float scale = 1.f;   // u = (p - center) * scale
     float freq[32] = {};
     float clampD = 1.f;  // training target clamp
-    float margin = 0.f; // validated bound of |pred - clamp(d)|
+    // validated bound of |pred| - |d| (how far the prediction may overstate the distance) over the
+    // held-out samples with |d| < limit: the only error that can make a brick cull wrong, checked only
+    // where a wrong cull can happen
+    float margin = 0.f;
+    float limit = 0.f;
+    float marginAll = 0.f;  // validated bound of |pred - clamp(d)| over all held-out samples
 };
 
 struct TrainOptions {
@@ -31,11 +36,12 @@ struct TrainOptions {
     float beta = 2.f;        // winding-number beta of the exact targets
     float lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};  // sampling box
     float marginScale = 1.25f, marginFloor = 0.f;
+    float limit = 0.f;  // |d| below which the one-sided margin is validated (0: everywhere)
     uint64_t seed = 1;
 };
 
 struct TrainStats {
-    float trainLoss = 0, valMaxErr = 0, margin = 0, sampleSeconds = 0, trainSeconds = 0;
+    float trainLoss = 0, valMaxErr = 0, margin = 0, sampleSeconds = 0, trainSeconds = 0, valOverestimate = 0, limit = 0;
     int steps = 0;
 };
 
