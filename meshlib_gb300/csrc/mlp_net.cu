@@ -27,10 +27,7 @@ namespace gbfwn {
 
 namespace {
 
-constexpr int kF = 192, kH = 128, kFreq = 32;
-constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kH * kF, kOffW2 = kOffB1 + kH, kOffB2 = kOffW2 + kH * kH, kOffW3 = kOffB2 + kH,
-              kOffB3 = kOffW3 + kH * kH, kOffW4 = kOffB3 + kH, kOffB4 = kOffW4 + kH * kH, kOffW5 = kOffB4 + kH,
-              kOffB5 = kOffW5 + kH;
+constexpr int kF = kMlpF, kH = kMlpH, kFreq = kMlpFreq;
 static_assert(kOffB5 + 1 == kSurrogateParams, "parameter layout");
 
 inline unsigned nblk(int64_t n, int t) { return unsigned((n + t - 1) / t); }
@@ -46,112 +43,6 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
 }
 __device__ __forceinline__ float urand(uint32_t seed, uint32_t i, uint32_t k) {
     return (hash32(seed * 0x9e3779b9u ^ hash32(i * 4u + k)) >> 8) * (1.f / 16777216.f);
-}
-
-// ---------------------------------------------------------------- features
-__global__ void featuresKernel(const float* __restrict__ pts, const int32_t* __restrict__ idx, const int32_t* __restrict__ offPtr,
-                               int64_t idxMod, int n, int nPad, NetMeta meta, __nv_bfloat16* __restrict__ F,
-                               __nv_bfloat16* __restrict__ FT) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nPad) return;
-    float u[3] = {0.f, 0.f, 0.f};
-    const bool live = i < n;
-    if (live) {
-        int64_t j = i;
-        if (idx) j = idx[(int64_t(offPtr ? *offPtr : 0) + i) % idxMod];
-        for (int a = 0; a < 3; ++a) u[a] = (pts[3 * j + a] - meta.center[a]) * meta.scale;
-    }
-    for (int a = 0; a < 3; ++a)
-        for (int k = 0; k < kFreq; ++k) {
-            float sv = 0.f, cv = 0.f;
-            if (live) sincosf(meta.freq[k] * u[a], &sv, &cv);
-            const int c = 64 * a + 2 * k;
-            const __nv_bfloat16 bs = __float2bfloat16(sv), bc = __float2bfloat16(cv);
-            F[int64_t(i) * kF + c] = bs;
-            F[int64_t(i) * kF + c + 1] = bc;
-            if (FT) {
-                FT[int64_t(c) * nPad + i] = bs;
-                FT[int64_t(c + 1) * nPad + i] = bc;
-            }
-        }
-}
-
-// ---------------------------------------------------------------- output layer, loss, dZ4
-// One warp per row (4 hidden units per lane).  Training mode (target != null): loss, gradients of
-// w5, b5, b4 and dZ4 = g * w5 * silu'(z4) in bf16 (+ transposed).  Inference mode: y only.
-__global__ void outputKernel(const __nv_bfloat16* __restrict__ H4, const float* __restrict__ Z4, int n, int nPad,
-                             const float* __restrict__ params, const float* __restrict__ target,
-                             const int32_t* __restrict__ idx, const int32_t* __restrict__ offPtr, int64_t idxMod,
-                             float clampD, float* __restrict__ y, float* __restrict__ grads, float* __restrict__ loss,
-                             __nv_bfloat16* __restrict__ dZ4, __nv_bfloat16* __restrict__ dZ4T) {
-    __shared__ float sW5[kH], sB4[kH];
-    __shared__ float sLoss, sB5;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int j = threadIdx.x; j < kH; j += blockDim.x) {
-        sW5[j] = 0.f;
-        sB4[j] = 0.f;
-    }
-    if (threadIdx.x == 0) {
-        sLoss = 0.f;
-        sB5 = 0.f;
-    }
-    __syncthreads();
-    const float* w5 = params + kOffW5;
-    const float b5 = params[kOffB5];
-    float aw5[4] = {0, 0, 0, 0}, ab4[4] = {0, 0, 0, 0}, aloss = 0.f, ab5 = 0.f;
-    const float invN = 1.f / float(n);
-    for (int row = blockIdx.x * (blockDim.x >> 5) + warp; row < nPad; row += gridDim.x * (blockDim.x >> 5)) {
-        float h[4], acc = 0.f;
-        for (int q = 0; q < 4; ++q) {
-            const int j = lane + 32 * q;
-            h[q] = __bfloat162float(H4[int64_t(row) * kH + j]);
-            acc += h[q] * w5[j];
-        }
-        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        const float yv = acc + b5;
-        if (!target) {
-            if (lane == 0 && row < n) y[row] = yv;
-            continue;
-        }
-        float g = 0.f;
-        if (row < n) {
-            const int64_t j = idx ? idx[(int64_t(offPtr ? *offPtr : 0) + row) % idxMod] : row;
-            const float t = fminf(fmaxf(target[j], -clampD), clampD);
-            const float r = yv - t;
-            aloss += (lane == 0) ? r * r * invN : 0.f;
-            g = 2.f * r * invN;
-            ab5 += (lane == 0) ? g : 0.f;
-        }
-        for (int q = 0; q < 4; ++q) {
-            const int j = lane + 32 * q;
-            aw5[q] += g * h[q];
-            const float z = Z4[int64_t(row) * kH + j];
-            const float s = 1.f / (1.f + __expf(-z));
-            const float dz = g * w5[j] * s * (1.f + z * (1.f - s));
-            ab4[q] += dz;
-            const __nv_bfloat16 db = __float2bfloat16(dz);
-            dZ4[int64_t(row) * kH + j] = db;
-            dZ4T[int64_t(j) * nPad + row] = db;
-        }
-    }
-    if (!target) return;
-    for (int q = 0; q < 4; ++q) {
-        atomicAdd(&sW5[lane + 32 * q], aw5[q]);
-        atomicAdd(&sB4[lane + 32 * q], ab4[q]);
-    }
-    if (lane == 0) {
-        atomicAdd(&sLoss, aloss);
-        atomicAdd(&sB5, ab5);
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < kH; j += blockDim.x) {
-        atomicAdd(&grads[kOffW5 + j], sW5[j]);
-        atomicAdd(&grads[kOffB4 + j], sB4[j]);
-    }
-    if (threadIdx.x == 0) {
-        atomicAdd(&grads[kOffB5], sB5);
-        atomicAdd(loss, sLoss);
-    }
 }
 
 // ---------------------------------------------------------------- Adam + weight packing
@@ -180,17 +71,26 @@ __global__ void stepCounterKernel(int32_t* step, int32_t* off, int batch, int ba
     *off = (s % batchesPerEpoch) * batch;
 }
 
-// bf16 copies of W1..W4 (row-major [out x in]) and transposes of W2..W4 ([in x out])
+// bf16 copies of W1..W4: row-major [out x in] (inference) and the shared-memory images of the fused
+// training step (mlp.cuh: 128-row x 64-column K-major blocks with the 128-byte swizzle)
+__device__ __forceinline__ int64_t imageIndex(int block, int r, int c) {  // element (r, c) of a 64-column block
+    return int64_t(block) * (kImgBlockBytes / 2) + r * 64 + (((c >> 3) ^ (r & 7)) << 3) + (c & 7);
+}
 __global__ void packKernel(const float* __restrict__ params, __nv_bfloat16* __restrict__ W1, __nv_bfloat16* __restrict__ W234,
-                           __nv_bfloat16* __restrict__ WT234) {
+                           __nv_bfloat16* __restrict__ img) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < kH * kF) W1[i] = __float2bfloat16(params[kOffW1 + i]);
+    if (i < kH * kF) {
+        const __nv_bfloat16 w = __float2bfloat16(params[kOffW1 + i]);
+        const int r = i / kF, c = i % kF;
+        W1[i] = w;
+        img[imageIndex(c / 64, r, c % 64)] = w;
+    }
     if (i < 3 * kH * kH) {
         const int l = i / (kH * kH), r = (i / kH) % kH, c = i % kH;
         const int off = (l == 0 ? kOffW2 : l == 1 ? kOffW3 : kOffW4);
-        const float w = params[off + r * kH + c];
-        W234[i] = __float2bfloat16(w);
-        WT234[l * kH * kH + c * kH + r] = __float2bfloat16(w);
+        const __nv_bfloat16 w = __float2bfloat16(params[off + r * kH + c]);
+        W234[i] = w;
+        img[imageIndex(3 + 2 * l + c / 64, r, c % 64)] = w;
     }
 }
 
@@ -461,9 +361,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) inferKernel(const float* __r
 // ------------------------------------------------------------------------------------------------
 struct SurrogateNet::Work {
     int batch = 0;
-    __nv_bfloat16 *F = nullptr, *FT = nullptr;
-    float* Z[4] = {};
-    __nv_bfloat16 *H[4] = {}, *HT[4] = {}, *dZ[4] = {}, *dZT[4] = {};
+    __nv_bfloat16* spill = nullptr;  // 32 KB per 128-row tile of a training step
 };
 
 SurrogateNet::~SurrogateNet() { release(); }
@@ -488,7 +386,7 @@ cudaError_t SurrogateNet::alloc(void** p, size_t bytes) {
 
 cudaError_t SurrogateNet::init(uint64_t seed) {
     cudaError_t e;
-    if ((e = prepareGemm())) return e;
+    if ((e = prepareTrainStep())) return e;
     if ((e = cudaFuncSetAttribute(inferKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem)))) return e;
     if ((e = alloc((void**)&params_, sizeof(float) * kSurrogateParams))) return e;
     if ((e = alloc((void**)&grads_, sizeof(float) * kSurrogateParams))) return e;
@@ -496,7 +394,7 @@ cudaError_t SurrogateNet::init(uint64_t seed) {
     if ((e = alloc((void**)&v_, sizeof(float) * kSurrogateParams))) return e;
     if ((e = alloc((void**)&W1_, sizeof(__nv_bfloat16) * kH * kF))) return e;
     if ((e = alloc((void**)&W234_, sizeof(__nv_bfloat16) * 3 * kH * kH))) return e;
-    if ((e = alloc((void**)&WT234_, sizeof(__nv_bfloat16) * 3 * kH * kH))) return e;
+    if ((e = alloc((void**)&img_, size_t(kImgBlockBytes) * kImgBlocks))) return e;
     if ((e = alloc((void**)&counters_, sizeof(int32_t) * 4))) return e;
     if ((e = alloc((void**)&scalars_, sizeof(float) * 8))) return e;
     for (int k = 0; k < kFreq; ++k) meta.freq[k] = float(M_PI * std::pow(2.0, k / 5.0));
@@ -531,7 +429,7 @@ cudaError_t SurrogateNet::getParams(float* hostParams, cudaStream_t s) const {
 }
 
 cudaError_t SurrogateNet::pack(cudaStream_t s) {
-    packKernel<<<nblk(3 * kH * kH, 256), 256, 0, s>>>(params_, W1_, W234_, WT234_);
+    packKernel<<<nblk(3 * kH * kH, 256), 256, 0, s>>>(params_, W1_, W234_, img_);
     return cudaGetLastError();
 }
 
@@ -539,75 +437,34 @@ cudaError_t SurrogateNet::ensureWork(int batchPad) {
     if (work_) return cudaSuccess;  // sized once per network; inference walks larger inputs in chunks
     work_ = new Work;
     work_->batch = batchPad;
-    cudaError_t e;
-    const size_t B = size_t(batchPad);
-    if ((e = alloc((void**)&work_->F, sizeof(__nv_bfloat16) * B * kF))) return e;
-    if ((e = alloc((void**)&work_->FT, sizeof(__nv_bfloat16) * B * kF))) return e;
-    for (int l = 0; l < 4; ++l) {
-        if ((e = alloc((void**)&work_->Z[l], sizeof(float) * B * kH))) return e;
-        if ((e = alloc((void**)&work_->H[l], sizeof(__nv_bfloat16) * B * kH))) return e;
-        if ((e = alloc((void**)&work_->HT[l], sizeof(__nv_bfloat16) * B * kH))) return e;
-        if ((e = alloc((void**)&work_->dZ[l], sizeof(__nv_bfloat16) * B * kH))) return e;
-        if ((e = alloc((void**)&work_->dZT[l], sizeof(__nv_bfloat16) * B * kH))) return e;
-    }
-    return cudaSuccess;
+    return alloc((void**)&work_->spill, size_t(kImgBlockBytes) * 2 * size_t((batchPad + 127) / 128));
 }
 
 // One training (or gradient-only) step over `n` rows taken from pts/targets through idx (or the
-// first n rows when idx is null), padded to nPad rows.  Leaves the loss in scalars_[0].
+// first n rows when idx is null), padded to nPad rows: the fused forward + backward kernel
+// (mlp_train.cu), then Adam, the bf16 repacking and the batch offset.  Leaves the loss in scalars_[0].
 cudaError_t SurrogateNet::step(const float* pts, const float* targets, const int32_t* idx, int64_t idxMod, int n, int nPad,
                                bool update, int totalSteps, float lr, cudaStream_t s) {
-    Work& w = *work_;
+    if (!work_ || nPad > work_->batch) return cudaErrorInvalidValue;
     cudaError_t e;
-    const int32_t* off = idx ? counters_ + 1 : nullptr;
-    featuresKernel<<<nblk(nPad, 128), 128, 0, s>>>(pts, idx, off, idxMod, n, nPad, meta, w.F, w.FT);
-    const __nv_bfloat16* Wl[4] = {W1_, W234_, W234_ + kH * kH, W234_ + 2 * kH * kH};
-    const int offB[4] = {kOffB1, kOffB2, kOffB3, kOffB4};
-    for (int l = 0; l < 4; ++l) {
-        GemmEpilogue ep;
-        ep.mode = GemmEpilogue::kForward;
-        ep.bias = params_ + offB[l];
-        ep.Z = w.Z[l];
-        ep.ldz = kH;
-        ep.H = w.H[l];
-        ep.ldh = kH;
-        ep.HT = w.HT[l];
-        ep.ldht = nPad;
-        ep.status = reinterpret_cast<unsigned*>(counters_ + 3);
-        const __nv_bfloat16* A = l == 0 ? w.F : w.H[l - 1];
-        if ((e = launchGemmBf16(A, l == 0 ? kF : kH, Wl[l], l == 0 ? kF : kH, nPad, kH, l == 0 ? kF : kH, 1, ep, s))) return e;
-    }
     if ((e = cudaMemsetAsync(grads_, 0, sizeof(float) * kSurrogateParams, s))) return e;
     if ((e = cudaMemsetAsync(scalars_, 0, sizeof(float), s))) return e;
-    outputKernel<<<std::min<unsigned>(nblk(nPad, 8), 1024u), 256, 0, s>>>(w.H[3], w.Z[3], n, nPad, params_, targets, idx, off,
-                                                                          idxMod, meta.clampD, nullptr, grads_, scalars_,
-                                                                          w.dZ[3], w.dZT[3]);
-    const int offW[4] = {kOffW1, kOffW2, kOffW3, kOffW4};
-    const int splitK = std::max(1, std::min(16, nPad / 1024));
-    for (int l = 3; l >= 0; --l) {
-        // weight gradient: dW_l = dZ_l^T * act_{l-1}, K = rows
-        GemmEpilogue gw;
-        gw.mode = GemmEpilogue::kStoreF32;
-        gw.D = grads_ + offW[l];
-        gw.ldd = l == 0 ? kF : kH;
-        gw.status = reinterpret_cast<unsigned*>(counters_ + 3);
-        const __nv_bfloat16* Bop = l == 0 ? w.FT : w.HT[l - 1];
-        if ((e = launchGemmBf16(w.dZT[l], nPad, Bop, nPad, kH, l == 0 ? kF : kH, nPad, splitK, gw, s))) return e;
-        if (l == 0) break;
-        // activation gradient of layer l-1: dZ_{l-1} = (dZ_l * W_l) .* silu'(Z_{l-1})
-        GemmEpilogue gb;
-        gb.mode = GemmEpilogue::kBackward;
-        gb.Z = w.Z[l - 1];
-        gb.ldz = kH;
-        gb.H = w.dZ[l - 1];
-        gb.ldh = kH;
-        gb.HT = w.dZT[l - 1];
-        gb.ldht = nPad;
-        gb.dbias = grads_ + offB[l - 1];
-        gb.status = reinterpret_cast<unsigned*>(counters_ + 3);
-        const __nv_bfloat16* WT = WT234_ + (l - 1) * kH * kH;
-        if ((e = launchGemmBf16(w.dZ[l], kH, WT, kH, nPad, kH, kH, 1, gb, s))) return e;
-    }
+    TrainStepArgs a;
+    a.pts = pts;
+    a.targets = targets;
+    a.idx = idx;
+    a.offPtr = idx ? counters_ + 1 : nullptr;
+    a.idxMod = idxMod;
+    a.n = n;
+    a.nPad = nPad;
+    a.clampD = meta.clampD;
+    a.params = params_;
+    a.img = img_;
+    a.spill = work_->spill;
+    a.grads = grads_;
+    a.loss = scalars_;
+    a.status = reinterpret_cast<unsigned*>(counters_ + 3);
+    if ((e = launchTrainStep(a, meta, s))) return e;
     if (!update) return cudaGetLastError();
     adamKernel<<<nblk(kSurrogateParams, 256), 256, 0, s>>>(params_, grads_, m_, v_, kSurrogateParams, counters_, totalSteps, lr,
                                                           0.9f, 0.99f, 1e-8f);
