@@ -28,7 +28,8 @@ namespace gbfwn {
 
 namespace {
 
-constexpr int kT = 256;                 // 8 warps: TMEM lane quarter (warp % 4) x column half (warp / 4)
+constexpr int kT = 512;                 // 16 warps: TMEM lane quarter (warp % 4) x column quarter (warp / 4)
+constexpr int kParts = kT / 128;        // threads per row in the epilogues (and in the feature pass)
 constexpr uint32_t kBlk = kImgBlockBytes;  // 16 KB: 128 rows x 64 bf16 columns
 // slots of the dynamic shared memory (offsets from its 1024-byte aligned base)
 constexpr uint32_t kX0 = 0, kX1 = 3 * kBlk, kY0 = 6 * kBlk, kY1 = 8 * kBlk, kY2 = 10 * kBlk, kY3 = 12 * kBlk;
@@ -49,10 +50,32 @@ __device__ __forceinline__ uint64_t descMN128(uint32_t saddr) {
     return d;
 }
 
-__device__ __forceinline__ float siluf(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float siluf(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 __device__ __forceinline__ float siluGradf(float z) {
-    const float s = 1.f / (1.f + __expf(-z));
+    const float s = __fdividef(1.f, 1.f + __expf(-z));
     return s * (1.f + z * (1.f - s));
+}
+
+// 32 consecutive FP32 TMEM columns of this thread's lane: two loads, one wait
+__device__ __forceinline__ void tmemLoad32(uint32_t taddr, float v[32]) {
+    uint32_t r[32];
+    umma::tmemLoad16Async(taddr, r);
+    umma::tmemLoad16Async(taddr + 16, r + 16);
+    umma::tmemWaitLoads16(r);
+    umma::tmemWaitLoads16(r + 16);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void loadParams16(const float* p, float v[16]) {  // p 16-byte aligned
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float4 x = __ldg(reinterpret_cast<const float4*>(p) + i);
+        v[4 * i] = x.x;
+        v[4 * i + 1] = x.y;
+        v[4 * i + 2] = x.z;
+        v[4 * i + 3] = x.w;
+    }
 }
 __device__ __forceinline__ uint32_t packBf16x2(float a, float b) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
@@ -148,9 +171,11 @@ __device__ __forceinline__ void endPhase() {
 }
 
 // Features of this CTA's rows into the 48 KB K-major tile F (axis a = block a; column 2k / 2k + 1 =
-// sin / cos of frequency k): thread (row, half) writes frequencies 16 half .. 16 half + 15.
+// sin / cos of frequency k): thread (row, part) writes frequencies 8 part .. 8 part + 7.
 __device__ void featuresTile(uint8_t* F, const TrainStepArgs& a, const NetMeta& meta, int rowBase) {
     const int t = threadIdx.x, row = t & 127, fh = t >> 7;
+    constexpr int kChunks = 8 / kParts;  // 16-byte chunks (4 frequencies each, 8 per axis) per thread and axis
+    static_assert(kChunks * kParts == 8, "every chunk of every axis written once");
     const int i = rowBase + row;
     float u[3] = {0.f, 0.f, 0.f};
     if (i < a.n) {
@@ -160,7 +185,7 @@ __device__ void featuresTile(uint8_t* F, const TrainStepArgs& a, const NetMeta& 
     }
     const bool live = i < a.n;
     for (int ax = 0; ax < 3; ++ax)
-        for (int c = 4 * fh; c < 4 * fh + 4; ++c) {
+        for (int c = kChunks * fh; c < kChunks * fh + kChunks; ++c) {
             uint32_t w[4];
             for (int q = 0; q < 4; ++q) {
                 float sv = 0.f, cv = 0.f;
@@ -180,12 +205,12 @@ __global__ void __launch_bounds__(kT, 1) trainStepKernel(TrainStepArgs a, NetMet
     __shared__ int failed;
     // column sums of the epilogues (colA, colB); the output layer's per-row partial dot products
     // use the same 1 KB before its column sums start (the tiles take all but ~2 KB of the 227 KB)
-    __shared__ float colBuf[256];
+    __shared__ float colBuf[256];  // kT >= 256
     __shared__ float blockSum[2];
     float* colA = colBuf;
     float* colB = colBuf + 128;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int q = warp & 3, hf = warp >> 2;
+    const int q = warp & 3, hf = warp >> 2;  // hf: this thread's column part (of kParts)
     const int row = 32 * q + lane;  // this thread's row in every epilogue
     const int rowBase = blockIdx.x * 128;
     const int gRow = rowBase + row;
@@ -201,7 +226,7 @@ __global__ void __launch_bounds__(kT, 1) trainStepKernel(TrainStepArgs a, NetMet
         failed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    colBuf[t] = 0.f;
+    if (t < 256) colBuf[t] = 0.f;
     if (t < 2) blockSum[t] = 0.f;
     umma::fenceBeforeSync();
     __syncthreads();
@@ -223,24 +248,34 @@ __global__ void __launch_bounds__(kT, 1) trainStepKernel(TrainStepArgs a, NetMet
     // forward epilogue of hidden layer l (1..3): H_l = bf16(silu(Z_l + b_l)) into tile `out`
     auto forwardEpilogue = [&](int l, uint8_t* out) {
         const float* bias = a.params + (l == 1 ? kOffB1 : l == 2 ? kOffB2 : kOffB3);
-        for (int c0 = 64 * hf; c0 < 64 * hf + 64; c0 += 16) {
-            float v[16];
-            umma::tmemLoad16(tq + uint32_t(128 * (l - 1) + c0), v);
+        const int cb = 32 * hf;
+        float v[32];
+        tmemLoad32(tq + uint32_t(128 * (l - 1) + cb), v);
+        for (int h = 0; h < 2; ++h) {
+            float b[16];
+            loadParams16(bias + cb + 16 * h, b);
             uint32_t w[8];
-            for (int j = 0; j < 16; j += 2) w[j / 2] = packBf16x2(siluf(v[j] + bias[c0 + j]), siluf(v[j + 1] + bias[c0 + j + 1]));
-            storeRow16(out, row, c0, w);
+            for (int j = 0; j < 16; j += 2)
+                w[j / 2] = packBf16x2(siluf(v[16 * h + j] + b[j]), siluf(v[16 * h + j + 1] + b[j + 1]));
+            storeRow16(out, row, cb + 16 * h, w);
         }
     };
     // backward epilogue: dZ_{l} = bf16(dH * silu'(Z_l + b_l)) into tile `out` from dH at TMEM column
     // 384 and Z_l at 128 (l - 1); bias gradient sums into colA
     auto backwardEpilogue = [&](int l, uint8_t* out) {
         const float* bias = a.params + (l == 1 ? kOffB1 : l == 2 ? kOffB2 : kOffB3);
-        for (int c0 = 64 * hf; c0 < 64 * hf + 64; c0 += 16) {
-            float g[16], z[16];
-            umma::tmemLoad16(tq + uint32_t(384 + c0), g);
-            umma::tmemLoad16(tq + uint32_t(128 * (l - 1) + c0), z);
+        const int cb = 32 * hf;
+        for (int h = 0; h < 2; ++h) {
+            const int c0 = cb + 16 * h;
+            uint32_t rg[16], rz[16];
+            umma::tmemLoad16Async(tq + uint32_t(384 + c0), rg);
+            umma::tmemLoad16Async(tq + uint32_t(128 * (l - 1) + c0), rz);
+            umma::tmemWaitLoads16(rg);
+            umma::tmemWaitLoads16(rz);
+            float b[16], g[16];
+            loadParams16(bias + c0, b);
             uint32_t w[8];
-            for (int j = 0; j < 16; ++j) g[j] *= siluGradf(z[j] + bias[c0 + j]);
+            for (int j = 0; j < 16; ++j) g[j] = __uint_as_float(rg[j]) * siluGradf(__uint_as_float(rz[j]) + b[j]);
             for (int j = 0; j < 16; j += 2) w[j / 2] = packBf16x2(g[j], g[j + 1]);
             storeRow16(out, row, c0, w);
             colAdd(colA, c0, g);
@@ -248,8 +283,8 @@ __global__ void __launch_bounds__(kT, 1) trainStepKernel(TrainStepArgs a, NetMet
     };
     // gradient of W_l from TMEM column `col` (N columns of input per row = output unit `row`)
     auto weightGradEpilogue = [&](uint32_t col, int N, int off) {
-        const int half = N / 2;
-        for (int c0 = half * hf; c0 < half * hf + half; c0 += 16) {
+        const int part = N / kParts;  // 32 (N = 128) or 48 (N = 192) columns per thread
+        for (int c0 = part * hf; c0 < part * hf + part; c0 += 16) {
             float v[16];
             umma::tmemLoad16(tq + col + uint32_t(c0), v);
             float* g = a.grads + off + int64_t(row) * N + c0;
@@ -318,15 +353,27 @@ __global__ void __launch_bounds__(kT, 1) trainStepKernel(TrainStepArgs a, NetMet
     {
         const float* b4 = a.params + kOffB4;
         const float* w5 = a.params + kOffW5;
+        const int cb = 32 * hf;
+        float z4[32], b4v[32], w5v[32];
+        tmemLoad32(tq + uint32_t(384 + cb), z4);
+        loadParams16(b4 + cb, b4v);
+        loadParams16(b4 + cb + 16, b4v + 16);
+        loadParams16(w5 + cb, w5v);
+        loadParams16(w5 + cb + 16, w5v + 16);
         float acc = 0.f;
-        for (int c0 = 64 * hf; c0 < 64 * hf + 64; c0 += 16) {
-            float v[16];
-            umma::tmemLoad16(tq + uint32_t(384 + c0), v);
-            for (int j = 0; j < 16; ++j) acc += __bfloat162float(__float2bfloat16(siluf(v[j] + b4[c0 + j]))) * w5[c0 + j];
+        for (int j = 0; j < 32; ++j) {
+            z4[j] += b4v[j];
+            acc += __bfloat162float(__float2bfloat16(siluf(z4[j]))) * w5v[j];
         }
-        colBuf[128 * hf + row] = acc;  // per-row partial dot products of the two column halves
+        // per-row partial dot products of the kParts column parts, in the spilled tile's slot (its
+        // bulk store has read it: thread 0 waited for that before this phase, hence the barrier)
+        float* rowPart = reinterpret_cast<float*>(Y1);
         __syncthreads();
-        const float y = colBuf[row] + colBuf[128 + row] + a.params[kOffB5];
+        rowPart[128 * hf + row] = acc;
+        __syncthreads();
+        float ysum = a.params[kOffB5];
+        for (int p2 = 0; p2 < kParts; ++p2) ysum += rowPart[128 * p2 + row];
+        const float y = ysum;
         float g = 0.f, l2 = 0.f;
         if (gRow < a.n) {
             int64_t j = gRow;
@@ -337,7 +384,7 @@ __global__ void __launch_bounds__(kT, 1) trainStepKernel(TrainStepArgs a, NetMet
             g = 2.f * r * invN;
             l2 = r * r * invN;
         }
-        if (hf == 0) {  // warp-uniform: one of the two threads of each row counts it
+        if (hf == 0) {  // warp-uniform: one of the kParts threads of each row counts it
             float gs = g;
             for (int o = 16; o; o >>= 1) {
                 l2 += __shfl_xor_sync(FULLMASK, l2, o);
@@ -348,17 +395,14 @@ __global__ void __launch_bounds__(kT, 1) trainStepKernel(TrainStepArgs a, NetMet
                 atomicAdd(&blockSum[1], gs);
             }
         }
-        __syncthreads();
-        colBuf[t] = 0.f;  // the partial sums are read: the buffer becomes the column sums
-        __syncthreads();
-        for (int c0 = 64 * hf; c0 < 64 * hf + 64; c0 += 16) {
+        for (int h = 0; h < 2; ++h) {
+            const int c0 = cb + 16 * h;
             float v[16], gw[16];
-            umma::tmemLoad16(tq + uint32_t(384 + c0), v);
             uint32_t w[8];
             for (int jj = 0; jj < 16; ++jj) {
-                const float z = v[jj] + b4[c0 + jj];
+                const float z = z4[16 * h + jj];
                 gw[jj] = g * __bfloat162float(__float2bfloat16(siluf(z)));  // w5 gradient term
-                v[jj] = g * w5[c0 + jj] * siluGradf(z);                     // dZ4 (FP32)
+                v[jj] = g * w5v[16 * h + jj] * siluGradf(z);                // dZ4 (FP32)
             }
             for (int jj = 0; jj < 16; jj += 2) w[jj / 2] = packBf16x2(v[jj], v[jj + 1]);
             storeRow16(Y3, row, c0, w);
