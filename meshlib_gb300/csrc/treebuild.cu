@@ -41,17 +41,34 @@ struct Elem {  // one leaf during construction (40 bytes)
     float mn[3], mx[3];
 };
 
+// The comparison key of the large-segment levels, kept beside the elements in the same order (one
+// 16-byte load, so the radix passes do not stream the 40-byte elements): c[3], then the id.
+struct __align__(16) Key {
+    float c[3];
+    int32_t id;
+};
+
 __device__ __forceinline__ uint32_t orderedBits(float f) {
     uint32_t b = __float_as_uint(f == 0.f ? 0.f : f);  // -0 and +0 compare equal in the reference
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
 // 128-bit key of an element under dims (d2 most significant): w[0] is the most significant word.
-__device__ __forceinline__ void keyWords(const Elem& e, int d2, int d1, int d0, uint32_t w[4]) {
+__device__ __forceinline__ void keyWords(const Key& e, int d2, int d1, int d0, uint32_t w[4]) {
     w[0] = orderedBits(e.c[d2]);
     w[1] = orderedBits(e.c[d1]);
     w[2] = orderedBits(e.c[d0]);
     w[3] = uint32_t(e.id) ^ 0x80000000u;
+}
+
+__device__ __forceinline__ Key loadKey(const Key* k, int32_t p) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(k) + p);
+    Key r;
+    r.c[0] = v.x;
+    r.c[1] = v.y;
+    r.c[2] = v.z;
+    r.id = __float_as_int(v.w);
+    return r;
 }
 
 __device__ __forceinline__ int keyByte(const uint32_t w[4], int b) {  // b = 0 is the most significant byte
@@ -194,7 +211,8 @@ __global__ void validFaces(const int32_t* __restrict__ tris, int64_t nt, int64_t
 
 // MRMesh/MRAABBTree.cpp:15-29: box of the three vertices, then one ulp outwards (MRBox.h:260-270)
 __global__ void makeLeaves(const float* __restrict__ verts, const int32_t* __restrict__ tris, int64_t nt,
-                           const int32_t* __restrict__ flag, const int32_t* __restrict__ pos, Elem* __restrict__ out) {
+                           const int32_t* __restrict__ flag, const int32_t* __restrict__ pos, Elem* __restrict__ out,
+                           Key* __restrict__ keys) {
     const int64_t f = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (f >= nt || !flag[f]) return;
     Elem e;
@@ -211,6 +229,7 @@ __global__ void makeLeaves(const float* __restrict__ verts, const int32_t* __res
         e.c[d] = e.mn[d] + e.mx[d];
     }
     out[pos[f]] = e;
+    keys[pos[f]] = Key{{e.c[0], e.c[1], e.c[2]}, e.id};
 }
 
 __device__ __forceinline__ void writeLeaf(const Elem& e, int32_t node, int32_t slot, RefNode* nodes, int32_t* irs, int2* range,
@@ -331,7 +350,7 @@ __global__ void segNodes(const Seg* __restrict__ segs, int nseg, const int* __re
     writeInternal(mn, mx, segs[s].root, segs[s].first, segs[s].num, nodes, irs, range, nNodes);
 }
 
-__global__ void radixHist(const Elem* __restrict__ el, int32_t n, const int32_t* __restrict__ segOf,
+__global__ void radixHist(const Key* __restrict__ keys, int32_t n, const int32_t* __restrict__ segOf,
                           const SegState* __restrict__ st, int* __restrict__ hist, const int* __restrict__ prevPending) {
     if (prevPending && *prevPending == 0) return;  // every segment finished in an earlier pass
     const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -341,7 +360,7 @@ __global__ void radixHist(const Elem* __restrict__ el, int32_t n, const int32_t*
         const SegState S = st[s];
         if (!S.done) {
             uint32_t w[4];
-            keyWords(el[p], (S.dims >> 4) & 3, (S.dims >> 2) & 3, S.dims & 3, w);
+            keyWords(loadKey(keys, p), (S.dims >> 4) & 3, (S.dims >> 2) & 3, S.dims & 3, w);
             if (cmpPrefix(w, S.prefix, S.nbytes) == 0) key = 256 * s + keyByte(w, S.nbytes);
         }
     }
@@ -404,7 +423,7 @@ __global__ void radixSelect(const Seg* __restrict__ segs, int nseg, SegState* __
     }
 }
 
-__global__ void partFlags(const Elem* __restrict__ el, int32_t n, const int32_t* __restrict__ segOf,
+__global__ void partFlags(const Key* __restrict__ keys, int32_t n, const int32_t* __restrict__ segOf,
                           const SegState* __restrict__ st, int32_t* __restrict__ flag) {
     const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
@@ -413,7 +432,7 @@ __global__ void partFlags(const Elem* __restrict__ el, int32_t n, const int32_t*
     if (s >= 0) {
         const SegState S = st[s];
         uint32_t w[4];
-        keyWords(el[p], (S.dims >> 4) & 3, (S.dims >> 2) & 3, S.dims & 3, w);
+        keyWords(loadKey(keys, p), (S.dims >> 4) & 3, (S.dims >> 2) & 3, S.dims & 3, w);
         f = cmpPrefix(w, S.prefix, S.nbytes) < 0 ? 1 : 0;  // strictly below the median element: left
     }
     flag[p] = f;
@@ -421,7 +440,8 @@ __global__ void partFlags(const Elem* __restrict__ el, int32_t n, const int32_t*
 
 // also writes the element's segment at the next level: child c of segment s is entry 2s + c of the
 // next segment list, or -1 when that child is finished elsewhere (kSmall leaves or fewer)
-__global__ void partScatter(const Elem* __restrict__ el, Elem* __restrict__ out, int32_t n, const Seg* __restrict__ segs,
+__global__ void partScatter(const Elem* __restrict__ el, Elem* __restrict__ out, const Key* __restrict__ keys,
+                            Key* __restrict__ keysOut, int32_t n, const Seg* __restrict__ segs,
                             const int32_t* __restrict__ segOf, int32_t* __restrict__ segOfNext,
                             const int32_t* __restrict__ flag, const int32_t* __restrict__ scan) {
     const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -436,6 +456,7 @@ __global__ void partScatter(const Elem* __restrict__ el, Elem* __restrict__ out,
         if ((left ? k : num - k) > kSmall) next = 2 * s + (left ? 0 : 1);
     }
     out[dst] = el[p];
+    reinterpret_cast<float4*>(keysOut)[dst] = __ldg(reinterpret_cast<const float4*>(keys) + p);
     segOfNext[dst] = next;
 }
 
@@ -628,12 +649,15 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
     if (n == 0) return cudaSuccess;
     const int64_t nNodes = 2 * int64_t(n) - 1;
     Elem *el = nullptr, *el2 = nullptr;
+    Key *keys = nullptr, *keys2 = nullptr;
     if ((e = A.alloc((void**)&el, sizeof(Elem) * size_t(n)))) return e;
     if ((e = A.alloc((void**)&el2, sizeof(Elem) * size_t(n)))) return e;
+    if ((e = A.alloc((void**)&keys, sizeof(Key) * size_t(n)))) return e;
+    if ((e = A.alloc((void**)&keys2, sizeof(Key) * size_t(n)))) return e;
     if ((e = P.alloc((void**)&nodes, sizeof(RefNode) * size_t(nNodes)))) return e;
     if ((e = A.alloc((void**)&irs, sizeof(int32_t) * 2 * size_t(nNodes)))) return e;
     if ((e = A.alloc((void**)&range, sizeof(int2) * size_t(nNodes)))) return e;
-    makeLeaves<<<blocks(nt, 256), 256, 0, s>>>(dVerts, dTris, nt, flag, pos, el);
+    makeLeaves<<<blocks(nt, 256), 256, 0, s>>>(dVerts, dTris, nt, flag, pos, el, keys);
     // segment lists: at most 2^L entries at level L; the large-segment levels stop below n / kSmall
     int maxSegs = 1;
     while (maxSegs < 2 * (n / kSmall + 1)) maxSegs <<= 1;
@@ -672,7 +696,7 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
             if ((e = cudaMemsetAsync(pend, 0, sizeof(int32_t) * 16, s))) return e;
             for (int pass = 0; pass < 16; ++pass) {
                 const int* prev = pass ? pend + pass - 1 : nullptr;
-                radixHist<<<blocks(n, 256), 256, 0, s>>>(el, n, segOf, st, hist, prev);
+                radixHist<<<blocks(n, 256), 256, 0, s>>>(keys, n, segOf, st, hist, prev);
                 radixSelect<<<blocks(int64_t(nseg) * 32, 256), 256, 0, s>>>(segA, nseg, st, hist, pend + pass, prev);
                 if ((pass + 1) % kGroup && pass != 15) continue;
                 int32_t pending = 0;
@@ -680,10 +704,11 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
                 if ((e = cudaStreamSynchronize(s))) return e;
                 if (pending == 0) break;
             }
-            partFlags<<<blocks(n, 256), 256, 0, s>>>(el, n, segOf, st, flag);
+            partFlags<<<blocks(n, 256), 256, 0, s>>>(keys, n, segOf, st, flag);
             if ((e = exclusiveScan(flag, scan, n, sums, misc + 1, s))) return e;
-            partScatter<<<blocks(n, 256), 256, 0, s>>>(el, el2, n, segA, segOf, segOf2, flag, scan);
+            partScatter<<<blocks(n, 256), 256, 0, s>>>(el, el2, keys, keys2, n, segA, segOf, segOf2, flag, scan);
             std::swap(el, el2);
+            std::swap(keys, keys2);
             std::swap(segOf, segOf2);
             segChildren<<<blocks(nseg, 128), 128, 0, s>>>(segA, nseg, segB, el, small, misc + 3, nodes, irs, range, nNodes);
             std::swap(segA, segB);
