@@ -15,7 +15,11 @@
  *    vector (x, y, z); `xf` is 12 floats: the 3x3 linear part row by row, then the translation
  *    (MRMesh/MRAffineXf.h:46).
  *  - Calls without a `_dev` suffix take and return HOST memory and are synchronous, like
- *    `MR::Cuda::FastWindingNumber`.  `_dev` calls take DEVICE pointers and only enqueue work on
+ *    `MR::Cuda::FastWindingNumber`.  Where the GPU reads and writes pageable host memory itself
+ *    (Grace-Blackwell's coherent NVLink-C2C) and the caller's grid buffer is already populated (a
+ *    std::vector that was resized, a buffer reused across calls), a whole-grid call without a
+ *    progress callback writes the grid straight into that buffer instead of into a device buffer
+ *    followed by a copy; the values are the same either way.  `_dev` calls take DEVICE pointers and only enqueue work on
  *    `stream`: NULL = the handle's own stream; any cudaStream_t, including cudaStreamLegacy
  *    (0x1) and cudaStreamPerThread (0x2), is accepted.
  *  - A handle owns one work-queue counter and staging buffers: calls on the same handle must not

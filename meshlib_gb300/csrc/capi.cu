@@ -14,6 +14,11 @@
 #include <string>
 #include <vector>
 
+#if defined(__linux__)
+#include <sys/mman.h>
+#include <unistd.h>
+#endif
+
 #include "../../include/gbfwn.h"
 #include "common.cuh"
 #include "handle.cuh"
@@ -470,6 +475,36 @@ GBFWN_API int gbfwn_from_grid_with_distances_slab_dev(gbfwn_handle h, const int3
 // ------------------------------------------------------------------------- host-memory calls
 namespace {
 
+// True when the kernel can write the `bytes` at host address p itself: the device accesses pageable
+// host memory through the CPU's page tables (cudaDevAttrPageableMemoryAccess: Grace-Blackwell's
+// coherent NVLink-C2C) and every page of the range is already populated (mincore), as a
+// std::vector that was resized or a buffer reused from an earlier call is.  A GPU write to a page the
+// CPU has not touched yet takes a page fault (measured on GB300: about 0.35 ms per MB, far slower
+// than a copy), so such ranges, and every other platform, take the device buffer + copy path.
+bool directHostWritable(int device, const void* p, size_t bytes) {
+#if defined(__linux__)
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (!pageable || !p || bytes == 0) return false;
+    const long page = sysconf(_SC_PAGESIZE);
+    if (page <= 0) return false;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p), lo = a & ~uintptr_t(page - 1), hi = a + bytes;
+    std::vector<unsigned char> resident((hi - lo + size_t(page) - 1) / size_t(page));
+    if (mincore(reinterpret_cast<void*>(lo), hi - lo, resident.data()) != 0) return false;
+    for (unsigned char v : resident)
+        if (!(v & 1)) return false;
+    return true;
+#else
+    (void)device;
+    (void)p;
+    (void)bytes;
+    return false;
+#endif
+}
+
 // Computes a grid in slabs of whole XY layers.  Each slab's kernel writes into the device output
 // buffer; the copy stream waits for it and moves it to `hostOut` (if not null) and/or hands it to
 // `slab` (by-parts mode, with `overlap` layers shared between consecutive slabs).
@@ -508,9 +543,19 @@ int runGrid(gbfwn_mesh_s* h, const int32_t dims[3], LaunchFn launch, float* host
     }
     // device buffer: the whole grid in host mode, two slab buffers in by-parts mode
     const bool whole = !slab;
+    cudaError_t e = cudaSuccess;
+    // one launch straight into the caller's memory when the GPU can write it in place (no device
+    // buffer, no copy: the results cross NVLink-C2C as the kernel stores them)
+    if (whole && hostOut && !cb && slabs.size() == 1 && directHostWritable(h->device, hostOut, layer * size_t(nz) * sizeof(float))) {
+        if ((e = h->resetStatus(h->stream))) return cudaFail(e, what);
+        GridRange r{dims[0], dims[1], dims[2], 0, nz, 0};
+        if ((e = launch(r, hostOut, h->stream))) return cudaFail(e, what);
+        if ((e = cudaStreamSynchronize(h->stream))) return cudaFail(e, what);
+        return h->checkStatus();
+    }
     const size_t slabBytes = layer * size_t(slabLayers) * sizeof(float);
     const size_t need = whole ? layer * size_t(nz) * sizeof(float) : 2 * slabBytes;
-    cudaError_t e = h->ensure(&h->outBuf, &h->outCap, need);
+    e = h->ensure(&h->outBuf, &h->outCap, need);
     if (!e) e = h->ensureEvents(2 * slabs.size() + 2);
     if (e) return cudaFail(e, what);
     if ((e = h->resetStatus(h->stream))) return cudaFail(e, what);
@@ -732,13 +777,13 @@ GBFWN_API int gbfwn_from_grid_with_distances_by_parts(gbfwn_handle h, const int3
 // tree build.  Kept per handle: vertices, triangles, face -> slot, the reference nodes and dipoles
 // (32 B each per node, for export and refit), the wide query records (128 B closest-point + 64 B
 // winding-number per internal node) and leaf triangles (48 B): 384 B per face.  Build work arrays,
-// all alive until the build ends: two 40-byte leaf records, flags, ranks and ranges per node,
-// segment lists and histograms, parents, arrival counters and oriented-box bookkeeping: under 212 B
-// per face.  32 MiB cover the rounding of the thirty-odd allocations.
+// all alive until the build ends: two 40-byte leaf records and two 16-byte sort keys, flags, ranks and
+// ranges per node, segment lists and histograms, parents, arrival counters and oriented-box
+// bookkeeping: under 244 B per face.  32 MiB cover the rounding of the thirty-odd allocations.
 GBFWN_API size_t gbfwn_mesh_memory(int64_t nv, int64_t nt) {
     const size_t v = size_t(std::max<int64_t>(nv, 0)), n = size_t(std::max<int64_t>(nt, 0));
     const size_t kept = v * 12 + n * (12 + 4) + (2 * n) * (32 + 32) + n * (128 + 64) + n * 48;
-    const size_t build = n * 212;
+    const size_t build = n * 244;
     return kept + build + (size_t(32) << 20);
 }
 GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t dims[3]) {

@@ -357,3 +357,28 @@ def test_grid_beyond_2_31_voxels(fwncls):
         wn = o.exact_wn(pts[mism])
         assert (np.abs(wn - 0.5) < TAU).all()
     del out
+
+
+def test_host_grid_into_populated_and_fresh_buffers(fwn_lib):
+    """Whole-grid host calls write straight into a caller buffer whose pages are populated (where the
+    GPU can access pageable host memory) and go through a device buffer and a copy otherwise; both
+    give the device entry point's grid bit for bit."""
+    import torch
+
+    import meshlib_gb300 as M
+    v, f = mg.noisy_torus(seed=4)
+    g = M.FastWindingNumber(v, f)
+    dims = (37, 29, 23)
+    _, xf = mg.grid_for(v, 37)
+    n = int(np.prod(dims))
+    d = torch.empty(n, device="cuda")
+    g.calcFromGridWithDistances_dev(dims, xf, d.data_ptr(), stream=0)
+    w = torch.empty(n, device="cuda")
+    g.calcFromGrid_dev(dims, xf, w.data_ptr(), stream=0)
+    torch.cuda.synchronize()
+    ref_d, ref_w = d.cpu().numpy(), w.cpu().numpy()
+    for make in (lambda: np.full(n, 7.0, np.float32), lambda: np.empty(n, np.float32)):
+        out = make()
+        g.calcFromGridWithDistances(dims, xf, out=out)
+        assert np.array_equal(out.view(np.int32), ref_d.view(np.int32))
+    assert np.array_equal(g.calcFromGrid(dims, xf).view(np.int32), ref_w.view(np.int32))
