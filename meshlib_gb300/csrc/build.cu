@@ -154,11 +154,12 @@ __global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, co
 }
 
 // Oriented bounding box of every non-root node, written into its parent's closest-point record
-// (layout in common.cuh).  Frame: n = the node's dipole direction dirArea (the area-weighted
-// normal of its triangles), t and u completing an orthonormal basis; extents = the range of the
-// projections of all the node's triangle vertices, widened by a relative margin that covers the
-// FP32 rounding of the projections here and at query time, so the box distance stays a lower
-// bound of the distance to every triangle inside.  The node's leaves are the contiguous slots
+// (layout in common.cuh).  Both children of a node are boxed in the PARENT's frame: n = the parent's
+// dipole direction dirArea (the area-weighted normal of its triangles), t and u completing an
+// orthonormal basis, so a query projects itself once per record for both children.  Extents = the
+// range of the projections of all the node's triangle vertices, widened by a relative margin that
+// covers the FP32 rounding of the projections here and at query time, so the box distance stays a
+// lower bound of the distance to every triangle inside.  The node's leaves are the contiguous slots
 // range[i] = (first, count).  Nodes of up to kObbChunk leaves: obbKernel (a thread for a node of up
 // to 4 leaves, a warp for a larger one); larger ones (the top levels, about 2n / kObbChunk nodes):
 // one warp per chunk of kObbChunk leaves,
@@ -230,11 +231,16 @@ __device__ __forceinline__ void writeObb(int64_t i, const Frame& f, const float 
     const int side = (i == int64_t(p) + 1) ? 0 : 1;
     const int32_t k = irank[i];
     const int32_t link = k >= 0 ? k : ~slot[i];
-    float4* dst = cp + 8 * int64_t(irank[p]) + 4 * side;
-    dst[0] = make_float4(f.t[0], f.t[1], f.t[2], c[0]);
-    dst[1] = make_float4(f.u[0], f.u[1], f.u[2], c[1]);
-    dst[2] = make_float4(f.n[0], f.n[1], f.n[2], c[2]);
-    dst[3] = make_float4(e[0], e[1], e[2], __int_as_float(link));
+    float4* dst = cp + 6 * int64_t(irank[p]);
+    if (side == 0) {  // the left child also writes the (shared) frame
+        dst[0] = make_float4(f.t[0], f.t[1], f.t[2], f.u[0]);
+        dst[1] = make_float4(f.u[1], f.u[2], f.n[0], f.n[1]);
+        dst[2] = make_float4(f.n[2], c[0], c[1], c[2]);
+        dst[3] = make_float4(e[0], e[1], e[2], __int_as_float(link));
+    } else {
+        dst[4] = make_float4(c[0], c[1], c[2], e[0]);
+        dst[5] = make_float4(e[1], e[2], __int_as_float(link), 0.f);
+    }
 }
 
 // Nodes of up to kObbThread leaves (three quarters of all nodes): one thread each; larger ones up to
@@ -250,7 +256,7 @@ __global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const 
     int2 r = make_int2(0, 0);
     if (i < nNodes && i != 0) r = range[i];
     if (r.y >= 1 && r.y <= kObbThread) {
-        const Frame f = nodeFrame(dip8, i);
+        const Frame f = nodeFrame(dip8, parent[i]);
         float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
         for (int sidx = r.x; sidx < r.x + r.y; ++sidx) {
             for (int k = 0; k < 3; ++k) {
@@ -271,7 +277,7 @@ __global__ void obbKernel(int64_t nNodes, const float* __restrict__ dip8, const 
         big &= big - 1;
         const int64_t j = i - lane + src;
         const int first = __shfl_sync(0xffffffffu, r.x, src), num = __shfl_sync(0xffffffffu, r.y, src);
-        const Frame f = nodeFrame(dip8, j);
+        const Frame f = nodeFrame(dip8, parent[j]);
         float lo[3], hi[3];
         projRange(f, tri, first, first + num, lane, lo, hi);
         if (lane == 0) writeObb(j, f, lo, hi, parent, irank, slot, cp);
@@ -306,7 +312,7 @@ __global__ void obbAccInit(int* __restrict__ acc, const int32_t* __restrict__ nB
 __global__ void obbChunkKernel(int64_t nNodes, const float* __restrict__ dip8, const int2* __restrict__ range,
                                const float4* __restrict__ tri, const int32_t* __restrict__ chunkStart,
                                const int32_t* __restrict__ totalChunks, const int32_t* __restrict__ bigIdx,
-                               int64_t maxBig, int* __restrict__ acc) {
+                               int64_t maxBig, int* __restrict__ acc, const int32_t* __restrict__ parent) {
     const int lane = threadIdx.x & 31;
     const int64_t nWarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
     const int total = *totalChunks;
@@ -319,7 +325,7 @@ __global__ void obbChunkKernel(int64_t nNodes, const float* __restrict__ dip8, c
         const int64_t i = lo_;
         const int2 r = range[i];
         const int a = r.x + int(w - chunkStart[i]) * kObbChunk, b = min(a + kObbChunk, r.x + r.y);
-        const Frame f = nodeFrame(dip8, i);
+        const Frame f = nodeFrame(dip8, parent[i]);
         float lo[3], hi[3];
         projRange(f, tri, a, b, lane, lo, hi);
         if (lane == 0 && bigIdx[i] < maxBig) {
@@ -341,7 +347,7 @@ __global__ void obbBigKernel(int64_t nNodes, const float* __restrict__ dip8, con
     const int* d = acc + 6 * int64_t(bigIdx[i]);
     const float lo[3] = {orderedVal(d[0]), orderedVal(d[1]), orderedVal(d[2])};
     const float hi[3] = {orderedVal(d[3]), orderedVal(d[4]), orderedVal(d[5])};
-    writeObb(i, nodeFrame(dip8, i), lo, hi, parent, irank, slot, cp);
+    writeObb(i, nodeFrame(dip8, parent[i]), lo, hi, parent, irank, slot, cp);
 }
 
 // ------------------------------------------------------------------------------------ refit
@@ -461,7 +467,7 @@ static cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, c
     if ((e = T.alloc((void**)&parent, sizeof(int32_t) * size_t(nNodes)))) return e;
     if ((e = T.alloc((void**)&arrive, sizeof(int32_t) * size_t(nNodes)))) return e;
     const int64_t nInt = std::max<int64_t>(out.nInternal, 1);
-    if (!out.cp && (e = P.alloc((void**)&out.cp, sizeof(float4) * 8 * size_t(nInt)))) return e;
+    if (!out.cp && (e = P.alloc((void**)&out.cp, sizeof(float4) * 6 * size_t(nInt)))) return e;
     if (!out.dip && (e = P.alloc((void**)&out.dip, sizeof(float4) * 4 * size_t(nInt)))) return e;
     if (!out.tri && (e = P.alloc((void**)&out.tri, sizeof(float4) * 3 * size_t(out.nLeaves)))) return e;
     const unsigned B = blocksFor(nNodes, 256);
@@ -489,7 +495,7 @@ static cudaError_t finishDeviceTree(const float* dVerts, const int32_t* dTris, c
     if ((e = exclusiveScanI32(isBig, bigIdx, nNodes, sums, totals + 1, s))) return e;
     obbAccInit<<<blocksFor(6 * maxBig, 256), 256, 0, s>>>(acc, totals + 1, maxBig);
     obbChunkKernel<<<unsigned(numSMs()) * 8, 256, 0, s>>>(nNodes, out.dip8, range, out.tri, chunkStart, totals, bigIdx, maxBig,
-                                                           acc);
+                                                           acc, parent);
     obbBigKernel<<<B, 256, 0, s>>>(nNodes, out.dip8, isBig, bigIdx, maxBig, acc, parent, irs, irs + nNodes, out.cp);
     return cudaGetLastError();
 }

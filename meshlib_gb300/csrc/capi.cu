@@ -775,14 +775,14 @@ GBFWN_API int gbfwn_from_grid_with_distances_by_parts(gbfwn_handle h, const int3
 // Memory estimators (the reference's: MRViewer/MRCudaAccessor.cpp:162-194).  Callers compare them
 // with the free device memory before choosing the GPU path, so they cover the peak, which is the
 // tree build.  Kept per handle: vertices, triangles, face -> slot, the reference nodes and dipoles
-// (32 B each per node, for export and refit), the wide query records (128 B closest-point + 64 B
-// winding-number per internal node) and leaf triangles (48 B): 384 B per face.  Build work arrays,
+// (32 B each per node, for export and refit), the wide query records (96 B closest-point + 64 B
+// winding-number per internal node) and leaf triangles (48 B): 352 B per face.  Build work arrays,
 // all alive until the build ends: two 40-byte leaf records and two 16-byte sort keys, flags, ranks and
 // ranges per node, segment lists and histograms, parents, arrival counters and oriented-box
 // bookkeeping: under 244 B per face.  32 MiB cover the rounding of the thirty-odd allocations.
 GBFWN_API size_t gbfwn_mesh_memory(int64_t nv, int64_t nt) {
     const size_t v = size_t(std::max<int64_t>(nv, 0)), n = size_t(std::max<int64_t>(nt, 0));
-    const size_t kept = v * 12 + n * (12 + 4) + (2 * n) * (32 + 32) + n * (128 + 64) + n * 48;
+    const size_t kept = v * 12 + n * (12 + 4) + (2 * n) * (32 + 32) + n * (96 + 64) + n * 48;
     const size_t build = n * 244;
     return kept + build + (size_t(32) << 20);
 }

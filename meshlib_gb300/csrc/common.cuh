@@ -23,9 +23,11 @@ static_assert(sizeof(RefNode) == 32, "reference node is 32 bytes");
 // read gives everything a traversal step needs; children are fetched as float4, all lanes of a
 // warp read the same record, so each load is a broadcast).
 //
-//  cp  [internal k] 8 x float4 : per child (left, then right) an oriented bounding box
-//                                {t.xyz, ct} {u.xyz, cu} {n.xyz, cn} {et, eu, en, link}
-//                                (orthonormal frame t,u,n; centre and half extents along it)
+//  cp  [internal k] 6 x float4 : the frame of node k (orthonormal t, u, n: the area-weighted normal
+//                                of its triangles completed to a basis) and, in that one frame, the
+//                                centre c and half extents e of each child's box:
+//                                {t.xyz, u.x} {u.yz, n.xy} {n.z, cL} {eL, lLink} {cR, eR.x}
+//                                {eR.yz, rLink, 0}
 //  dip [internal k] 4 x float4 : {lpos.xyz, l rr}  {l dirArea.xyz, lLink} {rpos.xyz, r rr} {r dirArea.xyz, rLink}
 //  tri [leaf slot s] 3 x float4: {a.xyz, face} {b.xyz, 0} {c.xyz, 0}
 //

@@ -215,15 +215,39 @@ __device__ __forceinline__ float boxDistSq(const float4& mn, const float4& mx, c
     return r;
 }
 
-// Squared distance from p to an oriented box {t, ct} {u, cu} {n, cn} {et, eu, en, link}: a lower
-// bound of the distance to any triangle of the subtree (the extents carry a rounding margin).
-__device__ __forceinline__ float obbDistSq(const float4& a, const float4& b, const float4& c, const float4& e,
-                                           const float3& p) {
-    const float pt = fmaf(a.x, p.x, fmaf(a.y, p.y, a.z * p.z)) - a.w;
-    const float pu = fmaf(b.x, p.x, fmaf(b.y, p.y, b.z * p.z)) - b.w;
-    const float pn = fmaf(c.x, p.x, fmaf(c.y, p.y, c.z * p.z)) - c.w;
-    const float dt = fmaxf(fabsf(pt) - e.x, 0.f), du = fmaxf(fabsf(pu) - e.y, 0.f), dn = fmaxf(fabsf(pn) - e.z, 0.f);
+// A closest-point record (layout in common.cuh): the node's frame and both children's boxes in it.
+struct CpRecord {
+    float3 t, u, n;
+    float3 cl, el, cr, er;
+    int ll, rl;
+};
+__device__ __forceinline__ CpRecord loadCp(const float4* rec) {
+    const float4 r0 = ld4(rec), r1 = ld4(rec + 1), r2 = ld4(rec + 2), r3 = ld4(rec + 3), r4 = ld4(rec + 4), r5 = ld4(rec + 5);
+    CpRecord c;
+    c.t = make_float3(r0.x, r0.y, r0.z);
+    c.u = make_float3(r0.w, r1.x, r1.y);
+    c.n = make_float3(r1.z, r1.w, r2.x);
+    c.cl = make_float3(r2.y, r2.z, r2.w);
+    c.el = make_float3(r3.x, r3.y, r3.z);
+    c.cr = make_float3(r4.x, r4.y, r4.z);
+    c.er = make_float3(r4.w, r5.x, r5.y);
+    c.ll = __float_as_int(r3.w);
+    c.rl = __float_as_int(r5.z);
+    return c;
+}
+
+// Squared distance from the point with frame coordinates x to the box (centre c, half extents e)
+// in that frame: a lower bound of the distance to any triangle of the subtree (the extents carry a
+// rounding margin).
+__device__ __forceinline__ float frameBoxDistSq(const float3& x, const float3& c, const float3& e) {
+    const float dt = fmaxf(fabsf(x.x - c.x) - e.x, 0.f), du = fmaxf(fabsf(x.y - c.y) - e.y, 0.f),
+                dn = fmaxf(fabsf(x.z - c.z) - e.z, 0.f);
     return fmaf(dt, dt, fmaf(du, du, dn * dn));
+}
+
+__device__ __forceinline__ float3 toFrame(const CpRecord& r, const float3& p) {
+    return make_float3(fmaf(r.t.x, p.x, fmaf(r.t.y, p.y, r.t.z * p.z)), fmaf(r.u.x, p.x, fmaf(r.u.y, p.y, r.u.z * p.z)),
+                       fmaf(r.n.x, p.x, fmaf(r.n.y, p.y, r.n.z * p.z)));
 }
 
 // Affine map of a mesh-space point (rows of A, left-to-right dots, then + b: MRMesh/MRMatrix3.h:127-130).
@@ -254,13 +278,12 @@ __device__ __forceinline__ float mappedBoxDistSq(const Xf& xf, const float3& c, 
     return r;
 }
 
-// obbDistSq for a tree seen through the affine map xf
-__device__ __forceinline__ float obbDistSqXf(const Xf& xf, const float4& a, const float4& b, const float4& c, const float4& e,
-                                            const float3& p) {
-    const float3 t = make_float3(a.x, a.y, a.z), u = make_float3(b.x, b.y, b.z), n = make_float3(c.x, c.y, c.z);
-    const float3 ctr = make_float3(fmaf(a.w, t.x, fmaf(b.w, u.x, c.w * n.x)), fmaf(a.w, t.y, fmaf(b.w, u.y, c.w * n.y)),
-                                   fmaf(a.w, t.z, fmaf(b.w, u.z, c.w * n.z)));
-    return mappedBoxDistSq(xf, ctr, t, u, n, make_float3(e.x, e.y, e.z), p);
+// a child's box of a record seen through the affine map xf
+__device__ __forceinline__ float frameBoxDistSqXf(const Xf& xf, const CpRecord& r, const float3& c, const float3& e,
+                                                 const float3& p) {
+    const float3 ctr = make_float3(fmaf(c.x, r.t.x, fmaf(c.y, r.u.x, c.z * r.n.x)), fmaf(c.x, r.t.y, fmaf(c.y, r.u.y, c.z * r.n.y)),
+                                   fmaf(c.x, r.t.z, fmaf(c.y, r.u.z, c.z * r.n.z)));
+    return mappedBoxDistSq(xf, ctr, r.t, r.u, r.n, e, p);
 }
 
 // root box (axis-aligned, min/max) seen through xf
@@ -381,19 +404,21 @@ __device__ float cpPacket(const QueryTree& t, const float3& q, bool active, floa
         int node;
         unsigned m;
         st.pop(node, m);
-        const float4* rec = t.cp + 8 * int64_t(node);
+        const CpRecord rec = loadCp(t.cp + 6 * int64_t(node));
         const bool mine = ((m >> lane) & 1u) && !done;
+        const int ll = rec.ll, rl = rec.rl;
         float dl, dr;
-        int ll, rl;
-        {
-            const float4 a = ld4(rec), b = ld4(rec + 1), c = ld4(rec + 2), e = ld4(rec + 3);
-            dl = mine ? (TREEXF ? obbDistSqXf(*txf, a, b, c, e, q) : obbDistSq(a, b, c, e, q)) : FLT_MAX;
-            ll = __float_as_int(e.w);
+        if (TREEXF) {
+            dl = frameBoxDistSqXf(*txf, rec, rec.cl, rec.el, q);
+            dr = frameBoxDistSqXf(*txf, rec, rec.cr, rec.er, q);
+        } else {
+            const float3 x = toFrame(rec, q);  // one projection for both children
+            dl = frameBoxDistSq(x, rec.cl, rec.el);
+            dr = frameBoxDistSq(x, rec.cr, rec.er);
         }
-        {
-            const float4 a = ld4(rec + 4), b = ld4(rec + 5), c = ld4(rec + 6), e = ld4(rec + 7);
-            dr = mine ? (TREEXF ? obbDistSqXf(*txf, a, b, c, e, q) : obbDistSq(a, b, c, e, q)) : FLT_MAX;
-            rl = __float_as_int(e.w);
+        if (!mine) {
+            dl = FLT_MAX;
+            dr = FLT_MAX;
         }
         const bool gl = mine && dl < resSq, gr = mine && dr < resSq;
         const unsigned ml = __ballot_sync(FULL, gl), mr = __ballot_sync(FULL, gr);

@@ -50,10 +50,10 @@ def test_memory_estimators(fwn_lib):
     assert est["from_grid"] - est["mesh"] == 512 ** 3 * 4
     # points in and results out, Morton order and its sort scratch
     assert est["from_vector"] - est["mesh"] == 4_000_000 * 40 + 4096
-    # the peak is the build: 384 B kept and up to 244 B of work arrays per face, 12 B per vertex
+    # the peak is the build: 352 B kept and up to 244 B of work arrays per face, 12 B per vertex
     L = fwn_lib
     one, two = L.gbfwn_mesh_memory(655362, 1310720), L.gbfwn_mesh_memory(655362, 2 * 1310720)
-    assert (two - one) == 628 * 1310720 and one == est["mesh"]
+    assert (two - one) == 596 * 1310720 and one == est["mesh"]
     assert L.gbfwn_mesh_memory(2 * 655362, 1310720) - one == 12 * 655362
 
 
