@@ -447,12 +447,14 @@ __device__ float cpPacket(const QueryTree& t, const float3& q, bool active, floa
 
 // ------------------------------------------------------------------ kernels
 constexpr int kThreads = 256;
-// Resident blocks per SM of the kernels that run the closest-point walk (40 registers, some spilled):
-// more warps hide the dependent record loads better than registers help.  Measured at 512^3 on
-// 1.31 M triangles: 4 blocks (64 registers) 129 ms, 5 (48) 120 ms, 6 (40) 115 ms, 7-8 150 ms (spills).
-// The winding-number-only walks keep 4 (23.4 -> 25.1 ms at 6); so do self-intersections and the
-// batched kernel, which measured slower with more warps.
-constexpr int kDistBlocks = 6;
+// Resident blocks per SM of the kernels that run the closest-point walk (48 registers, a few values
+// spilled): more warps hide the dependent record loads better than registers help, up to the point
+// where spills take over.  Measured at 512^3 on 1.31 M triangles with the 128-byte two-frame records:
+// 4 blocks (64 registers) 129 ms, 5 (48) 120 ms, 6 (40) 115 ms, 7-8 150 ms; with the 96-byte one-frame
+// records: 5 blocks 108.5 ms, 6 blocks 110.0 ms, 7 blocks 144.5 ms.  The winding-number-only walks keep
+// 4 (23.4 -> 25.1 ms at 6); so do self-intersections and the batched kernel, which measured slower with
+// more warps.
+constexpr int kDistBlocks = 5;
 constexpr int kTX = 4, kTY = 4, kTZ = 2;  // voxel tile of one warp
 
 struct TileGrid {
