@@ -524,7 +524,10 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
                 }
                 int best = active ? seed : -1;
                 const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
-                seed = best;
+                // next tile: the bottom layer's lanes start from the triangle of the voxel one layer
+                // below them (this tile's top layer), the others from their own voxel two layers below
+                const int fromBelow = __shfl_sync(FULL, best, lane + (kTZ - 1) * kTX * kTY * (lz == 0));
+                seed = lz == 0 ? fromBelow : best;
                 const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
                 const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
                 const float d = __fsqrt_rn(dsq);
@@ -955,7 +958,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const Bat
             }
             int best = active ? seed : -1;
             const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
-            seed = best;
+            // the bottom layer's lanes continue from the voxel one layer below (as gridKernel does)
+            const int fromBelow = __shfl_sync(FULL, best, lane + (TZ - 1) * TX * TY * (lz == 0));
+            seed = lz == 0 ? fromBelow : best;
             const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
             const float w = fwnPacket<PRECISE>(t, q, active && valid, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
             const float d = __fsqrt_rn(dsq);
