@@ -143,19 +143,19 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 
 
 # DRAM bytes (read + write) of one launch of the signed-distance grid kernel at 512^3 on this
-# workload: dram__bytes_read.sum 754,624,256 + dram__bytes_write.sum 611,213,824 from one ncu
+# workload: dram__bytes_read.sum 594,597,120 + dram__bytes_write.sum 608,213,504 from one ncu
 # capture of the same kernel (a constant copied from that capture, not measured by this run; the
 # committed profile summary under profiles/ gives the command).  536,870,912 of the written bytes
 # are the output grid.
-KERNEL_DRAM_BYTES_512 = 754_624_256 + 611_213_824
+KERNEL_DRAM_BYTES_512 = 594_597_120 + 608_213_504
 
 
 # Counters of the signed-distance grid kernel at 256^3 on this workload from one ncu capture
 # (constants copied from that capture, not measured by this run): FMA-pipe utilisation
 # (sm__pipe_fma_cycles_active), issue-slot utilisation and active lanes per warp instruction.
-KERNEL_FMA_PIPE_ACTIVE = 0.321
-KERNEL_ISSUE_ACTIVE = 0.860
-KERNEL_LANES_PER_INSTR = 21.5
+KERNEL_FMA_PIPE_ACTIVE = 0.309
+KERNEL_ISSUE_ACTIVE = 0.839
+KERNEL_LANES_PER_INSTR = 25.1
 
 
 def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
@@ -743,7 +743,7 @@ def main():
                         "fma_pipe_active_ncu": KERNEL_FMA_PIPE_ACTIVE,
                         "note": "reference-equivalent FLOP/s counts the reference traversal's box tests, projections, "
                                 "dipoles and solid angles per voxel; the packet traversal does far fewer, and ncu shows the "
-                                "FMA pipe 32% busy: the kernel is bound by instruction issue and dependent loads"}
+                                "FMA pipe 31% busy: the kernel is bound by instruction issue and dependent loads"}
         line["cpu_baseline"] = {"value": rate, "unit": "voxels/s", "cores": thr, "kind": "port", "sample": desc}
         line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d, extra=prec_extra, M=M, device=local)
     if rank == 0:
