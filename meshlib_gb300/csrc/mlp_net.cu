@@ -21,6 +21,7 @@
 #include "handle.cuh"
 #include "mlp.cuh"
 #include "surrogate.cuh"
+#include "mlp_tiles.cuh"
 #include "umma.cuh"
 
 namespace gbfwn {
@@ -71,26 +72,21 @@ __global__ void stepCounterKernel(int32_t* step, int32_t* off, int batch, int ba
     *off = (s % batchesPerEpoch) * batch;
 }
 
-// bf16 copies of W1..W4: row-major [out x in] (inference) and the shared-memory images of the fused
-// training step (mlp.cuh: 128-row x 64-column K-major blocks with the 128-byte swizzle)
+// bf16 copies of W1..W4 as the shared-memory images the fused training step and inference copy in
+// (mlp.cuh: 128-row x 64-column K-major blocks with the 128-byte swizzle)
 __device__ __forceinline__ int64_t imageIndex(int block, int r, int c) {  // element (r, c) of a 64-column block
     return int64_t(block) * (kImgBlockBytes / 2) + r * 64 + (((c >> 3) ^ (r & 7)) << 3) + (c & 7);
 }
-__global__ void packKernel(const float* __restrict__ params, __nv_bfloat16* __restrict__ W1, __nv_bfloat16* __restrict__ W234,
-                           __nv_bfloat16* __restrict__ img) {
+__global__ void packKernel(const float* __restrict__ params, __nv_bfloat16* __restrict__ img) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < kH * kF) {
-        const __nv_bfloat16 w = __float2bfloat16(params[kOffW1 + i]);
         const int r = i / kF, c = i % kF;
-        W1[i] = w;
-        img[imageIndex(c / 64, r, c % 64)] = w;
+        img[imageIndex(c / 64, r, c % 64)] = __float2bfloat16(params[kOffW1 + i]);
     }
     if (i < 3 * kH * kH) {
         const int l = i / (kH * kH), r = (i / kH) % kH, c = i % kH;
         const int off = (l == 0 ? kOffW2 : l == 1 ? kOffW3 : kOffW4);
-        const __nv_bfloat16 w = __float2bfloat16(params[off + r * kH + c]);
-        W234[i] = w;
-        img[imageIndex(3 + 2 * l + c / 64, r, c % 64)] = w;
+        img[imageIndex(3 + 2 * l + c / 64, r, c % 64)] = __float2bfloat16(params[off + r * kH + c]);
     }
 }
 
@@ -217,68 +213,58 @@ __global__ void exactLowerBound(const float* __restrict__ d, int n, float* __res
 }
 
 // ---------------------------------------------------------------- fused inference
-// The whole network for 128 points per step in one persistent CTA per SM (256 threads): the bf16
-// weights (W1 as three 64-wide K blocks, W2..W4 as two each: 144 KB) are staged once into shared
-// memory with the 128-byte swizzle; per tile the threads write the Fourier features straight into
-// the swizzled activation tile (axis a = K block a), one thread issues the layer's tcgen05 MMAs
-// (M = N = 128, K = 16 each) into a 128-column TMEM accumulator and commits them to an mbarrier,
-// and the epilogue (warp w: TMEM lanes 32 (w % 4).., columns 64 (w / 4)..) adds the bias, applies
-// SiLU, rounds to bf16 and writes the next layer's input tile in place -- the activations never
-// leave the SM.  Rounding points are the training path's (features, h1..h4 in bf16; FP32
+// The whole network for 128 points per step in one persistent CTA per SM (512 threads): the bf16
+// weight images (W1 as three 64-wide K blocks, W2..W4 as two: 144 KB, already in the 128-byte swizzle)
+// arrive once by TMA bulk copy; per tile the threads write the Fourier features straight into the
+// swizzled activation tile (axis a = K block a), one thread issues the layer's tcgen05 MMAs
+// (M = N = 128, K = 16 each) into a 128-column TMEM accumulator and commits them to an mbarrier, and
+// the epilogue (warp w: TMEM lanes 32 (w % 4).., columns 32 (w / 4)..) adds the bias, applies SiLU,
+// rounds to bf16 and writes the next layer's input tile in place -- the activations never leave the
+// SM.  Rounding points and SiLU arithmetic are the training step's (features, h1..h4 in bf16; FP32
 // accumulation); the output layer sums bf16(h4) * w5 in FP32.  A timed-out wait sets status bit 1.
-constexpr int kInferThreads = 256;
+constexpr int kInferThreads = 512;
+constexpr int kInferParts = kInferThreads / 128;  // threads per row
 constexpr int kTileBytes = 128 * 128;  // one 128-row x 64-column bf16 K block
-constexpr size_t kInferSmem = 1024 + size_t(kTileBytes) * (3 + 6 + 3);
-
-__device__ __forceinline__ uint32_t packBf16(float a, float b) {
-    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
-    return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-__device__ __forceinline__ void stageWeights(uint8_t* tile, const __nv_bfloat16* src, int ld) {
-    for (int idx = threadIdx.x; idx < 128 * 8; idx += blockDim.x) {
-        const int r = idx >> 3, c = idx & 7;
-        const uint4 v = *reinterpret_cast<const uint4*>(src + int64_t(r) * ld + c * 8);
-        *reinterpret_cast<uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4)) = v;
-    }
-}
+constexpr size_t kInferSmem = 1024 + size_t(kTileBytes) * (kImgBlocks + 3);
 
 __global__ void __launch_bounds__(kInferThreads, 1) inferKernel(const float* __restrict__ pts, int n, NetMeta meta,
-                                                                 const __nv_bfloat16* __restrict__ W1,
-                                                                 const __nv_bfloat16* __restrict__ W234,
+                                                                 const __nv_bfloat16* __restrict__ img,
                                                                  const float* __restrict__ params, float* __restrict__ out,
                                                                  unsigned* status) {
     extern __shared__ __align__(1024) uint8_t smemRaw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
-    uint8_t* wt = smem;                     // 9 weight tiles: W1 blocks 0..2, then W2, W3, W4 blocks 0..1
-    uint8_t* at = smem + 9 * kTileBytes;    // 3 activation tiles
-    __shared__ __align__(8) uint64_t bar;
+    uint8_t* wt = smem;                             // 9 weight blocks: W1 0..2, W2 3..4, W3 5..6, W4 7..8
+    uint8_t* at = smem + kImgBlocks * kTileBytes;   // 3 activation blocks
+    __shared__ __align__(8) uint64_t bar, barW;
     __shared__ uint32_t tmemBase;
-    __shared__ float partial[2][128];
+    __shared__ float partial[kInferParts][128];
     __shared__ int failed;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    for (int b = 0; b < 3; ++b) stageWeights(wt + b * kTileBytes, W1 + 64 * b, kF);
-    for (int l = 0; l < 3; ++l)
-        for (int b = 0; b < 2; ++b) stageWeights(wt + (3 + 2 * l + b) * kTileBytes, W234 + int64_t(l) * kH * kH + 64 * b, kH);
     if (warp == 0) umma::tmemAlloc(&tmemBase, 128);
     if (t == 0) {
         umma::mbarInit(&bar, 1);
+        umma::mbarInit(&barW, 1);
         failed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        umma::bulkLoad(wt, img, uint32_t(kImgBlocks) * kTileBytes, &barW);
     }
     umma::fenceBeforeSync();
     __syncthreads();
     umma::fenceAfterSync();
     const uint32_t tmem = tmemBase;
     constexpr uint32_t idesc = umma::idescBf16(128, 128);
-    const int q = warp & 3, half = warp >> 2;  // TMEM lane quarter, column half
+    const int q = warp & 3, part = warp >> 2;  // TMEM lane quarter, column part
     const int erow = 32 * q + lane;            // this thread's row in the epilogue
+    const int cb = 32 * part;                  // its first column
+    const uint32_t tq = tmem + (uint32_t(32 * q) << 16);
     const float b5 = params[kOffB5];
     uint32_t phase = 0;
+    bool weightsIn = false;  // the weight copy's barrier has completed (thread 0)
     const int numTiles = (n + 127) / 128;
     for (int tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
-        // features: thread (row, half) writes frequencies 16 half .. 16 half + 15 of every axis
+        // features: thread (row, part) writes frequencies 8 part .. 8 part + 7 of every axis
         {
+            constexpr int kChunks = 8 / kInferParts;
             const int row = t & 127, fh = t >> 7;
             const int64_t i = int64_t(tile) * 128 + row;
             const bool live = i < n;
@@ -286,12 +272,12 @@ __global__ void __launch_bounds__(kInferThreads, 1) inferKernel(const float* __r
             if (live)
                 for (int a = 0; a < 3; ++a) u[a] = (pts[3 * i + a] - meta.center[a]) * meta.scale;
             for (int a = 0; a < 3; ++a)
-                for (int c = 4 * fh; c < 4 * fh + 4; ++c) {  // chunk c = frequencies 4c .. 4c + 3
+                for (int c = kChunks * fh; c < kChunks * fh + kChunks; ++c) {  // chunk c = frequencies 4c .. 4c + 3
                     uint32_t w[4];
                     for (int j = 0; j < 4; ++j) {
                         float sv = 0.f, cv = 0.f;
                         if (live) sincosf(meta.freq[4 * c + j] * u[a], &sv, &cv);
-                        w[j] = packBf16(sv, cv);
+                        w[j] = mlp::packBf16x2(sv, cv);
                     }
                     *reinterpret_cast<uint4*>(at + a * kTileBytes + row * 128 + ((c ^ (row & 7)) << 4)) =
                         make_uint4(w[0], w[1], w[2], w[3]);
@@ -303,6 +289,10 @@ __global__ void __launch_bounds__(kInferThreads, 1) inferKernel(const float* __r
             __syncthreads();
             if (t == 0) {
                 umma::fenceAfterSync();
+                if (!weightsIn) {
+                    weightsIn = umma::mbarWait(&barW, 0);
+                    if (!weightsIn) atomicOr(&failed, 1);
+                }
                 const int nk = layer == 0 ? 3 : 2;
                 const uint8_t* wb = wt + (layer == 0 ? 0 : 3 + 2 * (layer - 1)) * kTileBytes;
                 for (int b = 0; b < nk; ++b) {
@@ -319,36 +309,38 @@ __global__ void __launch_bounds__(kInferThreads, 1) inferKernel(const float* __r
             if (failed) break;
             umma::fenceAfterSync();
             const float* bias = params + (layer == 0 ? kOffB1 : layer == 1 ? kOffB2 : layer == 2 ? kOffB3 : kOffB4);
+            float v[32];
+            umma::tmemLoad32(tq + uint32_t(cb), v);
             float acc5 = 0.f;
-            for (int c0 = 0; c0 < 64; c0 += 16) {
-                const int col0 = 64 * half + c0;
-                float v[16];
-                umma::tmemLoad16(tmem + (uint32_t(32 * q) << 16) + uint32_t(col0), v);
+            for (int h = 0; h < 2; ++h) {
+                float b[16];
+                mlp::loadParams16(bias + cb + 16 * h, b);
                 uint32_t w[8];
-                for (int j = 0; j < 16; j += 2) {
-                    const float z0 = v[j] + bias[col0 + j], z1 = v[j + 1] + bias[col0 + j + 1];
-                    const float h0 = z0 / (1.f + __expf(-z0)), h1 = z1 / (1.f + __expf(-z1));
-                    w[j / 2] = packBf16(h0, h1);
-                    if (layer == 3) {
+                for (int j = 0; j < 16; j += 2) w[j / 2] = mlp::packBf16x2(mlp::silu(v[16 * h + j] + b[j]), mlp::silu(v[16 * h + j + 1] + b[j + 1]));
+                if (layer < 3) {
+                    mlp::storeRow16(at, erow, cb + 16 * h, w);  // next layer's input, in place
+                } else {
+                    float w5[16];
+                    mlp::loadParams16(params + kOffW5 + cb + 16 * h, w5);
+                    for (int j = 0; j < 16; j += 2) {
                         const __nv_bfloat162 hb = *reinterpret_cast<const __nv_bfloat162*>(&w[j / 2]);
-                        acc5 += __low2float(hb) * params[kOffW5 + col0 + j] + __high2float(hb) * params[kOffW5 + col0 + j + 1];
+                        acc5 += __low2float(hb) * w5[j] + __high2float(hb) * w5[j + 1];
                     }
                 }
-                if (layer < 3) {  // next layer's input: column block `half`, chunks c0 / 8 and c0 / 8 + 1
-                    uint8_t* dst = at + half * kTileBytes + erow * 128;
-                    const int ca = c0 / 8, cb = c0 / 8 + 1;
-                    *reinterpret_cast<uint4*>(dst + ((ca ^ (erow & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
-                    *reinterpret_cast<uint4*>(dst + ((cb ^ (erow & 7)) << 4)) = make_uint4(w[4], w[5], w[6], w[7]);
-                }
             }
-            if (layer == 3) partial[half][erow] = acc5;
+            if (layer == 3) partial[part][erow] = acc5;
         }
         if (failed) break;
         __syncthreads();
         if (t < 128) {
             const int64_t i = int64_t(tile) * 128 + t;
-            if (i < n) out[i] = partial[0][t] + partial[1][t] + b5;
+            float y = b5;
+            for (int p2 = 0; p2 < kInferParts; ++p2) y += partial[p2][t];
+            if (i < n) out[i] = y;
         }
+    }
+    if (t == 0 && !weightsIn) {  // no tile, or a timed-out wait: the weight copy must land before the CTA exits
+        if (!umma::mbarWait(&barW, 0)) atomicOr(&failed, 1);
     }
     if (failed && t == 0 && status) atomicOr(status, 2u);
     umma::fenceBeforeSync();
@@ -392,8 +384,6 @@ cudaError_t SurrogateNet::init(uint64_t seed) {
     if ((e = alloc((void**)&grads_, sizeof(float) * kSurrogateParams))) return e;
     if ((e = alloc((void**)&m_, sizeof(float) * kSurrogateParams))) return e;
     if ((e = alloc((void**)&v_, sizeof(float) * kSurrogateParams))) return e;
-    if ((e = alloc((void**)&W1_, sizeof(__nv_bfloat16) * kH * kF))) return e;
-    if ((e = alloc((void**)&W234_, sizeof(__nv_bfloat16) * 3 * kH * kH))) return e;
     if ((e = alloc((void**)&img_, size_t(kImgBlockBytes) * kImgBlocks))) return e;
     if ((e = alloc((void**)&counters_, sizeof(int32_t) * 4))) return e;
     if ((e = alloc((void**)&scalars_, sizeof(float) * 8))) return e;
@@ -429,7 +419,7 @@ cudaError_t SurrogateNet::getParams(float* hostParams, cudaStream_t s) const {
 }
 
 cudaError_t SurrogateNet::pack(cudaStream_t s) {
-    packKernel<<<nblk(3 * kH * kH, 256), 256, 0, s>>>(params_, W1_, W234_, img_);
+    packKernel<<<nblk(3 * kH * kH, 256), 256, 0, s>>>(params_, img_);
     return cudaGetLastError();
 }
 
@@ -478,7 +468,7 @@ cudaError_t SurrogateNet::infer(const float* pts, int64_t n, float* out, cudaStr
     if (n > int64_t(INT32_MAX) - 128) return cudaErrorInvalidValue;
     const int tiles = int((n + 127) / 128);
     const int grid = std::max(1, std::min(tiles, numSMs()));
-    inferKernel<<<grid, kInferThreads, kInferSmem, s>>>(pts, int(n), meta, W1_, W234_, params_, out,
+    inferKernel<<<grid, kInferThreads, kInferSmem, s>>>(pts, int(n), meta, img_, params_, out,
                                                         reinterpret_cast<unsigned*>(counters_ + 3));
     return cudaGetLastError();
 }

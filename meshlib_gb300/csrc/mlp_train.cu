@@ -22,11 +22,21 @@
 #include "common.cuh"
 #include "mlp.cuh"
 #include "surrogate.cuh"
+#include "mlp_tiles.cuh"
 #include "umma.cuh"
 
 namespace gbfwn {
 
 namespace {
+
+using mlp::loadParams16;
+using mlp::packBf16x2;
+using mlp::storeRow16;
+using umma::bulkLoad;
+using umma::bulkStore;
+using umma::tmemLoad32;
+__device__ __forceinline__ float siluf(float z) { return mlp::silu(z); }
+__device__ __forceinline__ float siluGradf(float z) { return mlp::siluGrad(z); }
 
 constexpr int kT = 512;                 // 16 warps: TMEM lane quarter (warp % 4) x column quarter (warp / 4)
 constexpr int kParts = kT / 128;        // threads per row in the epilogues (and in the feature pass)
@@ -50,38 +60,6 @@ __device__ __forceinline__ uint64_t descMN128(uint32_t saddr) {
     return d;
 }
 
-__device__ __forceinline__ float siluf(float z) { return __fdividef(z, 1.f + __expf(-z)); }
-__device__ __forceinline__ float siluGradf(float z) {
-    const float s = __fdividef(1.f, 1.f + __expf(-z));
-    return s * (1.f + z * (1.f - s));
-}
-
-// 32 consecutive FP32 TMEM columns of this thread's lane: two loads, one wait
-__device__ __forceinline__ void tmemLoad32(uint32_t taddr, float v[32]) {
-    uint32_t r[32];
-    umma::tmemLoad16Async(taddr, r);
-    umma::tmemLoad16Async(taddr + 16, r + 16);
-    umma::tmemWaitLoads16(r);
-    umma::tmemWaitLoads16(r + 16);
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void loadParams16(const float* p, float v[16]) {  // p 16-byte aligned
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const float4 x = __ldg(reinterpret_cast<const float4*>(p) + i);
-        v[4 * i] = x.x;
-        v[4 * i + 1] = x.y;
-        v[4 * i + 2] = x.z;
-        v[4 * i + 3] = x.w;
-    }
-}
-__device__ __forceinline__ uint32_t packBf16x2(float a, float b) {
-    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
-    return *reinterpret_cast<const uint32_t*>(&v);
-}
-
 // one thread: D[tmem] = A * B^T over K (multiple of 16), M = 128, N columns; operands in shared memory
 __device__ __forceinline__ void mmaTile(uint32_t tmem, uint32_t a, bool aMN, uint32_t b, bool bMN, int N, int K) {
     const uint32_t idesc = umma::idescBf16(128, N) | (aMN ? 1u << 15 : 0u) | (bMN ? 1u << 16 : 0u);
@@ -90,22 +68,6 @@ __device__ __forceinline__ void mmaTile(uint32_t tmem, uint32_t a, bool aMN, uin
         const uint64_t db = bMN ? descMN128(b + 2048u * s) : umma::descK128(b + uint32_t(s / 4) * uint32_t(N) * 128u + 32u * (s % 4));
         umma::mmaBf16(tmem, da, db, idesc, s > 0 ? 1u : 0u);
     }
-}
-
-// bulk copy global -> shared completing on mbarrier `bar` (bytes: multiple of 16, both 16-byte aligned)
-__device__ __forceinline__ void bulkLoad(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(umma::smemAddr(bar)), "r"(bytes) : "memory");
-    for (uint32_t o = 0; o < bytes; o += kBlk)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                         umma::smemAddr(static_cast<uint8_t*>(dst) + o)),
-                     "l"(static_cast<const uint8_t*>(src) + o), "r"(bytes - o < kBlk ? bytes - o : kBlk), "r"(umma::smemAddr(bar))
-                     : "memory");
-}
-
-__device__ __forceinline__ void bulkStore(void* dst, const void* src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst), "r"(umma::smemAddr(src)), "r"(bytes)
-                 : "memory");
-    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
 }
 
 __device__ __forceinline__ void redAdd4(float* p, float a, float b, float c, float d) {
@@ -139,14 +101,6 @@ __device__ __forceinline__ float warpColumnSum16(float v[16], int lane) {
         v[0] = keep + __shfl_xor_sync(FULLMASK, send, 2);
     }
     return v[0] + __shfl_xor_sync(FULLMASK, v[0], 1);
-}
-
-// 16 bf16 values (8 packed words) of row r, columns c0..c0+15 (c0 % 16 == 0), into a K-major tile
-__device__ __forceinline__ void storeRow16(uint8_t* tile, int r, int c0, const uint32_t w[8]) {
-    uint8_t* dst = tile + (c0 / 64) * kBlk + r * 128;
-    const int ca = (c0 % 64) / 8;
-    *reinterpret_cast<uint4*>(dst + ((ca ^ (r & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
-    *reinterpret_cast<uint4*>(dst + (((ca + 1) ^ (r & 7)) << 4)) = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
 struct Sync {

@@ -75,8 +75,7 @@ private:
     void release();
     std::vector<void*> mem_;
     float *params_ = nullptr, *grads_ = nullptr, *m_ = nullptr, *v_ = nullptr, *scalars_ = nullptr;
-    __nv_bfloat16 *W1_ = nullptr, *W234_ = nullptr;  // row-major bf16 weights (inference)
-    __nv_bfloat16* img_ = nullptr;                   // shared-memory images of W1..W4 (training)
+    __nv_bfloat16* img_ = nullptr;  // bf16 shared-memory images of W1..W4 (training and inference)
     int32_t* counters_ = nullptr;  // [0] step, [1] batch offset, [3] status
     Work* work_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;

@@ -117,5 +117,36 @@ __device__ __forceinline__ void tmemWaitLoads16(uint32_t r[16]) {
                  : "memory");
 }
 
+// 32 consecutive FP32 TMEM columns of this thread's lane: two loads, one tied wait each.
+__device__ __forceinline__ void tmemLoad32(uint32_t taddr, float v[32]) {
+    uint32_t r[32];
+    tmemLoad16Async(taddr, r);
+    tmemLoad16Async(taddr + 16, r + 16);
+    tmemWaitLoads16(r);
+    tmemWaitLoads16(r + 16);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// TMA bulk copy global -> shared completing on mbarrier `bar`, issued by one thread: arms the
+// barrier with the byte count, then copies in pieces of at most 16 KB (addresses 16-byte aligned,
+// bytes a multiple of 16).
+__device__ __forceinline__ void bulkLoad(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    constexpr uint32_t kPiece = 16384;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smemAddr(bar)), "r"(bytes) : "memory");
+    for (uint32_t o = 0; o < bytes; o += kPiece)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                         smemAddr(static_cast<uint8_t*>(dst) + o)),
+                     "l"(static_cast<const uint8_t*>(src) + o), "r"(bytes - o < kPiece ? bytes - o : kPiece), "r"(smemAddr(bar))
+                     : "memory");
+}
+
+// TMA bulk copy shared -> global (one thread), committed as a bulk group.
+__device__ __forceinline__ void bulkStore(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst), "r"(smemAddr(src)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+
 }  // namespace umma
 }  // namespace gbfwn
