@@ -1,0 +1,2 @@
+#pragma once
+#include "tbb_serial.h"

@@ -1,7 +1,10 @@
 """Marching cubes on the GPU against the restated reference mesher (oracle/mc_oracle.cpp), bit for
 bit: the same points (every float equal), the same triangles in the same order, the same face map.
 Covers the reference's cases: NaN voxels (nullOutsideMinMax bands), parts (MarchingCubesByParts),
-both orientations, odd sizes, the vertex limit, and the fused distance-grid -> mesh call."""
+both orientations, odd sizes, the vertex limit, and the fused distance-grid -> mesh call; and, through
+tests/golden/mc_reference.npz, the outputs of MeshLib's own mesher compiled from its sources."""
+import os
+
 import numpy as np
 import pytest
 
@@ -296,3 +299,29 @@ def test_single_cells(M, vals):
     for li in (False, True):
         _same(M.marchingCubes(vol, M.MarchingCubesParams(lessInside=li, outVoxelPerFaceMap=True)),
               O.marching_cubes(vol, less_inside=li))
+
+
+_GOLDEN = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mc_reference.npz"))
+
+
+@pytest.mark.parametrize("name", [str(c) for c in _GOLDEN["cases"]])
+def test_matches_reference_mesher(M, name):
+    """The CUDA mesher against the outputs of MeshLib's own mesher (MRVoxels/MRMarchingCubes.cpp,
+    compiled from its sources) stored in tests/golden/mc_reference.npz: points bit for bit, the same
+    triangles in the same order, the same face map, and the reference's error messages."""
+    p = _GOLDEN[f"{name}/params"]
+    parts = _GOLDEN[f"{name}/parts"]
+    vol = _GOLDEN[f"{name}/vol"]
+    prm = M.MarchingCubesParams(origin=tuple(p[0:3]), voxelSize=tuple(p[3:6]), iso=float(p[6]), lessInside=bool(p[7]),
+                                maxVertices=int(p[8]), outVoxelPerFaceMap=True)
+    err = str(_GOLDEN[f"{name}/error"])
+    starts = parts if len(parts) else None
+    if err:
+        with pytest.raises(M.FwnError, match=err.rstrip(".")):
+            M.marchingCubes(vol, prm, partStarts=starts)
+        return
+    tm = M.marchingCubes(vol, prm, partStarts=starts)
+    ref = (_GOLDEN[f"{name}/points"], _GOLDEN[f"{name}/tris"], _GOLDEN[f"{name}/faceMap"])
+    assert tm.numPoints == len(ref[0]) and tm.numTris == len(ref[1])
+    if len(ref[0]):
+        _same(tm, ref)
