@@ -4,7 +4,7 @@
 // `VolumeMesher` (the engine of `marchingCubes(SimpleVolume)` and `MarchingCubesByParts`) so that
 // the CUDA mesher can be checked against it bit for bit.  Only the tests and the CPU-baseline leg
 // of the benchmark load it; the product never does.  It is itself pinned to MeshLib's own mesher,
-// compiled from the reference sources (oracle/ref/build_mc_ref.py): tests/test_mc_golden_cpu.py
+// compiled from the reference sources (oracle/ref/build_cpu_ref.py): tests/test_mc_golden_cpu.py
 // compares it with that mesher's outputs in tests/golden/mc_reference.npz, bit for bit.
 //
 // Reference files restated here (paths inside the MeshLib project):

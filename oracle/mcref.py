@@ -1,5 +1,5 @@
 """ctypes front-end of MeshLib's own CPU mesher, built from the reference sources into
-oracle/_ref/libmcref.so by oracle/ref/build_mc_ref.py (x86-64 hosts with a copy of the reference).
+oracle/_ref/libmcref.so by oracle/ref/build_cpu_ref.py (x86-64 hosts with a copy of the reference).
 
 TEST INFRASTRUCTURE ONLY: used to generate tests/golden/mc_reference.npz and, where the library
 exists, to re-check that fixture.  Same calling convention as oracle.marching_cubes.

@@ -1,5 +1,5 @@
 // C entry points around MeshLib's own mesher (MRVoxels/MRMarchingCubes.cpp, compiled from the
-// reference sources by oracle/ref/build_mc_ref.py), used only to produce the golden vectors that
+// reference sources by oracle/ref/build_cpu_ref.py), used only to produce the golden vectors that
 // pin the mesher oracle (oracle/mc_oracle.cpp) and, through them, the CUDA mesher.
 // TEST INFRASTRUCTURE ONLY: nothing in the product loads this.
 //

@@ -1,5 +1,5 @@
 """Generates tests/golden/mc_reference.npz: outputs of MeshLib's own CPU mesher
-(MRVoxels/MRMarchingCubes.cpp, compiled from the reference sources by oracle/ref/build_mc_ref.py and
+(MRVoxels/MRMarchingCubes.cpp, compiled from the reference sources by oracle/ref/build_cpu_ref.py and
 called through oracle/mcref.py) on small seeded volumes.
 
 Run on an x86-64 machine with a copy of the reference:
@@ -86,8 +86,8 @@ def cases():
 
 def main(path=OUT):
     import oracle.mcref as R
-    from oracle.ref import build_mc_ref
-    if build_mc_ref.build() is None:
+    from oracle.ref import build_cpu_ref
+    if not build_cpu_ref.build(targets=("libmcref.so",)):
         raise SystemExit("the reference mesher could not be built here (no copy of the reference)")
     arrays = {}
     names = []

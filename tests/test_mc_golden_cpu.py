@@ -1,7 +1,7 @@
 """The mesher oracle (oracle/mc_oracle.cpp) against MeshLib's own mesher, bit for bit.
 
 tests/golden/mc_reference.npz holds the outputs of the reference's MRVoxels/MRMarchingCubes.cpp,
-compiled from its own sources (oracle/ref/build_mc_ref.py) and run on seeded volumes by
+compiled from its own sources (oracle/ref/build_cpu_ref.py) and run on seeded volumes by
 tests/golden/make_mc_golden.py: the reference's own test input, distance and density volumes,
 z-blocks of several sizes, MarchingCubesByParts with even and uneven parts, NaN voxels, ragged and
 degenerate sizes, a volume with every crossing cube configuration, and the reference's error cases
