@@ -1,9 +1,10 @@
-// A serial stand-in for the parts of oneTBB that MeshLib's mesher translation unit
-// (MRVoxels/MRMarchingCubes.cpp) and the headers it includes use, so that the reference mesher can
-// be compiled from its own sources for the oracle's golden vectors without the un-vendored TBB.
-// Every parallel algorithm runs its body once over the whole range on the calling thread; the
-// mesher's output does not depend on the thread count (its vertex ids are block-local counts
-// shifted by prefix sums), except through the block partition, which is passed explicitly.
+// A serial stand-in for the parts of oneTBB that the MeshLib units compiled by
+// oracle/ref/build_cpu_ref.py (the mesher, and the winding-number path with its mesh, tree and
+// projection) use, so that the reference's CPU code can be compiled from its own sources for the
+// oracle's golden vectors without the un-vendored TBB.  Every parallel algorithm runs its body once
+// over the whole range on the calling thread.  The outputs do not depend on the thread count: the
+// mesher's vertex ids are block-local counts shifted by prefix sums (its block partition is passed
+// explicitly), and every winding-number / distance query is evaluated independently.
 // TEST INFRASTRUCTURE ONLY.
 #pragma once
 #include <algorithm>

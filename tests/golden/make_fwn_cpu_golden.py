@@ -13,7 +13,7 @@ Contents (float32 unless noted; digests are SHA-256 of the arrays' bytes):
                 sdf_band  the same with maxDistSq = (0.05 diag)^2, minDistSq = (0.01 diag)^2 (NaN outside)
                 fwn       calcFromGrid, beta 2
                 fwn_pts   calcFromVector at 2,048 seeded points with face 11 skipped
-                proj_dsq / proj_face   findProjection at the same points
+                proj_dsq / proj_face / proj_point   findProjection at the same points
   spheres_selfint   calcSelfIntersections bits (uint8) of two overlapping level-3 spheres
   ico_*         the 1,310,720-triangle noisy icosphere (seed 0, level 8) on grid_for(v, 512):
                 nodes_digest / dipoles_digest, ids (int64: 2,048 seeded voxels, half of them within
@@ -95,8 +95,8 @@ def main(out: str = OUT):
     res["torus_sdf_band"] = R.from_grid_with_distances(dims, xf, minDistSq=(0.01 * diag) ** 2, maxDistSq=(0.05 * diag) ** 2)
     res["torus_fwn"] = R.from_grid(dims, xf)
     res["torus_fwn_pts"] = R.from_vector(pts, skip_face=11)
-    dsq, face, _, _, _ = R.project(pts)
-    res["torus_proj_dsq"], res["torus_proj_face"] = dsq, face
+    dsq, face, point, _, _ = R.project(pts)
+    res["torus_proj_dsq"], res["torus_proj_face"], res["torus_proj_point"] = dsq, face, point
     res["digest_torus"] = np.array(digest(v, f, pts))
     sv, sf = spheres_inputs()
     res["spheres_selfint"] = FR.Reference(sv, sf).self_intersections().astype(np.uint8)

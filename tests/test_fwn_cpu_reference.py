@@ -142,7 +142,11 @@ def test_library_matches_cpu_reference_torus(gold, torus, fwn_lib):
         pr = M.PointsToMeshProjector.from_mesh(g).findProjections(pts)
         dd = np.abs(np.sqrt(pr["distSq"].astype(np.float64)) - np.sqrt(gold["torus_proj_dsq"].astype(np.float64)))
         assert dd.max() <= 1e-5 * diag
-        assert (pr["face"] == gold["torus_proj_face"]).mean() > 0.99  # the rest: ties at a shared vertex / edge
+        # a different face is a tie at the same closest point (a shared vertex or edge) but for queries
+        # equidistant from two parts of the surface within FP32 precision
+        diff = pr["face"] != gold["torus_proj_face"]
+        moved = np.abs(pr["point"][diff] - gold["torus_proj_point"][diff]).max(1) > 1e-5 * diag
+        assert moved.sum() <= max(2, len(pts) // 500)
 
 
 @pytest.mark.gpu
