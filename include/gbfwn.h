@@ -86,6 +86,21 @@ typedef int (*gbfwn_slab_cb)(const float* data, const int32_t dims[3], int32_t z
  * a few ulps of a triangle plane.  precise = 0: the reference's FP32 arithmetic, plain sums. */
 GBFWN_API void gbfwn_set_precise(gbfwn_handle h, int precise);
 
+/* Sign reuse in signed-distance grids (default on).  When the mesh's valid faces form a closed
+ * oriented surface (every edge used equally often in both directions; gbfwn_is_closed), the exact
+ * winding number is an integer that stays constant along any segment not meeting the surface.  A
+ * voxel whose neighbour below lies closer to it than that neighbour's distance to the surface then
+ * takes the neighbour's sign instead of evaluating its own winding number: the same sign, because
+ * both approximated winding numbers lie within their (far smaller than 0.5) approximation error of
+ * the same integer.  Used only with windingNumberBeta >= 2 and a threshold whose fractional part
+ * lies in (0.25, 0.75) (the default 0.5); distances are unaffected.  enable = 0 evaluates every
+ * voxel's winding number, as the reference does. */
+GBFWN_API void gbfwn_set_sign_reuse(gbfwn_handle h, int enable);
+
+/* 1 if the mesh's valid faces form a closed oriented surface (fingerprint of the directed edges,
+ * computed when the handle is created), else 0. */
+GBFWN_API int gbfwn_is_closed(gbfwn_handle h);
+
 /* Library version string. */
 GBFWN_API const char* gbfwn_version(void);
 

@@ -91,6 +91,8 @@ _SIGS = [
     ("gbfwn_version", ctypes.c_char_p, []),
     ("gbfwn_last_error", ctypes.c_char_p, []),
     ("gbfwn_set_precise", None, [_vp, ctypes.c_int]),
+    ("gbfwn_set_sign_reuse", None, [_vp, ctypes.c_int]),
+    ("gbfwn_is_closed", ctypes.c_int, [_vp]),
     ("gbfwn_create", ctypes.c_int, [_vp, _i64, _vp, _i64, ctypes.c_int, ctypes.POINTER(_vp)]),
     ("gbfwn_create_dev", ctypes.c_int, [_vp, _i64, _vp, _i64, ctypes.c_int, ctypes.POINTER(_vp)]),
     ("gbfwn_destroy", ctypes.c_int, [_vp]),
@@ -264,6 +266,16 @@ class FastWindingNumber:
 
     def set_precise(self, precise: bool):
         self._L.gbfwn_set_precise(self._h, 1 if precise else 0)
+
+    def set_sign_reuse(self, enable: bool):
+        """Signed-distance grids of a closed surface take a voxel's sign from the voxel below it when
+        no surface lies between them (default on; gbfwn_set_sign_reuse in include/gbfwn.h)."""
+        self._L.gbfwn_set_sign_reuse(self._h, 1 if enable else 0)
+
+    def is_closed(self) -> bool:
+        """True if the valid faces form a closed oriented surface (every edge used equally often in
+        both directions)."""
+        return bool(self._L.gbfwn_is_closed(self._h))
 
     def refit(self, verts: np.ndarray, changedVerts: Optional[np.ndarray] = None):
         """MR::AABBTree::refit + dipoles for moved vertices (same triangles).  ``changedVerts``: bool

@@ -449,8 +449,8 @@ inline unsigned blocksFor(int64_t n, int t) { return unsigned((n + t - 1) / t); 
 
 // Device tree construction of the reference topology (treebuild.cu).
 cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, int64_t& nLeaves,
-                             RefNode*& nodes, int32_t*& irs, int2*& range, Allocator& P, Allocator& A, cudaStream_t s,
-                             std::string& err);
+                             RefNode*& nodes, int32_t*& irs, int2*& range, bool& closed, Allocator& P, Allocator& A,
+                             cudaStream_t s, std::string& err);
 
 // Dipoles and the query layout on the device from the reference nodes in `out.nodes`; `irs` holds
 // the internal rank and leaf slot of every node, `range` its leaf-slot range (device arrays).
@@ -511,6 +511,7 @@ static cudaError_t setQueryRoot(DeviceTree& out, cudaStream_t s) {
     q.faceSlot = out.faceSlot;
     q.nLeaves = int32_t(out.nLeaves);
     q.nFaces = int32_t(out.nFaces);
+    q.closed = out.closed ? 1 : 0;
     if (nLeaves > 0) {  // root data for the kernels' parameter block
         float rd[8];
         RefNode r;
@@ -534,7 +535,7 @@ cudaError_t buildDeviceTree(const float* dVerts, int64_t nv, const int32_t* dTri
     int64_t nLeaves = 0;
     int32_t* irs = nullptr;
     int2* range = nullptr;
-    if ((e = gpuBuildTopology(dVerts, nv, dTris, nt, nLeaves, out.nodes, irs, range, P, T, s, err))) return e;
+    if ((e = gpuBuildTopology(dVerts, nv, dTris, nt, nLeaves, out.nodes, irs, range, out.closed, P, T, s, err))) return e;
     out.nFaces = nt;
     out.nLeaves = nLeaves;
     out.nInternal = nLeaves > 0 ? nLeaves - 1 : 0;

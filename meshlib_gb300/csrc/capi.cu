@@ -168,6 +168,7 @@ int createCommon(gbfwn_mesh_s* h, const std::string& where) {
     cudaError_t e = buildDeviceTree(h->dVerts, h->nv, h->dTris, h->nt, h->tree, h->treeMem, tmp, h->stream, err);
     cudaStreamSynchronize(h->stream);
     tmp.freeAll();
+    h->applySignReuse();
     if (e == cudaErrorInvalidValue && !err.empty()) return fail(GBFWN_INVALID, err);
     if (e) return cudaFail(e, where.c_str());
     return GBFWN_OK;
@@ -192,6 +193,24 @@ int newHandle(int device, gbfwn_mesh_s** out) {
     return GBFWN_OK;
 }
 
+// The column hand-over words of a signed-distance grid launch on stream s, grown on the handle's
+// stream (a launch on another stream waits for the growth).  Without them (allocation failure) the
+// launch runs as well, its columns starting cold.
+float* colStateFor(gbfwn_mesh_s* h, const GridRange& r, const DistOpts& o, cudaStream_t s, size_t* bytes) {
+    const size_t need = gridSdfColumnStateBytes(r, o);
+    *bytes = 0;
+    if (need == 0) return nullptr;
+    if (h->colCap < need) {
+        if (h->ensure(&h->colBuf, &h->colCap, need)) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (s != h->stream) cudaStreamSynchronize(h->stream);
+    }
+    *bytes = h->colCap;
+    return static_cast<float*>(h->colBuf);
+}
+
 int refitCommon(gbfwn_mesh_s* h, const uint64_t* dChanged, cudaStream_t s, const char* what) {
     ListAllocator tmp;  // refit work arrays
     tmp.device = h->device;
@@ -199,6 +218,7 @@ int refitCommon(gbfwn_mesh_s* h, const uint64_t* dChanged, cudaStream_t s, const
     cudaError_t e = refitDeviceTree(h->dVerts, h->nv, h->dTris, dChanged, h->tree, h->treeMem, tmp, s);
     cudaStreamSynchronize(s);
     tmp.freeAll();
+    h->applySignReuse();
     return e ? cudaFail(e, what) : GBFWN_OK;
 }
 
@@ -225,6 +245,15 @@ GBFWN_API int gbfwn_release_cached_memory(int device) {
 GBFWN_API void gbfwn_set_precise(gbfwn_handle h, int precise) {
     if (h) h->precise = precise ? 1 : 0;
 }
+
+GBFWN_API void gbfwn_set_sign_reuse(gbfwn_handle h, int enable) {
+    if (!h) return;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->signReuse = enable ? 1 : 0;
+    h->applySignReuse();
+}
+
+GBFWN_API int gbfwn_is_closed(gbfwn_handle h) { return h && h->tree.closed ? 1 : 0; }
 
 GBFWN_API int gbfwn_create(const float* verts, int64_t nv, const int32_t* tris, int64_t nt, int device, gbfwn_handle* out) {
     if (!out || nv < 0 || nt < 0 || (nv > 0 && !verts) || (nt > 0 && !tris)) return fail(GBFWN_INVALID, "gbfwn_create: bad arguments");
@@ -296,6 +325,7 @@ GBFWN_API int gbfwn_destroy(gbfwn_handle h) {
         poolFree(h->outBuf, h->stream);
         poolFree(h->inBuf, h->stream);
         poolFree(h->sortBuf, h->stream);
+        poolFree(h->colBuf, h->stream);
         if (h->stream) cudaStreamSynchronize(h->stream);
         for (auto ev : h->events) cudaEventDestroy(ev);
         if (h->stream) cudaStreamDestroy(h->stream);
@@ -441,7 +471,10 @@ GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t d
     DeviceGuard g(h->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
-    cudaError_t e = launchGridSdf(h->tree.q, r, X, toOpts(opts), h->precise, d_out, h->scratch, s);
+    const DistOpts o = toOpts(opts);
+    size_t colBytes = 0;
+    float* col = colStateFor(h, r, o, s, &colBytes);
+    cudaError_t e = launchGridSdf(h->tree.q, r, X, o, h->precise, d_out, h->scratch, s, col, colBytes);
     return e ? cudaFail(e, "gbfwn_from_grid_with_distances_dev") : GBFWN_OK;
 }
 
@@ -466,7 +499,10 @@ GBFWN_API int gbfwn_from_grid_with_distances_slab_dev(gbfwn_handle h, const int3
     DeviceGuard g(h->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     GridRange r{dims[0], dims[1], dims[2], z0, z1, z0};
-    cudaError_t e = launchGridSdf(h->tree.q, r, X, toOpts(opts), h->precise, d_out, h->scratch, s);
+    const DistOpts o = toOpts(opts);
+    size_t colBytes = 0;
+    float* col = colStateFor(h, r, o, s, &colBytes);
+    cudaError_t e = launchGridSdf(h->tree.q, r, X, o, h->precise, d_out, h->scratch, s, col, colBytes);
     return e ? cudaFail(e, "gbfwn_from_grid_with_distances_slab_dev") : GBFWN_OK;
 }
 
@@ -733,7 +769,9 @@ GBFWN_API int gbfwn_from_grid_with_distances(gbfwn_handle h, const int32_t dims[
     return runGrid(
         h, dims,
         [&](const GridRange& r, float* buf, cudaStream_t s) {
-            return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s);
+            size_t colBytes = 0;
+            float* col = colStateFor(h, r, o, s, &colBytes);
+            return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s, col, colBytes);
         },
         out, 0, 0, nullptr, nullptr, cb, user, "gbfwn_from_grid_with_distances");
 }
@@ -767,7 +805,9 @@ GBFWN_API int gbfwn_from_grid_with_distances_by_parts(gbfwn_handle h, const int3
     return runGrid(
         h, dims,
         [&](const GridRange& r, float* buf, cudaStream_t s) {
-            return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s);
+            size_t colBytes = 0;
+            float* col = colStateFor(h, r, o, s, &colBytes);
+            return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s, col, colBytes);
         },
         nullptr, layerOverlap, maxLayersPerSlab, slab, slabUser, cb, user, "gbfwn_from_grid_with_distances_by_parts");
 }
@@ -786,9 +826,13 @@ GBFWN_API size_t gbfwn_mesh_memory(int64_t nv, int64_t nt) {
     const size_t build = n * 244;
     return kept + build + (size_t(32) << 20);
 }
+// plus the result and, for signed distances, the columns' hand-over words: 128 B per column work
+// item of 16 or 32 tiles, or of fewer while under 50 items per resident warp remain
 GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t dims[3]) {
     const size_t vox = dims ? size_t(std::max(dims[0], 0)) * size_t(std::max(dims[1], 0)) * size_t(std::max(dims[2], 0)) : 0;
-    return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float);
+    const size_t tiles = (dims && vox) ? size_t(gridTiles(dims[0], dims[1], dims[2])) : 0;
+    const size_t items = std::min(tiles, tiles / 16 + size_t(50) * size_t(numSMs()) * 32);
+    return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float) + items * 32 * sizeof(float);
 }
 // staging: points in (12 B) and results out (4 B); from 8,192 points also the Morton order and its
 // sort scratch (6 int32 words per point)

@@ -43,6 +43,10 @@ struct QueryTree {
     float4 rootBox0, rootBox1;             // {min.xyz, rootLink} {max.xyz, 0}
     int32_t nLeaves;
     int32_t nFaces;
+    // 1: the faces form a closed oriented surface (every edge used equally often in both
+    // directions) and a signed-distance voxel may take its sign from the voxel below it when no
+    // surface lies between them (gridKernel); 0: every sign comes from its own winding number
+    int32_t closed;
 };
 
 struct Xf {
@@ -74,8 +78,11 @@ enum : unsigned {
 // queue ticket counter, [1] = status bits.  The launchers reset the ticket counter themselves.
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
                           unsigned* scratch, cudaStream_t s);
+// colState (optional, colBytes >= gridSdfColumnStateBytes): device words through which the columns of
+// the launch hand their top layer's distances, signs and closest triangles to the columns above.
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
-                          float* out, unsigned* scratch, cudaStream_t s);
+                          float* out, unsigned* scratch, cudaStream_t s, float* colState = nullptr, size_t colBytes = 0);
+size_t gridSdfColumnStateBytes(const GridRange& g, const DistOpts& o);
 // One mesh + grid of a batched launch (query.cu batchKernel): its tickets are
 // [tileBase, tileBase + batchTiles(...)): columns of up to kBatchSeg tiles of the launch's shape.
 struct BatchItem {
@@ -120,6 +127,7 @@ cudaError_t launchSelfIntersections(const QueryTree& t, float beta, int precise,
 // Tree/dipole construction (build.cu).
 struct DeviceTree {
     int64_t nFaces = 0, nLeaves = 0, nInternal = 0;
+    bool closed = false;  // the valid faces form a closed oriented surface (treebuild.cu, validFaces)
     RefNode* nodes = nullptr;   // 2n-1 reference nodes
     float* dip8 = nullptr;      // 2n-1 x 8 reference dipoles
     float4* cp = nullptr;

@@ -72,6 +72,8 @@ struct gbfwn_mesh_s {
     int64_t nv = 0, nt = 0;
     unsigned* scratch = nullptr;  // [0] ticket counter, [1] status bits
     int precise = 1;
+    int signReuse = 1;  // signed-distance grids of closed surfaces may take a voxel's sign from the voxel below
+    void applySignReuse() { tree.q.closed = (signReuse && tree.closed) ? 1 : 0; }
     // device staging reused across host-API calls
     void* outBuf = nullptr;
     size_t outCap = 0;
@@ -79,6 +81,8 @@ struct gbfwn_mesh_s {
     size_t inCap = 0;
     void* sortBuf = nullptr;  // Morton order + radix-sort scratch of point queries
     size_t sortCap = 0;
+    void* colBuf = nullptr;  // column hand-over words of signed-distance grid launches
+    size_t colCap = 0;
     std::vector<cudaEvent_t> events;
     std::mutex mu;  // calls on one handle are serialised (the reference is not re-entrant per object)
     std::atomic<int> batchRefs{0};  // live batches whose work items point into this handle's tree

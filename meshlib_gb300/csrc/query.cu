@@ -467,6 +467,12 @@ struct TileGrid {
     // work items: columns of up to segLen tiles along z (4 per brick: its 2 x 2 columns)
     int32_t segLen, segsZ;
     uint32_t numItems;
+    // optional hand-over between the columns of one launch (whole grids only): 32 words per work
+    // item, written when the item ends -- words 0..15 the signed squared distance of each top-layer
+    // voxel (negative inside, NaN when its sign is unknown), words 16..31 the leaf slot closest to it
+    // (-1 none) -- and read by the column above it when it starts; filled with 0xff bytes (NaN / -1)
+    // before the launch, so a column that starts before the one below it has ended starts cold
+    float* colState;
 };
 
 __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
@@ -475,11 +481,27 @@ __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
     return __shfl_sync(FULL, t, 0);
 }
 
-// A warp takes a column of tiles along z and walks it upwards; each lane starts its closest-point
-// search from the triangle that was closest to its voxel two layers below (the same lane of the
-// previous tile).  That triangle's distance is an upper bound the search would reach anyway, so the
-// minimum is unchanged, but it prunes from the first step (a third fewer node visits with an exact
-// bound, in a CPU model of the walk).
+// Whether a signed-distance voxel may take its sign from a voxel below it (closed surfaces only):
+// the exact winding number of a closed oriented surface is an integer, constant along any segment
+// that does not meet the surface, and the segment between two voxel centres meets none when it is
+// shorter than the lower voxel's distance to the surface.  The approximated winding numbers of both
+// voxels then lie within their approximation error of the same integer, so with the threshold away
+// from integers (fractional part in (0.25, 0.75)) and the dipole criterion at beta >= 2 they fall on
+// the same side of it, and the sign computed below is the one the upper voxel's own winding number
+// would give.
+__device__ __forceinline__ bool signReuseAllowed(const QueryTree& t, const DistOpts& o) {
+    const float fr = o.threshold - floorf(o.threshold);
+    return t.closed != 0 && o.beta >= 2.f && fr > 0.25f && fr < 0.75f;
+}
+
+// A warp takes a column of tiles along z and walks it upwards.  Each lane starts its closest-point
+// search from the triangle that was closest to a voxel just below its own: the bottom layer of a
+// tile from the voxel one layer below (the previous tile's top layer), the top layer from its own
+// voxel of the previous tile, two layers below.  That triangle's distance is an upper bound the
+// search would reach anyway, so the minimum is unchanged, but it prunes from the first step (a third
+// fewer node visits with an exact bound, in a CPU model of the walk).  On a closed surface the same
+// voxel below also lends its sign (signReuseAllowed) when its distance exceeds the step between the
+// two voxel centres, and the lane skips its winding-number walk.
 template <bool PRECISE, bool DIST>
 __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
                                                        float* __restrict__ out, unsigned* scratch) {
@@ -487,6 +509,7 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
     const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
     const float betaSq = __fmul_rn(o.beta, o.beta);
     const size_t sxy = size_t(g.nx) * g.ny;
+    const bool reuseOk = DIST && signReuseAllowed(t, o);
     for (;;) {
         const unsigned item = nextTicket(scratch, lane);
         if (item >= tg.numItems) break;
@@ -509,7 +532,18 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
             nSeg = min(tg.segLen, tg.tilesZ - sz * tg.segLen);
         }
         const int x = x0 + lx, y = y0 + ly;
-        int seed = -1;  // leaf slot closest to this lane's previous voxel
+        int seed = -1;  // leaf slot closest to the voxel below
+        // that voxel's squared distance with its side in the sign bit (negative inside), NaN when
+        // its sign is unknown
+        float below = __int_as_float(0x7fc00000);
+        const uint32_t colsPerSlab = uint32_t(tg.tilesX) * uint32_t(tg.tilesY);
+        if (DIST && tg.colState && !tg.bricks && item >= colsPerSlab) {
+            // the column below ended (its state was written) or not yet (0xff bytes: start cold); the
+            // voxel below both layers of the first tile is that column's top-layer voxel
+            const float* cs = tg.colState + size_t(item - colsPerSlab) * 32;
+            below = __ldcg(cs + (lane & 15));
+            seed = __float_as_int(__ldcg(cs + 16 + (lane & 15)));
+        }
         for (int j = 0; j < nSeg; ++j) {
             const int z = zBase + j * kTZ + lz;
             const bool active = x < g.nx && y < g.ny && z < g.z1;
@@ -524,19 +558,46 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
                 }
                 int best = active ? seed : -1;
                 const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
-                // next tile: the bottom layer's lanes start from the triangle of the voxel one layer
-                // below them (this tile's top layer), the others from their own voxel two layers below
-                const int fromBelow = __shfl_sync(FULL, best, lane + (kTZ - 1) * kTX * kTY * (lz == 0));
-                seed = lz == 0 ? fromBelow : best;
                 const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
-                const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
+                bool reuse = false;
+                if (reuseOk && fabsf(below) > 0.f) {
+                    // the voxel below (its centre recomputed exactly as it was evaluated) is farther
+                    // from the surface than from this voxel, with a margin for the FP32 rounding of
+                    // both centres and of the distance, relative to the coordinates' magnitude
+                    const float3 qb = xfPoint(xf, x, y, z - (lz == 0 ? 1 : kTZ));
+                    const float dx = q.x - qb.x, dy = q.y - qb.y, dz = q.z - qb.z;
+                    const float step = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                    const float db = sqrtf(fabsf(below));
+                    const float mag = fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z)));
+                    reuse = db > fmaf(step, 1.0001f, 2e-6f * fmaf(3.f, mag, db));
+                }
+                const float w = fwnPacket<PRECISE>(t, q, active && valid && !reuse, betaSq, -1, scratch + 1);
+                const bool inside = reuse ? signbit(below) : w > o.threshold;
                 const float d = __fsqrt_rn(dsq);
-                res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+                res = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
+                // next tile: the bottom layer's lanes take the voxel one layer below them (this tile's
+                // top layer), the others their own voxel two layers below.  A distance counts only when
+                // the search ran to the end (not cut short below minDistSq): no surface is closer then.
+                const int src = lane + (kTZ - 1) * kTX * kTY * (lz == 0);
+                const float mine = (active && valid && dsq >= o.minDistSq) ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000);
+                seed = __shfl_sync(FULL, best, src);
+                below = __shfl_sync(FULL, mine, src);
+                if (tg.colState && !tg.bricks && j == nSeg - 1) {
+                    // the column's last tile: every lane now holds the state of the top-layer voxel of
+                    // its (x, y); lanes 0..15 pass on the distances, lanes 16..31 (the same 16
+                    // columns) the seeds, at this work item's words (the item recomputed from the
+                    // column's position, so no register holds it through the walk)
+                    const uint32_t sz = uint32_t(zBase - g.z0) / uint32_t(tg.segLen * kTZ);
+                    const uint32_t it = uint32_t(x0) / kTX + uint32_t(tg.tilesX) * (uint32_t(y0) / kTY + uint32_t(tg.tilesY) * sz);
+                    tg.colState[size_t(it) * 32 + lane] = lane < 16 ? below : __int_as_float(seed);
+                }
             } else {
                 res = fwnPacket<PRECISE>(t, q, active, betaSq, -1, scratch + 1);
             }
             if (active) out[size_t(z - g.zOut) * sxy + size_t(y) * g.nx + x] = res;
         }
+        // every lane now holds the state of the top-layer voxel of its (x, y): lanes 0..15 pass on the
+        // distances, lanes 16..31 (the same 16 columns) the seeds
     }
 }
 
@@ -791,6 +852,7 @@ static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
     tg.numTiles = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.tilesZ);
     tg.bricks = nullptr;
     tg.bricksX = tg.bricksY = 0;
+    tg.colState = nullptr;
     // Longer columns reuse more seeds; shorter ones leave more items for the tail of the persistent
     // grid.  Measured at 256^3 / 512^3 on 1.3 M triangles: keep >= 25 items per (32-warps-per-SM)
     // resident warp, and columns of at most 32 tiles for unbanded signed distances (512^3: 16 tiles
@@ -827,9 +889,19 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
     return launchPersistent(gridKernel<false, false>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
+size_t gridSdfColumnStateBytes(const GridRange& g, const DistOpts& o) {
+    return size_t(tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16).numItems) * 32 * sizeof(float);
+}
+
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
-                          unsigned* scratch, cudaStream_t s) {
-    const TileGrid tg = tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16);
+                          unsigned* scratch, cudaStream_t s, float* colState, size_t colBytes) {
+    TileGrid tg = tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16);
+    const size_t need = size_t(tg.numItems) * 32 * sizeof(float);
+    if (colState && colBytes >= need && need > 0) {
+        cudaError_t e = cudaMemsetAsync(colState, 0xff, need, s);
+        if (e) return e;
+        tg.colState = colState;
+    }
     if (precise)
         return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
     return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);

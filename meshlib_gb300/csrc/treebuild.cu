@@ -199,14 +199,50 @@ __global__ void scanAdd(int32_t* out, int64_t n, const int32_t* sums) {
 }
 
 // ---------------------------------------------------------------- leaves
+// 64-bit mixing function (the splitmix64 finalizer of Steele, Lea and Flood, 2014).
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// H(a, b) - H(b, a) for the directed edge a -> b under the hash with the given seed.
+__device__ __forceinline__ uint64_t edgeTerm(uint32_t a, uint32_t b, uint64_t seed) {
+    return mix64(((uint64_t(a) << 32) | b) + seed) - mix64(((uint64_t(b) << 32) | a) + seed);
+}
+
+// Valid-face flags and the closedness fingerprint of the valid faces: the sum over their directed
+// edges a -> b of H(a, b) - H(b, a), for two seeded 64-bit hashes H.  An undirected edge {a, b}
+// contributes (n(a->b) - n(b->a)) (H(a, b) - H(b, a)), so both sums are zero when every edge is
+// used as often in each direction -- the faces form a closed oriented surface (a 2-cycle: possibly
+// non-manifold or self-intersecting), whose exact winding number is an integer constant on each
+// connected region of space off the surface -- and are both zero by chance for an open surface
+// with probability about 2^-128.
 __global__ void validFaces(const int32_t* __restrict__ tris, int64_t nt, int64_t nv, int32_t* __restrict__ flag,
-                           int32_t* __restrict__ err) {
+                           int32_t* __restrict__ err, unsigned long long* __restrict__ fingerprint) {
     const int64_t f = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-    if (f >= nt) return;
-    const int32_t a = tris[3 * f], b = tris[3 * f + 1], c = tris[3 * f + 2];
-    const bool valid = a >= 0 && b >= 0 && c >= 0;
-    if (a >= nv || b >= nv || c >= nv) atomicOr(err, 1);
-    flag[f] = valid ? 1 : 0;
+    uint64_t s0 = 0, s1 = 0;
+    if (f < nt) {
+        const int32_t a = tris[3 * f], b = tris[3 * f + 1], c = tris[3 * f + 2];
+        const bool valid = a >= 0 && b >= 0 && c >= 0;
+        if (a >= nv || b >= nv || c >= nv) atomicOr(err, 1);
+        flag[f] = valid ? 1 : 0;
+        if (valid) {
+            constexpr uint64_t k0 = 0x9e3779b97f4a7c15ull, k1 = 0xd1b54a32d192ed03ull;
+            s0 = edgeTerm(a, b, k0) + edgeTerm(b, c, k0) + edgeTerm(c, a, k0);
+            s1 = edgeTerm(a, b, k1) + edgeTerm(b, c, k1) + edgeTerm(c, a, k1);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (s0 | s1)) {
+        atomicAdd(fingerprint, (unsigned long long)s0);
+        atomicAdd(fingerprint + 1, (unsigned long long)s1);
+    }
 }
 
 // MRMesh/MRAABBTree.cpp:15-29: box of the three vertices, then one ulp outwards (MRBox.h:260-270)
@@ -619,10 +655,11 @@ cudaError_t exclusiveScan(const int32_t* in, int32_t* out, int64_t n, int32_t* s
 // temporary allocator A like every other work array.  nLeaves = number
 // of valid faces.  Returns cudaErrorInvalidValue with `err` set when a vertex id is out of range.
 cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTris, int64_t nt, int64_t& nLeaves,
-                             RefNode*& nodes, int32_t*& irs, int2*& range, Allocator& P, Allocator& A, cudaStream_t s,
-                             std::string& err) {
+                             RefNode*& nodes, int32_t*& irs, int2*& range, bool& closed, Allocator& P, Allocator& A,
+                             cudaStream_t s, std::string& err) {
     cudaError_t e;
     nLeaves = 0;
+    closed = false;
     nodes = nullptr;
     irs = nullptr;
     range = nullptr;
@@ -632,18 +669,20 @@ cudaError_t gpuBuildTopology(const float* dVerts, int64_t nv, const int32_t* dTr
     if ((e = A.alloc((void**)&flag, sizeof(int32_t) * size_t(nt)))) return e;
     if ((e = A.alloc((void**)&pos, sizeof(int32_t) * size_t(nt)))) return e;
     if ((e = A.alloc((void**)&sums, sizeof(int32_t) * size_t(nbMax)))) return e;
-    if ((e = A.alloc((void**)&misc, sizeof(int32_t) * 32))) return e;  // [0] error, [1] total, [3] nsmall, [16..31] pending per pass
+    // [0] error, [1] total, [3] nsmall, [4..7] closedness fingerprint (2 x u64), [16..31] pending per pass
+    if ((e = A.alloc((void**)&misc, sizeof(int32_t) * 32))) return e;
     int32_t* pend = misc + 16;
     if ((e = cudaMemsetAsync(misc, 0, sizeof(int32_t) * 8, s))) return e;
-    validFaces<<<blocks(nt, 256), 256, 0, s>>>(dTris, nt, nv, flag, misc);
+    validFaces<<<blocks(nt, 256), 256, 0, s>>>(dTris, nt, nv, flag, misc, reinterpret_cast<unsigned long long*>(misc + 4));
     if ((e = exclusiveScan(flag, pos, nt, sums, misc + 1, s))) return e;
-    int32_t hm[2];
+    int32_t hm[8];
     if ((e = cudaMemcpyAsync(hm, misc, sizeof(hm), cudaMemcpyDeviceToHost, s))) return e;
     if ((e = cudaStreamSynchronize(s))) return e;
     if (hm[0]) {
         err = "triangle vertex id out of range";
         return cudaErrorInvalidValue;
     }
+    closed = (hm[4] | hm[5] | hm[6] | hm[7]) == 0;
     const int32_t n = hm[1];
     nLeaves = n;
     if (n == 0) return cudaSuccess;

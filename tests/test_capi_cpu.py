@@ -47,7 +47,10 @@ def test_bad_arguments_rejected_without_gpu(fwn_lib):
 def test_memory_estimators(fwn_lib):
     import meshlib_gb300 as M
     est = M.memory_estimates(655362, 1310720, dims=(512, 512, 512), npts=4_000_000)
-    assert est["from_grid"] - est["mesh"] == 512 ** 3 * 4
+    # the result, and the signed-distance columns' hand-over words (128 B per column of >= 16 tiles,
+    # or of fewer tiles while under 50 items per resident warp remain)
+    extra = est["from_grid"] - est["mesh"] - 512 ** 3 * 4
+    assert 0 < extra <= 512 ** 3 // 4 + 50 * 160 * 32 * 128
     # points in and results out, Morton order and its sort scratch
     assert est["from_vector"] - est["mesh"] == 4_000_000 * 40 + 4096
     # the peak is the build: 352 B kept and up to 244 B of work arrays per face, 12 B per vertex
