@@ -494,6 +494,44 @@ __device__ __forceinline__ bool signReuseAllowed(const QueryTree& t, const DistO
     return t.closed != 0 && o.beta >= 2.f && fr > 0.25f && fr < 0.75f;
 }
 
+// True when a voxel at q may take the sign of the voxel at qb, whose squared distance to the surface
+// is belowSq (> 0, from a search that ran to the end): qb is farther from the surface than from q, so
+// the segment between them meets no surface.  The margin covers the FP32 rounding of both centres and
+// of the distance, relative to the coordinates' magnitude.  qb must be computed exactly as that
+// voxel's centre was (the same xfPoint call).
+__device__ __forceinline__ bool emptyBallCovers(const float3& q, const float3& qb, float belowSq) {
+    const float dx = q.x - qb.x, dy = q.y - qb.y, dz = q.z - qb.z;
+    const float step = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    const float db = sqrtf(belowSq);
+    const float mag = fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z)));
+    return db > fmaf(step, 1.0001f, 2e-6f * fmaf(3.f, mag, db));
+}
+
+// Sign reuse for one tile of TX x TY x TZ voxels (lane = lx + TX (ly + TY lz)) after its closest-point
+// searches.  below: the state of the voxel that precedes this lane's voxel (the previous tile's top
+// layer for the bottom layer, the lane's own voxel of the previous tile for the others): its squared
+// distance with its side in the sign bit, NaN when unknown; zb: that voxel's layer.  A lane above the
+// bottom layer may also take the sign of the voxel one layer below it in this tile, once that one's
+// sign is settled by reuse.  Returns whether the lane's sign is settled; *inside receives it.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ bool reuseSign(const Xf& xf, int x, int y, int z, int zb, int lz, const float3& q, float below,
+                                          bool complete, float dsq, bool* inside) {
+    bool reuse = fabsf(below) > 0.f && emptyBallCovers(q, xfPoint(xf, x, y, zb), fabsf(below));
+    bool in = signbit(below);
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int l = 1; l < TZ; ++l) {
+        const float e = __shfl_sync(FULL, (reuse && complete) ? (in ? -dsq : dsq) : __int_as_float(0x7fc00000),
+                                    lane >= TX * TY ? lane - TX * TY : lane);
+        if (lz == l && !reuse && fabsf(e) > 0.f && emptyBallCovers(q, xfPoint(xf, x, y, z - 1), fabsf(e))) {
+            reuse = true;
+            in = signbit(e);
+        }
+    }
+    *inside = in;
+    return reuse;
+}
+
 // A warp takes a column of tiles along z and walks it upwards.  Each lane starts its closest-point
 // search from the triangle that was closest to a voxel just below its own: the bottom layer of a
 // tile from the voxel one layer below (the previous tile's top layer), the top layer from its own
@@ -559,27 +597,19 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
                 int best = active ? seed : -1;
                 const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
                 const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
-                bool reuse = false;
-                if (reuseOk && fabsf(below) > 0.f) {
-                    // the voxel below (its centre recomputed exactly as it was evaluated) is farther
-                    // from the surface than from this voxel, with a margin for the FP32 rounding of
-                    // both centres and of the distance, relative to the coordinates' magnitude
-                    const float3 qb = xfPoint(xf, x, y, z - (lz == 0 ? 1 : kTZ));
-                    const float dx = q.x - qb.x, dy = q.y - qb.y, dz = q.z - qb.z;
-                    const float step = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                    const float db = sqrtf(fabsf(below));
-                    const float mag = fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z)));
-                    reuse = db > fmaf(step, 1.0001f, 2e-6f * fmaf(3.f, mag, db));
-                }
+                const bool complete = active && valid && dsq >= o.minDistSq;
+                bool reIn = false;
+                const bool reuse = reuseOk && reuseSign<kTX, kTY, kTZ>(xf, x, y, z, z - (lz == 0 ? 1 : kTZ), lz, q, below,
+                                                                      complete, dsq, &reIn);
                 const float w = fwnPacket<PRECISE>(t, q, active && valid && !reuse, betaSq, -1, scratch + 1);
-                const bool inside = reuse ? signbit(below) : w > o.threshold;
+                const bool inside = reuse ? reIn : w > o.threshold;
                 const float d = __fsqrt_rn(dsq);
                 res = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
                 // next tile: the bottom layer's lanes take the voxel one layer below them (this tile's
                 // top layer), the others their own voxel two layers below.  A distance counts only when
                 // the search ran to the end (not cut short below minDistSq): no surface is closer then.
                 const int src = lane + (kTZ - 1) * kTX * kTY * (lz == 0);
-                const float mine = (active && valid && dsq >= o.minDistSq) ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000);
+                const float mine = complete ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000);
                 seed = __shfl_sync(FULL, best, src);
                 below = __shfl_sync(FULL, mine, src);
                 if (tg.colState && !tg.bricks && j == nSeg - 1) {
@@ -1015,7 +1045,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const Bat
         const int x = tx * TX + lx, y = ty * TY + ly;
         const QueryTree& t = it.t;  // read through the cache, not copied into registers
         const DistOpts o = it.o;
+        const bool reuseOk = signReuseAllowed(t, o);
         int seed = -1;
+        float below = __int_as_float(0x7fc00000);  // the preceding voxel's signed squared distance (gridKernel)
         for (int j = 0; j < kBatchSeg; ++j) {
             const int z0 = (seg * kBatchSeg + j) * TZ;
             if (z0 >= it.g.nz) break;
@@ -1030,14 +1062,20 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const Bat
             }
             int best = active ? seed : -1;
             const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
-            // the bottom layer's lanes continue from the voxel one layer below (as gridKernel does)
-            const int fromBelow = __shfl_sync(FULL, best, lane + (TZ - 1) * TX * TY * (lz == 0));
-            seed = lz == 0 ? fromBelow : best;
             const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
-            const float w = fwnPacket<PRECISE>(t, q, active && valid, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
+            const bool complete = active && valid && dsq >= o.minDistSq;
+            bool reIn = false;
+            const bool reuse = reuseOk && reuseSign<TX, TY, TZ>(it.xf, x, y, z, z - (lz == 0 ? 1 : TZ), lz, q, below, complete,
+                                                                dsq, &reIn);
+            const float w = fwnPacket<PRECISE>(t, q, active && valid && !reuse, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
+            const bool inside = reuse ? reIn : w > o.threshold;
             const float d = __fsqrt_rn(dsq);
-            const float res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+            const float res = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
             if (active) it.out[(size_t(z) * it.g.ny + y) * it.g.nx + x] = res;
+            // the bottom layer's lanes continue from the voxel one layer below (as gridKernel does)
+            const int src = lane + (TZ - 1) * TX * TY * (lz == 0);
+            seed = __shfl_sync(FULL, best, src);
+            below = __shfl_sync(FULL, complete ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000), src);
         }
     }
 }
