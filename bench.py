@@ -159,19 +159,19 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 
 
 # DRAM bytes (read + write) of one launch of the signed-distance grid kernel at 512^3 on this
-# workload: dram__bytes_read.sum 594,597,120 + dram__bytes_write.sum 608,213,504 from one ncu
+# workload: dram__bytes_read.sum 630,731,776 + dram__bytes_write.sum 651,689,216 from one ncu
 # capture of the same kernel (a constant copied from that capture, not measured by this run; the
 # committed profile summary under profiles/ gives the command).  536,870,912 of the written bytes
 # are the output grid.
-KERNEL_DRAM_BYTES_512 = 594_597_120 + 608_213_504
+KERNEL_DRAM_BYTES_512 = 630_731_776 + 651_689_216
 
 
 # Counters of the signed-distance grid kernel at 256^3 on this workload from one ncu capture
 # (constants copied from that capture, not measured by this run): FMA-pipe utilisation
 # (sm__pipe_fma_cycles_active), issue-slot utilisation and active lanes per warp instruction.
-KERNEL_FMA_PIPE_ACTIVE = 0.309
+KERNEL_FMA_PIPE_ACTIVE = 0.311
 KERNEL_ISSUE_ACTIVE = 0.839
-KERNEL_LANES_PER_INSTR = 25.1
+KERNEL_LANES_PER_INSTR = 24.5
 
 
 def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
