@@ -455,7 +455,13 @@ constexpr int kThreads = 256;
 // 4 (23.4 -> 25.1 ms at 6); so do self-intersections and the batched kernel, which measured slower with
 // more warps.
 constexpr int kDistBlocks = 5;
-constexpr int kTX = 4, kTY = 4, kTZ = 2;  // voxel tile of one warp
+// Voxel tile of one warp.  Measured at 512^3 on 1.31 M triangles with sign reuse (the same grids for
+// every shape): 4x4x2 84.2 ms, 2x4x4 88.5, 4x2x4 88.6, 8x4x1 103.1, 4x8x1 102.8.
+constexpr int kTX = 4, kTY = 4, kTZ = 2;
+constexpr int kLayer = kTX * kTY;         // lanes per tile layer
+// an 8x8x8-voxel brick of the banded path: columns of kBrickSeg tiles, kBrickCols of them
+constexpr int kBrickColsX = 8 / kTX, kBrickCols = (8 / kTX) * (8 / kTY), kBrickSeg = 8 / kTZ;
+static_assert(kTX * kTY * kTZ == 32 && 8 % kTX == 0 && 8 % kTY == 0 && 8 % kTZ == 0, "tile shape");
 
 struct TileGrid {
     int32_t tilesX, tilesY, tilesZ;
@@ -464,12 +470,12 @@ struct TileGrid {
     // (2 x 2 x 4 tiles of 4x4x2) per brick
     const int32_t* bricks;
     int32_t bricksX, bricksY;
-    // work items: columns of up to segLen tiles along z (4 per brick: its 2 x 2 columns)
+    // work items: columns of up to segLen tiles along z (kBrickCols per brick)
     int32_t segLen, segsZ;
     uint32_t numItems;
-    // optional hand-over between the columns of one launch (whole grids only): 32 words per work
-    // item, written when the item ends -- words 0..15 the signed squared distance of each top-layer
-    // voxel (negative inside, NaN when its sign is unknown), words 16..31 the leaf slot closest to it
+    // optional hand-over between the columns of one launch (whole grids only): 2 x kLayer words per
+    // work item, written when the item ends -- words [0, kLayer) the signed squared distance of each
+    // top-layer voxel (negative inside, NaN when its sign is unknown), then the leaf slot closest to it
     // (-1 none) -- and read by the column above it when it starts; filled with 0xff bytes (NaN / -1)
     // before the launch, so a column that starts before the one below it has ended starts cold
     float* colState;
@@ -553,12 +559,12 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
         if (item >= tg.numItems) break;
         int x0, y0, zBase, nSeg;
         if (tg.bricks) {
-            const int b = tg.bricks[item >> 2], col = int(item & 3u);
+            const int b = tg.bricks[item / kBrickCols], col = int(item % kBrickCols);
             const int bx = b % tg.bricksX, by = (b / tg.bricksX) % tg.bricksY, bz = b / (tg.bricksX * tg.bricksY);
-            x0 = bx * 8 + (col & 1) * kTX;
-            y0 = by * 8 + (col >> 1) * kTY;
+            x0 = bx * 8 + (col % kBrickColsX) * kTX;
+            y0 = by * 8 + (col / kBrickColsX) * kTY;
             zBase = g.z0 + bz * 8;
-            nSeg = 4;
+            nSeg = kBrickSeg;
         } else {
             const int tx = int(item % unsigned(tg.tilesX));
             const unsigned rest = item / unsigned(tg.tilesX);
@@ -578,9 +584,9 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
         if (DIST && tg.colState && !tg.bricks && item >= colsPerSlab) {
             // the column below ended (its state was written) or not yet (0xff bytes: start cold); the
             // voxel below both layers of the first tile is that column's top-layer voxel
-            const float* cs = tg.colState + size_t(item - colsPerSlab) * 32;
-            below = __ldcg(cs + (lane & 15));
-            seed = __float_as_int(__ldcg(cs + 16 + (lane & 15)));
+            const float* cs = tg.colState + size_t(item - colsPerSlab) * (2 * kLayer);
+            below = __ldcg(cs + lane % kLayer);
+            seed = __float_as_int(__ldcg(cs + kLayer + lane % kLayer));
         }
         for (int j = 0; j < nSeg; ++j) {
             const int z = zBase + j * kTZ + lz;
@@ -612,22 +618,21 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
                 const float mine = complete ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000);
                 seed = __shfl_sync(FULL, best, src);
                 below = __shfl_sync(FULL, mine, src);
-                if (tg.colState && !tg.bricks && j == nSeg - 1) {
-                    // the column's last tile: every lane now holds the state of the top-layer voxel of
-                    // its (x, y); lanes 0..15 pass on the distances, lanes 16..31 (the same 16
-                    // columns) the seeds, at this work item's words (the item recomputed from the
-                    // column's position, so no register holds it through the walk)
+                if (tg.colState && !tg.bricks && j == nSeg - 1 && lz == kTZ - 1) {
+                    // the column's last tile: the top layer's lanes hold their own voxels' state and
+                    // pass on the distances and the seeds at this work item's words (the item
+                    // recomputed from the column's position, so no register holds it through the walk)
                     const uint32_t sz = uint32_t(zBase - g.z0) / uint32_t(tg.segLen * kTZ);
                     const uint32_t it = uint32_t(x0) / kTX + uint32_t(tg.tilesX) * (uint32_t(y0) / kTY + uint32_t(tg.tilesY) * sz);
-                    tg.colState[size_t(it) * 32 + lane] = lane < 16 ? below : __int_as_float(seed);
+                    float* cs = tg.colState + size_t(it) * (2 * kLayer) + (lane - (kTZ - 1) * kLayer);
+                    cs[0] = below;
+                    cs[kLayer] = __int_as_float(seed);
                 }
             } else {
                 res = fwnPacket<PRECISE>(t, q, active, betaSq, -1, scratch + 1);
             }
             if (active) out[size_t(z - g.zOut) * sxy + size_t(y) * g.nx + x] = res;
         }
-        // every lane now holds the state of the top-layer voxel of its (x, y): lanes 0..15 pass on the
-        // distances, lanes 16..31 (the same 16 columns) the seeds
     }
 }
 
@@ -904,7 +909,7 @@ cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf
     tg.bricksX = (g.nx + 7) / 8;
     tg.bricksY = (g.ny + 7) / 8;
     tg.numTiles = uint32_t(nBricks) * 16u;
-    tg.numItems = uint32_t(nBricks) * 4u;
+    tg.numItems = uint32_t(nBricks) * uint32_t(kBrickCols);
     if (precise)
         return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
     return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
@@ -920,13 +925,13 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
 }
 
 size_t gridSdfColumnStateBytes(const GridRange& g, const DistOpts& o) {
-    return size_t(tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16).numItems) * 32 * sizeof(float);
+    return size_t(tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16).numItems) * (2 * kLayer) * sizeof(float);
 }
 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
                           unsigned* scratch, cudaStream_t s, float* colState, size_t colBytes) {
     TileGrid tg = tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16);
-    const size_t need = size_t(tg.numItems) * 32 * sizeof(float);
+    const size_t need = size_t(tg.numItems) * (2 * kLayer) * sizeof(float);
     if (colState && colBytes >= need && need > 0) {
         cudaError_t e = cudaMemsetAsync(colState, 0xff, need, s);
         if (e) return e;
