@@ -259,11 +259,16 @@ GBFWN_API int gbfwn_create(const float* verts, int64_t nv, const int32_t* tris, 
     if (!out || nv < 0 || nt < 0 || (nv > 0 && !verts) || (nt > 0 && !tris)) return fail(GBFWN_INVALID, "gbfwn_create: bad arguments");
     if (nt > INT32_MAX / 2) return fail(GBFWN_INVALID, "gbfwn_create: too many triangles");
     *out = nullptr;
-    for (int64_t i = 0; i < 3 * nt; ++i)
-        if (tris[i] >= nv) return fail(GBFWN_INVALID, "gbfwn_create: triangle vertex id out of range");
     gbfwn_mesh_s* h = nullptr;
     int st = newHandle(device, &h);
-    if (st) return st;
+    if (st) {
+        // no device: an out-of-range vertex id is still reported as such (on a device the tree
+        // build's face validation rejects it before any vertex is read)
+        int32_t maxId = -1;
+        for (int64_t i = 0; i < 3 * nt; ++i) maxId = tris[i] > maxId ? tris[i] : maxId;
+        if (maxId >= nv) return fail(GBFWN_INVALID, "gbfwn_create: triangle vertex id out of range");
+        return st;
+    }
     DeviceGuard g(device);
     h->nv = nv;
     h->nt = nt;

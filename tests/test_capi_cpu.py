@@ -40,7 +40,7 @@ def test_bad_arguments_rejected_without_gpu(fwn_lib):
     assert L.gbfwn_destroy(None) == M.OK
     assert L.gbfwn_num_faces(None) == 0
     v = np.zeros((3, 3), np.float32)
-    t = np.array([[0, 1, 5]], np.int32)  # vertex id out of range: rejected before any device work
+    t = np.array([[0, 1, 5]], np.int32)  # vertex id out of range: reported as such even without a device
     assert L.gbfwn_create(v.ctypes.data, 3, t.ctypes.data, 1, 0, ctypes.byref(out)) == M.INVALID
 
 
