@@ -94,7 +94,10 @@ struct BatchItem {
     uint32_t tileBase;
 };
 constexpr int kBatchConfigs = 6;  // tile shape x block size variants
-constexpr int kBatchSeg = 4;      // tiles along z per work item (a column walked by one warp)
+// tiles along z per work item (a column walked by one warp).  64-mesh batch, best configuration, the
+// same outputs: 4 tiles 54.9 ms, 8 54.4, 16 52.9, 24 52.4, 32 52.1 (sign reuse makes long columns pay;
+// 16 leaves more items for the load balance of batches of small grids)
+constexpr int kBatchSeg = 16;
 const char* batchConfigName(int config);
 uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz);
 cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,
