@@ -119,8 +119,19 @@ int main() {
         return 1;
     }
     const int mcSame = whole.tris == byParts.tris && whole.faceMap == byParts.faceMap && whole.tris == fused.tris;
+    // the knobs: the torus is closed, and the grid without sign reuse is the same grid
+    const int closed = fwn.isClosed() ? 1 : 0;
+    fwn.setSignReuse(false);
+    std::vector<float> sdPlain;
+    if (auto r2 = fwn.calcFromGridWithDistances(sdPlain, dims, xf, gbfwn::DistanceToMeshOptions{}); !r2) {
+        std::printf("ERROR sdf plain %s\n", r2.error().c_str());
+        return 1;
+    }
+    fwn.setSignReuse(true);
+    const int reuseSame = sdPlain == sd ? 1 : 0;
     std::printf("OK sum_sd=%.6f sum_wn=%.6f neg=%d parts_equal=%d selfint=%d cancel_status=%d proj_max_diff=%.3g "
-                "mc_tris=%zu mc_points=%zu mc_same=%d\n",
-                sumSd, sumWn, neg, same, nbits, c.status(), maxDiff, whole.tris.size() / 3, whole.points.size() / 3, mcSame);
+                "mc_tris=%zu mc_points=%zu mc_same=%d closed=%d reuse_same=%d\n",
+                sumSd, sumWn, neg, same, nbits, c.status(), maxDiff, whole.tris.size() / 3, whole.points.size() / 3, mcSame,
+                closed, reuseSame);
     return 0;
 }

@@ -52,6 +52,8 @@ def test_adapter_matches_python(tmp_path):
     # marching-cubes adapter: the same mesh as the Python front-end; by parts and fused give the same
     # triangles (points of parts differ only in the rounding of z)
     assert kv["mc_same"] == "1"
+    # knobs: the torus is a closed surface; switching sign reuse off gives the same grid
+    assert kv["closed"] == "1" and kv["reuse_same"] == "1"
     prm = M.MarchingCubesParams(origin=tuple(xf[9:12] - 0.5 * xf[[0, 4, 8]]), voxelSize=tuple(xf[[0, 4, 8]]),
                                 lessInside=True)
     tm = M.marchingCubes(sd.reshape(8, 16, 16), prm)
