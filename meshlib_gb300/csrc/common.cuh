@@ -103,10 +103,10 @@ uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz);
 cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,
                            cudaStream_t s);
 
-// Signed distance on a list of 8x8x8-voxel bricks of the grid (brick b = bx + by * ceil(nx/8) +
-// bz * ceil(nx/8) * ceil(ny/8)); voxels outside the bricks are not written.
+// Signed distance on runs of 8x8x8-voxel bricks of the grid: runs[i] = (bx, by, bz0, count), the
+// `count` bricks (bx, by, bz0 .. bz0 + count - 1), nBricks in all; voxels outside them are not written.
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
-                                float* out, const int32_t* bricks, int32_t nBricks, unsigned* scratch, cudaStream_t s);
+                                float* out, const int4* runs, int32_t nRuns, int32_t nBricks, unsigned* scratch, cudaStream_t s);
 // Point queries; `order` (optional) is a permutation of [0, n): points are processed in that order
 // (mortonOrder gives a spatially coherent one) and results land at their original indices.
 cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,

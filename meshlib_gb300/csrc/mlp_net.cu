@@ -179,9 +179,31 @@ __global__ void brickKeepKernel(const float* __restrict__ lowerBound, int nb, fl
     keep[b] = (lb - radius >= band) ? 0 : 1;
 }
 
-__global__ void compactKernel(const int32_t* __restrict__ keep, const int32_t* __restrict__ pos, int nb, int32_t* __restrict__ list) {
+// Runs of kept bricks stacked in z, at most kRunBricks long: a run starts at a kept brick whose brick
+// below is not kept, or at every kRunBricks-th brick layer.  A run's tile columns carry their seeds
+// and signs from brick to brick.  512^3, band 0.01 diag, exact pass over the 30,016 kept bricks:
+// 1 brick per run 10.06 ms, 2 9.83 ms, 4 9.77 ms, unlimited 14.2 ms (the runs down the sides of the
+// shape are long and leave the tail to a few warps).
+constexpr int kRunBricks = 2;
+__global__ void runStartKernel(const int32_t* __restrict__ keep, int3 bd, int32_t* __restrict__ start) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nb && keep[b]) list[pos[b]] = b;
+    const int nb = bd.x * bd.y * bd.z;
+    if (b >= nb) return;
+    const int layer = bd.x * bd.y;
+    start[b] = (keep[b] && (b < layer || !keep[b - layer] || (b / layer) % kRunBricks == 0)) ? 1 : 0;
+}
+
+// (bx, by, bz0, count) of every run, in the order of their first bricks
+__global__ void runKernel(const int32_t* __restrict__ keep, const int32_t* __restrict__ start, const int32_t* __restrict__ pos,
+                          int3 bd, int4* __restrict__ runs) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nb = bd.x * bd.y * bd.z;
+    if (b >= nb || !start[b]) return;
+    const int layer = bd.x * bd.y;
+    const int bx = b % bd.x, by = (b / bd.x) % bd.y, bz = b / layer;
+    int n = 1;
+    while (bz + n < bd.z && (bz + n) % kRunBricks != 0 && keep[b + n * layer]) ++n;
+    runs[pos[b]] = make_int4(bx, by, bz, n);
 }
 
 // NaN everywhere (voxels of culled bricks stay NaN); 16-byte stores when p is 16-byte aligned
@@ -600,7 +622,8 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     radius *= 1.0001f;
     cudaError_t e;
     float *centers = nullptr, *lb = nullptr, *tmp = nullptr;
-    int32_t *keep = nullptr, *pos = nullptr, *list = nullptr, *sums = nullptr, *total = nullptr;
+    int32_t *keep = nullptr, *pos = nullptr, *start = nullptr, *sums = nullptr, *total = nullptr;
+    int4* runs = nullptr;
     std::vector<void*> mem;
     int dev = 0;
     cudaGetDevice(&dev);
@@ -619,9 +642,10 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     if ((e = A((void**)&tmp, sizeof(float) * size_t(nb)))) return done(e);
     if ((e = A((void**)&keep, sizeof(int32_t) * size_t(nb)))) return done(e);
     if ((e = A((void**)&pos, sizeof(int32_t) * size_t(nb)))) return done(e);
-    if ((e = A((void**)&list, sizeof(int32_t) * size_t(nb)))) return done(e);
+    if ((e = A((void**)&start, sizeof(int32_t) * size_t(nb)))) return done(e);
+    if ((e = A((void**)&runs, sizeof(int4) * size_t(nb)))) return done(e);
     if ((e = A((void**)&sums, sizeof(int32_t) * size_t(nb / 1024 + 2)))) return done(e);
-    if ((e = A((void**)&total, sizeof(int32_t)))) return done(e);
+    if ((e = A((void**)&total, 2 * sizeof(int32_t)))) return done(e);
     cudaEvent_t ev[4];
     for (auto& x : ev) cudaEventCreate(&x);
     cudaEventRecord(ev[0], s);
@@ -640,15 +664,18 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
         exactLowerBound<<<nblk(nb, 256), 256, 0, s>>>(tmp, nb, lb);
     }
     brickKeepKernel<<<nblk(nb, 256), 256, 0, s>>>(lb, nb, band, radius, keep);
-    if ((e = exclusiveScanI32(keep, pos, nb, sums, total, s))) return done(e);
-    compactKernel<<<nblk(nb, 256), 256, 0, s>>>(keep, pos, nb, list);
-    int32_t kept = 0;
-    if ((e = cudaMemcpyAsync(&kept, total, sizeof(int32_t), cudaMemcpyDeviceToHost, s))) return done(e);
+    if ((e = exclusiveScanI32(keep, pos, nb, sums, total, s))) return done(e);  // the kept count
+    runStartKernel<<<nblk(nb, 256), 256, 0, s>>>(keep, bd, start);
+    if ((e = exclusiveScanI32(start, pos, nb, sums, total + 1, s))) return done(e);
+    runKernel<<<nblk(nb, 256), 256, 0, s>>>(keep, start, pos, bd, runs);
+    int32_t counts[2] = {0, 0};  // kept bricks, runs
+    if ((e = cudaMemcpyAsync(counts, total, sizeof(counts), cudaMemcpyDeviceToHost, s))) return done(e);
     cudaEventRecord(ev[1], s);
     fillNanKernel<<<unsigned(numSMs()) * 8, 256, 0, s>>>(out, int64_t(g.nx) * g.ny * g.nz);
     if ((e = cudaStreamSynchronize(s))) return done(e);
     cudaEventRecord(ev[2], s);
-    if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, list, kept, scratch, s))) return done(e);
+    const int32_t kept = counts[0];
+    if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, runs, counts[1], kept, scratch, s))) return done(e);
     cudaEventRecord(ev[3], s);
     if ((e = cudaStreamSynchronize(s))) return done(e);
     cudaEventElapsedTime(&st.cullMs, ev[0], ev[1]);

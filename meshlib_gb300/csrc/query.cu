@@ -466,11 +466,11 @@ static_assert(kTX * kTY * kTZ == 32 && 8 % kTX == 0 && 8 % kTY == 0 && 8 % kTZ =
 struct TileGrid {
     int32_t tilesX, tilesY, tilesZ;
     uint32_t numTiles;
-    // optional list of 8x8x8-voxel bricks to cover instead of the whole range: 16 warp tiles
-    // (2 x 2 x 4 tiles of 4x4x2) per brick
-    const int32_t* bricks;
-    int32_t bricksX, bricksY;
-    // work items: columns of up to segLen tiles along z (kBrickCols per brick)
+    // optional runs of 8x8x8-voxel bricks to cover instead of the whole range: (bx, by, bz0, count),
+    // `count` bricks stacked from brick layer bz0 upwards; kBrickCols tile columns per run, each
+    // walked through the whole run, so its state carries from brick to brick
+    const int4* runs;
+    // work items: columns of up to segLen tiles along z (kBrickCols per brick run)
     int32_t segLen, segsZ;
     uint32_t numItems;
     // optional hand-over between the columns of one launch (whole grids only): 2 x kLayer words per
@@ -558,13 +558,13 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
         const unsigned item = nextTicket(scratch, lane);
         if (item >= tg.numItems) break;
         int x0, y0, zBase, nSeg;
-        if (tg.bricks) {
-            const int b = tg.bricks[item / kBrickCols], col = int(item % kBrickCols);
-            const int bx = b % tg.bricksX, by = (b / tg.bricksX) % tg.bricksY, bz = b / (tg.bricksX * tg.bricksY);
-            x0 = bx * 8 + (col % kBrickColsX) * kTX;
-            y0 = by * 8 + (col / kBrickColsX) * kTY;
-            zBase = g.z0 + bz * 8;
-            nSeg = kBrickSeg;
+        if (tg.runs) {
+            const int4 r = tg.runs[item / kBrickCols];
+            const int col = int(item % kBrickCols);
+            x0 = r.x * 8 + (col % kBrickColsX) * kTX;
+            y0 = r.y * 8 + (col / kBrickColsX) * kTY;
+            zBase = g.z0 + r.z * 8;
+            nSeg = kBrickSeg * r.w;
         } else {
             const int tx = int(item % unsigned(tg.tilesX));
             const unsigned rest = item / unsigned(tg.tilesX);
@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
         // its sign is unknown
         float below = __int_as_float(0x7fc00000);
         const uint32_t colsPerSlab = uint32_t(tg.tilesX) * uint32_t(tg.tilesY);
-        if (DIST && tg.colState && !tg.bricks && item >= colsPerSlab) {
+        if (DIST && tg.colState && !tg.runs && item >= colsPerSlab) {
             // the column below ended (its state was written) or not yet (0xff bytes: start cold); the
             // voxel below both layers of the first tile is that column's top-layer voxel
             const float* cs = tg.colState + size_t(item - colsPerSlab) * (2 * kLayer);
@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
                 const float mine = complete ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000);
                 seed = __shfl_sync(FULL, best, src);
                 below = __shfl_sync(FULL, mine, src);
-                if (tg.colState && !tg.bricks && j == nSeg - 1 && lz == kTZ - 1) {
+                if (tg.colState && !tg.runs && j == nSeg - 1 && lz == kTZ - 1) {
                     // the column's last tile: the top layer's lanes hold their own voxels' state and
                     // pass on the distances and the seeds at this work item's words (the item
                     // recomputed from the column's position, so no register holds it through the walk)
@@ -885,8 +885,7 @@ static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
     tg.tilesY = (g.ny + kTY - 1) / kTY;
     tg.tilesZ = (g.z1 - g.z0 + kTZ - 1) / kTZ;
     tg.numTiles = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.tilesZ);
-    tg.bricks = nullptr;
-    tg.bricksX = tg.bricksY = 0;
+    tg.runs = nullptr;
     tg.colState = nullptr;
     // Longer columns reuse more seeds; shorter ones leave more items for the tail of the persistent
     // grid.  Measured at 256^3 / 512^3 on 1.3 M triangles: keep >= 25 items per (32-warps-per-SM)
@@ -903,13 +902,11 @@ static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
 }
 
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
-                                float* out, const int32_t* bricks, int32_t nBricks, unsigned* scratch, cudaStream_t s) {
+                                float* out, const int4* runs, int32_t nRuns, int32_t nBricks, unsigned* scratch, cudaStream_t s) {
     TileGrid tg = tileGridFor(g);
-    tg.bricks = bricks;
-    tg.bricksX = (g.nx + 7) / 8;
-    tg.bricksY = (g.ny + 7) / 8;
+    tg.runs = runs;
     tg.numTiles = uint32_t(nBricks) * 16u;
-    tg.numItems = uint32_t(nBricks) * uint32_t(kBrickCols);
+    tg.numItems = uint32_t(nRuns) * uint32_t(kBrickCols);
     if (precise)
         return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
     return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
