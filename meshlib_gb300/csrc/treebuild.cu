@@ -533,15 +533,20 @@ struct SubSeg {
     int32_t bmin[3], bmax[3];
 };
 
-constexpr size_t kFinishSmem = sizeof(Elem) * 2 * kSmall + sizeof(SubSeg) * kSmall + sizeof(int16_t) * kSmall + 16;
+// two element buffers, the sub-segments of two levels, each element's sort key for the current level
+// (16 bytes, 16-byte aligned after the elements), its sub-segment, the sub-segment counts
+constexpr size_t kFinishSmem =
+    sizeof(Elem) * 2 * kSmall + sizeof(float4) * kSmall + sizeof(SubSeg) * kSmall + sizeof(int16_t) * kSmall + 16;
 
 __global__ void __launch_bounds__(kSmall) finishSmall(const Elem* __restrict__ el, const Seg* __restrict__ small,
                                                    RefNode* nodes, int32_t* irs, int2* range, int64_t nNodes) {
     extern __shared__ __align__(16) unsigned char smem[];
     Elem(*buf)[kSmall] = reinterpret_cast<Elem(*)[kSmall]>(smem);
-    SubSeg(*sub)[kSmall / 2] = reinterpret_cast<SubSeg(*)[kSmall / 2]>(smem + sizeof(Elem) * 2 * kSmall);
-    int16_t* sid = reinterpret_cast<int16_t*>(smem + sizeof(Elem) * 2 * kSmall + sizeof(SubSeg) * kSmall);
-    int* nsub = reinterpret_cast<int*>(smem + sizeof(Elem) * 2 * kSmall + sizeof(SubSeg) * kSmall + sizeof(int16_t) * kSmall);
+    float4* key = reinterpret_cast<float4*>(smem + sizeof(Elem) * 2 * kSmall);
+    unsigned char* rest = smem + sizeof(Elem) * 2 * kSmall + sizeof(float4) * kSmall;
+    SubSeg(*sub)[kSmall / 2] = reinterpret_cast<SubSeg(*)[kSmall / 2]>(rest);
+    int16_t* sid = reinterpret_cast<int16_t*>(rest + sizeof(SubSeg) * kSmall);
+    int* nsub = reinterpret_cast<int*>(rest + sizeof(SubSeg) * kSmall + sizeof(int16_t) * kSmall);
     const Seg S = small[blockIdx.x];
     const int t = threadIdx.x;
     for (int i = t; i < S.num; i += blockDim.x) {
@@ -590,6 +595,15 @@ __global__ void __launch_bounds__(kSmall) finishSmall(const Elem* __restrict__ e
             writeInternal(mn, mx, q.root, S.first + q.first, q.num, nodes, irs, range, nNodes);
         }
         __syncthreads();
+        // each element's key in its sub-segment's order: (c[d2], c[d1], c[d0], id), one 16-byte load
+        for (int i = t; i < S.num; i += blockDim.x) {
+            const int j = sid[i];
+            if (j < 0) continue;
+            const int dims = sub[cur][j].dims;
+            const Elem& e = buf[cur][i];
+            key[i] = make_float4(e.c[(dims >> 4) & 3], e.c[(dims >> 2) & 3], e.c[dims & 3], __int_as_float(e.id));
+        }
+        __syncthreads();
         // rank of every element inside its sub-segment = its position after the split
         for (int i = t; i < S.num; i += blockDim.x) {
             const int j = sid[i];
@@ -598,19 +612,18 @@ __global__ void __launch_bounds__(kSmall) finishSmall(const Elem* __restrict__ e
                 continue;
             }
             const SubSeg q = sub[cur][j];
-            const int d0 = q.dims & 3, d1 = (q.dims >> 2) & 3, d2 = (q.dims >> 4) & 3;
-            const Elem e = buf[cur][i];
+            const float4 me = key[i];
+            const int myId = __float_as_int(me.w);
             int rank = 0;
             for (int o = q.first; o < q.first + q.num; ++o) {
-                const Elem& f = buf[cur][o];
-                bool less;
-                if (f.c[d2] != e.c[d2]) less = f.c[d2] < e.c[d2];
-                else if (f.c[d1] != e.c[d1]) less = f.c[d1] < e.c[d1];
-                else if (f.c[d0] != e.c[d0]) less = f.c[d0] < e.c[d0];
-                else less = f.id < e.id;
+                const float4 f = key[o];
+                const bool less = f.x != me.x   ? f.x < me.x
+                                  : f.y != me.y ? f.y < me.y
+                                  : f.z != me.z ? f.z < me.z
+                                                : __float_as_int(f.w) < myId;
                 rank += less ? 1 : 0;
             }
-            buf[cur ^ 1][q.first + rank] = e;
+            buf[cur ^ 1][q.first + rank] = buf[cur][i];
         }
         __syncthreads();
         if (t == 0) nsub[cur ^ 1] = 0;
