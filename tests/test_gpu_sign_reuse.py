@@ -106,3 +106,24 @@ def test_not_applied_where_it_does_not_hold(M):
     for opts in (M.DistanceToMeshOptions(windingNumberThreshold=0.9), M.DistanceToMeshOptions(windingNumberBeta=1.5)):
         _, on, off = _grids(M, v, f, 48, opts)
         _same(on, off)
+
+
+def test_reuse_identical_at_benchmark_scale(M):
+    """The 1,310,720-triangle icosphere on a 256^3 grid: with the sign reuse and the column hand-over
+    the grid equals the grid that evaluates every voxel's winding number, unbanded and banded."""
+    import torch
+    v, f = mg.noisy_icosphere(seed=0, level=8)
+    dims, xf = mg.grid_for(v, 256)
+    g = M.FastWindingNumber(v, f)
+    assert g.is_closed()
+    band = 0.01 * mg.diag(v)
+    for opts in (None, M.DistanceToMeshOptions(maxDistSq=band * band)):
+        res = []
+        for enable in (True, False):
+            g.set_sign_reuse(enable)
+            out = torch.empty(int(np.prod(dims)), device="cuda")
+            g.calcFromGridWithDistances_dev(dims, xf, out.data_ptr(), options=opts, stream=0)
+            torch.cuda.synchronize()
+            res.append(out.cpu().numpy())
+        _same(*res)
+    g.set_sign_reuse(True)
