@@ -526,7 +526,7 @@ def main():
     out_h = np.empty(nvox, np.float32) if world == 1 else torch.empty(slab_vox, dtype=torch.float32, pin_memory=True)
     e2e_dev = torch.empty(max(slab_vox, 1), dtype=torch.float32, device="cuda") if world > 1 else None
     e2e_times, create_times = [], []
-    for i in range(0 if args.no_e2e else max(1, args.steps // 2) + 1):
+    for i in range(0 if args.no_e2e else max(3, args.steps) + 1):  # the first step warms the host buffer up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         g = M.FastWindingNumber(v, f, device=local)

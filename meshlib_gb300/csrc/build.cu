@@ -509,6 +509,7 @@ static cudaError_t setQueryRoot(DeviceTree& out, cudaStream_t s) {
     q.dip = out.dip;
     q.tri = out.tri;
     q.faceSlot = out.faceSlot;
+    q.nodes = reinterpret_cast<const float4*>(out.nodes);
     q.nLeaves = int32_t(out.nLeaves);
     q.nFaces = int32_t(out.nFaces);
     q.closed = out.closed ? 1 : 0;

@@ -39,13 +39,15 @@ struct QueryTree {
     const float4* __restrict__ dip;
     const float4* __restrict__ tri;
     const int32_t* __restrict__ faceSlot;  // face -> slot, -1 for invalid faces
+    const float4* __restrict__ nodes;      // the reference nodes (RefNode: {min.xyz, max.x} {max.yz, l, r})
     float4 rootDip0, rootDip1;             // {pos.xyz, rr} {dirArea.xyz, rootLink}
     float4 rootBox0, rootBox1;             // {min.xyz, rootLink} {max.xyz, 0}
     int32_t nLeaves;
     int32_t nFaces;
     // 1: the faces form a closed oriented surface (every edge used equally often in both
-    // directions) and a signed-distance voxel may take its sign from the voxel below it when no
-    // surface lies between them (gridKernel); 0: every sign comes from its own winding number
+    // directions): a signed-distance voxel may take its sign from the voxel below it when no surface
+    // lies between them, and otherwise from the signed count of surface crossings of a ray
+    // (gridKernel); 0: every sign comes from its own winding number
     int32_t closed;
 };
 

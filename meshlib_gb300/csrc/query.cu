@@ -500,6 +500,106 @@ __device__ __forceinline__ bool signReuseAllowed(const QueryTree& t, const DistO
     return t.closed != 0 && o.beta >= 2.f && fr > 0.25f && fr < 0.75f;
 }
 
+// ------------------------------------------------------------------ ray crossings (closed surfaces)
+// Kahan's 2x2 determinant a*b - c*d: relative error at most 2u (Jeannerod, Louvet and Muller, 2013),
+// so its sign is exact and it is 0 exactly when a*b == c*d.
+__device__ __forceinline__ float det2(float a, float b, float c, float d) {
+    const float w = __fmul_rn(c, d);
+    const float e = fmaf(-c, d, w);
+    const float f = fmaf(a, b, -w);
+    return __fadd_rn(f, e);
+}
+
+// Sign of the edge function E(P, Q) = Px Qy - Py Qx of a projected edge P -> Q (coordinates relative
+// to the ray's origin), exact, with E = 0 broken by simulation of simplicity: the origin moved by
+// (eps, eps^2), eps -> 0, changes E by eps (Py - Qy) + eps^2 (Qx - Px).  Swapping P and Q flips the
+// sign, so a ray meets exactly one of two triangles that share an edge on the same side of it, and
+// both or neither of two that fold over it.  0 only for a degenerate edge.
+__device__ __forceinline__ int edgeSign(float px, float py, float qx, float qy) {
+    const float e = det2(px, qy, py, qx);
+    if (e != 0.f) return e > 0.f ? 1 : -1;
+    if (py != qy) return py > qy ? 1 : -1;
+    if (qx != px) return qx > px ? 1 : -1;
+    return 0;
+}
+
+// Signed crossing of the vertical ray from q (up: +z, else -z) with triangle ABC: the crossing's
+// contribution to the winding number at q, +1 where the ray passes to the side the triangle's normal
+// points to and -1 the other way (a ray from inside a closed outward-oriented surface leaves it once
+// more than it enters), 0 when it misses.  The triangle is translated to the ray's origin in FP32, the
+// same way in every triangle that shares a vertex, so the translated mesh is closed as well and every
+// ray crosses it an exact number of times.  A crossing at the origin itself (q on the surface, where
+// the winding number decides between 0 and 1 by its approximation) sets *onSurface instead.
+__device__ __forceinline__ int rayCross(const float3& q, const float4& A, const float4& B, const float4& C, bool up,
+                                        bool* onSurface) {
+    const float ax = __fsub_rn(A.x, q.x), ay = __fsub_rn(A.y, q.y), bx = __fsub_rn(B.x, q.x), by = __fsub_rn(B.y, q.y),
+                cx = __fsub_rn(C.x, q.x), cy = __fsub_rn(C.y, q.y);
+    const int u = edgeSign(bx, by, cx, cy);
+    if (u == 0) return 0;
+    const int v = edgeSign(cx, cy, ax, ay);
+    if (v != u) return 0;
+    const int w = edgeSign(ax, ay, bx, by);
+    if (w != u) return 0;
+    // inside the projected triangle, whose orientation (the sign of its normal's z) is u; the plane
+    // meets the ray at z - qz = T / (U + V + W) with barycentric weights U, V, W
+    const float U = det2(bx, cy, by, cx), V = det2(cx, ay, cy, ax), W = det2(ax, by, ay, bx);
+    const float az = __fsub_rn(A.z, q.z), bz = __fsub_rn(B.z, q.z), cz = __fsub_rn(C.z, q.z);
+    float T = fmaf(U, az, fmaf(V, bz, __fmul_rn(W, cz)));
+    const float mag = fabsf(U * az) + fabsf(V * bz) + fabsf(W * cz);
+    if (fabsf(T) <= 1e-6f * mag) {  // close to the plane: the height again in FP64 from exact weights
+        const double Ud = double(bx) * double(cy) - double(by) * double(cx);
+        const double Vd = double(cx) * double(ay) - double(cy) * double(ax);
+        const double Wd = double(ax) * double(by) - double(ay) * double(bx);
+        const double Td = Ud * (double(A.z) - double(q.z)) + Vd * (double(B.z) - double(q.z)) + Wd * (double(C.z) - double(q.z));
+        T = Td > 0.0 ? 1.f : (Td < 0.0 ? -1.f : 0.f);
+    }
+    if (T == 0.f) {
+        *onSurface = true;
+        return 0;
+    }
+    const bool above = (T > 0.f) == (u > 0);
+    if (above != up) return 0;
+    return up ? u : -u;
+}
+
+// The exact winding number of a closed oriented surface at each lane's q with `need`: the signed
+// number of crossings of the vertical ray from q (up when the warp's first lane lies in the upper
+// half of the mesh's box, which shortens the rays), over the reference nodes' boxes (a ray meets a box
+// when its (x, y) lies in the box's footprint and the box reaches past q along the ray).
+// *onSurface: q lies on the surface (the caller evaluates the winding number there instead).
+__device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsigned* status, bool* onSurface) {
+    const int lane = threadIdx.x & 31;
+    int c = 0;
+    const unsigned m0 = __ballot_sync(FULL, need);
+    if (!m0 || t.nLeaves == 0) return 0;
+    const bool up = __shfl_sync(FULL, q.z, __ffs(m0) - 1) >= 0.5f * (t.rootBox0.z + t.rootBox1.z);
+    WarpStack st;
+    st.push(lane, 0, m0);
+    bool overflow = false;
+    while (st.sp > 0) {
+        int node;
+        unsigned m;
+        st.pop(node, m);
+        const float4 n0 = ld4(t.nodes + 2 * int64_t(node)), n1 = ld4(t.nodes + 2 * int64_t(node) + 1);
+        const bool hit = ((m >> lane) & 1u) && q.x >= n0.x && q.x <= n0.w && q.y >= n0.y && q.y <= n1.x &&
+                         (up ? n1.y >= q.z : n0.z <= q.z);
+        const unsigned mh = __ballot_sync(FULL, hit);
+        if (!mh) continue;
+        const int l = __float_as_int(n1.z), r = __float_as_int(n1.w);
+        if (r < 0) {  // a leaf: l is its face
+            const float4* tr = t.tri + 3 * int64_t(t.faceSlot[l]);
+            const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+            if (hit) c += rayCross(q, A, B, C, up, onSurface);
+        } else {
+            if (!st.push(lane, r, mh)) overflow = true;
+            if (!st.push(lane, l, mh)) overflow = true;
+            if (overflow) break;
+        }
+    }
+    if (overflow && lane == 0) atomicOr(status, kStatusStackOverflow);
+    return c;
+}
+
 // True when a voxel at q may take the sign of the voxel at qb, whose squared distance to the surface
 // is belowSq (> 0, from a search that ran to the end): qb is farther from the surface than from q, so
 // the segment between them meets no surface.  The margin covers the FP32 rounding of both centres and
@@ -607,8 +707,13 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
                 bool reIn = false;
                 const bool reuse = reuseOk && reuseSign<kTX, kTY, kTZ>(xf, x, y, z, z - (lz == 0 ? 1 : kTZ), lz, q, below,
                                                                       complete, dsq, &reIn);
-                const float w = fwnPacket<PRECISE>(t, q, active && valid && !reuse, betaSq, -1, scratch + 1);
-                const bool inside = reuse ? reIn : w > o.threshold;
+                // closed surface: the exact winding number from ray crossings, but the approximated
+                // one (the reference's decision) for a voxel on the surface; otherwise the latter
+                bool onSurface = false;
+                const int cw = reuseOk ? rayWinding(t, q, active && valid && !reuse, scratch + 1, &onSurface) : 0;
+                const bool fwn = reuseOk ? onSurface : (active && valid);
+                const float w = fwnPacket<PRECISE>(t, q, fwn, betaSq, -1, scratch + 1);
+                const bool inside = reuse ? reIn : (fwn ? w > o.threshold : float(cw) > o.threshold);
                 const float d = __fsqrt_rn(dsq);
                 res = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
                 // next tile: the bottom layer's lanes take the voxel one layer below them (this tile's
@@ -671,9 +776,15 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) vectorKernel
                 const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
                 seed = best;
                 const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
-                const float w = fwnPacket<PRECISE>(t, q, active && valid, betaSq, -1, scratch + 1);
+                // closed surfaces: the exact winding number from ray crossings (gridKernel)
+                bool onSurface = false;
+                const bool rays = signReuseAllowed(t, o);
+                const int cw = rays ? rayWinding(t, q, active && valid, scratch + 1, &onSurface) : 0;
+                const bool fwn = rays ? onSurface : (active && valid);
+                const float w = fwnPacket<PRECISE>(t, q, fwn, betaSq, -1, scratch + 1);
+                const bool inside = fwn ? w > o.threshold : float(cw) > o.threshold;
                 const float d = __fsqrt_rn(dsq);
-                res = valid ? (w > o.threshold ? -d : d) : __int_as_float(0x7fc00000);
+                res = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
             } else {
                 res = fwnPacket<PRECISE>(t, q, active, betaSq, skipSlot, scratch + 1);
             }
@@ -1069,8 +1180,11 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const Bat
             bool reIn = false;
             const bool reuse = reuseOk && reuseSign<TX, TY, TZ>(it.xf, x, y, z, z - (lz == 0 ? 1 : TZ), lz, q, below, complete,
                                                                 dsq, &reIn);
-            const float w = fwnPacket<PRECISE>(t, q, active && valid && !reuse, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
-            const bool inside = reuse ? reIn : w > o.threshold;
+            bool onSurface = false;  // as gridKernel: ray crossings on closed surfaces
+            const int cw = reuseOk ? rayWinding(t, q, active && valid && !reuse, scratch + 1, &onSurface) : 0;
+            const bool fwn = reuseOk ? onSurface : (active && valid);
+            const float w = fwnPacket<PRECISE>(t, q, fwn, __fmul_rn(o.beta, o.beta), -1, scratch + 1);
+            const bool inside = reuse ? reIn : (fwn ? w > o.threshold : float(cw) > o.threshold);
             const float d = __fsqrt_rn(dsq);
             const float res = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
             if (active) it.out[(size_t(z) * it.g.ny + y) * it.g.nx + x] = res;
