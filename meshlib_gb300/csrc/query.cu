@@ -567,12 +567,15 @@ __device__ __forceinline__ int rayCross(const float3& q, const float4& A, const 
 // half of the mesh's box, which shortens the rays), over the reference nodes' boxes (a ray meets a box
 // when its (x, y) lies in the box's footprint and the box reaches past q along the ray).
 // *onSurface: q lies on the surface (the caller evaluates the winding number there instead).
-__device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsigned* status, bool* onSurface) {
+// skipSlot: a leaf slot whose triangle the lane's ray ignores (-1: none); *upOut: the rays' direction.
+__device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsigned* status, bool* onSurface, int skipSlot = -1,
+                          bool* upOut = nullptr) {
     const int lane = threadIdx.x & 31;
     int c = 0;
     const unsigned m0 = __ballot_sync(FULL, need);
     if (!m0 || t.nLeaves == 0) return 0;
     const bool up = __shfl_sync(FULL, q.z, __ffs(m0) - 1) >= 0.5f * (t.rootBox0.z + t.rootBox1.z);
+    if (upOut) *upOut = up;
     WarpStack st;
     st.push(lane, 0, m0);
     bool overflow = false;
@@ -587,9 +590,10 @@ __device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsign
         if (!mh) continue;
         const int l = __float_as_int(n1.z), r = __float_as_int(n1.w);
         if (r < 0) {  // a leaf: l is its face
-            const float4* tr = t.tri + 3 * int64_t(t.faceSlot[l]);
+            const int slot = t.faceSlot[l];
+            const float4* tr = t.tri + 3 * int64_t(slot);
             const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
-            if (hit) c += rayCross(q, A, B, C, up, onSurface);
+            if (hit && slot != skipSlot) c += rayCross(q, A, B, C, up, onSurface);
         } else {
             if (!st.push(lane, r, mh)) overflow = true;
             if (!st.push(lane, l, mh)) overflow = true;
@@ -927,6 +931,7 @@ __global__ void __launch_bounds__(kThreads, 4) selfIntKernel(QueryTree t, float 
     const int lane = threadIdx.x & 31;
     const float betaSq = __fmul_rn(beta, beta);
     const uint64_t numTiles = (uint64_t(t.nLeaves) + 31) / 32;
+    const bool rays = t.closed != 0 && beta >= 2.f && !wn;  // see below
     for (;;) {
         const unsigned tile = nextTicket(scratch, lane);
         if (tile >= numTiles) break;
@@ -943,10 +948,36 @@ __global__ void __launch_bounds__(kThreads, 4) selfIntKernel(QueryTree t, float 
                             __fmul_rn(third, __fadd_rn(__fadd_rn(A.z, B.z), C.z)));
             face = __float_as_int(A.w);
         }
-        const float w = fwnPacket<PRECISE>(t, q, active, betaSq, active ? slot : -1, scratch + 1);
+        // Closed surfaces, bits only: the ray from the centroid that ignores its own face counts the
+        // exact winding number on the side of the face the ray leaves into; the other side differs by
+        // one, by the face's orientation.  The reference's value (its own face skipped) lies halfway,
+        // so the face is flagged when the smaller side is <= -1 or >= 1.  A face whose centroid does
+        // not fall strictly inside its own projection (near-vertical or degenerate), or that lies on
+        // another face, gets the approximated winding number as before.
+        bool fwn = active, flag = false;
+        if (rays) {
+            int orient = 0;  // the sign of the face normal's z, exact
+            if (active) {
+                const float4* tr = t.tri + 3 * int64_t(slot);
+                const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+                const float ax = __fsub_rn(A.x, q.x), ay = __fsub_rn(A.y, q.y), bx = __fsub_rn(B.x, q.x),
+                            by = __fsub_rn(B.y, q.y), cx = __fsub_rn(C.x, q.x), cy = __fsub_rn(C.y, q.y);
+                const int e0 = edgeSign(bx, by, cx, cy), e1 = edgeSign(cx, cy, ax, ay), e2 = edgeSign(ax, ay, bx, by);
+                if (e0 != 0 && e0 == e1 && e1 == e2) orient = e0;
+            }
+            bool onSurface = false, up = true;
+            const int wd = rayWinding(t, q, active && orient != 0, scratch + 1, &onSurface, active ? slot : -1, &up);
+            fwn = active && (orient == 0 || onSurface);
+            if (active && !fwn) {
+                const int a = up ? orient : -orient;  // +1: the face's normal points along the ray
+                const int m = a > 0 ? wd : wd + a;    // the smaller of the two sides, wd and wd + a
+                flag = m <= -1 || m >= 1;
+            }
+        }
+        const float w = fwnPacket<PRECISE>(t, q, fwn, betaSq, active ? slot : -1, scratch + 1);
         if (active) {
             if (wn) wn[face] = w;
-            if (w < 0.f || w > 1.f) atomicOr((unsigned long long*)bits + (face >> 6), 1ull << (face & 63));
+            if (fwn ? (w < 0.f || w > 1.f) : flag) atomicOr((unsigned long long*)bits + (face >> 6), 1ull << (face & 63));
         }
     }
 }

@@ -127,3 +127,22 @@ def test_reuse_identical_at_benchmark_scale(M):
             res.append(out.cpu().numpy())
         _same(*res)
     g.set_sign_reuse(True)
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_self_intersection_bits_by_rays(M, precise):
+    """calcSelfIntersections without winding numbers takes a closed mesh's bits from ray crossings; they
+    equal the bits of the winding-number walk (with_wn=True) on self-intersecting and clean closed
+    meshes, and open meshes keep the walk."""
+    cases = [mg.overlapping_spheres(seed=0, level=5), mg.overlapping_spheres(seed=1, level=6), mg.noisy_icosphere(seed=2, level=6)]
+    v, f = mg.noisy_torus(seed=3)
+    cases.append((v, f))
+    cases.append((v, f[:-50]))  # open
+    flagged = 0
+    for v, f in cases:
+        g = M.FastWindingNumber(v, f, precise=precise)
+        fast = g.calcSelfIntersections()
+        walk, _ = g.calcSelfIntersections(with_wn=True)
+        assert np.array_equal(fast, walk)
+        flagged += int(fast.sum())
+    assert flagged > 0
