@@ -721,7 +721,9 @@ def main():
                        "l2": "flushed between steps (512 MB write)",
                        "parallelism": f"z-slabs x{world} (one grid split by layers, mesh replicated, no collective)"},
             "replicas": replicas,
-            "gpu_launches": args.steps,  # one gridKernel launch per timed step (its counter reset is a memset)
+            # per timed step: the column-ray sign pass (closed mesh, vertical z axis) and gridKernel (their
+            # ticket-counter resets and the hand-over fill are memsets)
+            "gpu_launches": args.steps * (2 if fwn.is_closed() else 1),
             "e2e": {"value": e2e_val, "unit": "voxels/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                     "d2h_bytes_per_step": int(slab_vox * 4), "s_per_step": e2e_s,
                     "s_create_per_step": float(np.mean(create_times)) if create_times else None},

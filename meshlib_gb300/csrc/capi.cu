@@ -193,11 +193,11 @@ int newHandle(int device, gbfwn_mesh_s** out) {
     return GBFWN_OK;
 }
 
-// The column hand-over words of a signed-distance grid launch on stream s, grown on the handle's
+// The column hand-over words (and column-ray sign bits) of a signed-distance grid launch on stream s, grown on the handle's
 // stream (a launch on another stream waits for the growth).  Without them (allocation failure) the
 // launch runs as well, its columns starting cold.
-float* colStateFor(gbfwn_mesh_s* h, const GridRange& r, const DistOpts& o, cudaStream_t s, size_t* bytes) {
-    const size_t need = gridSdfColumnStateBytes(r, o);
+float* colStateFor(gbfwn_mesh_s* h, const GridRange& r, const Xf& X, const DistOpts& o, cudaStream_t s, size_t* bytes) {
+    const size_t need = gridSdfColumnStateBytes(h->tree.q, r, X, o);
     *bytes = 0;
     if (need == 0) return nullptr;
     if (h->colCap < need) {
@@ -453,6 +453,11 @@ GBFWN_API int gbfwn_make_signed_by_winding_number_dev(gbfwn_handle h, const int3
     DeviceGuard g(h->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     const int64_t n = int64_t(dims[0]) * dims[1] * dims[2];
+    if (signColumnsApply(h->tree.q, X, beta, threshold)) {  // closed mesh, z axis vertical: one ray per column
+        GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
+        const cudaError_t e = launchSignColumns(h->tree.q, r, X, beta, threshold, h->precise, nullptr, d_values, h->scratch, s);
+        return e ? cudaFail(e, "gbfwn_make_signed_by_winding_number_dev") : GBFWN_OK;
+    }
     float* wn = nullptr;
     cudaError_t e = g_failAllocs > 0 ? (--g_failAllocs, cudaErrorMemoryAllocation)
                                      : cudaMallocAsync((void**)&wn, sizeof(float) * size_t(n), s);
@@ -478,7 +483,7 @@ GBFWN_API int gbfwn_from_grid_with_distances_dev(gbfwn_handle h, const int32_t d
     GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
     const DistOpts o = toOpts(opts);
     size_t colBytes = 0;
-    float* col = colStateFor(h, r, o, s, &colBytes);
+    float* col = colStateFor(h, r, X, o, s, &colBytes);
     cudaError_t e = launchGridSdf(h->tree.q, r, X, o, h->precise, d_out, h->scratch, s, col, colBytes);
     return e ? cudaFail(e, "gbfwn_from_grid_with_distances_dev") : GBFWN_OK;
 }
@@ -506,7 +511,7 @@ GBFWN_API int gbfwn_from_grid_with_distances_slab_dev(gbfwn_handle h, const int3
     GridRange r{dims[0], dims[1], dims[2], z0, z1, z0};
     const DistOpts o = toOpts(opts);
     size_t colBytes = 0;
-    float* col = colStateFor(h, r, o, s, &colBytes);
+    float* col = colStateFor(h, r, X, o, s, &colBytes);
     cudaError_t e = launchGridSdf(h->tree.q, r, X, o, h->precise, d_out, h->scratch, s, col, colBytes);
     return e ? cudaFail(e, "gbfwn_from_grid_with_distances_slab_dev") : GBFWN_OK;
 }
@@ -775,7 +780,7 @@ GBFWN_API int gbfwn_from_grid_with_distances(gbfwn_handle h, const int32_t dims[
         h, dims,
         [&](const GridRange& r, float* buf, cudaStream_t s) {
             size_t colBytes = 0;
-            float* col = colStateFor(h, r, o, s, &colBytes);
+            float* col = colStateFor(h, r, X, o, s, &colBytes);
             return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s, col, colBytes);
         },
         out, 0, 0, nullptr, nullptr, cb, user, "gbfwn_from_grid_with_distances");
@@ -811,7 +816,7 @@ GBFWN_API int gbfwn_from_grid_with_distances_by_parts(gbfwn_handle h, const int3
         h, dims,
         [&](const GridRange& r, float* buf, cudaStream_t s) {
             size_t colBytes = 0;
-            float* col = colStateFor(h, r, o, s, &colBytes);
+            float* col = colStateFor(h, r, X, o, s, &colBytes);
             return launchGridSdf(h->tree.q, r, X, o, h->precise, buf, h->scratch, s, col, colBytes);
         },
         nullptr, layerOverlap, maxLayersPerSlab, slab, slabUser, cb, user, "gbfwn_from_grid_with_distances_by_parts");
@@ -837,7 +842,8 @@ GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t di
     const size_t vox = dims ? size_t(std::max(dims[0], 0)) * size_t(std::max(dims[1], 0)) * size_t(std::max(dims[2], 0)) : 0;
     const size_t tiles = (dims && vox) ? size_t(gridTiles(dims[0], dims[1], dims[2])) : 0;
     const size_t items = std::min(tiles, tiles / 16 + size_t(50) * size_t(numSMs()) * 32);
-    return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float) + items * 32 * sizeof(float);
+    const size_t bits = dims && vox ? size_t((dims[0] + 31) / 32) * size_t(dims[1]) * size_t(dims[2]) * 4 : 0;
+    return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float) + items * 32 * sizeof(float) + bits;
 }
 // staging: points in (12 B) and results out (4 B); from 8,192 points also the Morton order and its
 // sort scratch (6 int32 words per point)

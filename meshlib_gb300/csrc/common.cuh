@@ -81,10 +81,18 @@ enum : unsigned {
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
                           unsigned* scratch, cudaStream_t s);
 // colState (optional, colBytes >= gridSdfColumnStateBytes): device words through which the columns of
-// the launch hand their top layer's distances, signs and closest triangles to the columns above.
+// the launch hand their top layer's distances, signs and closest triangles to the columns above,
+// followed, on a closed mesh whose grid has a vertical z axis (signColumnsApply), by the inside bits
+// of the column rays, computed first.
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                           float* out, unsigned* scratch, cudaStream_t s, float* colState = nullptr, size_t colBytes = 0);
-size_t gridSdfColumnStateBytes(const GridRange& g, const DistOpts& o);
+size_t gridSdfColumnStateBytes(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o);
+// Signs of a closed mesh's grid from one vertical ray per (x, y) column (query.cu, signColumnsKernel):
+// applicable when signColumnsApply; writes inside bits (one 32-bit word per 32 voxels along x, layout
+// (z - zOut, y, x / 32)) or negates `values` where the voxel is inside.
+bool signColumnsApply(const QueryTree& t, const Xf& xf, float beta, float threshold);
+cudaError_t launchSignColumns(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, float threshold, int precise,
+                              uint32_t* bits, float* values, unsigned* scratch, cudaStream_t s);
 // One mesh + grid of a batched launch (query.cu batchKernel): its tickets are
 // [tileBase, tileBase + batchTiles(...)): columns of up to kBatchSeg tiles of the launch's shape.
 struct BatchItem {

@@ -479,6 +479,10 @@ struct TileGrid {
     // (-1 none) -- and read by the column above it when it starts; filled with 0xff bytes (NaN / -1)
     // before the launch, so a column that starts before the one below it has ended starts cold
     float* colState;
+    // optional inside bits of every voxel of the range (signColumnsKernel's layout: one word per 32
+    // voxels along x, (z - zOut, y, x / 32)); when given, the signed-distance kernel takes its signs
+    // from them instead of its own walks
+    const uint32_t* signBits;
 };
 
 __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
@@ -604,6 +608,154 @@ __device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsign
     return c;
 }
 
+// ------------------------------------------------------------------ sign columns (closed surfaces)
+// One upward vertical ray per (x, y) column of a grid whose z axis is the world's (xf's third column
+// (0, 0, +s)): every voxel of the column lies on that ray, so the exact winding number of a voxel is
+// the signed number of the ray's crossings above it.  The crossings' heights come from the exact
+// weights in FP64 (error below 1e-15 of the mesh's largest |z|); a voxel within 1e-12 of that of a
+// crossing's height (on the surface, up to rounding), and every voxel of a column with more than
+// kColumnCrossings crossings above its first voxel, gets the approximated winding number of the
+// winding-number walk instead.
+constexpr int kColumnCrossings = 24;
+
+// Crossing of the upward ray from q with triangle ABC: its height (FP64) and sign (the contribution
+// to the winding number below it), false when the ray's line misses the triangle (the same exact,
+// watertight projection test as rayCross).
+__device__ __forceinline__ bool columnCross(const float3& q, const float4& A, const float4& B, const float4& C, double* z, int* sign) {
+    const float ax = __fsub_rn(A.x, q.x), ay = __fsub_rn(A.y, q.y), bx = __fsub_rn(B.x, q.x), by = __fsub_rn(B.y, q.y),
+                cx = __fsub_rn(C.x, q.x), cy = __fsub_rn(C.y, q.y);
+    const int u = edgeSign(bx, by, cx, cy);
+    if (u == 0) return false;
+    if (edgeSign(cx, cy, ax, ay) != u || edgeSign(ax, ay, bx, by) != u) return false;
+    const double U = double(bx) * double(cy) - double(by) * double(cx);
+    const double V = double(cx) * double(ay) - double(cy) * double(ax);
+    const double W = double(ax) * double(by) - double(ay) * double(bx);
+    const double det = U + V + W;
+    if (det == 0.0) return false;
+    *z = (U * double(A.z) + V * double(B.z) + W * double(C.z)) / det;
+    *sign = u;
+    return true;
+}
+
+// For the grid columns of the launch (32 consecutive x per warp, in segments of kColumnSeg layers,
+// each with its own ray): inside = (winding number of the voxel > threshold), written as bits (one
+// word per 32 voxels along x, layout (z - zOut, y, x / 32)) or applied to `values` (negated where
+// inside; value index (z - zOut) nx ny + y nx + x).  The range [z0, z1) of dims is covered.
+constexpr int kColumnSeg = 128;
+
+template <bool PRECISE>
+__global__ void __launch_bounds__(kThreads) signColumnsKernel(QueryTree t, GridRange g, Xf xf, float threshold, float beta,
+                                                          uint32_t* __restrict__ bits, float* __restrict__ values,
+                                                          unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const float betaSq = __fmul_rn(beta, beta);
+    const int wordsX = (g.nx + 31) >> 5;
+    const int segs = (g.z1 - g.z0 + kColumnSeg - 1) / kColumnSeg;
+    const uint64_t items = uint64_t(wordsX) * uint64_t(g.ny) * uint64_t(segs);
+    const size_t sxy = size_t(g.nx) * g.ny;
+    // the heights' rounding error is below 1e-15 of the largest |z| of the mesh
+    const double zTol = 1e-12 * double(fmaxf(fabsf(t.rootBox0.z), fabsf(t.rootBox1.z)));
+    double zs[kColumnCrossings];
+    int sg[kColumnCrossings];
+    for (;;) {
+        const unsigned item = nextTicket(scratch, lane);
+        if (item >= items) break;
+        const int wx = int(item % unsigned(wordsX));
+        const unsigned rest = item / unsigned(wordsX);
+        const int y = int(rest % unsigned(g.ny));
+        const int zs0 = g.z0 + int(rest / unsigned(g.ny)) * kColumnSeg, zs1 = min(g.z1, zs0 + kColumnSeg);
+        const int x = wx * 32 + lane;
+        const bool active = x < g.nx;
+        const int xc = active ? x : 0;
+        const float3 q0 = xfPoint(xf, xc, y, zs0);
+        // the ray: a packet walk over the reference nodes collecting the crossings above q0, by height
+        int n = 0;
+        bool overflow = false;
+        {
+            WarpStack st;
+            st.push(lane, 0, __ballot_sync(FULL, active));
+            bool stackFull = false;
+            while (st.sp > 0 && t.nLeaves > 0) {
+                int node;
+                unsigned m;
+                st.pop(node, m);
+                const float4 n0 = ld4(t.nodes + 2 * int64_t(node)), n1 = ld4(t.nodes + 2 * int64_t(node) + 1);
+                const bool hit = ((m >> lane) & 1u) && q0.x >= n0.x && q0.x <= n0.w && q0.y >= n0.y && q0.y <= n1.x && n1.y >= q0.z;
+                const unsigned mh = __ballot_sync(FULL, hit);
+                if (!mh) continue;
+                const int l = __float_as_int(n1.z), r = __float_as_int(n1.w);
+                if (r < 0) {
+                    const float4* tr = t.tri + 3 * int64_t(t.faceSlot[l]);
+                    const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+                    double z;
+                    int sgn;
+                    if (hit && columnCross(q0, A, B, C, &z, &sgn) && z >= double(q0.z) - zTol) {
+                        if (n < kColumnCrossings) {
+                            int k = n++;
+                            while (k > 0 && zs[k - 1] > z) {
+                                zs[k] = zs[k - 1];
+                                sg[k] = sg[k - 1];
+                                --k;
+                            }
+                            zs[k] = z;
+                            sg[k] = sgn;
+                        } else {
+                            overflow = true;
+                        }
+                    }
+                } else if (!st.push(lane, r, mh) || !st.push(lane, l, mh)) {
+                    stackFull = true;
+                    break;
+                }
+            }
+            if (stackFull) {
+                overflow = true;  // every lane of the warp falls back
+                if (lane == 0) atomicOr(scratch + 1, kStatusStackOverflow);
+            }
+        }
+        // the sweep up the segment, 32 layers at a time: w = signed crossings above the voxel
+        int w = 0, p = 0;
+        for (int k = 0; k < n; ++k) w += sg[k];
+        for (int zc = zs0; zc < zs1; zc += 32) {
+            const int kn = min(32, zs1 - zc);
+            uint32_t in = 0, amb = 0;  // bit k: the voxel at zc + k
+            for (int k = 0; k < kn; ++k) {
+                const double vz = double(xfPoint(xf, xc, y, zc + k).z);
+                while (p < n && zs[p] < vz) {
+                    w -= sg[p];
+                    ++p;
+                }
+                if (overflow || (p < n && zs[p] - vz <= zTol) || (p > 0 && vz - zs[p - 1] <= zTol))
+                    amb |= 1u << k;
+                else if (float(w) > threshold)
+                    in |= 1u << k;
+            }
+            if (!active) amb = in = 0;
+            if (__any_sync(FULL, amb != 0)) {  // on the surface (up to rounding): the winding-number walk
+                for (int k = 0; k < kn; ++k) {
+                    const bool need = (amb >> k) & 1u;
+                    if (!__any_sync(FULL, need)) continue;
+                    const float wf = fwnPacket<PRECISE>(t, xfPoint(xf, xc, y, zc + k), need, betaSq, -1, scratch + 1);
+                    if (need && wf > threshold) in |= 1u << k;
+                }
+            }
+            if (values) {
+                float* vp = values + size_t(zc - g.zOut) * sxy + size_t(y) * g.nx + xc;
+#pragma unroll 8
+                for (int k = 0; k < kn; ++k)
+                    if ((in >> k) & 1u) vp[size_t(k) * sxy] = -vp[size_t(k) * sxy];
+            } else {
+                uint32_t mine = 0;  // lane k stores layer zc + k's word
+                for (int k = 0; k < kn; ++k) {
+                    const uint32_t word = __ballot_sync(FULL, (in >> k) & 1u);
+                    if (lane == k) mine = word;
+                }
+                if (lane < kn) bits[(size_t(zc + lane - g.zOut) * g.ny + y) * wordsX + wx] = mine;
+            }
+        }
+    }
+}
+
 // True when a voxel at q may take the sign of the voxel at qb, whose squared distance to the surface
 // is belowSq (> 0, from a search that ran to the end): qb is farther from the surface than from q, so
 // the segment between them meets no surface.  The margin covers the FP32 rounding of both centres and
@@ -650,14 +802,15 @@ __device__ __forceinline__ bool reuseSign(const Xf& xf, int x, int y, int z, int
 // fewer node visits with an exact bound, in a CPU model of the walk).  On a closed surface the same
 // voxel below also lends its sign (signReuseAllowed) when its distance exceeds the step between the
 // two voxel centres, and the lane skips its winding-number walk.
-template <bool PRECISE, bool DIST>
+template <bool PRECISE, bool DIST, bool BITS = false>
 __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
                                                        float* __restrict__ out, unsigned* scratch) {
     const int lane = threadIdx.x & 31;
     const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
     const float betaSq = __fmul_rn(o.beta, o.beta);
     const size_t sxy = size_t(g.nx) * g.ny;
-    const bool reuseOk = DIST && signReuseAllowed(t, o);
+    const bool reuseOk = DIST && !BITS && signReuseAllowed(t, o);
+    const int wordsX = (g.nx + 31) >> 5;
     for (;;) {
         const unsigned item = nextTicket(scratch, lane);
         if (item >= tg.numItems) break;
@@ -689,7 +842,7 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
             // the column below ended (its state was written) or not yet (0xff bytes: start cold); the
             // voxel below both layers of the first tile is that column's top-layer voxel
             const float* cs = tg.colState + size_t(item - colsPerSlab) * (2 * kLayer);
-            below = __ldcg(cs + lane % kLayer);
+            if (!BITS) below = __ldcg(cs + lane % kLayer);
             seed = __float_as_int(__ldcg(cs + kLayer + lane % kLayer));
         }
         for (int j = 0; j < nSeg; ++j) {
@@ -708,25 +861,30 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
                 const float dsq = cpPacket<PRECISE, true>(t, q, active, up, o.minDistSq, scratch + 1, &best);
                 const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
                 const bool complete = active && valid && dsq >= o.minDistSq;
-                bool reIn = false;
-                const bool reuse = reuseOk && reuseSign<kTX, kTY, kTZ>(xf, x, y, z, z - (lz == 0 ? 1 : kTZ), lz, q, below,
-                                                                      complete, dsq, &reIn);
-                // closed surface: the exact winding number from ray crossings, but the approximated
-                // one (the reference's decision) for a voxel on the surface; otherwise the latter
-                bool onSurface = false;
-                const int cw = reuseOk ? rayWinding(t, q, active && valid && !reuse, scratch + 1, &onSurface) : 0;
-                const bool fwn = reuseOk ? onSurface : (active && valid);
-                const float w = fwnPacket<PRECISE>(t, q, fwn, betaSq, -1, scratch + 1);
-                const bool inside = reuse ? reIn : (fwn ? w > o.threshold : float(cw) > o.threshold);
+                bool inside;
+                if (BITS) {  // the column rays' signs
+                    const uint32_t word = active ? __ldg(tg.signBits + (size_t(z - g.zOut) * g.ny + y) * wordsX + (x >> 5)) : 0u;
+                    inside = (word >> (x & 31)) & 1u;
+                } else {
+                    bool reIn = false;
+                    const bool reuse = reuseOk && reuseSign<kTX, kTY, kTZ>(xf, x, y, z, z - (lz == 0 ? 1 : kTZ), lz, q, below,
+                                                                          complete, dsq, &reIn);
+                    // closed surface: the exact winding number from ray crossings, but the approximated
+                    // one (the reference's decision) for a voxel on the surface; otherwise the latter
+                    bool onSurface = false;
+                    const int cw = reuseOk ? rayWinding(t, q, active && valid && !reuse, scratch + 1, &onSurface) : 0;
+                    const bool fwn = reuseOk ? onSurface : (active && valid);
+                    const float w = fwnPacket<PRECISE>(t, q, fwn, betaSq, -1, scratch + 1);
+                    inside = reuse ? reIn : (fwn ? w > o.threshold : float(cw) > o.threshold);
+                }
                 const float d = __fsqrt_rn(dsq);
                 res = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
                 // next tile: the bottom layer's lanes take the voxel one layer below them (this tile's
                 // top layer), the others their own voxel two layers below.  A distance counts only when
                 // the search ran to the end (not cut short below minDistSq): no surface is closer then.
                 const int src = lane + (kTZ - 1) * kTX * kTY * (lz == 0);
-                const float mine = complete ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000);
                 seed = __shfl_sync(FULL, best, src);
-                below = __shfl_sync(FULL, mine, src);
+                if (!BITS) below = __shfl_sync(FULL, complete ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000), src);
                 if (tg.colState && !tg.runs && j == nSeg - 1 && lz == kTZ - 1) {
                     // the column's last tile: the top layer's lanes hold their own voxels' state and
                     // pass on the distances and the seeds at this work item's words (the item
@@ -1029,6 +1187,7 @@ static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
     tg.numTiles = uint32_t(uint64_t(tg.tilesX) * tg.tilesY * tg.tilesZ);
     tg.runs = nullptr;
     tg.colState = nullptr;
+    tg.signBits = nullptr;
     // Longer columns reuse more seeds; shorter ones leave more items for the tail of the persistent
     // grid.  Measured at 256^3 / 512^3 on 1.3 M triangles: keep >= 25 items per (32-warps-per-SM)
     // resident warp, and columns of at most 32 tiles for unbanded signed distances (512^3: 16 tiles
@@ -1054,6 +1213,19 @@ cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf
     return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
+bool signColumnsApply(const QueryTree& t, const Xf& xf, float beta, float threshold) {
+    const float fr = threshold - floorf(threshold);
+    return t.closed && beta >= 2.f && fr > 0.25f && fr < 0.75f && xf.a[2] == 0.f && xf.a[5] == 0.f && xf.a[8] > 0.f;
+}
+
+cudaError_t launchSignColumns(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, float threshold, int precise,
+                              uint32_t* bits, float* values, unsigned* scratch, cudaStream_t s) {
+    const uint64_t items = uint64_t((g.nx + 31) / 32) * uint64_t(g.ny) * uint64_t((g.z1 - g.z0 + kColumnSeg - 1) / kColumnSeg);
+    if (precise)
+        return launchPersistent(signColumnsKernel<true>, items, scratch, s, t, g, xf, threshold, beta, bits, values, scratch);
+    return launchPersistent(signColumnsKernel<false>, items, scratch, s, t, g, xf, threshold, beta, bits, values, scratch);
+}
+
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
                           unsigned* scratch, cudaStream_t s) {
     const TileGrid tg = tileGridFor(g);
@@ -1063,8 +1235,14 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
     return launchPersistent(gridKernel<false, false>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
 }
 
-size_t gridSdfColumnStateBytes(const GridRange& g, const DistOpts& o) {
-    return size_t(tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16).numItems) * (2 * kLayer) * sizeof(float);
+// Column hand-over words, then (when the column rays apply) the inside bits of the range.
+static size_t signBitsBytes(const GridRange& g) {
+    return size_t((g.nx + 31) >> 5) * size_t(g.ny) * size_t(g.z1 - g.z0) * sizeof(uint32_t);
+}
+
+size_t gridSdfColumnStateBytes(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o) {
+    const size_t col = size_t(tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16).numItems) * (2 * kLayer) * sizeof(float);
+    return col + (signColumnsApply(t, xf, o.beta, o.threshold) ? signBitsBytes(g) : 0);
 }
 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
@@ -1075,6 +1253,15 @@ cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, 
         cudaError_t e = cudaMemsetAsync(colState, 0xff, need, s);
         if (e) return e;
         tg.colState = colState;
+        if (signColumnsApply(t, xf, o.beta, o.threshold) && colBytes >= need + signBitsBytes(g)) {
+            // closed surface, vertical z axis: the signs from one ray per column segment first
+            uint32_t* bits = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(colState) + need);
+            if ((e = launchSignColumns(t, g, xf, o.beta, o.threshold, precise, bits, nullptr, scratch, s))) return e;
+            tg.signBits = bits;
+            if (precise)
+                return launchPersistent(gridKernel<true, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+            return launchPersistent(gridKernel<false, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+        }
     }
     if (precise)
         return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);

@@ -146,3 +146,88 @@ def test_self_intersection_bits_by_rays(M, precise):
         assert np.array_equal(fast, walk)
         flagged += int(fast.sum())
     assert flagged > 0
+
+
+def _signed_pass(M, g, dims, xf, vals, enable, thr=0.5):
+    import torch
+    g.set_sign_reuse(enable)
+    d = torch.from_numpy(vals.copy()).cuda()
+    g.makeSignedByWindingNumber_dev(dims, xf, d.data_ptr(), threshold=thr, stream=0)
+    torch.cuda.synchronize()
+    g.set_sign_reuse(True)
+    return d.cpu().numpy()
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_sign_columns_identical(M, precise):
+    """makeSignedByWindingNumber on a closed mesh with the grid's z axis vertical takes each column's
+    signs from one upward ray (the signed count of crossings above each voxel); the negated voxels equal
+    those of the winding-number walk at every voxel: clean, self-intersecting (winding number 2), far
+    from the origin, a stack of 16 spheres (32 crossings per column, more than one ray keeps: those
+    columns take the walk), ragged and z-scaled grids, thresholds 0.5 and 0.3, and rotated grids
+    (the walk)."""
+    rng = np.random.default_rng(11)
+    v, f = mg.noisy_icosphere(seed=1, level=5)
+    stack_v = np.concatenate([v * 0.4 + np.float32([0, 0, 1.0 * k]) for k in range(16)]).astype(np.float32)
+    stack_f = np.concatenate([f + k * len(v) for k in range(16)]).astype(np.int32)
+    cases = [mg.noisy_torus(seed=4), mg.overlapping_spheres(seed=3, level=5), ((v + np.float32(3.0e3)).astype(np.float32), f),
+             (stack_v, stack_f)]
+    negated = 0
+    for cv, cf in cases:
+        g = M.FastWindingNumber(cv, cf, precise=precise)
+        assert g.is_closed()
+        dims, xf = mg.grid_for(cv, 72)
+        xf = np.asarray(xf, np.float32).copy()
+        grids = [(tuple(dims), xf)]
+        ragged = xf.copy()
+        ragged[8] *= 0.5  # z pitch halved, twice the layers
+        grids.append(((dims[0] - 5, dims[1] - 3, 2 * dims[2] + 1), ragged))
+        for gd, gx in grids:
+            vals = rng.uniform(0.1, 1.0, int(np.prod(gd))).astype(np.float32)
+            for thr in (0.5, 0.3):
+                a = _signed_pass(M, g, gd, gx, vals, True, thr)
+                b = _signed_pass(M, g, gd, gx, vals, False, thr)
+                assert np.array_equal(a, b)
+                negated += int((a < 0).sum())
+    assert negated > 0
+    # a rotated grid keeps the walk (and the same result either way)
+    cv, cf = cases[0]
+    g = M.FastWindingNumber(cv, cf, precise=precise)
+    dims, xf = mg.grid_for(cv, 40)
+    c, s = np.float32(np.cos(0.3)), np.float32(np.sin(0.3))
+    rot = np.asarray(xf, np.float32).copy()
+    rot[:9] = (rot[:9].reshape(3, 3) @ np.array([[1, 0, 0], [0, c, -s], [0, s, c]], np.float32)).reshape(-1)
+    vals = rng.uniform(0.1, 1.0, int(np.prod(dims))).astype(np.float32)
+    assert np.array_equal(_signed_pass(M, g, dims, rot, vals, True), _signed_pass(M, g, dims, rot, vals, False))
+
+
+def test_sign_columns_identical_at_benchmark_scale(M):
+    """The 1,310,720-triangle icosphere, 256^3: the column rays negate the same voxels as the walk."""
+    v, f = mg.noisy_icosphere(seed=0, level=8)
+    dims, xf = mg.grid_for(v, 256)
+    g = M.FastWindingNumber(v, f)
+    vals = np.random.default_rng(2).uniform(0.1, 1.0, int(np.prod(dims))).astype(np.float32)
+    a = _signed_pass(M, g, dims, xf, vals, True)
+    b = _signed_pass(M, g, dims, xf, vals, False)
+    assert np.array_equal(a, b) and (a < 0).any()
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_reuse_and_rays_identical_on_tilted_grids(M, precise):
+    """A grid whose z axis is not vertical has no column rays: its signs come from sign reuse and one
+    ray per voxel, and equal the winding-number walk's, with and without a band."""
+    for v, f in (mg.noisy_torus(seed=6), mg.overlapping_spheres(seed=4, level=5)):
+        g = M.FastWindingNumber(v, f, precise=precise)
+        dims, xf = mg.grid_for(v, 64)
+        c, s = np.float32(np.cos(0.2)), np.float32(np.sin(0.2))
+        tilt = np.asarray(xf, np.float32).copy()
+        tilt[:9] = (tilt[:9].reshape(3, 3) @ np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]], np.float32)).reshape(-1)
+        band = 0.03 * mg.diag(v)
+        for opts in (None, M.DistanceToMeshOptions(maxDistSq=band * band)):
+            res = []
+            for enable in (True, False):
+                g.set_sign_reuse(enable)
+                res.append(g.calcFromGridWithDistances(dims, tilt, opts))
+            g.set_sign_reuse(True)
+            _same(*res)
+            assert (res[0] < 0).any()
