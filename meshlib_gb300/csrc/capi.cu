@@ -193,11 +193,10 @@ int newHandle(int device, gbfwn_mesh_s** out) {
     return GBFWN_OK;
 }
 
-// The column hand-over words (and column-ray sign bits) of a signed-distance grid launch on stream s, grown on the handle's
-// stream (a launch on another stream waits for the growth).  Without them (allocation failure) the
-// launch runs as well, its columns starting cold.
-float* colStateFor(gbfwn_mesh_s* h, const GridRange& r, const Xf& X, const DistOpts& o, cudaStream_t s, size_t* bytes) {
-    const size_t need = gridSdfColumnStateBytes(h->tree.q, r, X, o);
+// The handle's grid work buffer (column hand-over words, inside bits and crossing lists of a grid
+// launch on stream s), at least `need` bytes, grown on the handle's stream (a launch on another
+// stream waits for the growth); nullptr when it cannot grow, and the launch runs without it.
+void* workFor(gbfwn_mesh_s* h, size_t need, cudaStream_t s, size_t* bytes) {
     *bytes = 0;
     if (need == 0) return nullptr;
     if (h->colCap < need) {
@@ -208,7 +207,11 @@ float* colStateFor(gbfwn_mesh_s* h, const GridRange& r, const Xf& X, const DistO
         if (s != h->stream) cudaStreamSynchronize(h->stream);
     }
     *bytes = h->colCap;
-    return static_cast<float*>(h->colBuf);
+    return h->colBuf;
+}
+
+float* colStateFor(gbfwn_mesh_s* h, const GridRange& r, const Xf& X, const DistOpts& o, cudaStream_t s, size_t* bytes) {
+    return static_cast<float*>(workFor(h, gridSdfColumnStateBytes(h->tree.q, r, X, o), s, bytes));
 }
 
 int refitCommon(gbfwn_mesh_s* h, const uint64_t* dChanged, cudaStream_t s, const char* what) {
@@ -455,7 +458,10 @@ GBFWN_API int gbfwn_make_signed_by_winding_number_dev(gbfwn_handle h, const int3
     const int64_t n = int64_t(dims[0]) * dims[1] * dims[2];
     if (signColumnsApply(h->tree.q, X, beta, threshold)) {  // closed mesh, z axis vertical: one ray per column
         GridRange r{dims[0], dims[1], dims[2], 0, dims[2], 0};
-        const cudaError_t e = launchSignColumns(h->tree.q, r, X, beta, threshold, h->precise, nullptr, d_values, h->scratch, s);
+        size_t workBytes = 0;
+        void* work = workFor(h, signColumnsWorkBytes(r), s, &workBytes);
+        const cudaError_t e =
+            launchSignColumns(h->tree.q, r, X, beta, threshold, h->precise, nullptr, d_values, work, workBytes, h->scratch, s);
         return e ? cudaFail(e, "gbfwn_make_signed_by_winding_number_dev") : GBFWN_OK;
     }
     float* wn = nullptr;
@@ -842,7 +848,10 @@ GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t di
     const size_t vox = dims ? size_t(std::max(dims[0], 0)) * size_t(std::max(dims[1], 0)) * size_t(std::max(dims[2], 0)) : 0;
     const size_t tiles = (dims && vox) ? size_t(gridTiles(dims[0], dims[1], dims[2])) : 0;
     const size_t items = std::min(tiles, tiles / 16 + size_t(50) * size_t(numSMs()) * 32);
-    const size_t bits = dims && vox ? size_t((dims[0] + 31) / 32) * size_t(dims[1]) * size_t(dims[2]) * 4 : 0;
+    // the inside bits of a closed mesh's grid and its columns' crossing lists (72 bytes per column)
+    const size_t bits = dims && vox ? size_t((dims[0] + 31) / 32) * size_t(dims[1]) * size_t(dims[2]) * 4 +
+                                          size_t(dims[0]) * size_t(dims[1]) * 72 + 512
+                                    : 0;
     return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float) + items * 32 * sizeof(float) + bits;
 }
 // staging: points in (12 B) and results out (4 B); from 8,192 points also the Morton order and its

@@ -83,7 +83,7 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
 // colState (optional, colBytes >= gridSdfColumnStateBytes): device words through which the columns of
 // the launch hand their top layer's distances, signs and closest triangles to the columns above,
 // followed, on a closed mesh whose grid has a vertical z axis (signColumnsApply), by the inside bits
-// of the column rays, computed first.
+// of the grid's columns and the columns' crossing lists, computed first (launchSignColumns).
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                           float* out, unsigned* scratch, cudaStream_t s, float* colState = nullptr, size_t colBytes = 0);
 size_t gridSdfColumnStateBytes(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o);
@@ -91,8 +91,11 @@ size_t gridSdfColumnStateBytes(const QueryTree& t, const GridRange& g, const Xf&
 // applicable when signColumnsApply; writes inside bits (one 32-bit word per 32 voxels along x, layout
 // (z - zOut, y, x / 32)) or negates `values` where the voxel is inside.
 bool signColumnsApply(const QueryTree& t, const Xf& xf, float beta, float threshold);
+// work (optional, workBytes >= signColumnsWorkBytes): the columns' crossing lists, filled from the
+// triangles first; without it every column casts its own ray.
+size_t signColumnsWorkBytes(const GridRange& g);
 cudaError_t launchSignColumns(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, float threshold, int precise,
-                              uint32_t* bits, float* values, unsigned* scratch, cudaStream_t s);
+                              uint32_t* bits, float* values, void* work, size_t workBytes, unsigned* scratch, cudaStream_t s);
 // One mesh + grid of a batched launch (query.cu batchKernel): its tickets are
 // [tileBase, tileBase + batchTiles(...)): columns of up to kBatchSeg tiles of the launch's shape.
 struct BatchItem {

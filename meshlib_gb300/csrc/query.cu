@@ -22,6 +22,7 @@
 // so the set of dipole terms and exact solid angles summed for a query is the reference's set.
 // Work is handed out by a persistent grid pulling tiles from an atomic ticket counter.
 #include <cfloat>
+#include <cmath>
 #include <cstdint>
 
 #include "common.cuh"
@@ -637,6 +638,103 @@ __device__ __forceinline__ bool columnCross(const float3& q, const float4& A, co
     return true;
 }
 
+// Crossing lists of the grid's columns, filled by columnRasterKernel: per column the number of
+// crossings at or above the range's first voxel (may exceed kColumnSlots: the column then casts its
+// own ray), bit k of signMask the sign of entry k (1: +1), and entry k's tolerance bounds {lo, hi}
+// (as in signColumnsKernel) at zz[k * ncols + column].  Index space of the columns:
+// (fx, fy) = inv ((X, Y) - org); a column centre's FP32 (X, Y) lies within half of (ex, ey) of the
+// exact one.
+constexpr int kColumnSlots = 8;
+struct ColumnLists {
+    uint32_t* count;
+    uint32_t* signMask;
+    float2* zz;
+    int64_t ncols;
+    float inv[4], org[2];
+    float ex, ey;
+};
+
+__device__ __forceinline__ void columnAdd(const ColumnLists& cl, const GridRange& g, const Xf& xf, double zTol, int ix, int iy,
+                                          const float4& A, const float4& B, const float4& C) {
+    const float3 q0 = xfPoint(xf, ix, iy, g.z0);
+    double z;
+    int sgn;
+    if (!columnCross(q0, A, B, C, &z, &sgn)) return;
+    const float zl = __double2float_ru(z - zTol), zh = __double2float_rd(z + zTol);
+    if (q0.z > zh) return;  // below the range's first voxel
+    const int64_t col = int64_t(iy) * g.nx + ix;
+    const uint32_t k = atomicAdd(cl.count + col, 1u);
+    if (k < uint32_t(kColumnSlots)) {
+        cl.zz[size_t(k) * size_t(cl.ncols) + size_t(col)] = make_float2(zl, zh);
+        if (sgn > 0) atomicOr(cl.signMask + col, 1u << k);
+    }
+}
+
+// One lane per triangle: the columns whose centre (x, y) may fall in the triangle's (x, y) bounds
+// (the bounds widened by twice the centres' rounding, mapped to index space) are tested
+// with the ray test of columnCross, which adds each crossing to its column's list.  A triangle
+// over more than 16 candidate columns is taken by the whole warp, its lanes striding over them.
+__global__ void __launch_bounds__(kThreads) columnRasterKernel(QueryTree t, GridRange g, Xf xf, ColumnLists cl) {
+    const int lane = threadIdx.x & 31;
+    const double zTol = 1e-12 * double(fmaxf(fabsf(t.rootBox0.z), fabsf(t.rootBox1.z)));
+    const int64_t n = t.nLeaves;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+        const int64_t i = i0 + lane;
+        const bool active = i < n;
+        float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, C = A;
+        int ix0 = 0, iy0 = 0, w = 0, h = 0;
+        if (active) {
+            const float4* tr = t.tri + 3 * i;
+            A = ld4(tr);
+            B = ld4(tr + 1);
+            C = ld4(tr + 2);
+            // the widened bounds relative to the grid's origin, mapped to index space in FP32 with
+            // their error bound as margin (8 ulps of the terms' magnitudes; FP64 issues far slower)
+            const float x0 = __fsub_rn(__fsub_rn(fminf(A.x, fminf(B.x, C.x)), cl.ex), cl.org[0]);
+            const float x1 = __fadd_rn(__fsub_rn(fmaxf(A.x, fmaxf(B.x, C.x)), cl.org[0]), cl.ex);
+            const float y0 = __fsub_rn(__fsub_rn(fminf(A.y, fminf(B.y, C.y)), cl.ey), cl.org[1]);
+            const float y1 = __fadd_rn(__fsub_rn(fmaxf(A.y, fmaxf(B.y, C.y)), cl.org[1]), cl.ey);
+            float fx0 = FLT_MAX, fx1 = -FLT_MAX, fy0 = FLT_MAX, fy1 = -FLT_MAX;
+            const bool finite = x0 <= x1 && y0 <= y1;  // (no candidates for non-finite bounds)
+            for (int c = 0; c < 4 && finite; ++c) {
+                const float X = (c & 1) ? x1 : x0, Y = (c & 2) ? y1 : y0;
+                const float tx = fabsf(cl.inv[0] * X) + fabsf(cl.inv[1] * Y), ty = fabsf(cl.inv[2] * X) + fabsf(cl.inv[3] * Y);
+                const float fx = fmaf(cl.inv[0], X, cl.inv[1] * Y), fy = fmaf(cl.inv[2], X, cl.inv[3] * Y);
+                fx0 = fminf(fx0, fx - 1e-6f * tx);
+                fx1 = fmaxf(fx1, fx + 1e-6f * tx);
+                fy0 = fminf(fy0, fy - 1e-6f * ty);
+                fy1 = fmaxf(fy1, fy + 1e-6f * ty);
+            }
+            // the candidates: ceil(f0) .. floor(f1), clamped to the grid (compared in FP32 before any
+            // conversion, so bounds beyond int range convert nothing)
+            const float cx0 = fmaxf(0.f, ceilf(fx0)), cx1 = fminf(float(g.nx - 1), floorf(fx1));
+            const float cy0 = fmaxf(0.f, ceilf(fy0)), cy1 = fminf(float(g.ny - 1), floorf(fy1));
+            if (finite && cx0 <= cx1 && cy0 <= cy1) {
+                ix0 = int(cx0);
+                iy0 = int(cy0);
+                w = int(cx1) - ix0 + 1;
+                h = int(cy1) - iy0 + 1;
+            }
+        }
+        const int64_t nc = int64_t(w) * h;
+        if (nc <= 16) {
+            for (int c = 0; c < int(nc); ++c) columnAdd(cl, g, xf, zTol, ix0 + c % w, iy0 + c / w, A, B, C);
+        }
+        unsigned big = __ballot_sync(FULL, nc > 16);
+        while (big) {
+            const int b = __ffs(big) - 1;
+            big &= big - 1;
+            const float4 Ab = make_float4(__shfl_sync(FULL, A.x, b), __shfl_sync(FULL, A.y, b), __shfl_sync(FULL, A.z, b), 0.f);
+            const float4 Bb = make_float4(__shfl_sync(FULL, B.x, b), __shfl_sync(FULL, B.y, b), __shfl_sync(FULL, B.z, b), 0.f);
+            const float4 Cb = make_float4(__shfl_sync(FULL, C.x, b), __shfl_sync(FULL, C.y, b), __shfl_sync(FULL, C.z, b), 0.f);
+            const int bx0 = __shfl_sync(FULL, ix0, b), by0 = __shfl_sync(FULL, iy0, b), bw = __shfl_sync(FULL, w, b);
+            const int64_t bn = int64_t(bw) * __shfl_sync(FULL, h, b);
+            for (int64_t c = lane; c < bn; c += 32) columnAdd(cl, g, xf, zTol, bx0 + int(c % bw), by0 + int(c / bw), Ab, Bb, Cb);
+        }
+    }
+}
+
 // For the grid columns of the launch (32 consecutive x per warp, in segments of kColumnSeg layers,
 // each with its own ray): inside = (winding number of the voxel > threshold), written as bits (one
 // word per 32 voxels along x, layout (z - zOut, y, x / 32)) or applied to `values` (negated where
@@ -644,9 +742,9 @@ __device__ __forceinline__ bool columnCross(const float3& q, const float4& A, co
 constexpr int kColumnSeg = 128;
 
 template <bool PRECISE>
-__global__ void __launch_bounds__(kThreads) signColumnsKernel(QueryTree t, GridRange g, Xf xf, float threshold, float beta,
+__global__ void __launch_bounds__(kThreads, 4) signColumnsKernel(QueryTree t, GridRange g, Xf xf, float threshold, float beta,
                                                           uint32_t* __restrict__ bits, float* __restrict__ values,
-                                                          unsigned* scratch) {
+                                                          ColumnLists cl, unsigned* scratch) {
     const int lane = threadIdx.x & 31;
     const float betaSq = __fmul_rn(beta, beta);
     const int wordsX = (g.nx + 31) >> 5;
@@ -655,7 +753,10 @@ __global__ void __launch_bounds__(kThreads) signColumnsKernel(QueryTree t, GridR
     const size_t sxy = size_t(g.nx) * g.ny;
     // the heights' rounding error is below 1e-15 of the largest |z| of the mesh
     const double zTol = 1e-12 * double(fmaxf(fabsf(t.rootBox0.z), fabsf(t.rootBox1.z)));
-    double zs[kColumnCrossings];
+    // per crossing (ascending): the FP32 bounds of its tolerance interval [z - zTol, z + zTol] rounded
+    // outwards, so that for a voxel centre vz (a float) vz < lo <=> vz < z - zTol and vz > hi <=>
+    // vz > z + zTol: the sweep compares in FP32 (FP64 issues at a small fraction of the FP32 rate)
+    float lo[kColumnCrossings], hi[kColumnCrossings];
     int sg[kColumnCrossings];
     for (;;) {
         const unsigned item = nextTicket(scratch, lane);
@@ -668,12 +769,36 @@ __global__ void __launch_bounds__(kThreads) signColumnsKernel(QueryTree t, GridR
         const bool active = x < g.nx;
         const int xc = active ? x : 0;
         const float3 q0 = xfPoint(xf, xc, y, zs0);
-        // the ray: a packet walk over the reference nodes collecting the crossings above q0, by height
+        // the column's crossings from its list, or, without lists or when the list overflowed, from
+        // the ray: a packet walk over the reference nodes collecting the crossings above q0; by height
         int n = 0;
         bool overflow = false;
-        {
+        bool ray = active && !cl.count;
+        if (cl.count && active) {
+            const int64_t col = int64_t(y) * g.nx + x;
+            const uint32_t c = __ldg(cl.count + col);
+            if (c <= uint32_t(kColumnSlots)) {
+                const uint32_t mask = __ldg(cl.signMask + col);
+                for (uint32_t e = 0; e < c; ++e) {
+                    const float2 zz = __ldg(cl.zz + size_t(e) * size_t(cl.ncols) + size_t(col));
+                    int k = n++;
+                    while (k > 0 && lo[k - 1] > zz.x) {
+                        lo[k] = lo[k - 1];
+                        hi[k] = hi[k - 1];
+                        sg[k] = sg[k - 1];
+                        --k;
+                    }
+                    lo[k] = zz.x;
+                    hi[k] = zz.y;
+                    sg[k] = ((mask >> e) & 1u) ? 1 : -1;
+                }
+            } else {
+                ray = true;
+            }
+        }
+        if (__any_sync(FULL, ray)) {
             WarpStack st;
-            st.push(lane, 0, __ballot_sync(FULL, active));
+            st.push(lane, 0, __ballot_sync(FULL, ray));
             bool stackFull = false;
             while (st.sp > 0 && t.nLeaves > 0) {
                 int node;
@@ -689,15 +814,20 @@ __global__ void __launch_bounds__(kThreads) signColumnsKernel(QueryTree t, GridR
                     const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
                     double z;
                     int sgn;
-                    if (hit && columnCross(q0, A, B, C, &z, &sgn) && z >= double(q0.z) - zTol) {
-                        if (n < kColumnCrossings) {
+                    if (hit && columnCross(q0, A, B, C, &z, &sgn)) {
+                        const float zl = __double2float_ru(z - zTol), zh = __double2float_rd(z + zTol);
+                        if (q0.z > zh) {
+                            // below the segment's first voxel: no voxel of it is below this crossing
+                        } else if (n < kColumnCrossings) {
                             int k = n++;
-                            while (k > 0 && zs[k - 1] > z) {
-                                zs[k] = zs[k - 1];
+                            while (k > 0 && lo[k - 1] > zl) {
+                                lo[k] = lo[k - 1];
+                                hi[k] = hi[k - 1];
                                 sg[k] = sg[k - 1];
                                 --k;
                             }
-                            zs[k] = z;
+                            lo[k] = zl;
+                            hi[k] = zh;
                             sg[k] = sgn;
                         } else {
                             overflow = true;
@@ -720,12 +850,12 @@ __global__ void __launch_bounds__(kThreads) signColumnsKernel(QueryTree t, GridR
             const int kn = min(32, zs1 - zc);
             uint32_t in = 0, amb = 0;  // bit k: the voxel at zc + k
             for (int k = 0; k < kn; ++k) {
-                const double vz = double(xfPoint(xf, xc, y, zc + k).z);
-                while (p < n && zs[p] < vz) {
+                const float vz = xfPoint(xf, xc, y, zc + k).z;
+                while (p < n && vz > hi[p]) {  // crossings passed: below the voxel
                     w -= sg[p];
                     ++p;
                 }
-                if (overflow || (p < n && zs[p] - vz <= zTol) || (p > 0 && vz - zs[p - 1] <= zTol))
+                if (overflow || (p < n && vz >= lo[p]))  // within the next crossing's tolerance
                     amb |= 1u << k;
                 else if (float(w) > threshold)
                     in |= 1u << k;
@@ -1215,15 +1345,46 @@ cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf
 
 bool signColumnsApply(const QueryTree& t, const Xf& xf, float beta, float threshold) {
     const float fr = threshold - floorf(threshold);
-    return t.closed && beta >= 2.f && fr > 0.25f && fr < 0.75f && xf.a[2] == 0.f && xf.a[5] == 0.f && xf.a[8] > 0.f;
+    return t.closed && beta >= 2.f && fr > 0.25f && fr < 0.75f && xf.a[2] == 0.f && xf.a[5] == 0.f && xf.a[8] > 0.f &&
+           double(xf.a[0]) * xf.a[4] - double(xf.a[1]) * xf.a[3] != 0.0;
+}
+
+size_t signColumnsWorkBytes(const GridRange& g) {
+    const size_t ncols = size_t(g.nx) * size_t(g.ny);
+    return ((2 * sizeof(uint32_t) + kColumnSlots * sizeof(float2)) * ncols + 255) & ~size_t(255);
 }
 
 cudaError_t launchSignColumns(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, float threshold, int precise,
-                              uint32_t* bits, float* values, unsigned* scratch, cudaStream_t s) {
+                              uint32_t* bits, float* values, void* work, size_t workBytes, unsigned* scratch, cudaStream_t s) {
+    ColumnLists cl{};
+    const size_t ncols = size_t(g.nx) * size_t(g.ny);
+    if (work && workBytes >= signColumnsWorkBytes(g) && t.nLeaves > 0) {
+        // zz first (8-byte aligned), then the counts and sign masks, cleared together
+        cl.zz = static_cast<float2*>(work);
+        cl.count = reinterpret_cast<uint32_t*>(cl.zz + kColumnSlots * ncols);
+        cl.signMask = cl.count + ncols;
+        cl.ncols = int64_t(ncols);
+        const double a0 = xf.a[0], a1 = xf.a[1], a3 = xf.a[3], a4 = xf.a[4], det = a0 * a4 - a1 * a3;
+        cl.inv[0] = float(a4 / det);
+        cl.inv[1] = float(-a1 / det);
+        cl.inv[2] = float(-a3 / det);
+        cl.inv[3] = float(a0 / det);
+        cl.org[0] = xf.b[0];
+        cl.org[1] = xf.b[1];
+        // xfPoint's four roundings of x = a0 i + a1 j + 0 k + b0: at most 2 ulps of the largest magnitude
+        const auto margin = [](double m) { return float(4.0 * std::ldexp(1.0, std::ilogb(m > 0 ? m : 1e-30) - 23)); };
+        cl.ex = margin(std::fabs(a0) * (g.nx - 1) + std::fabs(a1) * (g.ny - 1) + std::fabs(double(xf.b[0])));
+        cl.ey = margin(std::fabs(a3) * (g.nx - 1) + std::fabs(a4) * (g.ny - 1) + std::fabs(double(xf.b[1])));
+        cudaError_t e = cudaMemsetAsync(cl.count, 0, 2 * sizeof(uint32_t) * ncols, s);
+        if (e) return e;
+        int blocks = int(std::min<int64_t>((int64_t(t.nLeaves) + kThreads - 1) / kThreads, int64_t(numSMs()) * 16));
+        columnRasterKernel<<<blocks, kThreads, 0, s>>>(t, g, xf, cl);
+        if ((e = cudaGetLastError())) return e;
+    }
     const uint64_t items = uint64_t((g.nx + 31) / 32) * uint64_t(g.ny) * uint64_t((g.z1 - g.z0 + kColumnSeg - 1) / kColumnSeg);
     if (precise)
-        return launchPersistent(signColumnsKernel<true>, items, scratch, s, t, g, xf, threshold, beta, bits, values, scratch);
-    return launchPersistent(signColumnsKernel<false>, items, scratch, s, t, g, xf, threshold, beta, bits, values, scratch);
+        return launchPersistent(signColumnsKernel<true>, items, scratch, s, t, g, xf, threshold, beta, bits, values, cl, scratch);
+    return launchPersistent(signColumnsKernel<false>, items, scratch, s, t, g, xf, threshold, beta, bits, values, cl, scratch);
 }
 
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
@@ -1242,7 +1403,7 @@ static size_t signBitsBytes(const GridRange& g) {
 
 size_t gridSdfColumnStateBytes(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o) {
     const size_t col = size_t(tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16).numItems) * (2 * kLayer) * sizeof(float);
-    return col + (signColumnsApply(t, xf, o.beta, o.threshold) ? signBitsBytes(g) : 0);
+    return col + (signColumnsApply(t, xf, o.beta, o.threshold) ? ((signBitsBytes(g) + 255) & ~size_t(255)) + signColumnsWorkBytes(g) : 0);
 }
 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
@@ -1254,9 +1415,14 @@ cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, 
         if (e) return e;
         tg.colState = colState;
         if (signColumnsApply(t, xf, o.beta, o.threshold) && colBytes >= need + signBitsBytes(g)) {
-            // closed surface, vertical z axis: the signs from one ray per column segment first
-            uint32_t* bits = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(colState) + need);
-            if ((e = launchSignColumns(t, g, xf, o.beta, o.threshold, precise, bits, nullptr, scratch, s))) return e;
+            // closed surface, vertical z axis: the signs from the columns' crossings first
+            char* base = reinterpret_cast<char*>(colState);
+            uint32_t* bits = reinterpret_cast<uint32_t*>(base + need);
+            const size_t lists = need + ((signBitsBytes(g) + 255) & ~size_t(255));
+            void* work = colBytes >= lists + signColumnsWorkBytes(g) ? base + lists : nullptr;
+            if ((e = launchSignColumns(t, g, xf, o.beta, o.threshold, precise, bits, nullptr, work, work ? colBytes - lists : 0,
+                                       scratch, s)))
+                return e;
             tg.signBits = bits;
             if (precise)
                 return launchPersistent(gridKernel<true, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);

@@ -47,9 +47,10 @@ def test_bad_arguments_rejected_without_gpu(fwn_lib):
 def test_memory_estimators(fwn_lib):
     import meshlib_gb300 as M
     est = M.memory_estimates(655362, 1310720, dims=(512, 512, 512), npts=4_000_000)
-    # the result, and the signed-distance columns' hand-over words (128 B per column of >= 16 tiles,
-    # or of fewer tiles while under 50 items per resident warp remain)
-    extra = est["from_grid"] - est["mesh"] - 512 ** 3 * 4
+    # the result, the signed-distance columns' hand-over words (128 B per column of >= 16 tiles, or of
+    # fewer tiles while under 50 items per resident warp remain), and for closed meshes the inside
+    # bits (1 bit per voxel) and the crossing lists (72 B per grid column)
+    extra = est["from_grid"] - est["mesh"] - 512 ** 3 * 4 - 512 ** 3 // 8 - 512 * 512 * 72 - 512
     assert 0 < extra <= 512 ** 3 // 4 + 50 * 160 * 32 * 128
     # points in and results out, Morton order and its sort scratch
     assert est["from_vector"] - est["mesh"] == 4_000_000 * 40 + 4096

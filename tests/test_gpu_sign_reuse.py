@@ -161,17 +161,23 @@ def _signed_pass(M, g, dims, xf, vals, enable, thr=0.5):
 @pytest.mark.parametrize("precise", [True, False])
 def test_sign_columns_identical(M, precise):
     """makeSignedByWindingNumber on a closed mesh with the grid's z axis vertical takes each column's
-    signs from one upward ray (the signed count of crossings above each voxel); the negated voxels equal
-    those of the winding-number walk at every voxel: clean, self-intersecting (winding number 2), far
-    from the origin, a stack of 16 spheres (32 crossings per column, more than one ray keeps: those
-    columns take the walk), ragged and z-scaled grids, thresholds 0.5 and 0.3, and rotated grids
+    signs from its crossings (the signed count of crossings above each voxel; the columns' crossing lists
+    filled from the triangles); the negated voxels equal those of the winding-number walk at every
+    voxel: clean, self-intersecting (winding number 2), far from the origin, a stack of 16 spheres (32
+    crossings per column: more than a list holds, those columns cast their own ray, more than a ray
+    keeps, they take the walk), coarse meshes (a cube, an 80-face sphere: triangles over many
+    columns), ragged, z-scaled and turned (about z) grids, thresholds 0.5 and 0.3, and tilted grids
     (the walk)."""
     rng = np.random.default_rng(11)
     v, f = mg.noisy_icosphere(seed=1, level=5)
     stack_v = np.concatenate([v * 0.4 + np.float32([0, 0, 1.0 * k]) for k in range(16)]).astype(np.float32)
     stack_f = np.concatenate([f + k * len(v) for k in range(16)]).astype(np.int32)
+    cube_v = np.array([[x, y, z] for z in (0, 1) for y in (0, 1) for x in (0, 1)], np.float32)
+    cube_f = np.array([[0, 2, 3], [0, 3, 1], [4, 5, 7], [4, 7, 6], [0, 1, 5], [0, 5, 4], [2, 6, 7], [2, 7, 3], [0, 4, 6],
+                       [0, 6, 2], [1, 3, 7], [1, 7, 5]], np.int32)
+    iv, iff = mg.icosphere(1)
     cases = [mg.noisy_torus(seed=4), mg.overlapping_spheres(seed=3, level=5), ((v + np.float32(3.0e3)).astype(np.float32), f),
-             (stack_v, stack_f)]
+             (stack_v, stack_f), (cube_v, cube_f), (iv.astype(np.float32), iff.astype(np.int32))]
     negated = 0
     for cv, cf in cases:
         g = M.FastWindingNumber(cv, cf, precise=precise)
@@ -182,6 +188,11 @@ def test_sign_columns_identical(M, precise):
         ragged = xf.copy()
         ragged[8] *= 0.5  # z pitch halved, twice the layers
         grids.append(((dims[0] - 5, dims[1] - 3, 2 * dims[2] + 1), ragged))
+        turned = xf.copy()  # columns still vertical, the grid turned about z
+        c, s = np.float32(np.cos(0.4)), np.float32(np.sin(0.4))
+        turned[:9] = (np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]], np.float32) @ turned[:9].reshape(3, 3)).reshape(-1)
+        turned[9:] = 0.5 * (cv.min(0) + cv.max(0)) - turned[:9].reshape(3, 3) @ (0.5 * np.array(dims, np.float32))
+        grids.append((tuple(dims), turned))
         for gd, gx in grids:
             vals = rng.uniform(0.1, 1.0, int(np.prod(gd))).astype(np.float32)
             for thr in (0.5, 0.3):
@@ -231,3 +242,44 @@ def test_reuse_and_rays_identical_on_tilted_grids(M, precise):
             g.set_sign_reuse(True)
             _same(*res)
             assert (res[0] < 0).any()
+
+
+def test_signed_distance_grids_from_column_lists(M):
+    """Signed-distance grids whose signs come from the columns' crossing lists equal the grids whose
+    every sign comes from the winding-number walk: a turned (about z) grid, a coarse cube, 16 stacked
+    spheres (overflowing lists), a band, and the slab calls of the same grid."""
+    import torch
+    v, f = mg.noisy_icosphere(seed=5, level=5)
+    stack_v = np.concatenate([v * 0.4 + np.float32([0, 0, 1.0 * k]) for k in range(16)]).astype(np.float32)
+    stack_f = np.concatenate([f + k * len(v) for k in range(16)]).astype(np.int32)
+    cube_v = np.array([[x, y, z] for z in (0, 1) for y in (0, 1) for x in (0, 1)], np.float32) * np.float32(1.7)
+    cube_f = np.array([[0, 2, 3], [0, 3, 1], [4, 5, 7], [4, 7, 6], [0, 1, 5], [0, 5, 4], [2, 6, 7], [2, 7, 3], [0, 4, 6],
+                       [0, 6, 2], [1, 3, 7], [1, 7, 5]], np.int32)
+    for cv, cf in ((v, f), (cube_v, cube_f), (stack_v, stack_f)):
+        g = M.FastWindingNumber(cv, cf)
+        dims, xf = mg.grid_for(cv, 60)
+        dims = (dims[0] + 3, dims[1] - 2, dims[2] + 1)
+        turned = np.asarray(xf, np.float32).copy()
+        c, s = np.float32(np.cos(0.7)), np.float32(np.sin(0.7))
+        turned[:9] = (np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]], np.float32) @ turned[:9].reshape(3, 3)).reshape(-1)
+        turned[9:] = 0.5 * (cv.min(0) + cv.max(0)) - turned[:9].reshape(3, 3) @ (0.5 * np.array(dims, np.float32))
+        band = 0.05 * mg.diag(cv)
+        for gx in (np.asarray(xf, np.float32), turned):
+            for opts in (None, M.DistanceToMeshOptions(maxDistSq=band * band)):
+                res = []
+                for enable in (True, False):
+                    g.set_sign_reuse(enable)
+                    res.append(g.calcFromGridWithDistances(dims, gx, opts))
+                g.set_sign_reuse(True)
+                _same(*res)
+        n = int(np.prod(dims))
+        whole = torch.empty(n, device="cuda")
+        g.calcFromGridWithDistances_dev(dims, turned, whole.data_ptr(), stream=0)
+        parts = []
+        for z0, z1 in ((0, 7), (7, 30), (30, dims[2])):
+            t = torch.empty((z1 - z0) * dims[0] * dims[1], device="cuda")
+            g.calcFromGridWithDistancesSlab_dev(dims, turned, z0, z1, t.data_ptr(), stream=0)
+            parts.append(t)
+        torch.cuda.synchronize()
+        assert torch.equal(torch.cat(parts).view(torch.int32), whole.view(torch.int32))
+        assert (whole < 0).any()
