@@ -118,8 +118,12 @@ cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTil
 
 // Signed distance on runs of 8x8x8-voxel bricks of the grid: runs[i] = (bx, by, bz0, count), the
 // `count` bricks (bx, by, bz0 .. bz0 + count - 1), nBricks in all; voxels outside them are not written.
+// signBits (optional): the grid's inside bits from launchSignColumns, used for the signs.
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
-                                float* out, const int4* runs, int32_t nRuns, int32_t nBricks, unsigned* scratch, cudaStream_t s);
+                                float* out, const int4* runs, int32_t nRuns, int32_t nBricks, const uint32_t* signBits,
+                                unsigned* scratch, cudaStream_t s);
+// Bytes of the inside bits of a grid range (one 32-bit word per 32 voxels along x).
+size_t signBitsBytes(const GridRange& g);
 // Point queries; `order` (optional) is a permutation of [0, n): points are processed in that order
 // (mortonOrder gives a spatially coherent one) and results land at their original indices.
 cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, float beta, int32_t skipFace, int precise,

@@ -646,6 +646,14 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     if ((e = A((void**)&runs, sizeof(int4) * size_t(nb)))) return done(e);
     if ((e = A((void**)&sums, sizeof(int32_t) * size_t(nb / 1024 + 2)))) return done(e);
     if ((e = A((void**)&total, 2 * sizeof(int32_t)))) return done(e);
+    // closed mesh, vertical z axis: the signs from the columns' crossings (bits, then crossing lists)
+    uint32_t* bits = nullptr;
+    void* lists = nullptr;
+    const bool columns = signColumnsApply(t, xf, o.beta, o.threshold);
+    if (columns) {
+        if ((e = A((void**)&bits, signBitsBytes(g)))) return done(e);
+        if ((e = A(&lists, signColumnsWorkBytes(g)))) return done(e);
+    }
     cudaEvent_t ev[4];
     for (auto& x : ev) cudaEventCreate(&x);
     cudaEventRecord(ev[0], s);
@@ -675,7 +683,10 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     if ((e = cudaStreamSynchronize(s))) return done(e);
     cudaEventRecord(ev[2], s);
     const int32_t kept = counts[0];
-    if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, runs, counts[1], kept, scratch, s))) return done(e);
+    if (kept > 0 && columns &&
+        (e = launchSignColumns(t, g, xf, o.beta, o.threshold, precise, bits, nullptr, lists, signColumnsWorkBytes(g), scratch, s)))
+        return done(e);
+    if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, runs, counts[1], kept, bits, scratch, s))) return done(e);
     cudaEventRecord(ev[3], s);
     if ((e = cudaStreamSynchronize(s))) return done(e);
     cudaEventElapsedTime(&st.cullMs, ev[0], ev[1]);

@@ -1333,11 +1333,18 @@ static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
 }
 
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
-                                float* out, const int4* runs, int32_t nRuns, int32_t nBricks, unsigned* scratch, cudaStream_t s) {
+                                float* out, const int4* runs, int32_t nRuns, int32_t nBricks, const uint32_t* signBits,
+                                unsigned* scratch, cudaStream_t s) {
     TileGrid tg = tileGridFor(g);
     tg.runs = runs;
     tg.numTiles = uint32_t(nBricks) * 16u;
     tg.numItems = uint32_t(nRuns) * uint32_t(kBrickCols);
+    if (signBits) {
+        tg.signBits = signBits;
+        if (precise)
+            return launchPersistent(gridKernel<true, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+        return launchPersistent(gridKernel<false, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+    }
     if (precise)
         return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
     return launchPersistent(gridKernel<false, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
@@ -1397,7 +1404,7 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
 }
 
 // Column hand-over words, then (when the column rays apply) the inside bits of the range.
-static size_t signBitsBytes(const GridRange& g) {
+size_t signBitsBytes(const GridRange& g) {
     return size_t((g.nx + 31) >> 5) * size_t(g.ny) * size_t(g.z1 - g.z0) * sizeof(uint32_t);
 }
 
