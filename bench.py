@@ -159,19 +159,19 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 
 
 # DRAM bytes (read + write) of one launch of the signed-distance grid kernel at 512^3 on this
-# workload: dram__bytes_read.sum 630,731,776 + dram__bytes_write.sum 651,689,216 from one ncu
+# workload: dram__bytes_read.sum 441,793,024 + dram__bytes_write.sum 591,700,992 from one ncu
 # capture of the same kernel (a constant copied from that capture, not measured by this run; the
 # committed profile summary under profiles/ gives the command).  536,870,912 of the written bytes
 # are the output grid.
-KERNEL_DRAM_BYTES_512 = 630_731_776 + 651_689_216
+KERNEL_DRAM_BYTES_512 = 441_793_024 + 591_700_992
 
 
 # Counters of the signed-distance grid kernel at 256^3 on this workload from one ncu capture
 # (constants copied from that capture, not measured by this run): FMA-pipe utilisation
 # (sm__pipe_fma_cycles_active), issue-slot utilisation and active lanes per warp instruction.
-KERNEL_FMA_PIPE_ACTIVE = 0.311
-KERNEL_ISSUE_ACTIVE = 0.839
-KERNEL_LANES_PER_INSTR = 24.5
+KERNEL_FMA_PIPE_ACTIVE = 0.328
+KERNEL_ISSUE_ACTIVE = 0.880
+KERNEL_LANES_PER_INSTR = 24.55
 
 
 def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
@@ -747,7 +747,9 @@ def main():
                                     "of HBM peak; the warp-packet walk reads each record once per 32 voxels from L1/L2. "
                                     "The bound that holds is instruction issue: dram_frac_actual (measured DRAM bytes "
                                     "per launch / step time / peak) is well under 1 %, issue_active_ncu is the busy "
-                                    "fraction of the issue slots (ncu, 256^3 capture)"}
+                                    "fraction of the issue slots (ncu, 256^3 capture)",
+                            "duration": "the timed step's CUDA-event time: the grid kernel and, before it, the column sign "
+                                        "pass (crossing lists + column sweep, 0.33 ms of the step in the ncu launch list)"}
         try:
             fp32_peak = fp32_peak_tflops(local)
         except Exception as ex:  # measurement support only; the line stays valid without it
@@ -761,7 +763,7 @@ def main():
                         "fma_pipe_active_ncu": KERNEL_FMA_PIPE_ACTIVE,
                         "note": "reference-equivalent FLOP/s counts the reference traversal's box tests, projections, "
                                 "dipoles and solid angles per voxel; the packet traversal does far fewer, and ncu shows the "
-                                "FMA pipe 31% busy: the kernel is bound by instruction issue and dependent loads"}
+                                "FMA pipe 33% busy: the kernel is bound by instruction issue and dependent loads"}
         line["cpu_baseline"] = cpu_baseline_fields(rate, thr, desc)
         line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d, extra=prec_extra, M=M, device=local)
     if rank == 0:
