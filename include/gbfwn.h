@@ -86,15 +86,19 @@ typedef int (*gbfwn_slab_cb)(const float* data, const int32_t dims[3], int32_t z
  * a few ulps of a triangle plane.  precise = 0: the reference's FP32 arithmetic, plain sums. */
 GBFWN_API void gbfwn_set_precise(gbfwn_handle h, int precise);
 
-/* Sign reuse in signed-distance grids (default on).  When the mesh's valid faces form a closed
- * oriented surface (every edge used equally often in both directions; gbfwn_is_closed), the exact
- * winding number is an integer that stays constant along any segment not meeting the surface.  A
- * voxel whose neighbour below lies closer to it than that neighbour's distance to the surface then
- * takes the neighbour's sign instead of evaluating its own winding number: the same sign, because
- * both approximated winding numbers lie within their (far smaller than 0.5) approximation error of
- * the same integer.  Used only with windingNumberBeta >= 2 and a threshold whose fractional part
- * lies in (0.25, 0.75) (the default 0.5); distances are unaffected.  enable = 0 evaluates every
- * voxel's winding number, as the reference does. */
+/* Exact signs on closed surfaces (default on).  When the mesh's valid faces form a closed oriented
+ * surface (every edge used equally often in both directions; gbfwn_is_closed), the exact winding
+ * number is an integer, constant along any segment not meeting the surface, to which the
+ * reference's approximated winding number rounds with windingNumberBeta >= 2 and a threshold whose
+ * fractional part lies in (0.25, 0.75) (the default 0.5).  Under those conditions:
+ *  - a grid whose z axis is vertical (xf's third column (0, 0, +s); any rotation about z) takes the
+ *    signs of its voxels from its columns: the signed number of crossings of the column above each
+ *    voxel (signed-distance grids and gbfwn_make_signed_by_winding_number_dev);
+ *  - other grids, and points, take a voxel's sign from the voxel below it when no surface lies
+ *    between them, or from the crossings of one vertical ray;
+ * and a voxel or point on the surface (up to rounding) evaluates its approximated winding number.
+ * Distances are unaffected.  enable = 0 evaluates every voxel's winding number, as the reference
+ * does. */
 GBFWN_API void gbfwn_set_sign_reuse(gbfwn_handle h, int enable);
 
 /* 1 if the mesh's valid faces form a closed oriented surface (fingerprint of the directed edges,
@@ -367,9 +371,11 @@ GBFWN_API int gbfwn_batch_graph_launch(gbfwn_batch b, void* stream);
 
 /* makeSignedByWindingNumber (MRVoxels/MRVDBConversions.cpp:491-571) on a dense device grid: the
  * winding number of every voxel (centre = xf applied to (x, y, z), as for gbfwn_from_grid) is computed
- * and each value whose voxel's winding number exceeds `threshold` is negated in place.  MeshLib's VDB
- * path reaches the same computation through IFastWindingNumberByParts::calcFromGridByParts; this is
- * for grids that already live in device memory.  Enqueued on `stream` (NULL = the handle's). */
+ * and each value whose voxel's winding number exceeds `threshold` is negated in place (on closed
+ * meshes with a vertical grid z axis from the columns' crossings, see gbfwn_set_sign_reuse; the
+ * handle's work buffer grows by 72 bytes per grid column for them).  MeshLib's VDB path reaches the
+ * same computation through IFastWindingNumberByParts::calcFromGridByParts; this is for grids that
+ * already live in device memory.  Enqueued on `stream` (NULL = the handle's). */
 GBFWN_API int gbfwn_make_signed_by_winding_number_dev(gbfwn_handle h, const int32_t dims[3], const float xf[12],
                                                       float beta, float threshold, float* d_values, void* stream);
 

@@ -172,8 +172,8 @@ public:
     const Result& creation() const { return created_; }
     gbfwn_handle handle() const { return h_.get(); }
 
-    // Knobs of include/gbfwn.h: compensated sums and FP64 near-plane fallbacks (default on); sign
-    // reuse between neighbouring voxels of closed meshes in signed-distance grids (default on).
+    // Knobs of include/gbfwn.h: compensated sums and FP64 near-plane fallbacks (default on); exact
+    // signs of closed meshes from column crossings, neighbouring voxels or rays (default on).
     void setPrecise(bool precise) { gbfwn_set_precise(h_.get(), precise ? 1 : 0); }
     void setSignReuse(bool enable) { gbfwn_set_sign_reuse(h_.get(), enable ? 1 : 0); }
     bool isClosed() const { return gbfwn_is_closed(h_.get()) != 0; }

@@ -268,8 +268,9 @@ class FastWindingNumber:
         self._L.gbfwn_set_precise(self._h, 1 if precise else 0)
 
     def set_sign_reuse(self, enable: bool):
-        """Signed-distance grids of a closed surface take a voxel's sign from the voxel below it when
-        no surface lies between them (default on; gbfwn_set_sign_reuse in include/gbfwn.h)."""
+        """Exact signs on a closed surface (default on; gbfwn_set_sign_reuse in include/gbfwn.h): grids
+        with a vertical z axis from their columns' crossings, other grids and points from the voxel
+        below or one vertical ray; off evaluates every winding number, as the reference does."""
         self._L.gbfwn_set_sign_reuse(self._h, 1 if enable else 0)
 
     def is_closed(self) -> bool:
