@@ -283,3 +283,34 @@ def test_signed_distance_grids_from_column_lists(M):
         torch.cuda.synchronize()
         assert torch.equal(torch.cat(parts).view(torch.int32), whole.view(torch.int32))
         assert (whole < 0).any()
+
+
+def test_column_signs_on_small_and_outlying_grids(M):
+    """Column signs on grids of one voxel, of fewer than 32 voxels per row, wholly inside and wholly
+    outside the mesh, and reaching far past it: the same grids as the winding-number walk."""
+    v, f = mg.noisy_torus(seed=9)
+    g = M.FastWindingNumber(v, f)
+    lo, hi = v.min(0), v.max(0)
+    mid = 0.5 * (lo + hi)
+    cases = []
+    for dims, pitch, origin in (((1, 1, 1), 0.1, mid), ((5, 3, 2), 0.05, lo), ((31, 2, 40), 0.02, lo),
+                                ((8, 8, 8), 0.01, np.float32([hi[0] + 1.0, mid[1], mid[2]])),  # outside, beside the mesh
+                                ((16, 16, 64), 0.2, lo - 3.0)):  # reaching far past it
+        xf = np.zeros(12, np.float32)
+        xf[0] = xf[4] = xf[8] = pitch
+        xf[9:12] = origin
+        cases.append((dims, xf))
+    # a grid around a point inside the torus tube
+    vi, fi = mg.noisy_icosphere(seed=2, level=5)
+    gi = M.FastWindingNumber(vi, fi)
+    xf = np.zeros(12, np.float32)
+    xf[0] = xf[4] = xf[8] = 0.01
+    xf[9:12] = -0.05
+    for gg, dims, x in [(g, d, x) for d, x in cases] + [(gi, (10, 10, 10), xf)]:
+        res = []
+        for enable in (True, False):
+            gg.set_sign_reuse(enable)
+            res.append(gg.calcFromGridWithDistances(dims, x))
+        gg.set_sign_reuse(True)
+        _same(*res)
+    assert (res[0] < 0).all()  # the last grid lies inside the sphere
