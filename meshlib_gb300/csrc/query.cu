@@ -520,12 +520,56 @@ __device__ __forceinline__ float det2(float a, float b, float c, float d) {
 // (eps, eps^2), eps -> 0, changes E by eps (Py - Qy) + eps^2 (Qx - Px).  Swapping P and Q flips the
 // sign, so a ray meets exactly one of two triangles that share an edge on the same side of it, and
 // both or neither of two that fold over it.  0 only for a degenerate edge.
-__device__ __forceinline__ int edgeSign(float px, float py, float qx, float qy) {
-    const float e = det2(px, qy, py, qx);
+__device__ __forceinline__ int edgeSignOf(float e, float px, float py, float qx, float qy) {
     if (e != 0.f) return e > 0.f ? 1 : -1;
     if (py != qy) return py > qy ? 1 : -1;
     if (qx != px) return qx > px ? 1 : -1;
     return 0;
+}
+__device__ __forceinline__ int edgeSign(float px, float py, float qx, float qy) {
+    return edgeSignOf(det2(px, qy, py, qx), px, py, qx, qy);
+}
+
+// Squared distance from the origin to the segment P -> Q in the plane (a test of closeness only: fast
+// division, FP32).
+__device__ __forceinline__ float segDistSq0(float px, float py, float qx, float qy) {
+    const float dx = qx - px, dy = qy - py;
+    const float dd = fmaf(dx, dx, dy * dy);
+    float s = dd > 0.f ? __fdividef(-fmaf(px, dx, py * dy), dd) : 0.f;
+    s = fminf(fmaxf(s, 0.f), 1.f);
+    const float rx = fmaf(s, dx, px), ry = fmaf(s, dy, py);
+    return fmaf(rx, rx, ry * ry);
+}
+
+// Whether the origin lies within sqrt(epsSq) of the boundary of the projected triangle (a, b, c):
+// a vertical ray through it runs through an edge or a vertex, or along a vertical triangle, where a
+// point of the ray may lie on the surface without a crossing at its height.
+__device__ __forceinline__ bool nearProjection(float ax, float ay, float bx, float by, float cx, float cy, float epsSq) {
+    return segDistSq0(ax, ay, bx, by) <= epsSq || segDistSq0(bx, by, cx, cy) <= epsSq || segDistSq0(cx, cy, ax, ay) <= epsSq;
+}
+// For a triangle whose projection has (next to) no area — a vertical triangle, which no vertical ray
+// crosses though a point of the ray may lie on it — whether the origin lies within sqrt(epsSq) of
+// the projection.  e = E(b, c), E(c, a), E(a, b): the edge functions, whose sum is twice the
+// projected area.  Other triangles need no such test: a point of the ray on one of them is a crossing
+// at that height (or, on a shared edge, the crossing of its neighbour), which the height tolerance
+// covers.
+__device__ __forceinline__ bool nearVerticalTriangle(float ax, float ay, float bx, float by, float cx, float cy, float ebc, float eca,
+                                                     float eab, float epsSq) {
+    const float lbc = fmaf(cx - bx, cx - bx, (cy - by) * (cy - by)), lca = fmaf(ax - cx, ax - cx, (ay - cy) * (ay - cy)),
+                lab = fmaf(bx - ax, bx - ax, (by - ay) * (by - ay));
+    if (fabsf(ebc + eca + eab) > 1e-6f * (lbc + lca + lab)) return false;
+    return nearProjection(ax, ay, bx, by, cx, cy, epsSq);
+}
+
+// Tolerances of the vertical-ray tests of a mesh: zTol on heights (1e-12 of the largest |z|, far above
+// the FP64 heights' rounding) and epsSq on the (x, y) closeness to a triangle's boundary (4e-6 of the
+// largest |x|, |y|: a few tens of FP32 ulps).
+__device__ __forceinline__ double rayZTol(const QueryTree& t) {
+    return 1e-12 * double(fmaxf(fabsf(t.rootBox0.z), fabsf(t.rootBox1.z)));
+}
+__device__ __forceinline__ float rayEpsSq(const QueryTree& t) {
+    const float e = 4e-6f * fmaxf(fmaxf(fabsf(t.rootBox0.x), fabsf(t.rootBox1.x)), fmaxf(fabsf(t.rootBox0.y), fabsf(t.rootBox1.y)));
+    return e * e;
 }
 
 // Signed crossing of the vertical ray from q (up: +z, else -z) with triangle ABC: the crossing's
@@ -534,11 +578,18 @@ __device__ __forceinline__ int edgeSign(float px, float py, float qx, float qy) 
 // more than it enters), 0 when it misses.  The triangle is translated to the ray's origin in FP32, the
 // same way in every triangle that shares a vertex, so the translated mesh is closed as well and every
 // ray crosses it an exact number of times.  A crossing at the origin itself (q on the surface, where
-// the winding number decides between 0 and 1 by its approximation) sets *onSurface instead.
+// the winding number decides between 0 and 1 by its approximation) sets *onSurface instead, and so
+// does a vertical triangle whose z range holds q's and whose projection passes within sqrt(epsSq) of
+// q (q may lie on it, and no vertical ray crosses it).
 __device__ __forceinline__ int rayCross(const float3& q, const float4& A, const float4& B, const float4& C, bool up,
-                                        bool* onSurface) {
+                                        bool* onSurface, float epsSq, float zTolF) {
     const float ax = __fsub_rn(A.x, q.x), ay = __fsub_rn(A.y, q.y), bx = __fsub_rn(B.x, q.x), by = __fsub_rn(B.y, q.y),
                 cx = __fsub_rn(C.x, q.x), cy = __fsub_rn(C.y, q.y);
+    if (q.z >= __fsub_rd(fminf(A.z, fminf(B.z, C.z)), zTolF) && q.z <= __fadd_ru(fmaxf(A.z, fmaxf(B.z, C.z)), zTolF) &&
+        nearVerticalTriangle(ax, ay, bx, by, cx, cy, det2(bx, cy, by, cx), det2(cx, ay, cy, ax), det2(ax, by, ay, bx), epsSq)) {
+        *onSurface = true;
+        return 0;
+    }
     const int u = edgeSign(bx, by, cx, cy);
     if (u == 0) return 0;
     const int v = edgeSign(cx, cy, ax, ay);
@@ -581,6 +632,7 @@ __device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsign
     if (!m0 || t.nLeaves == 0) return 0;
     const bool up = __shfl_sync(FULL, q.z, __ffs(m0) - 1) >= 0.5f * (t.rootBox0.z + t.rootBox1.z);
     if (upOut) *upOut = up;
+    const float epsSq = rayEpsSq(t), zTolF = __double2float_ru(rayZTol(t));
     WarpStack st;
     st.push(lane, 0, m0);
     bool overflow = false;
@@ -598,7 +650,7 @@ __device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsign
             const int slot = t.faceSlot[l];
             const float4* tr = t.tri + 3 * int64_t(slot);
             const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
-            if (hit && slot != skipSlot) c += rayCross(q, A, B, C, up, onSurface);
+            if (hit && slot != skipSlot) c += rayCross(q, A, B, C, up, onSurface, epsSq, zTolF);
         } else {
             if (!st.push(lane, r, mh)) overflow = true;
             if (!st.push(lane, l, mh)) overflow = true;
@@ -619,29 +671,51 @@ __device__ int rayWinding(const QueryTree& t, const float3& q, bool need, unsign
 // winding-number walk instead.
 constexpr int kColumnCrossings = 24;
 
-// Crossing of the upward ray from q with triangle ABC: its height (FP64) and sign (the contribution
-// to the winding number below it), false when the ray's line misses the triangle (the same exact,
-// watertight projection test as rayCross).
-__device__ __forceinline__ bool columnCross(const float3& q, const float4& A, const float4& B, const float4& C, double* z, int* sign) {
+// The entry of triangle ABC in the list of the vertical column through q's (x, y): where the column
+// crosses the triangle (the same exact, watertight projection test as rayCross), the tolerance
+// interval of the crossing's height (FP64, from the exact weights) and its sign, the contribution to
+// the winding number below it; where the column passes within sqrt(epsSq) of a vertical triangle
+// (nearVerticalTriangle: a voxel there may lie on the surface at any height of the triangle), an
+// interval over the triangle's z range, plus zTol.
+// The FP32 bounds compare with a voxel centre vz (a float) as the interval does: vz < lo <=> vz below
+// it, vz > hi <=> vz above it (rounded outwards where widened).  false: no entry.
+__device__ __forceinline__ bool columnEntry(const float3& q, const float4& A, const float4& B, const float4& C, double zTol,
+                                            float zTolF, float epsSq, float* lo, float* hi, int* sign) {
     const float ax = __fsub_rn(A.x, q.x), ay = __fsub_rn(A.y, q.y), bx = __fsub_rn(B.x, q.x), by = __fsub_rn(B.y, q.y),
                 cx = __fsub_rn(C.x, q.x), cy = __fsub_rn(C.y, q.y);
-    const int u = edgeSign(bx, by, cx, cy);
-    if (u == 0) return false;
-    if (edgeSign(cx, cy, ax, ay) != u || edgeSign(ax, ay, bx, by) != u) return false;
-    const double U = double(bx) * double(cy) - double(by) * double(cx);
-    const double V = double(cx) * double(ay) - double(cy) * double(ax);
-    const double W = double(ax) * double(by) - double(ay) * double(bx);
-    const double det = U + V + W;
-    if (det == 0.0) return false;
-    *z = (U * double(A.z) + V * double(B.z) + W * double(C.z)) / det;
-    *sign = u;
+    const float ebc = det2(bx, cy, by, cx), eca = det2(cx, ay, cy, ax), eab = det2(ax, by, ay, bx);
+    const bool near = nearVerticalTriangle(ax, ay, bx, by, cx, cy, ebc, eca, eab, epsSq);
+    const int u = edgeSignOf(ebc, bx, by, cx, cy);
+    bool cross = u != 0 && edgeSignOf(eca, cx, cy, ax, ay) == u && edgeSignOf(eab, ax, ay, bx, by) == u;
+    float l = FLT_MAX, h = -FLT_MAX;
+    if (cross) {
+        const double U = double(bx) * double(cy) - double(by) * double(cx);
+        const double V = double(cx) * double(ay) - double(cy) * double(ax);
+        const double W = double(ax) * double(by) - double(ay) * double(bx);
+        const double det = U + V + W;
+        if (det != 0.0) {
+            const double z = (U * double(A.z) + V * double(B.z) + W * double(C.z)) / det;
+            l = __double2float_ru(z - zTol);
+            h = __double2float_rd(z + zTol);
+        } else {
+            cross = false;
+        }
+    }
+    if (!cross && !near) return false;
+    if (near) {
+        l = fminf(l, __fsub_rd(fminf(A.z, fminf(B.z, C.z)), zTolF));
+        h = fmaxf(h, __fadd_ru(fmaxf(A.z, fmaxf(B.z, C.z)), zTolF));
+    }
+    *lo = l;
+    *hi = h;
+    *sign = cross ? u : 0;
     return true;
 }
 
 // Crossing lists of the grid's columns, filled by columnRasterKernel: per column the number of
 // crossings at or above the range's first voxel (may exceed kColumnSlots: the column then casts its
-// own ray), bit k of signMask the sign of entry k (1: +1), and entry k's tolerance bounds {lo, hi}
-// (as in signColumnsKernel) at zz[k * ncols + column].  Index space of the columns:
+// own ray), bits 2k, 2k + 1 of signMask the sign of entry k (00: 0, 01: +1, 11: -1), and entry k's
+// bounds {lo, hi} (columnEntry) at zz[k * ncols + column].  Index space of the columns:
 // (fx, fy) = inv ((X, Y) - org); a column centre's FP32 (X, Y) lies within half of (ex, ey) of the
 // exact one.
 constexpr int kColumnSlots = 8;
@@ -654,19 +728,18 @@ struct ColumnLists {
     float ex, ey;
 };
 
-__device__ __forceinline__ void columnAdd(const ColumnLists& cl, const GridRange& g, const Xf& xf, double zTol, int ix, int iy,
-                                          const float4& A, const float4& B, const float4& C) {
+__device__ __forceinline__ void columnAdd(const ColumnLists& cl, const GridRange& g, const Xf& xf, double zTol, float zTolF,
+                                          float epsSq, int ix, int iy, const float4& A, const float4& B, const float4& C) {
     const float3 q0 = xfPoint(xf, ix, iy, g.z0);
-    double z;
+    float zl, zh;
     int sgn;
-    if (!columnCross(q0, A, B, C, &z, &sgn)) return;
-    const float zl = __double2float_ru(z - zTol), zh = __double2float_rd(z + zTol);
+    if (!columnEntry(q0, A, B, C, zTol, zTolF, epsSq, &zl, &zh, &sgn)) return;
     if (q0.z > zh) return;  // below the range's first voxel
     const int64_t col = int64_t(iy) * g.nx + ix;
     const uint32_t k = atomicAdd(cl.count + col, 1u);
     if (k < uint32_t(kColumnSlots)) {
         cl.zz[size_t(k) * size_t(cl.ncols) + size_t(col)] = make_float2(zl, zh);
-        if (sgn > 0) atomicOr(cl.signMask + col, 1u << k);
+        if (sgn != 0) atomicOr(cl.signMask + col, (sgn > 0 ? 1u : 3u) << (2 * k));
     }
 }
 
@@ -676,7 +749,8 @@ __device__ __forceinline__ void columnAdd(const ColumnLists& cl, const GridRange
 // over more than 16 candidate columns is taken by the whole warp, its lanes striding over them.
 __global__ void __launch_bounds__(kThreads) columnRasterKernel(QueryTree t, GridRange g, Xf xf, ColumnLists cl) {
     const int lane = threadIdx.x & 31;
-    const double zTol = 1e-12 * double(fmaxf(fabsf(t.rootBox0.z), fabsf(t.rootBox1.z)));
+    const double zTol = rayZTol(t);
+    const float zTolF = __double2float_ru(zTol), epsSq = rayEpsSq(t);
     const int64_t n = t.nLeaves;
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
@@ -719,7 +793,7 @@ __global__ void __launch_bounds__(kThreads) columnRasterKernel(QueryTree t, Grid
         }
         const int64_t nc = int64_t(w) * h;
         if (nc <= 16) {
-            for (int c = 0; c < int(nc); ++c) columnAdd(cl, g, xf, zTol, ix0 + c % w, iy0 + c / w, A, B, C);
+            for (int c = 0; c < int(nc); ++c) columnAdd(cl, g, xf, zTol, zTolF, epsSq, ix0 + c % w, iy0 + c / w, A, B, C);
         }
         unsigned big = __ballot_sync(FULL, nc > 16);
         while (big) {
@@ -730,7 +804,8 @@ __global__ void __launch_bounds__(kThreads) columnRasterKernel(QueryTree t, Grid
             const float4 Cb = make_float4(__shfl_sync(FULL, C.x, b), __shfl_sync(FULL, C.y, b), __shfl_sync(FULL, C.z, b), 0.f);
             const int bx0 = __shfl_sync(FULL, ix0, b), by0 = __shfl_sync(FULL, iy0, b), bw = __shfl_sync(FULL, w, b);
             const int64_t bn = int64_t(bw) * __shfl_sync(FULL, h, b);
-            for (int64_t c = lane; c < bn; c += 32) columnAdd(cl, g, xf, zTol, bx0 + int(c % bw), by0 + int(c / bw), Ab, Bb, Cb);
+            for (int64_t c = lane; c < bn; c += 32)
+                columnAdd(cl, g, xf, zTol, zTolF, epsSq, bx0 + int(c % bw), by0 + int(c / bw), Ab, Bb, Cb);
         }
     }
 }
@@ -740,6 +815,78 @@ __global__ void __launch_bounds__(kThreads) columnRasterKernel(QueryTree t, Grid
 // word per 32 voxels along x, layout (z - zOut, y, x / 32)) or applied to `values` (negated where
 // inside; value index (z - zOut) nx ny + y nx + x).  The range [z0, z1) of dims is covered.
 constexpr int kColumnSeg = 128;
+
+// Inside bits (bit k: the voxel at zc + k) of the voxels of a column chunk marked in `amb`, from their
+// approximated winding numbers.  Out of line, as columnRay: few voxels take it.
+template <bool PRECISE>
+__device__ __noinline__ uint32_t columnWalks(const QueryTree& t, const Xf& xf, int xc, int y, int zc, int kn, uint32_t amb,
+                                             float betaSq, float threshold, unsigned* status) {
+    uint32_t in = 0;
+    for (int k = 0; k < kn; ++k) {
+        const bool need = (amb >> k) & 1u;
+        if (!__any_sync(FULL, need)) continue;
+        const float wf = fwnPacket<PRECISE>(t, xfPoint(xf, xc, y, zc + k), need, betaSq, -1, status);
+        if (need && wf > threshold) in |= 1u << k;
+    }
+    return in;
+}
+
+// The entries of the columns of the lanes with `ray` from their own vertical ray: a packet walk over
+// the reference nodes (a node when the lane's (x, y) lies in its box's footprint and the box reaches
+// q0's height) adding each triangle's columnEntry to the lane's list, by lo; past kColumnCrossings
+// entries, or when the stack overflows (the whole warp), *overflow is set.  Out of line: only
+// columns whose list overflowed, or launches without lists, take it, and its registers stay out of
+// the sweep.
+__device__ __noinline__ void columnRay(const QueryTree& t, float3 q0, bool ray, double zTol, float zTolF, float epsSq, float* lo,
+                                       float* hi, int* sg, int* nOut, bool* overflowOut, unsigned* status) {
+    const int lane = threadIdx.x & 31;
+    int n = *nOut;
+    bool overflow = *overflowOut;
+    WarpStack st;
+    st.push(lane, 0, __ballot_sync(FULL, ray));
+    bool stackFull = false;
+    while (st.sp > 0 && t.nLeaves > 0) {
+        int node;
+        unsigned m;
+        st.pop(node, m);
+        const float4 n0 = ld4(t.nodes + 2 * int64_t(node)), n1 = ld4(t.nodes + 2 * int64_t(node) + 1);
+        const bool hit = ((m >> lane) & 1u) && q0.x >= n0.x && q0.x <= n0.w && q0.y >= n0.y && q0.y <= n1.x && n1.y >= q0.z;
+        const unsigned mh = __ballot_sync(FULL, hit);
+        if (!mh) continue;
+        const int l = __float_as_int(n1.z), r = __float_as_int(n1.w);
+        if (r < 0) {
+            const float4* tr = t.tri + 3 * int64_t(t.faceSlot[l]);
+            const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+            float zl, zh;
+            int sgn;
+            if (hit && columnEntry(q0, A, B, C, zTol, zTolF, epsSq, &zl, &zh, &sgn) && !(q0.z > zh)) {
+                if (n < kColumnCrossings) {
+                    int k = n++;
+                    while (k > 0 && lo[k - 1] > zl) {
+                        lo[k] = lo[k - 1];
+                        hi[k] = hi[k - 1];
+                        sg[k] = sg[k - 1];
+                        --k;
+                    }
+                    lo[k] = zl;
+                    hi[k] = zh;
+                    sg[k] = sgn;
+                } else {
+                    overflow = true;
+                }
+            }
+        } else if (!st.push(lane, r, mh) || !st.push(lane, l, mh)) {
+            stackFull = true;
+            break;
+        }
+    }
+    if (stackFull) {
+        overflow = true;  // every lane of the warp falls back
+        if (lane == 0) atomicOr(status, kStatusStackOverflow);
+    }
+    *nOut = n;
+    *overflowOut = overflow;
+}
 
 template <bool PRECISE>
 __global__ void __launch_bounds__(kThreads, 4) signColumnsKernel(QueryTree t, GridRange g, Xf xf, float threshold, float beta,
@@ -751,11 +898,11 @@ __global__ void __launch_bounds__(kThreads, 4) signColumnsKernel(QueryTree t, Gr
     const int segs = (g.z1 - g.z0 + kColumnSeg - 1) / kColumnSeg;
     const uint64_t items = uint64_t(wordsX) * uint64_t(g.ny) * uint64_t(segs);
     const size_t sxy = size_t(g.nx) * g.ny;
-    // the heights' rounding error is below 1e-15 of the largest |z| of the mesh
-    const double zTol = 1e-12 * double(fmaxf(fabsf(t.rootBox0.z), fabsf(t.rootBox1.z)));
-    // per crossing (ascending): the FP32 bounds of its tolerance interval [z - zTol, z + zTol] rounded
-    // outwards, so that for a voxel centre vz (a float) vz < lo <=> vz < z - zTol and vz > hi <=>
-    // vz > z + zTol: the sweep compares in FP32 (FP64 issues at a small fraction of the FP32 rate)
+    const double zTol = rayZTol(t);
+    const float zTolF = __double2float_ru(zTol), epsSq = rayEpsSq(t);
+    // per entry (ascending lo; columnEntry): the FP32 bounds of its interval, so that for a voxel
+    // centre vz (a float) vz < lo <=> vz below the interval and vz > hi <=> vz above it: the sweep
+    // compares in FP32 (FP64 issues at a small fraction of the FP32 rate)
     float lo[kColumnCrossings], hi[kColumnCrossings];
     int sg[kColumnCrossings];
     for (;;) {
@@ -790,59 +937,14 @@ __global__ void __launch_bounds__(kThreads, 4) signColumnsKernel(QueryTree t, Gr
                     }
                     lo[k] = zz.x;
                     hi[k] = zz.y;
-                    sg[k] = ((mask >> e) & 1u) ? 1 : -1;
+                    const uint32_t m2 = (mask >> (2 * e)) & 3u;
+                    sg[k] = m2 == 1u ? 1 : (m2 == 3u ? -1 : 0);
                 }
             } else {
                 ray = true;
             }
         }
-        if (__any_sync(FULL, ray)) {
-            WarpStack st;
-            st.push(lane, 0, __ballot_sync(FULL, ray));
-            bool stackFull = false;
-            while (st.sp > 0 && t.nLeaves > 0) {
-                int node;
-                unsigned m;
-                st.pop(node, m);
-                const float4 n0 = ld4(t.nodes + 2 * int64_t(node)), n1 = ld4(t.nodes + 2 * int64_t(node) + 1);
-                const bool hit = ((m >> lane) & 1u) && q0.x >= n0.x && q0.x <= n0.w && q0.y >= n0.y && q0.y <= n1.x && n1.y >= q0.z;
-                const unsigned mh = __ballot_sync(FULL, hit);
-                if (!mh) continue;
-                const int l = __float_as_int(n1.z), r = __float_as_int(n1.w);
-                if (r < 0) {
-                    const float4* tr = t.tri + 3 * int64_t(t.faceSlot[l]);
-                    const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
-                    double z;
-                    int sgn;
-                    if (hit && columnCross(q0, A, B, C, &z, &sgn)) {
-                        const float zl = __double2float_ru(z - zTol), zh = __double2float_rd(z + zTol);
-                        if (q0.z > zh) {
-                            // below the segment's first voxel: no voxel of it is below this crossing
-                        } else if (n < kColumnCrossings) {
-                            int k = n++;
-                            while (k > 0 && lo[k - 1] > zl) {
-                                lo[k] = lo[k - 1];
-                                hi[k] = hi[k - 1];
-                                sg[k] = sg[k - 1];
-                                --k;
-                            }
-                            lo[k] = zl;
-                            hi[k] = zh;
-                            sg[k] = sgn;
-                        } else {
-                            overflow = true;
-                        }
-                    }
-                } else if (!st.push(lane, r, mh) || !st.push(lane, l, mh)) {
-                    stackFull = true;
-                    break;
-                }
-            }
-            if (stackFull) {
-                overflow = true;  // every lane of the warp falls back
-                if (lane == 0) atomicOr(scratch + 1, kStatusStackOverflow);
-            }
-        }
+        if (__any_sync(FULL, ray)) columnRay(t, q0, ray, zTol, zTolF, epsSq, lo, hi, sg, &n, &overflow, scratch + 1);
         // the sweep up the segment, 32 layers at a time: w = signed crossings above the voxel
         int w = 0, p = 0;
         for (int k = 0; k < n; ++k) w += sg[k];
@@ -851,24 +953,21 @@ __global__ void __launch_bounds__(kThreads, 4) signColumnsKernel(QueryTree t, Gr
             uint32_t in = 0, amb = 0;  // bit k: the voxel at zc + k
             for (int k = 0; k < kn; ++k) {
                 const float vz = xfPoint(xf, xc, y, zc + k).z;
-                while (p < n && vz > hi[p]) {  // crossings passed: below the voxel
+                // entries passed (below the voxel) leave w; the walk stops at the first entry reaching
+                // up to vz, and every entry after it starts above lo[p] (ascending lo): so the voxel
+                // lies in an interval iff vz >= lo[p], and otherwise every entry left is above it
+                while (p < n && vz > hi[p]) {
                     w -= sg[p];
                     ++p;
                 }
-                if (overflow || (p < n && vz >= lo[p]))  // within the next crossing's tolerance
+                if (overflow || (p < n && vz >= lo[p]))  // on the surface, up to rounding: the walk decides
                     amb |= 1u << k;
                 else if (float(w) > threshold)
                     in |= 1u << k;
             }
             if (!active) amb = in = 0;
-            if (__any_sync(FULL, amb != 0)) {  // on the surface (up to rounding): the winding-number walk
-                for (int k = 0; k < kn; ++k) {
-                    const bool need = (amb >> k) & 1u;
-                    if (!__any_sync(FULL, need)) continue;
-                    const float wf = fwnPacket<PRECISE>(t, xfPoint(xf, xc, y, zc + k), need, betaSq, -1, scratch + 1);
-                    if (need && wf > threshold) in |= 1u << k;
-                }
-            }
+            // on the surface (up to rounding): the winding-number walk
+            if (__any_sync(FULL, amb != 0)) in |= columnWalks<PRECISE>(t, xf, xc, y, zc, kn, amb, betaSq, threshold, scratch + 1);
             if (values) {
                 float* vp = values + size_t(zc - g.zOut) * sxy + size_t(y) * g.nx + xc;
 #pragma unroll 8

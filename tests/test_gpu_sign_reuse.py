@@ -314,3 +314,31 @@ def test_column_signs_on_small_and_outlying_grids(M):
         gg.set_sign_reuse(True)
         _same(*res)
     assert (res[0] < 0).all()  # the last grid lies inside the sphere
+
+
+def test_column_signs_with_vertices_on_column_centres(M):
+    """A cube and an octahedron whose vertices, edges and faces lie exactly on voxel centres and grid
+    columns (rays through vertices and along edges, vertical faces in the rays' planes, voxels on the
+    faces): the column signs equal the winding-number walk's at every voxel."""
+    cube_v = np.array([[x, y, z] for z in (0, 1) for y in (0, 1) for x in (0, 1)], np.float32) * np.float32(1.5) + np.float32(0.5)
+    cube_f = np.array([[0, 2, 3], [0, 3, 1], [4, 5, 7], [4, 7, 6], [0, 1, 5], [0, 5, 4], [2, 6, 7], [2, 7, 3], [0, 4, 6],
+                       [0, 6, 2], [1, 3, 7], [1, 7, 5]], np.int32)
+    octa_v = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32) + np.float32(1.25)
+    octa_f = np.array([[0, 2, 4], [2, 1, 4], [1, 3, 4], [3, 0, 4], [2, 0, 5], [1, 2, 5], [3, 1, 5], [0, 3, 5]], np.int32)
+    xf = np.zeros(12, np.float32)
+    xf[0] = xf[4] = xf[8] = 0.25  # voxel centres at multiples of 0.25, the vertices among them
+    flipped = 0
+    for cv, cf in ((cube_v, cube_f), (octa_v, octa_f)):
+        g = M.FastWindingNumber(cv, cf)
+        assert g.is_closed()
+        for opts in (None, M.DistanceToMeshOptions(maxDistSq=0.3 ** 2)):
+            res = []
+            for enable in (True, False):
+                g.set_sign_reuse(enable)
+                res.append(g.calcFromGridWithDistances((11, 11, 11), xf, opts))
+            g.set_sign_reuse(True)
+            _same(*res)
+            flipped += int((res[0] < 0).sum())
+        vals = np.random.default_rng(1).uniform(0.1, 1.0, 11 ** 3).astype(np.float32)
+        assert np.array_equal(_signed_pass(M, g, (11, 11, 11), xf, vals, True), _signed_pass(M, g, (11, 11, 11), xf, vals, False))
+    assert flipped > 0
