@@ -136,8 +136,14 @@ __global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, co
         const int32_t s = slot[i];
         const int32_t* t = tris + 3 * int64_t(nd.l);
         const float3 a = vload(verts, t[0]), b = vload(verts, t[1]), c = vload(verts, t[2]);
+        // b.w flags a triangle whose (x, y) projection has (next to) no area: vertical rays never
+        // cross it, though a point of one may lie on it (the rays' on-surface rule)
+        const float e1x = b.x - a.x, e1y = b.y - a.y, e2x = c.x - a.x, e2y = c.y - a.y;
+        const float area2 = fmaf(e1x, e2y, -e1y * e2x);
+        const float len2 = fmaf(e1x, e1x, e1y * e1y) + fmaf(e2x, e2x, e2y * e2y) + fmaf(c.x - b.x, c.x - b.x, (c.y - b.y) * (c.y - b.y));
+        const float vertical = fabsf(area2) <= 1e-5f * len2 ? 1.f : 0.f;
         tri[3 * int64_t(s) + 0] = make_float4(a.x, a.y, a.z, __int_as_float(nd.l));
-        tri[3 * int64_t(s) + 1] = make_float4(b.x, b.y, b.z, 0.f);
+        tri[3 * int64_t(s) + 1] = make_float4(b.x, b.y, b.z, vertical);
         tri[3 * int64_t(s) + 2] = make_float4(c.x, c.y, c.z, 0.f);
         faceSlot[nd.l] = s;
         return;

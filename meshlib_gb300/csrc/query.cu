@@ -547,19 +547,6 @@ __device__ __forceinline__ float segDistSq0(float px, float py, float qx, float 
 __device__ __forceinline__ bool nearProjection(float ax, float ay, float bx, float by, float cx, float cy, float epsSq) {
     return segDistSq0(ax, ay, bx, by) <= epsSq || segDistSq0(bx, by, cx, cy) <= epsSq || segDistSq0(cx, cy, ax, ay) <= epsSq;
 }
-// For a triangle whose projection has (next to) no area — a vertical triangle, which no vertical ray
-// crosses though a point of the ray may lie on it — whether the origin lies within sqrt(epsSq) of
-// the projection.  e = E(b, c), E(c, a), E(a, b): the edge functions, whose sum is twice the
-// projected area.  Other triangles need no such test: a point of the ray on one of them is a crossing
-// at that height (or, on a shared edge, the crossing of its neighbour), which the height tolerance
-// covers.
-__device__ __forceinline__ bool nearVerticalTriangle(float ax, float ay, float bx, float by, float cx, float cy, float ebc, float eca,
-                                                     float eab, float epsSq) {
-    const float lbc = fmaf(cx - bx, cx - bx, (cy - by) * (cy - by)), lca = fmaf(ax - cx, ax - cx, (ay - cy) * (ay - cy)),
-                lab = fmaf(bx - ax, bx - ax, (by - ay) * (by - ay));
-    if (fabsf(ebc + eca + eab) > 1e-6f * (lbc + lca + lab)) return false;
-    return nearProjection(ax, ay, bx, by, cx, cy, epsSq);
-}
 
 // Tolerances of the vertical-ray tests of a mesh: zTol on heights (1e-12 of the largest |z|, far above
 // the FP64 heights' rounding) and epsSq on the (x, y) closeness to a triangle's boundary (4e-6 of the
@@ -579,14 +566,15 @@ __device__ __forceinline__ float rayEpsSq(const QueryTree& t) {
 // same way in every triangle that shares a vertex, so the translated mesh is closed as well and every
 // ray crosses it an exact number of times.  A crossing at the origin itself (q on the surface, where
 // the winding number decides between 0 and 1 by its approximation) sets *onSurface instead, and so
-// does a vertical triangle whose z range holds q's and whose projection passes within sqrt(epsSq) of
-// q (q may lie on it, and no vertical ray crosses it).
+// does a vertical triangle (flagged in B.w when the leaf records are packed: a projection with next
+// to no area) whose z range holds q's and whose projection passes within sqrt(epsSq) of q (q may lie
+// on it, and no vertical ray crosses it).
 __device__ __forceinline__ int rayCross(const float3& q, const float4& A, const float4& B, const float4& C, bool up,
                                         bool* onSurface, float epsSq, float zTolF) {
     const float ax = __fsub_rn(A.x, q.x), ay = __fsub_rn(A.y, q.y), bx = __fsub_rn(B.x, q.x), by = __fsub_rn(B.y, q.y),
                 cx = __fsub_rn(C.x, q.x), cy = __fsub_rn(C.y, q.y);
-    if (q.z >= __fsub_rd(fminf(A.z, fminf(B.z, C.z)), zTolF) && q.z <= __fadd_ru(fmaxf(A.z, fmaxf(B.z, C.z)), zTolF) &&
-        nearVerticalTriangle(ax, ay, bx, by, cx, cy, det2(bx, cy, by, cx), det2(cx, ay, cy, ax), det2(ax, by, ay, bx), epsSq)) {
+    if (B.w != 0.f && q.z >= __fsub_rd(fminf(A.z, fminf(B.z, C.z)), zTolF) && q.z <= __fadd_ru(fmaxf(A.z, fmaxf(B.z, C.z)), zTolF) &&
+        nearProjection(ax, ay, bx, by, cx, cy, epsSq)) {
         *onSurface = true;
         return 0;
     }
@@ -675,18 +663,17 @@ constexpr int kColumnCrossings = 24;
 // crosses the triangle (the same exact, watertight projection test as rayCross), the tolerance
 // interval of the crossing's height (FP64, from the exact weights) and its sign, the contribution to
 // the winding number below it; where the column passes within sqrt(epsSq) of a vertical triangle
-// (nearVerticalTriangle: a voxel there may lie on the surface at any height of the triangle), an
-// interval over the triangle's z range, plus zTol.
+// (flagged in B.w: a voxel there may lie on the surface at any height of the triangle), an interval
+// over the triangle's z range, plus zTol.
 // The FP32 bounds compare with a voxel centre vz (a float) as the interval does: vz < lo <=> vz below
 // it, vz > hi <=> vz above it (rounded outwards where widened).  false: no entry.
 __device__ __forceinline__ bool columnEntry(const float3& q, const float4& A, const float4& B, const float4& C, double zTol,
                                             float zTolF, float epsSq, float* lo, float* hi, int* sign) {
     const float ax = __fsub_rn(A.x, q.x), ay = __fsub_rn(A.y, q.y), bx = __fsub_rn(B.x, q.x), by = __fsub_rn(B.y, q.y),
                 cx = __fsub_rn(C.x, q.x), cy = __fsub_rn(C.y, q.y);
-    const float ebc = det2(bx, cy, by, cx), eca = det2(cx, ay, cy, ax), eab = det2(ax, by, ay, bx);
-    const bool near = nearVerticalTriangle(ax, ay, bx, by, cx, cy, ebc, eca, eab, epsSq);
-    const int u = edgeSignOf(ebc, bx, by, cx, cy);
-    bool cross = u != 0 && edgeSignOf(eca, cx, cy, ax, ay) == u && edgeSignOf(eab, ax, ay, bx, by) == u;
+    const bool near = B.w != 0.f && nearProjection(ax, ay, bx, by, cx, cy, epsSq);
+    const int u = edgeSign(bx, by, cx, cy);
+    bool cross = u != 0 && edgeSign(cx, cy, ax, ay) == u && edgeSign(ax, ay, bx, by) == u;
     float l = FLT_MAX, h = -FLT_MAX;
     if (cross) {
         const double U = double(bx) * double(cy) - double(by) * double(cx);
