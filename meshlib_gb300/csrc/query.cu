@@ -1438,8 +1438,12 @@ cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf
 
 bool signColumnsApply(const QueryTree& t, const Xf& xf, float beta, float threshold) {
     const float fr = threshold - floorf(threshold);
+    // the (x, y) map must be well conditioned: the raster pass maps triangle bounds back to columns
+    // through its inverse, in FP32
+    const double det = double(xf.a[0]) * xf.a[4] - double(xf.a[1]) * xf.a[3];
+    const double scale = (std::fabs(double(xf.a[0])) + std::fabs(double(xf.a[1]))) * (std::fabs(double(xf.a[3])) + std::fabs(double(xf.a[4])));
     return t.closed && beta >= 2.f && fr > 0.25f && fr < 0.75f && xf.a[2] == 0.f && xf.a[5] == 0.f && xf.a[8] > 0.f &&
-           double(xf.a[0]) * xf.a[4] - double(xf.a[1]) * xf.a[3] != 0.0;
+           std::fabs(det) >= 1e-6 * scale && std::fabs(det) > 1e-30 && scale < 1e30;
 }
 
 size_t signColumnsWorkBytes(const GridRange& g) {

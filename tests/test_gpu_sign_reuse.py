@@ -342,3 +342,29 @@ def test_column_signs_with_vertices_on_column_centres(M):
         vals = np.random.default_rng(1).uniform(0.1, 1.0, 11 ** 3).astype(np.float32)
         assert np.array_equal(_signed_pass(M, g, (11, 11, 11), xf, vals, True), _signed_pass(M, g, (11, 11, 11), xf, vals, False))
     assert flipped > 0
+
+
+def test_column_signs_on_mirrored_grids(M):
+    """Grids mirrored along x (column signs, the index map's determinant negative) and along z (no
+    column signs: z must point up): the same grids as the winding-number walk, and the mirrored grids
+    hold the unmirrored one's values in mirrored order."""
+    v, f = mg.noisy_torus(seed=10)
+    g = M.FastWindingNumber(v, f)
+    dims, xf = mg.grid_for(v, 48)
+    xf = np.asarray(xf, np.float32)
+    plain = g.calcFromGridWithDistances(dims, xf).reshape(dims[2], dims[1], dims[0])
+    mx = xf.copy()
+    mx[0] = -xf[0]
+    mx[9] = xf[9] + xf[0] * (dims[0] - 1)
+    mz = xf.copy()
+    mz[8] = -xf[8]
+    mz[11] = xf[11] + xf[8] * (dims[2] - 1)
+    for gx, flip in ((mx, 2), (mz, 0)):
+        res = []
+        for enable in (True, False):
+            g.set_sign_reuse(enable)
+            res.append(g.calcFromGridWithDistances(dims, gx))
+        g.set_sign_reuse(True)
+        _same(*res)
+        mirrored = res[0].reshape(dims[2], dims[1], dims[0])
+        assert np.array_equal(np.signbit(np.flip(mirrored, axis=flip)), np.signbit(plain))
