@@ -144,7 +144,9 @@ __global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, co
         const float vertical = fabsf(area2) <= 1e-5f * len2 ? 1.f : 0.f;
         tri[3 * int64_t(s) + 0] = make_float4(a.x, a.y, a.z, __int_as_float(nd.l));
         tri[3 * int64_t(s) + 1] = make_float4(b.x, b.y, b.z, vertical);
-        tri[3 * int64_t(s) + 2] = make_float4(c.x, c.y, c.z, 0.f);
+        tri[3 * int64_t(s) + 2] = make_float4(c.x, c.y, c.z,
+                                              nearPlaneLevel(make_float4(a.x, a.y, a.z, 0.f), make_float4(b.x, b.y, b.z, 0.f),
+                                                             make_float4(c.x, c.y, c.z, 0.f)));
         faceSlot[nd.l] = s;
         return;
     }

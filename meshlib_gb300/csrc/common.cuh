@@ -51,6 +51,17 @@ struct QueryTree {
     int32_t closed;
 };
 
+// Squared-distance level below which the precise triangle distance is re-evaluated in FP64 (the
+// query lies within about 1e-4 edge lengths of the triangle): 1e-8 of |b - a|^2 + |c - a|^2, rounded
+// the same way wherever it is computed.  Kept in the leaf records (the fourth word of c).
+__device__ __forceinline__ float nearPlaneLevel(const float4& a, const float4& b, const float4& c) {
+    const float abx = __fsub_rn(b.x, a.x), aby = __fsub_rn(b.y, a.y), abz = __fsub_rn(b.z, a.z);
+    const float acx = __fsub_rn(c.x, a.x), acy = __fsub_rn(c.y, a.y), acz = __fsub_rn(c.z, a.z);
+    const float s = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(abx, abx), __fmul_rn(aby, aby)), __fmul_rn(abz, abz)),
+                              __fadd_rn(__fadd_rn(__fmul_rn(acx, acx), __fmul_rn(acy, acy)), __fmul_rn(acz, acz)));
+    return __fmul_rn(1e-8f, s);
+}
+
 struct Xf {
     float a[9];  // rows
     float b[3];
@@ -118,10 +129,16 @@ cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTil
 
 // Signed distance on runs of 8x8x8-voxel bricks of the grid: runs[i] = (bx, by, bz0, count), the
 // `count` bricks (bx, by, bz0 .. bz0 + count - 1), nBricks in all; voxels outside them are not written.
-// signBits (optional): the grid's inside bits from launchSignColumns, used for the signs.
+// signBits (optional): the grid's inside bits from launchSignColumns, used for the signs; fix (with
+// them, pairFixBytesForRuns bytes): the precise paired walk's fix list, without which precise grids
+// take the one-voxel walk.
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                                 float* out, const int4* runs, int32_t nRuns, int32_t nBricks, const uint32_t* signBits,
-                                unsigned* scratch, cudaStream_t s);
+                                void* fix, unsigned* scratch, cudaStream_t s);
+// Bytes of the precise paired walk's fix list for nTiles warp tiles in nItems work items, and for
+// brick runs.
+size_t pairFixBytes(uint32_t nTiles, uint32_t nItems);
+size_t pairFixBytesForRuns(int32_t nRuns, int32_t nBricks);
 // Bytes of the inside bits of a grid range (one 32-bit word per 32 voxels along x).
 size_t signBitsBytes(const GridRange& g);
 // Point queries; `order` (optional) is a permutation of [0, n): points are processed in that order

@@ -686,7 +686,9 @@ cudaError_t bandedGrid(const QueryTree& t, SurrogateNet* net, const GridRange& g
     if (kept > 0 && columns &&
         (e = launchSignColumns(t, g, xf, o.beta, o.threshold, precise, bits, nullptr, lists, signColumnsWorkBytes(g), scratch, s)))
         return done(e);
-    if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, runs, counts[1], kept, bits, scratch, s))) return done(e);
+    void* fix = nullptr;  // the precise paired walk's fix list
+    if (kept > 0 && columns && precise && (e = A(&fix, pairFixBytesForRuns(counts[1], kept)))) return done(e);
+    if (kept > 0 && (e = launchGridSdfBricks(t, g, xf, o, precise, out, runs, counts[1], kept, bits, fix, scratch, s))) return done(e);
     cudaEventRecord(ev[3], s);
     if ((e = cudaStreamSynchronize(s))) return done(e);
     cudaEventElapsedTime(&st.cullMs, ev[0], ev[1]);

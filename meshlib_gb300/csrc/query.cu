@@ -336,25 +336,29 @@ __device__ __noinline__ float triDistSqFp64(const float3 p, const float4 A, cons
     return dot3rn(qx, qy, qz, qx, qy, qz);
 }
 
-// Squared distance from p to a triangle.  FP32 projection; in precise mode a query that lands
-// within ~1e-4 triangle edge lengths of the triangle is re-projected in FP64.
+// Squared distance from p to a triangle (a leaf record: C.w holds its nearPlaneLevel).  FP32
+// projection; in precise mode a query that lands within ~1e-4 triangle edge lengths of the triangle
+// (below C.w) is re-projected in FP64.
 template <bool PRECISE>
 __device__ __forceinline__ float triDistSq(const float3& p, const float4& A, const float4& B, const float4& C) {
     const V3T<float> pf{p.x, p.y, p.z}, af{A.x, A.y, A.z}, bf{B.x, B.y, B.z}, cf{C.x, C.y, C.z};
     const V3T<float> pr = closestPoint<float>(pf, af, bf, cf);
     const V3T<float> d = vsub(pr, pf);
     float ds = dot3rn(d.x, d.y, d.z, d.x, d.y, d.z);
-    if (PRECISE) {
-        const V3T<float> ab = vsub(bf, af), ac = vsub(cf, af);
-        const float scale = vdot(ab, ab) + vdot(ac, ac);
-        if (ds < 1e-8f * scale) ds = triDistSqFp64(p, A, B, C);
-    }
+    if (PRECISE && ds < C.w) ds = triDistSqFp64(p, A, B, C);
     return ds;
 }
 
 __device__ __forceinline__ float4 xf4(const Xf* xf, const float4& v) {
     const float3 r = xfApply(*xf, v.x, v.y, v.z);
     return make_float4(r.x, r.y, r.z, v.w);
+}
+// A leaf triangle seen through the affine map *xf, its near-plane level recomputed for the mapped one.
+__device__ __forceinline__ void xfTri(const Xf* xf, float4& A, float4& B, float4& C) {
+    A = xf4(xf, A);
+    B = xf4(xf, B);
+    C = xf4(xf, C);
+    C.w = nearPlaneLevel(A, B, C);
 }
 
 // TRACK: remember the leaf slot of the best triangle in *best; TREEXF: the mesh is seen through
@@ -367,9 +371,7 @@ __device__ __forceinline__ void leafDist(const QueryTree& t, int slot, const flo
     float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
     if (go) {
         if (TREEXF) {
-            A = xf4(txf, A);
-            B = xf4(txf, B);
-            C = xf4(txf, C);
+            xfTri(txf, A, B, C);
         }
         const float ds = triDistSq<PRECISE>(q, A, B, C);
         if (ds < resSq) {
@@ -446,6 +448,92 @@ __device__ float cpPacket(const QueryTree& t, const float3& q, bool active, floa
     return resSq;
 }
 
+// One leaf triangle for the two queries of a lane (loaded once), in FP32; FLAG: a query that comes
+// within the triangle's near-plane level (where the precise distance would be re-evaluated in FP64)
+// sets its flag, and the caller evaluates that query again with the precise walk.
+template <bool FLAG>
+__device__ __forceinline__ void leafDist2(const QueryTree& t, int slot, const float3& qa, const float3& qb, bool goA, bool goB,
+                                          float& resA, float& resB, int& bestA, int& bestB, bool& doneA, bool& doneB,
+                                          bool& flagA, bool& flagB) {
+    const float4* tr = t.tri + 3 * int64_t(slot);
+    const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
+    if (goA) {
+        const float ds = triDistSq<false>(qa, A, B, C);
+        if (FLAG && ds < C.w) flagA = true;
+        if (ds < resA) {
+            resA = ds;
+            bestA = slot;
+            if (ds <= 0.f) doneA = true;
+        }
+    }
+    if (goB) {
+        const float ds = triDistSq<false>(qb, A, B, C);
+        if (FLAG && ds < C.w) flagB = true;
+        if (ds < resB) {
+            resB = ds;
+            bestB = slot;
+            if (ds <= 0.f) doneB = true;
+        }
+    }
+}
+
+// Two queries per lane in one packet walk (voxels qa and qb of the lane): a node is opened when either
+// query of any lane may hold a closer triangle, each query keeps its own bound and prunes its own
+// leaves, so each result is its exact minimum, as with cpPacket (no early stop: loSq = 0).  FP32
+// triangle distances; FLAG as leafDist2.
+template <bool FLAG>
+__device__ void cpPacket2(const QueryTree& t, const float3& qa, const float3& qb, bool activeA, bool activeB, float& resA,
+                          float& resB, int& bestA, int& bestB, bool& flagA, bool& flagB, unsigned* status) {
+    const int lane = threadIdx.x & 31;
+    if (t.nLeaves == 0) return;
+    const bool inA = activeA && boxDistSq(t.rootBox0, t.rootBox1, qa) < resA;
+    const bool inB = activeB && boxDistSq(t.rootBox0, t.rootBox1, qb) < resB;
+    const unsigned m0 = __ballot_sync(FULL, inA || inB);
+    if (!m0) return;
+    const int rootLink = __float_as_int(t.rootBox0.w);
+    bool doneA = !activeA, doneB = !activeB;
+    if (rootLink < 0) {
+        leafDist2<FLAG>(t, ~rootLink, qa, qb, inA, inB, resA, resB, bestA, bestB, doneA, doneB, flagA, flagB);
+        return;
+    }
+    WarpStack st;
+    st.push(lane, rootLink, m0);
+    bool overflow = false;
+    while (st.sp > 0) {
+        int node;
+        unsigned m;
+        st.pop(node, m);
+        const CpRecord rec = loadCp(t.cp + 6 * int64_t(node));
+        const bool mine = (m >> lane) & 1u;
+        const float3 xa = toFrame(rec, qa), xb = toFrame(rec, qb);
+        float dla = frameBoxDistSq(xa, rec.cl, rec.el), dra = frameBoxDistSq(xa, rec.cr, rec.er);
+        float dlb = frameBoxDistSq(xb, rec.cl, rec.el), drb = frameBoxDistSq(xb, rec.cr, rec.er);
+        const bool gla = mine && !doneA && dla < resA, gra = mine && !doneA && dra < resA;
+        const bool glb = mine && !doneB && dlb < resB, grb = mine && !doneB && drb < resB;
+        const bool gl = gla || glb, gr = gra || grb;
+        const unsigned ml = __ballot_sync(FULL, gl), mr = __ballot_sync(FULL, gr);
+        if ((ml | mr) == 0) continue;
+        const float dl = fminf(gla ? dla : FLT_MAX, glb ? dlb : FLT_MAX), dr = fminf(gra ? dra : FLT_MAX, grb ? drb : FLT_MAX);
+        const unsigned preferL = __ballot_sync(FULL, gl && gr ? dl < dr : gl);
+        const unsigned both = ml | mr;
+        const bool leftFirst = 2 * __popc(preferL & both) > __popc(both);
+        const int nearLink = leftFirst ? rec.ll : rec.rl, farLink = leftFirst ? rec.rl : rec.ll;
+        const unsigned nearM = leftFirst ? ml : mr, farM = leftFirst ? mr : ml;
+        const bool nearA = leftFirst ? gla : gra, nearB = leftFirst ? glb : grb;
+        const bool farA = leftFirst ? gra : gla, farB = leftFirst ? grb : glb;
+        const float farDA = leftFirst ? dra : dla, farDB = leftFirst ? drb : dlb;
+        if (nearM && nearLink < 0)
+            leafDist2<FLAG>(t, ~nearLink, qa, qb, nearA, nearB, resA, resB, bestA, bestB, doneA, doneB, flagA, flagB);
+        if (farM && farLink < 0)
+            leafDist2<FLAG>(t, ~farLink, qa, qb, farA && !doneA && farDA < resA, farB && !doneB && farDB < resB, resA, resB, bestA,
+                            bestB, doneA, doneB, flagA, flagB);
+        if (farM && farLink >= 0 && !st.push(lane, farLink, farM)) overflow = true;
+        if (nearM && nearLink >= 0 && !st.push(lane, nearLink, nearM)) overflow = true;
+        if (overflow) break;
+    }
+    if (overflow && lane == 0) atomicOr(status, kStatusStackOverflow);
+}
+
 // ------------------------------------------------------------------ kernels
 constexpr int kThreads = 256;
 // Resident blocks per SM of the kernels that run the closest-point walk (48 registers, a few values
@@ -456,6 +544,8 @@ constexpr int kThreads = 256;
 // 4 (23.4 -> 25.1 ms at 6); so do self-intersections and the batched kernel, which measured slower with
 // more warps.
 constexpr int kDistBlocks = 5;
+// Resident blocks per SM of the paired walk (two voxels per lane).
+constexpr int kPairBlocks = 5;
 // Voxel tile of one warp.  Measured at 512^3 on 1.31 M triangles with sign reuse (the same grids for
 // every shape): 4x4x2 84.2 ms, 2x4x4 88.5, 4x2x4 88.6, 8x4x1 103.1, 4x8x1 102.8.
 constexpr int kTX = 4, kTY = 4, kTZ = 2;
@@ -484,6 +574,11 @@ struct TileGrid {
     // voxels along x, (z - zOut, y, x / 32)); when given, the signed-distance kernel takes its signs
     // from them instead of its own walks
     const uint32_t* signBits;
+    // precise paired walks: the pair steps with voxels that came within a triangle's near-plane level,
+    // {item, first tile, lane mask of the lower voxels, of the upper ones}, re-walked by fixPairKernel;
+    // fixList[0].x counts them (capacity fixCap entries after it)
+    uint4* fixList;
+    uint32_t fixCap;
 };
 
 __device__ __forceinline__ unsigned nextTicket(unsigned* counter, int lane) {
@@ -1119,6 +1214,142 @@ __global__ void __launch_bounds__(kThreads, DIST ? kDistBlocks : 4) gridKernel(Q
     }
 }
 
+// Signed distances with the column pass's sign bits and no lower distance bound (minDistSq = 0): a
+// warp walks its column two tiles at a time, each lane taking its voxel of the lower tile and the one
+// two layers above it (a 4x4x4 block of voxels) through one shared packet walk (cpPacket2), so each
+// record read and stack step serves 64 voxels.  Both start from the triangle closest to the voxel
+// below the lower tile (as gridKernel's seeds); results are the exact minima, as gridKernel's.  In
+// precise mode the walk runs in FP32 and the voxels that came within a triangle's near-plane level
+// are listed for fixPairKernel, which walks them again with the precise distances.
+template <bool PRECISE>
+__global__ void __launch_bounds__(kThreads, kPairBlocks) gridPairKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
+                                                                        float* __restrict__ out, unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
+    const size_t sxy = size_t(g.nx) * g.ny;
+    const int wordsX = (g.nx + 31) >> 5;
+    for (;;) {
+        const unsigned item = nextTicket(scratch, lane);
+        if (item >= tg.numItems) break;
+        int x0, y0, zBase, nSeg;
+        if (tg.runs) {
+            const int4 r = tg.runs[item / kBrickCols];
+            const int col = int(item % kBrickCols);
+            x0 = r.x * 8 + (col % kBrickColsX) * kTX;
+            y0 = r.y * 8 + (col / kBrickColsX) * kTY;
+            zBase = g.z0 + r.z * 8;
+            nSeg = kBrickSeg * r.w;
+        } else {
+            const int tx = int(item % unsigned(tg.tilesX));
+            const unsigned rest = item / unsigned(tg.tilesX);
+            const int ty = int(rest % unsigned(tg.tilesY));
+            const int sz = int(rest / unsigned(tg.tilesY));
+            x0 = tx * kTX;
+            y0 = ty * kTY;
+            zBase = g.z0 + sz * tg.segLen * kTZ;
+            nSeg = min(tg.segLen, tg.tilesZ - sz * tg.segLen);
+        }
+        const int x = x0 + lx, y = y0 + ly;
+        int seed = -1;
+        const uint32_t colsPerSlab = uint32_t(tg.tilesX) * uint32_t(tg.tilesY);
+        if (tg.colState && !tg.runs && item >= colsPerSlab)
+            seed = __float_as_int(__ldcg(tg.colState + size_t(item - colsPerSlab) * (2 * kLayer) + kLayer + lane % kLayer));
+        for (int j = 0; j < nSeg; j += 2) {
+            const bool hasB = j + 1 < nSeg;
+            const int za = zBase + j * kTZ + lz, zb = za + kTZ;
+            const bool inXY = x < g.nx && y < g.ny;
+            const bool activeA = inXY && za < g.z1, activeB = inXY && hasB && zb < g.z1;
+            const float3 qa = xfPoint(xf, x, y, za), qb = xfPoint(xf, x, y, zb);
+            float ra = o.maxDistSq, rb = o.maxDistSq;
+            int ba = -1, bb = -1;
+            bool fa = false, fb = false;
+            if (seed >= 0 && (activeA || activeB)) {
+                bool da = false, db = false;
+                leafDist2<PRECISE>(t, seed, qa, qb, activeA, activeB, ra, rb, ba, bb, da, db, fa, fb);
+            }
+            cpPacket2<PRECISE>(t, qa, qb, activeA, activeB, ra, rb, ba, bb, fa, fb, scratch + 1);
+            if (PRECISE) {
+                const unsigned ma = __ballot_sync(FULL, fa), mb = __ballot_sync(FULL, fb);
+                if ((ma | mb) && lane == 0) {  // re-walked with the precise distances by fixPairKernel
+                    const uint32_t k = atomicAdd(&tg.fixList[0].x, 1u);
+                    if (k < tg.fixCap) tg.fixList[1 + k] = make_uint4(item, uint32_t(j), ma, mb);
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const bool active = h ? activeB : activeA;
+                const int z = h ? zb : za;
+                const float dsq = h ? rb : ra;
+                const bool valid = !(o.nullOutsideMinMax && dsq >= o.maxDistSq);
+                const uint32_t word = active ? __ldg(tg.signBits + (size_t(z - g.zOut) * g.ny + y) * wordsX + (x >> 5)) : 0u;
+                const bool inside = (word >> (x & 31)) & 1u;
+                const float d = __fsqrt_rn(dsq);
+                if (active) out[size_t(z - g.zOut) * sxy + size_t(y) * g.nx + x] = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
+            }
+            // next pair: the bottom layer's lanes continue from the voxel one layer below them, the
+            // others from their own last voxel (as gridKernel)
+            const int src = lane + (kTZ - 1) * kTX * kTY * (lz == 0);
+            seed = __shfl_sync(FULL, hasB ? bb : ba, src);
+            if (tg.colState && !tg.runs && j + 2 >= nSeg && lz == kTZ - 1) {
+                // the column's last tile: its top layer passes its closest triangles to the column above
+                const uint32_t sz = uint32_t(zBase - g.z0) / uint32_t(tg.segLen * kTZ);
+                const uint32_t it = uint32_t(x0) / kTX + uint32_t(tg.tilesX) * (uint32_t(y0) / kTY + uint32_t(tg.tilesY) * sz);
+                float* cs = tg.colState + size_t(it) * (2 * kLayer) + (lane - (kTZ - 1) * kLayer);
+                cs[0] = __int_as_float(0x7fc00000);
+                cs[kLayer] = __int_as_float(seed);
+            }
+        }
+    }
+}
+
+// The listed pair steps of a precise gridPairKernel launch: each flagged voxel's closest distance by
+// the precise walk (cpPacket, from maxDistSq), written with its sign bit.  Voxels never listed kept
+// FP32 distances no triangle came near the FP64 re-evaluation for: the precise walk's own.  A list
+// that overflowed (more flagged steps than a launch has) cannot happen: one entry per step at most.
+__global__ void __launch_bounds__(kThreads) fixPairKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, DistOpts o,
+                                                          float* __restrict__ out, unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
+    const size_t sxy = size_t(g.nx) * g.ny;
+    const int wordsX = (g.nx + 31) >> 5;
+    const uint32_t n = min(__ldcg(&tg.fixList[0].x), tg.fixCap);
+    for (;;) {
+        const unsigned e = nextTicket(scratch, lane);
+        if (e >= n) break;
+        const uint4 f = tg.fixList[1 + e];
+        const unsigned item = f.x;
+        int x0, y0, zBase;
+        if (tg.runs) {
+            const int4 r = tg.runs[item / kBrickCols];
+            const int col = int(item % kBrickCols);
+            x0 = r.x * 8 + (col % kBrickColsX) * kTX;
+            y0 = r.y * 8 + (col / kBrickColsX) * kTY;
+            zBase = g.z0 + r.z * 8;
+        } else {
+            const unsigned rest = item / unsigned(tg.tilesX);
+            x0 = int(item % unsigned(tg.tilesX)) * kTX;
+            y0 = int(rest % unsigned(tg.tilesY)) * kTY;
+            zBase = g.z0 + int(rest / unsigned(tg.tilesY)) * tg.segLen * kTZ;
+        }
+        const int x = x0 + lx, y = y0 + ly;
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            const bool need = ((h ? f.w : f.z) >> lane) & 1u;
+            if (!__any_sync(FULL, need)) continue;
+            const int z = zBase + (int(f.y) + h) * kTZ + lz;
+            const float3 q = xfPoint(xf, x, y, z);
+            const float dsq = cpPacket<true>(t, q, need, o.maxDistSq, 0.f, scratch + 1);
+            if (need) {
+                const bool valid = !(o.nullOutsideMinMax && dsq >= o.maxDistSq);
+                const uint32_t word = __ldg(tg.signBits + (size_t(z - g.zOut) * g.ny + y) * wordsX + (x >> 5));
+                const float d = __fsqrt_rn(dsq);
+                out[size_t(z - g.zOut) * sxy + size_t(y) * g.nx + x] =
+                    valid ? (((word >> (x & 31)) & 1u) ? -d : d) : __int_as_float(0x7fc00000);
+            }
+        }
+    }
+}
+
 // A warp takes `chunk` consecutive tiles of 32 points; with Morton-ordered points a lane's point in
 // one tile is near its point in the previous one, so (as in gridKernel) each lane starts its
 // closest-point search from the triangle closest to its previous point.
@@ -1259,9 +1490,7 @@ __global__ void __launch_bounds__(kThreads, kDistBlocks) projectKernel(QueryTree
                 const float4* tr = t.tri + 3 * int64_t(seed);
                 float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
                 if (TREEXF) {
-                    A = xf4(&txf, A);
-                    B = xf4(&txf, B);
-                    C = xf4(&txf, C);
+                    xfTri(&txf, A, B, C);
                 }
                 const float ds = triDistSq<PRECISE>(q, A, B, C);
                 if (ds < upS) {
@@ -1278,9 +1507,7 @@ __global__ void __launch_bounds__(kThreads, kDistBlocks) projectKernel(QueryTree
                 const float4* tr = t.tri + 3 * int64_t(best);
                 float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
                 if (TREEXF) {
-                    A = xf4(&txf, A);
-                    B = xf4(&txf, B);
-                    C = xf4(&txf, C);
+                    xfTri(&txf, A, B, C);
                 }
                 float3 pr;
                 float ba, bb;
@@ -1404,6 +1631,8 @@ static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
     tg.runs = nullptr;
     tg.colState = nullptr;
     tg.signBits = nullptr;
+    tg.fixList = nullptr;
+    tg.fixCap = 0;
     // Longer columns reuse more seeds; shorter ones leave more items for the tail of the persistent
     // grid.  Measured at 256^3 / 512^3 on 1.3 M triangles: keep >= 25 items per (32-warps-per-SM)
     // resident warp, and columns of at most 32 tiles for unbanded signed distances (512^3: 16 tiles
@@ -1418,18 +1647,41 @@ static TileGrid tileGridFor(const GridRange& g, int maxSegLen = 16) {
     return tg;
 }
 
+// Entries of the precise paired walk's fix list (after its counter): one per pair step at most.
+static uint32_t pairFixCap(const TileGrid& tg) { return tg.numTiles / 2 + tg.numItems + 1; }
+
+size_t pairFixBytes(uint32_t nTiles, uint32_t nItems) { return size_t(nTiles / 2 + nItems + 2) * sizeof(uint4); }
+size_t pairFixBytesForRuns(int32_t nRuns, int32_t nBricks) {
+    return pairFixBytes(uint32_t(nBricks) * 16u, uint32_t(nRuns) * uint32_t(kBrickCols));
+}
+
+// The signed distances of a grid (or of brick runs) with the column bits: the paired walk when there
+// is no lower distance bound (in precise mode with its fix list, when given, and the fix-up pass),
+// else the one-voxel walk.
+static cudaError_t launchWithBits(const QueryTree& t, const GridRange& g, TileGrid tg, const Xf& xf, const DistOpts& o, int precise,
+                                  float* out, uint4* fix, unsigned* scratch, cudaStream_t s) {
+    if (o.minDistSq <= 0.f && (!precise || fix)) {
+        if (!precise) return launchPersistent(gridPairKernel<false>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+        tg.fixList = fix;
+        tg.fixCap = pairFixCap(tg);
+        cudaError_t e = cudaMemsetAsync(fix, 0, sizeof(uint4), s);
+        if (e || (e = launchPersistent(gridPairKernel<true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch))) return e;
+        return launchPersistent(fixPairKernel, tg.fixCap, scratch, s, t, g, tg, xf, o, out, scratch);
+    }
+    if (precise) return launchPersistent(gridKernel<true, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+    return launchPersistent(gridKernel<false, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+}
+
 cudaError_t launchGridSdfBricks(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                                 float* out, const int4* runs, int32_t nRuns, int32_t nBricks, const uint32_t* signBits,
-                                unsigned* scratch, cudaStream_t s) {
+                                void* fix, unsigned* scratch, cudaStream_t s) {
     TileGrid tg = tileGridFor(g);
     tg.runs = runs;
     tg.numTiles = uint32_t(nBricks) * 16u;
     tg.numItems = uint32_t(nRuns) * uint32_t(kBrickCols);
     if (signBits) {
         tg.signBits = signBits;
-        if (precise)
-            return launchPersistent(gridKernel<true, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
-        return launchPersistent(gridKernel<false, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+        return launchWithBits(t, g, tg, xf, o, precise, out, static_cast<uint4*>(fix), scratch, s);
     }
     if (precise)
         return launchPersistent(gridKernel<true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
@@ -1499,9 +1751,13 @@ size_t signBitsBytes(const GridRange& g) {
 }
 
 size_t gridSdfColumnStateBytes(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o) {
-    const size_t col = size_t(tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16).numItems) * (2 * kLayer) * sizeof(float);
-    return col + (signColumnsApply(t, xf, o.beta, o.threshold) ? ((signBitsBytes(g) + 255) & ~size_t(255)) + signColumnsWorkBytes(g) : 0);
+    const TileGrid tg = tileGridFor(g, o.maxDistSq >= FLT_MAX ? 32 : 16);
+    const size_t col = size_t(tg.numItems) * (2 * kLayer) * sizeof(float);
+    if (!signColumnsApply(t, xf, o.beta, o.threshold)) return col;
+    return col + ((signBitsBytes(g) + 255) & ~size_t(255)) + signColumnsWorkBytes(g) +
+           (o.minDistSq <= 0.f ? pairFixBytes(tg.numTiles, tg.numItems) : 0);
 }
+
 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise, float* out,
                           unsigned* scratch, cudaStream_t s, float* colState, size_t colBytes) {
@@ -1521,9 +1777,11 @@ cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, 
                                        scratch, s)))
                 return e;
             tg.signBits = bits;
-            if (precise)
-                return launchPersistent(gridKernel<true, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
-            return launchPersistent(gridKernel<false, true, true>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);
+            const size_t fixAt = lists + signColumnsWorkBytes(g);
+            uint4* fix = (work && colBytes >= fixAt + pairFixBytes(tg.numTiles, tg.numItems))
+                             ? reinterpret_cast<uint4*>(base + fixAt)
+                             : nullptr;
+            return launchWithBits(t, g, tg, xf, o, precise, out, fix, scratch, s);
         }
     }
     if (precise)
