@@ -368,3 +368,29 @@ def test_column_signs_on_mirrored_grids(M):
         _same(*res)
         mirrored = res[0].reshape(dims[2], dims[1], dims[0])
         assert np.array_equal(np.signbit(np.flip(mirrored, axis=flip)), np.signbit(plain))
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_paired_walk_with_voxels_on_the_surface(M, precise):
+    """The paired walk (grids large enough for work items of several tiles) on a cube whose faces
+    hold 256^2-voxel layers and on the noisy sphere: voxels on the surface make the precise walk list
+    their pair steps for the fix-up pass; the grids equal the one-voxel walk's with the winding-number
+    signs, bit for bit, unbanded and banded."""
+    cube_v = np.array([[x, y, z] for z in (0, 1) for y in (0, 1) for x in (0, 1)], np.float32) * np.float32(1.5) + np.float32(0.5)
+    cube_f = np.array([[0, 2, 3], [0, 3, 1], [4, 5, 7], [4, 7, 6], [0, 1, 5], [0, 5, 4], [2, 6, 7], [2, 7, 3], [0, 4, 6],
+                       [0, 6, 2], [1, 3, 7], [1, 7, 5]], np.int32)
+    xf = np.zeros(12, np.float32)
+    xf[0] = xf[4] = xf[8] = 0.0125  # voxel centres at multiples of 1/80: the faces at 40 and 160
+    dims = (208, 208, 416)
+    v, f = mg.noisy_icosphere(seed=6, level=6)
+    dims2, xf2 = mg.grid_for(v, 256)
+    for cv, cf, d, x in ((cube_v, cube_f, dims, xf), (v, f, dims2, xf2)):
+        g = M.FastWindingNumber(cv, cf, precise=precise)
+        for opts in (None, M.DistanceToMeshOptions(maxDistSq=(0.02 * mg.diag(cv)) ** 2)):
+            res = []
+            for enable in (True, False):
+                g.set_sign_reuse(enable)
+                res.append(g.calcFromGridWithDistances(d, x, opts))
+            g.set_sign_reuse(True)
+            _same(*res)
+            assert (res[0] == 0).any() or cf is f
