@@ -448,18 +448,21 @@ __device__ float cpPacket(const QueryTree& t, const float3& q, bool active, floa
     return resSq;
 }
 
+// Per warp of a paired walk, the lanes whose lower / upper query came within a triangle's near-plane
+// level (kept in shared memory: set rarely, and no register carries them through the walk).
+__shared__ uint32_t sPairFix[8][2];
+
 // One leaf triangle for the two queries of a lane (loaded once), in FP32; FLAG: a query that comes
 // within the triangle's near-plane level (where the precise distance would be re-evaluated in FP64)
-// sets its flag, and the caller evaluates that query again with the precise walk.
+// sets its lane's bit in sPairFix, and the caller evaluates that query again with the precise walk.
 template <bool FLAG>
 __device__ __forceinline__ void leafDist2(const QueryTree& t, int slot, const float3& qa, const float3& qb, bool goA, bool goB,
-                                          float& resA, float& resB, int& bestA, int& bestB, bool& doneA, bool& doneB,
-                                          bool& flagA, bool& flagB) {
+                                          float& resA, float& resB, int& bestA, int& bestB, bool& doneA, bool& doneB) {
     const float4* tr = t.tri + 3 * int64_t(slot);
     const float4 A = ld4(tr), B = ld4(tr + 1), C = ld4(tr + 2);
     if (goA) {
         const float ds = triDistSq<false>(qa, A, B, C);
-        if (FLAG && ds < C.w) flagA = true;
+        if (FLAG && ds < C.w) atomicOr(&sPairFix[threadIdx.x >> 5][0], 1u << (threadIdx.x & 31));
         if (ds < resA) {
             resA = ds;
             bestA = slot;
@@ -468,7 +471,7 @@ __device__ __forceinline__ void leafDist2(const QueryTree& t, int slot, const fl
     }
     if (goB) {
         const float ds = triDistSq<false>(qb, A, B, C);
-        if (FLAG && ds < C.w) flagB = true;
+        if (FLAG && ds < C.w) atomicOr(&sPairFix[threadIdx.x >> 5][1], 1u << (threadIdx.x & 31));
         if (ds < resB) {
             resB = ds;
             bestB = slot;
@@ -483,7 +486,7 @@ __device__ __forceinline__ void leafDist2(const QueryTree& t, int slot, const fl
 // triangle distances; FLAG as leafDist2.
 template <bool FLAG>
 __device__ void cpPacket2(const QueryTree& t, const float3& qa, const float3& qb, bool activeA, bool activeB, float& resA,
-                          float& resB, int& bestA, int& bestB, bool& flagA, bool& flagB, unsigned* status) {
+                          float& resB, int& bestA, int& bestB, unsigned* status) {
     const int lane = threadIdx.x & 31;
     if (t.nLeaves == 0) return;
     const bool inA = activeA && boxDistSq(t.rootBox0, t.rootBox1, qa) < resA;
@@ -493,7 +496,7 @@ __device__ void cpPacket2(const QueryTree& t, const float3& qa, const float3& qb
     const int rootLink = __float_as_int(t.rootBox0.w);
     bool doneA = !activeA, doneB = !activeB;
     if (rootLink < 0) {
-        leafDist2<FLAG>(t, ~rootLink, qa, qb, inA, inB, resA, resB, bestA, bestB, doneA, doneB, flagA, flagB);
+        leafDist2<FLAG>(t, ~rootLink, qa, qb, inA, inB, resA, resB, bestA, bestB, doneA, doneB);
         return;
     }
     WarpStack st;
@@ -523,10 +526,10 @@ __device__ void cpPacket2(const QueryTree& t, const float3& qa, const float3& qb
         const bool farA = leftFirst ? gra : gla, farB = leftFirst ? grb : glb;
         const float farDA = leftFirst ? dra : dla, farDB = leftFirst ? drb : dlb;
         if (nearM && nearLink < 0)
-            leafDist2<FLAG>(t, ~nearLink, qa, qb, nearA, nearB, resA, resB, bestA, bestB, doneA, doneB, flagA, flagB);
+            leafDist2<FLAG>(t, ~nearLink, qa, qb, nearA, nearB, resA, resB, bestA, bestB, doneA, doneB);
         if (farM && farLink < 0)
             leafDist2<FLAG>(t, ~farLink, qa, qb, farA && !doneA && farDA < resA, farB && !doneB && farDB < resB, resA, resB, bestA,
-                            bestB, doneA, doneB, flagA, flagB);
+                            bestB, doneA, doneB);
         if (farM && farLink >= 0 && !st.push(lane, farLink, farM)) overflow = true;
         if (nearM && nearLink >= 0 && !st.push(lane, nearLink, nearM)) overflow = true;
         if (overflow) break;
@@ -536,6 +539,7 @@ __device__ void cpPacket2(const QueryTree& t, const float3& qa, const float3& qb
 
 // ------------------------------------------------------------------ kernels
 constexpr int kThreads = 256;
+static_assert(kThreads / 32 == sizeof(sPairFix) / sizeof(sPairFix[0]), "one sPairFix row per warp");
 // Resident blocks per SM of the kernels that run the closest-point walk (48 registers, a few values
 // spilled): more warps hide the dependent record loads better than registers help, up to the point
 // where spills take over.  Measured at 512^3 on 1.31 M triangles with the 128-byte two-frame records:
@@ -1266,14 +1270,18 @@ __global__ void __launch_bounds__(kThreads, kPairBlocks) gridPairKernel(QueryTre
             const float3 qa = xfPoint(xf, x, y, za), qb = xfPoint(xf, x, y, zb);
             float ra = o.maxDistSq, rb = o.maxDistSq;
             int ba = -1, bb = -1;
-            bool fa = false, fb = false;
+            if (PRECISE) {
+                if (lane == 0) sPairFix[threadIdx.x >> 5][0] = sPairFix[threadIdx.x >> 5][1] = 0u;
+                __syncwarp();
+            }
             if (seed >= 0 && (activeA || activeB)) {
                 bool da = false, db = false;
-                leafDist2<PRECISE>(t, seed, qa, qb, activeA, activeB, ra, rb, ba, bb, da, db, fa, fb);
+                leafDist2<PRECISE>(t, seed, qa, qb, activeA, activeB, ra, rb, ba, bb, da, db);
             }
-            cpPacket2<PRECISE>(t, qa, qb, activeA, activeB, ra, rb, ba, bb, fa, fb, scratch + 1);
+            cpPacket2<PRECISE>(t, qa, qb, activeA, activeB, ra, rb, ba, bb, scratch + 1);
             if (PRECISE) {
-                const unsigned ma = __ballot_sync(FULL, fa), mb = __ballot_sync(FULL, fb);
+                __syncwarp();
+                const unsigned ma = sPairFix[threadIdx.x >> 5][0], mb = sPairFix[threadIdx.x >> 5][1];
                 if ((ma | mb) && lane == 0) {  // re-walked with the precise distances by fixPairKernel
                     const uint32_t k = atomicAdd(&tg.fixList[0].x, 1u);
                     if (k < tg.fixCap) tg.fixList[1 + k] = make_uint4(item, uint32_t(j), ma, mb);
