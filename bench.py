@@ -159,19 +159,19 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 
 
 # DRAM bytes (read + write) of one launch of the signed-distance grid kernel at 512^3 on this
-# workload: dram__bytes_read.sum 441,793,024 + dram__bytes_write.sum 591,700,992 from one ncu
+# workload: dram__bytes_read.sum 567,815,168 + dram__bytes_write.sum 640,902,400 from one ncu
 # capture of the same kernel (a constant copied from that capture, not measured by this run; the
 # committed profile summary under profiles/ gives the command).  536,870,912 of the written bytes
 # are the output grid.
-KERNEL_DRAM_BYTES_512 = 441_793_024 + 591_700_992
+KERNEL_DRAM_BYTES_512 = 567_815_168 + 640_902_400
 
 
 # Counters of the signed-distance grid kernel at 256^3 on this workload from one ncu capture
 # (constants copied from that capture, not measured by this run): FMA-pipe utilisation
 # (sm__pipe_fma_cycles_active), issue-slot utilisation and active lanes per warp instruction.
-KERNEL_FMA_PIPE_ACTIVE = 0.328
-KERNEL_ISSUE_ACTIVE = 0.880
-KERNEL_LANES_PER_INSTR = 24.55
+KERNEL_FMA_PIPE_ACTIVE = 0.362
+KERNEL_ISSUE_ACTIVE = 0.878
+KERNEL_LANES_PER_INSTR = 25.09
 
 
 def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
@@ -721,9 +721,10 @@ def main():
                        "l2": "flushed between steps (512 MB write)",
                        "parallelism": f"z-slabs x{world} (one grid split by layers, mesh replicated, no collective)"},
             "replicas": replicas,
-            # per timed step: the column-ray sign pass (closed mesh, vertical z axis) and gridKernel (their
-            # ticket-counter resets and the hand-over fill are memsets)
-            "gpu_launches": args.steps * (2 if fwn.is_closed() else 1),
+            # per timed step: the column sign pass (crossing lists, column sweep: closed mesh, vertical z
+            # axis), the paired grid walk and its precise re-walk of the listed voxels (the ticket-counter
+            # resets, the hand-over fill and the list counters are memsets)
+            "gpu_launches": args.steps * (4 if fwn.is_closed() else 1),
             "e2e": {"value": e2e_val, "unit": "voxels/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                     "d2h_bytes_per_step": int(slab_vox * 4), "s_per_step": e2e_s,
                     "s_create_per_step": float(np.mean(create_times)) if create_times else None},
@@ -748,8 +749,9 @@ def main():
                                     "The bound that holds is instruction issue: dram_frac_actual (measured DRAM bytes "
                                     "per launch / step time / peak) is well under 1 %, issue_active_ncu is the busy "
                                     "fraction of the issue slots (ncu, 256^3 capture)",
-                            "duration": "the timed step's CUDA-event time: the grid kernel and, before it, the column sign "
-                                        "pass (crossing lists + column sweep, 0.33 ms of the step in the ncu launch list)"}
+                            "duration": "the timed step's CUDA-event time: the grid kernel (the paired walk, 65.2 ms of the "
+                                        "step in the ncu launch list) and, before it, the column sign pass (crossing lists + "
+                                        "column sweep, 0.33 ms) and after it the precise re-walk of the listed voxels (0.1 ms)"}
         try:
             fp32_peak = fp32_peak_tflops(local)
         except Exception as ex:  # measurement support only; the line stays valid without it
@@ -763,7 +765,7 @@ def main():
                         "fma_pipe_active_ncu": KERNEL_FMA_PIPE_ACTIVE,
                         "note": "reference-equivalent FLOP/s counts the reference traversal's box tests, projections, "
                                 "dipoles and solid angles per voxel; the packet traversal does far fewer, and ncu shows the "
-                                "FMA pipe 33% busy: the kernel is bound by instruction issue and dependent loads"}
+                                "FMA pipe 36% busy: the kernel is bound by instruction issue and dependent loads"}
         line["cpu_baseline"] = cpu_baseline_fields(rate, thr, desc)
         line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d, extra=prec_extra, M=M, device=local)
     if rank == 0:
