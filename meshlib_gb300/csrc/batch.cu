@@ -19,6 +19,8 @@ struct gbfwn_batch_s {
     BatchItem* dItems[kBatchConfigs] = {};
     uint32_t totalTiles[kBatchConfigs] = {};
     unsigned* scratch = nullptr;  // ticket counter + status word of this batch
+    bool pairOk = true;           // no item with a lower distance bound: the paired variants apply
+    void* fix = nullptr;          // the precise paired walk's list (counter + entries)
     cudaStream_t captureStream = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graphConfig = -1;
@@ -33,6 +35,7 @@ struct gbfwn_batch_s {
         for (auto* p : dItems)
             if (p) cudaFree(p);
         if (scratch) cudaFree(scratch);
+        if (fix) cudaFree(fix);
     }
 };
 
@@ -80,6 +83,7 @@ GBFWN_API int gbfwn_batch_create(const gbfwn_batch_item* items, int32_t n, gbfwn
             bi.o = DistOpts{it.opts.minDistSq, it.opts.maxDistSq, it.opts.nullOutsideMinMax, it.opts.windingNumberThreshold,
                             it.opts.windingNumberBeta};
             bi.out = it.d_out;
+            if (it.opts.minDistSq > 0.f) b->pairOk = false;
             bi.tileBase = uint32_t(base);
             base += batchTiles(c, it.dims[0], it.dims[1], it.dims[2]);
         }
@@ -92,6 +96,9 @@ GBFWN_API int gbfwn_batch_create(const gbfwn_batch_item* items, int32_t n, gbfwn
         if (!e) e = cudaMemcpy(b->dItems[c], h.data(), sizeof(BatchItem) * size_t(n), cudaMemcpyHostToDevice);
     }
     if (!e) e = devMalloc((void**)&b->scratch, 64);
+    uint32_t maxTiles = 0;
+    for (int c = 0; c < kBatchConfigs; ++c) maxTiles = std::max(maxTiles, b->totalTiles[c]);
+    if (!e && b->precise && b->pairOk) e = devMalloc(&b->fix, sizeof(uint4) * (size_t(batchFixCap(maxTiles)) + 1));
     if (!e) e = cudaMemset(b->scratch, 0, 64);
     if (!e) e = cudaStreamCreateWithFlags(&b->captureStream, cudaStreamNonBlocking);
     if (e) {
@@ -121,7 +128,7 @@ GBFWN_API int gbfwn_batch_run_dev(gbfwn_batch b, void* stream) {
     if (!b) return fail(GBFWN_INVALID, "gbfwn_batch_run_dev: null batch");
     DeviceGuard g(b->device);
     const cudaError_t e = launchBatchSdf(b->dItems[b->config], b->nItems, b->totalTiles[b->config], b->precise, b->config,
-                                         b->scratch, static_cast<cudaStream_t>(stream));
+                                         b->pairOk, b->fix, b->scratch, static_cast<cudaStream_t>(stream));
     return e ? cudaFail(e, "gbfwn_batch_run_dev") : GBFWN_OK;
 }
 
@@ -136,7 +143,7 @@ GBFWN_API int gbfwn_batch_graph_launch(gbfwn_batch b, void* stream) {
         e = cudaStreamBeginCapture(b->captureStream, cudaStreamCaptureModeThreadLocal);
         if (!e) {
             const cudaError_t le = launchBatchSdf(b->dItems[b->config], b->nItems, b->totalTiles[b->config], b->precise,
-                                                  b->config, b->scratch, b->captureStream);
+                                                  b->config, b->pairOk, b->fix, b->scratch, b->captureStream);
             e = cudaStreamEndCapture(b->captureStream, &graph);
             if (!e) e = le;
         }
@@ -163,7 +170,7 @@ GBFWN_API int gbfwn_batch_autotune(gbfwn_batch b, int32_t* best, float* times_ms
         float ms = FLT_MAX;
         for (int rep = 0; rep < 3 && !e; ++rep) {  // first repetition warms caches and loads the kernel
             cudaEventRecord(e0, s);
-            e = launchBatchSdf(b->dItems[c], b->nItems, b->totalTiles[c], b->precise, c, b->scratch, s);
+            e = launchBatchSdf(b->dItems[c], b->nItems, b->totalTiles[c], b->precise, c, b->pairOk, b->fix, b->scratch, s);
             cudaEventRecord(e1, s);
             if (!e) e = cudaEventSynchronize(e1);
             float t = 0.f;

@@ -117,15 +117,19 @@ struct BatchItem {
     float* out;
     uint32_t tileBase;
 };
-constexpr int kBatchConfigs = 6;  // tile shape x block size variants
+constexpr int kBatchShapes = 6;                  // tile shape x block size variants
+constexpr int kBatchConfigs = 2 * kBatchShapes;  // each with the one-voxel walk, then with the paired walk
 // tiles along z per work item (a column walked by one warp).  64-mesh batch, best configuration, the
 // same outputs: 4 tiles 54.9 ms, 8 54.4, 16 52.9, 24 52.4, 32 52.1 (sign reuse makes long columns pay;
 // 16 leaves more items for the load balance of batches of small grids)
 constexpr int kBatchSeg = 16;
 const char* batchConfigName(int config);
 uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz);
-cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,
-                           cudaStream_t s);
+// pairOk: every item has minDistSq = 0 (the paired variants need it); fix: the precise paired walk's
+// list, batchFixCap(totalTiles) entries after a 16-byte counter.
+uint32_t batchFixCap(uint32_t totalTiles);
+cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, bool pairOk,
+                           void* fix, unsigned* scratch, cudaStream_t s);
 
 // Signed distance on runs of 8x8x8-voxel bricks of the grid: runs[i] = (bx, by, bz0, count), the
 // `count` bricks (bx, by, bz0 .. bz0 + count - 1), nBricks in all; voxels outside them are not written.

@@ -483,11 +483,12 @@ __device__ __forceinline__ void leafDist2(const QueryTree& t, int slot, const fl
 // Two queries per lane in one packet walk (voxels qa and qb of the lane): a node is opened when either
 // query of any lane may hold a closer triangle, each query keeps its own bound and prunes its own
 // leaves, so each result is its exact minimum, as with cpPacket (no early stop: loSq = 0).  FP32
-// triangle distances; FLAG as leafDist2.  qb must lie straight above qa (same x and y).
+// triangle distances; FLAG as leafDist2.  vertical: qb lies straight above qa (same x and y), and its
+// frame coordinates follow from qa's.
 template <bool FLAG>
 __device__ void cpPacket2(const QueryTree& t, const float3& qa, const float3& qb, bool activeA, bool activeB, float& resA,
-                          float& resB, int& bestA, int& bestB, unsigned* status) {
-    const float dzB = qb.z - qa.z;  // qb = qa + (0, 0, dzB): the same x and y (a vertical grid column)
+                          float& resB, int& bestA, int& bestB, unsigned* status, bool vertical = true) {
+    const float dzB = qb.z - qa.z;  // vertical: qb = qa + (0, 0, dzB), the same x and y (a vertical grid column)
     const int lane = threadIdx.x & 31;
     if (t.nLeaves == 0) return;
     const bool inA = activeA && boxDistSq(t.rootBox0, t.rootBox1, qa) < resA;
@@ -513,7 +514,8 @@ __device__ void cpPacket2(const QueryTree& t, const float3& qa, const float3& qb
         // from qa's by the frame's z column: three FMAs instead of nine (the boxes' rounding margin,
         // 2e-6 of the coordinates, covers the few ulps this differs from projecting qb itself)
         const float3 xa = toFrame(rec, qa);
-        const float3 xb = make_float3(fmaf(dzB, rec.t.z, xa.x), fmaf(dzB, rec.u.z, xa.y), fmaf(dzB, rec.n.z, xa.z));
+        const float3 xb = vertical ? make_float3(fmaf(dzB, rec.t.z, xa.x), fmaf(dzB, rec.u.z, xa.y), fmaf(dzB, rec.n.z, xa.z))
+                                   : toFrame(rec, qb);
         float dla = frameBoxDistSq(xa, rec.cl, rec.el), dra = frameBoxDistSq(xa, rec.cr, rec.er);
         float dlb = frameBoxDistSq(xb, rec.cl, rec.el), drb = frameBoxDistSq(xb, rec.cr, rec.er);
         const bool gla = mine && !doneA && dla < resA, gra = mine && !doneA && dra < resA;
@@ -1955,6 +1957,147 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchKernel(const Bat
     }
 }
 
+// The item of a ticket of a batched launch (binary search over the items' first tickets).
+__device__ __forceinline__ int batchItemOf(const BatchItem* __restrict__ items, int nItems, unsigned ticket) {
+    int lo = 0, hi = nItems - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (items[mid].tileBase <= ticket) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// batchKernel with the paired walk (gridPairKernel's): the column of a ticket two tiles at a time,
+// each lane taking its voxel of the lower tile and the one TZ layers above through one packet walk
+// (cpPacket2), then the lower voxel's sign and the upper one's from it (the voxel below each, as in
+// batchKernel: sign reuse, rays, the winding-number walk).  Only for batches without a lower
+// distance bound (minDistSq = 0 in every item).  In precise mode the walk runs in FP32 and the pair
+// steps whose voxels came within a triangle's near-plane level are listed ({ticket, first tile, lane
+// masks}) for fixBatchKernel.
+template <bool PRECISE, int TX, int TY, int TZ, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) batchPairKernel(const BatchItem* __restrict__ items, int nItems,
+                                                                           uint32_t totalTiles, uint4* fix, uint32_t fixCap,
+                                                                           unsigned* scratch) {
+    static_assert(TX * TY * TZ == 32, "one voxel per lane");
+    static_assert(THREADS / 32 <= 8, "one sPairFix row per warp");
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / (TX * TY);
+    for (;;) {
+        const unsigned ticket = nextTicket(scratch, lane);
+        if (ticket >= totalTiles) break;
+        const int lo = batchItemOf(items, nItems, ticket);
+        __shared__ BatchItem sItem[THREADS / 32];
+        BatchItem& it = sItem[threadIdx.x >> 5];
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(items + lo);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&it);
+            __syncwarp();
+            for (int k = lane; k < int(sizeof(BatchItem) / 4); k += 32) dst[k] = src[k];
+            __syncwarp();
+        }
+        const unsigned local = ticket - it.tileBase;
+        const int tilesX = (it.g.nx + TX - 1) / TX, tilesY = (it.g.ny + TY - 1) / TY;
+        const int tx = int(local % unsigned(tilesX));
+        const unsigned rest = local / unsigned(tilesX);
+        const int ty = int(rest % unsigned(tilesY)), seg = int(rest / unsigned(tilesY));
+        const int x = tx * TX + lx, y = ty * TY + ly;
+        const QueryTree& t = it.t;
+        const DistOpts o = it.o;
+        const bool reuseOk = signReuseAllowed(t, o);
+        const bool vertical = it.xf.a[2] == 0.f && it.xf.a[5] == 0.f;
+        const float betaSq = __fmul_rn(o.beta, o.beta);
+        int seed = -1;
+        float below = __int_as_float(0x7fc00000);
+        for (int j = 0; j < kBatchSeg; j += 2) {
+            const int zA0 = (seg * kBatchSeg + j) * TZ;
+            if (zA0 >= it.g.nz) break;
+            const bool hasB = j + 1 < kBatchSeg && zA0 + TZ < it.g.nz;
+            const int za = zA0 + lz, zb = za + TZ;
+            const bool inXY = x < it.g.nx && y < it.g.ny;
+            const bool activeA = inXY && za < it.g.nz, activeB = inXY && hasB && zb < it.g.nz;
+            const float3 qa = xfPoint(it.xf, x, y, za), qb = xfPoint(it.xf, x, y, zb);
+            float ra = o.maxDistSq, rb = o.maxDistSq;
+            int ba = -1, bb = -1;
+            if (PRECISE) {
+                if (lane == 0) sPairFix[threadIdx.x >> 5][0] = sPairFix[threadIdx.x >> 5][1] = 0u;
+                __syncwarp();
+            }
+            if (seed >= 0 && (activeA || activeB)) {
+                bool da = false, db = false;
+                leafDist2<PRECISE>(t, seed, qa, qb, activeA, activeB, ra, rb, ba, bb, da, db);
+            }
+            cpPacket2<PRECISE>(t, qa, qb, activeA, activeB, ra, rb, ba, bb, scratch + 1, vertical);
+            if (PRECISE) {
+                __syncwarp();
+                const unsigned ma = sPairFix[threadIdx.x >> 5][0], mb = sPairFix[threadIdx.x >> 5][1];
+                if ((ma | mb) && lane == 0) {
+                    const uint32_t k = atomicAdd(&fix[0].x, 1u);
+                    if (k < fixCap) fix[1 + k] = make_uint4(ticket, uint32_t(j), ma, mb);
+                }
+            }
+            const int src = lane + (TZ - 1) * TX * TY * (lz == 0);
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {  // the lower voxel's sign, then the upper one's from it
+                const bool active = h ? activeB : activeA;
+                if (h && !__any_sync(FULL, active)) break;
+                const int z = h ? zb : za;
+                const float3& q = h ? qb : qa;
+                const float dsq = h ? rb : ra;
+                const bool valid = !(o.nullOutsideMinMax && (dsq < o.minDistSq || dsq >= o.maxDistSq));
+                const bool complete = active && valid && dsq >= o.minDistSq;
+                bool reIn = false;
+                const bool reuse = reuseOk && reuseSign<TX, TY, TZ>(it.xf, x, y, z, z - (lz == 0 ? 1 : TZ), lz, q, below, complete,
+                                                                    dsq, &reIn);
+                bool onSurface = false;
+                const int cw = reuseOk ? rayWinding(t, q, active && valid && !reuse, scratch + 1, &onSurface) : 0;
+                const bool fwn = reuseOk ? onSurface : (active && valid);
+                const float w = fwnPacket<PRECISE>(t, q, fwn, betaSq, -1, scratch + 1);
+                const bool inside = reuse ? reIn : (fwn ? w > o.threshold : float(cw) > o.threshold);
+                const float d = __fsqrt_rn(dsq);
+                if (active) it.out[(size_t(z) * it.g.ny + y) * it.g.nx + x] = valid ? (inside ? -d : d) : __int_as_float(0x7fc00000);
+                below = __shfl_sync(FULL, complete ? (inside ? -dsq : dsq) : __int_as_float(0x7fc00000), src);
+            }
+            seed = __shfl_sync(FULL, hasB ? bb : ba, src);
+        }
+    }
+}
+
+// The listed pair steps of a precise batchPairKernel launch: each flagged voxel's closest distance by
+// the precise walk, written with the sign its output already holds (decided by the sign pass, which
+// the distance's last bits do not move for a voxel this close to the surface).
+template <int TX, int TY, int TZ>
+__global__ void __launch_bounds__(kThreads) fixBatchKernel(const BatchItem* __restrict__ items, int nItems, uint4* fix,
+                                                           uint32_t fixCap, unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / (TX * TY);
+    const uint32_t n = min(__ldcg(&fix[0].x), fixCap);
+    for (;;) {
+        const unsigned e = nextTicket(scratch, lane);
+        if (e >= n) break;
+        const uint4 f = fix[1 + e];
+        const BatchItem& it = items[batchItemOf(items, nItems, f.x)];
+        const unsigned local = f.x - it.tileBase;
+        const int tilesX = (it.g.nx + TX - 1) / TX, tilesY = (it.g.ny + TY - 1) / TY;
+        const unsigned rest = local / unsigned(tilesX);
+        const int x = int(local % unsigned(tilesX)) * TX + lx, y = int(rest % unsigned(tilesY)) * TY + ly;
+        const int seg = int(rest / unsigned(tilesY));
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            const bool need = ((h ? f.w : f.z) >> lane) & 1u;
+            if (!__any_sync(FULL, need)) continue;
+            const int z = (seg * kBatchSeg + int(f.y) + h) * TZ + lz;
+            const float3 q = xfPoint(it.xf, x, y, z);
+            const float dsq = cpPacket<true>(it.t, q, need, it.o.maxDistSq, 0.f, scratch + 1);
+            if (need) {
+                float* p = it.out + (size_t(z) * it.g.ny + y) * it.g.nx + x;
+                const float old = *p;
+                const bool valid = !(it.o.nullOutsideMinMax && dsq >= it.o.maxDistSq);
+                if (old == old && valid) *p = copysignf(__fsqrt_rn(dsq), old);
+            }
+        }
+    }
+}
+
 template <bool PRECISE, int TX, int TY, int TZ, int THREADS>
 cudaError_t launchBatchT(const BatchItem* items, int nItems, uint32_t totalTiles, unsigned* scratch, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned), s);
@@ -1968,6 +2111,23 @@ cudaError_t launchBatchT(const BatchItem* items, int nItems, uint32_t totalTiles
     if (uint64_t(blocks) > maxBlocks) blocks = int(maxBlocks);
     k<<<blocks, THREADS, 0, s>>>(items, nItems, totalTiles, scratch);
     return cudaGetLastError();
+}
+
+template <bool PRECISE, int TX, int TY, int TZ, int THREADS>
+cudaError_t launchBatchPairT(const BatchItem* items, int nItems, uint32_t totalTiles, uint4* fix, uint32_t fixCap, unsigned* scratch,
+                             cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned), s);
+    if (!e && PRECISE) e = cudaMemsetAsync(fix, 0, sizeof(uint4), s);
+    if (e || totalTiles == 0) return e;
+    auto* k = batchPairKernel<PRECISE, TX, TY, TZ, THREADS>;
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, THREADS, 0);
+    int blocks = numSMs() * (perSm < 1 ? 1 : perSm);
+    const uint64_t maxBlocks = (uint64_t(totalTiles) + THREADS / 32 - 1) / (THREADS / 32);
+    if (uint64_t(blocks) > maxBlocks) blocks = int(maxBlocks);
+    k<<<blocks, THREADS, 0, s>>>(items, nItems, totalTiles, fix, fixCap, scratch);
+    if ((e = cudaGetLastError()) || !PRECISE) return e;
+    return launchPersistent(fixBatchKernel<TX, TY, TZ>, fixCap, scratch, s, items, nItems, fix, fixCap, scratch);
 }
 
 template <bool PRECISE>
@@ -1986,24 +2146,52 @@ cudaError_t launchBatchP(const BatchItem* items, int nItems, uint32_t totalTiles
 
 }  // namespace
 
+template <bool PRECISE>
+cudaError_t launchBatchPairP(const BatchItem* items, int nItems, uint32_t totalTiles, int config, uint4* fix, uint32_t fixCap,
+                             unsigned* scratch, cudaStream_t s) {
+    switch (config) {
+        case 0: return launchBatchPairT<PRECISE, 4, 4, 2, 256>(items, nItems, totalTiles, fix, fixCap, scratch, s);
+        case 1: return launchBatchPairT<PRECISE, 4, 4, 2, 128>(items, nItems, totalTiles, fix, fixCap, scratch, s);
+        case 2: return launchBatchPairT<PRECISE, 8, 4, 1, 256>(items, nItems, totalTiles, fix, fixCap, scratch, s);
+        case 3: return launchBatchPairT<PRECISE, 8, 4, 1, 128>(items, nItems, totalTiles, fix, fixCap, scratch, s);
+        case 4: return launchBatchPairT<PRECISE, 2, 4, 4, 256>(items, nItems, totalTiles, fix, fixCap, scratch, s);
+        case 5: return launchBatchPairT<PRECISE, 2, 4, 4, 128>(items, nItems, totalTiles, fix, fixCap, scratch, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 const char* batchConfigName(int config) {
-    static const char* names[kBatchConfigs] = {"tile 4x4x2, 256 threads", "tile 4x4x2, 128 threads",
-                                               "tile 8x4x1, 256 threads", "tile 8x4x1, 128 threads",
-                                               "tile 2x4x4, 256 threads", "tile 2x4x4, 128 threads"};
+    static const char* names[kBatchConfigs] = {
+        "tile 4x4x2, 256 threads",         "tile 4x4x2, 128 threads",         "tile 8x4x1, 256 threads",
+        "tile 8x4x1, 128 threads",         "tile 2x4x4, 256 threads",         "tile 2x4x4, 128 threads",
+        "tile 4x4x2, 256 threads, paired", "tile 4x4x2, 128 threads, paired", "tile 8x4x1, 256 threads, paired",
+        "tile 8x4x1, 128 threads, paired", "tile 2x4x4, 256 threads, paired", "tile 2x4x4, 128 threads, paired"};
     return (config >= 0 && config < kBatchConfigs) ? names[config] : "";
 }
 
 uint64_t batchTiles(int config, int32_t nx, int32_t ny, int32_t nz) {
-    static const int shape[kBatchConfigs][3] = {{4, 4, 2}, {4, 4, 2}, {8, 4, 1}, {8, 4, 1}, {2, 4, 4}, {2, 4, 4}};
-    const int* t = shape[(config >= 0 && config < kBatchConfigs) ? config : 0];
+    static const int shape[kBatchShapes][3] = {{4, 4, 2}, {4, 4, 2}, {8, 4, 1}, {8, 4, 1}, {2, 4, 4}, {2, 4, 4}};
+    const int* t = shape[(config >= 0 && config < kBatchConfigs) ? config % kBatchShapes : 0];
     const uint64_t tilesZ = uint64_t((nz + t[2] - 1) / t[2]);
     return uint64_t((nx + t[0] - 1) / t[0]) * uint64_t((ny + t[1] - 1) / t[1]) * ((tilesZ + kBatchSeg - 1) / kBatchSeg);
 }
 
-cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, unsigned* scratch,
-                           cudaStream_t s) {
-    if (precise) return launchBatchP<true>(items, nItems, totalTiles, config, scratch, s);
-    return launchBatchP<false>(items, nItems, totalTiles, config, scratch, s);
+uint32_t batchFixCap(uint32_t totalTiles) {  // one entry per pair step at most (kept below 2^31 entries)
+    return uint32_t(std::min<uint64_t>(uint64_t(totalTiles) * (kBatchSeg / 2) + 1, 0x7fffffffull));
+}
+
+cudaError_t launchBatchSdf(const BatchItem* items, int nItems, uint32_t totalTiles, int precise, int config, bool pairOk,
+                           void* fix, unsigned* scratch, cudaStream_t s) {
+    // a paired variant needs every item without a lower distance bound, and in precise mode the fix
+    // list; otherwise it runs as its one-voxel counterpart (the same grids)
+    if (config >= kBatchShapes && pairOk && (!precise || fix)) {
+        uint4* f = static_cast<uint4*>(fix);
+        const uint32_t cap = batchFixCap(totalTiles);
+        if (precise) return launchBatchPairP<true>(items, nItems, totalTiles, config - kBatchShapes, f, cap, scratch, s);
+        return launchBatchPairP<false>(items, nItems, totalTiles, config - kBatchShapes, f, cap, scratch, s);
+    }
+    if (precise) return launchBatchP<true>(items, nItems, totalTiles, config % kBatchShapes, scratch, s);
+    return launchBatchP<false>(items, nItems, totalTiles, config % kBatchShapes, scratch, s);
 }
 
 }  // namespace gbfwn

@@ -1,6 +1,7 @@
 """Batched persistent launch: every grid of an uneven batch equals the single-mesh result (bit for
 bit: each voxel makes the same decisions and sums its terms in the same order whatever warp tile it
-shares), for every tile-shape / block-size variant and through the CUDA-graph replay."""
+shares), for every tile-shape / block-size variant, with the one-voxel and the paired walk, and through
+the CUDA-graph replay."""
 import numpy as np
 import pytest
 
@@ -41,7 +42,7 @@ def test_batch_matches_single_calls(fwn_lib, tmp_path, monkeypatch):
             fin = ~torch.isnan(r)
             assert torch.equal(r[fin], o[fin]), c
     rec = b.autotune()
-    assert rec["cached"] is False and len(rec["times_ms"]) == 6
+    assert rec["cached"] is False and len(rec["times_ms"]) == len(M.Batch.configs()) == 12
     assert M.Batch(items).autotune()["cached"] is True
     for o in outs:
         o.fill_(7.0)
