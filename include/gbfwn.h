@@ -341,8 +341,10 @@ GBFWN_API int gbfwn_from_grid_with_distances_banded_dev(gbfwn_handle h, gbfwn_su
  * Batched signed-distance grids (no counterpart in the reference, which handles one mesh per
  * call): many meshes, each with its own grid, options and device output, computed by ONE
  * persistent kernel fed from a single work queue.  Grids are queued most expensive first (voxels x
- * log2 triangles) so that uneven batches balance.  Six kernel variants (voxel-tile shape x block
- * size) can be timed on the batch and the fastest kept; a batch can be replayed from a CUDA graph. */
+ * log2 triangles) so that uneven batches balance.  Twelve kernel variants (voxel-tile shape x block
+ * size, each with a one-voxel and a paired walk; the paired ones run as their one-voxel counterparts
+ * when an item has minDistSq > 0) can be timed on the batch and the fastest kept; a batch can be
+ * replayed from a CUDA graph. */
 typedef struct gbfwn_batch_s* gbfwn_batch;
 
 /* A batch keeps device pointers into every item's mesh and output: each item's handle and d_out must
