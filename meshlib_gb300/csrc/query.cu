@@ -203,6 +203,96 @@ __device__ float fwnPacket(const QueryTree& t, const float3& q, bool active, flo
     return __fmul_rn(INV_4PI, PRECISE ? __fsub_rn(acc.s, acc.c) : acc.s);
 }
 
+// Winding numbers of two queries per lane in one packet walk (voxels qa and qb of the lane): the stack
+// carries a lane mask per query, each query takes its own far / near decisions into its own sum in
+// its own depth-first order, so each result equals fwnPacket's for that query bit for bit, while the
+// records and stack steps are shared by 64 queries.
+template <bool PRECISE>
+__device__ void fwnPacket2(const QueryTree& t, const float3& qa, const float3& qb, bool activeA, bool activeB, float betaSq,
+                           unsigned* status, float* wa, float* wb) {
+    const int lane = threadIdx.x & 31;
+    Acc<PRECISE> accA, accB;
+    const float INV_4PI = 1.0f / (4 * 3.14159265358979f);
+    *wa = *wb = 0.f;
+    if (__ballot_sync(FULL, activeA || activeB) == 0 || t.nLeaves == 0) return;
+    const bool needA = activeA && !dipoleTerm<PRECISE>(t.rootDip0, t.rootDip1, qa, betaSq, accA);
+    const bool needB = activeB && !dipoleTerm<PRECISE>(t.rootDip0, t.rootDip1, qb, betaSq, accB);
+    const unsigned rootA = __ballot_sync(FULL, needA), rootB = __ballot_sync(FULL, needB);
+    // stack: node and the two masks, one entry per lane
+    int stNode = 0;
+    unsigned stA = 0, stB = 0;
+    int sp = 0;
+    if (rootA | rootB) {
+        const int rootLink = __float_as_int(t.rootDip1.w);
+        if (rootLink < 0) {
+            leafSolidAngle<PRECISE>(t, ~rootLink, qa, needA, -1, accA);
+            leafSolidAngle<PRECISE>(t, ~rootLink, qb, needB, -1, accB);
+        } else {
+            if (lane == 0) {
+                stNode = rootLink;
+                stA = rootA;
+                stB = rootB;
+            }
+            sp = 1;
+        }
+    }
+    bool overflow = false;
+    while (sp > 0) {
+        --sp;
+        const int node = __shfl_sync(FULL, stNode, sp);
+        const unsigned mA = __shfl_sync(FULL, stA, sp), mB = __shfl_sync(FULL, stB, sp);
+        const float4* rec = t.dip + 4 * int64_t(node);
+        const float4 l0 = ld4(rec), l1 = ld4(rec + 1), r0 = ld4(rec + 2), r1 = ld4(rec + 3);
+        bool nlA = false, nrA = false, nlB = false, nrB = false;
+        if ((mA >> lane) & 1u) {
+            nlA = !dipoleTerm<PRECISE>(l0, l1, qa, betaSq, accA);
+            nrA = !dipoleTerm<PRECISE>(r0, r1, qa, betaSq, accA);
+        }
+        if ((mB >> lane) & 1u) {
+            nlB = !dipoleTerm<PRECISE>(l0, l1, qb, betaSq, accB);
+            nrB = !dipoleTerm<PRECISE>(r0, r1, qb, betaSq, accB);
+        }
+        const unsigned mlA = __ballot_sync(FULL, nlA), mrA = __ballot_sync(FULL, nrA);
+        const unsigned mlB = __ballot_sync(FULL, nlB), mrB = __ballot_sync(FULL, nrB);
+        const int ll = __float_as_int(l1.w), rl = __float_as_int(r1.w);
+        // right subtree below left on the stack, so the left subtree is summed first (as fwnPacket)
+        if (mrA | mrB) {
+            if (rl < 0) {
+                leafSolidAngle<PRECISE>(t, ~rl, qa, nrA, -1, accA);
+                leafSolidAngle<PRECISE>(t, ~rl, qb, nrB, -1, accB);
+            } else if (sp >= kStackDepth) {
+                overflow = true;
+            } else {
+                if (lane == sp) {
+                    stNode = rl;
+                    stA = mrA;
+                    stB = mrB;
+                }
+                ++sp;
+            }
+        }
+        if (mlA | mlB) {
+            if (ll < 0) {
+                leafSolidAngle<PRECISE>(t, ~ll, qa, nlA, -1, accA);
+                leafSolidAngle<PRECISE>(t, ~ll, qb, nlB, -1, accB);
+            } else if (sp >= kStackDepth) {
+                overflow = true;
+            } else {
+                if (lane == sp) {
+                    stNode = ll;
+                    stA = mlA;
+                    stB = mlB;
+                }
+                ++sp;
+            }
+        }
+        if (overflow) break;
+    }
+    if (overflow && lane == 0) atomicOr(status, kStatusStackOverflow);
+    *wa = __fmul_rn(INV_4PI, PRECISE ? __fsub_rn(accA.s, accA.c) : accA.s);
+    *wb = __fmul_rn(INV_4PI, PRECISE ? __fsub_rn(accB.s, accB.c) : accB.s);
+}
+
 // ------------------------------------------------------------------ closest point (packet DFS)
 __device__ __forceinline__ float boxDistSq(const float4& mn, const float4& mx, const float3& p) {
     // MRMesh/MRBox.h:207-220 (reference arithmetic)
@@ -1321,6 +1411,37 @@ __global__ void __launch_bounds__(kThreads, kPairBlocks) gridPairKernel(QueryTre
     }
 }
 
+// Winding numbers of a grid two tiles at a time (fwnPacket2): each lane takes its voxel of the lower
+// tile and the one kTZ layers above; the same values as gridKernel<PRECISE, false>, bit for bit.
+template <bool PRECISE>
+__global__ void __launch_bounds__(kThreads, 4) gridFwnPairKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, float beta,
+                                                                 float* __restrict__ out, unsigned* scratch) {
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % kTX, ly = (lane / kTX) % kTY, lz = lane / (kTX * kTY);
+    const float betaSq = __fmul_rn(beta, beta);
+    const size_t sxy = size_t(g.nx) * g.ny;
+    for (;;) {
+        const unsigned item = nextTicket(scratch, lane);
+        if (item >= tg.numItems) break;
+        const int tx = int(item % unsigned(tg.tilesX));
+        const unsigned rest = item / unsigned(tg.tilesX);
+        const int ty = int(rest % unsigned(tg.tilesY));
+        const int sz = int(rest / unsigned(tg.tilesY));
+        const int x = tx * kTX + lx, y = ty * kTY + ly;
+        const int zBase = g.z0 + sz * tg.segLen * kTZ;
+        const int nSeg = min(tg.segLen, tg.tilesZ - sz * tg.segLen);
+        for (int j = 0; j < nSeg; j += 2) {
+            const int za = zBase + j * kTZ + lz, zb = za + kTZ;
+            const bool inXY = x < g.nx && y < g.ny;
+            const bool activeA = inXY && za < g.z1, activeB = inXY && j + 1 < nSeg && zb < g.z1;
+            float wa, wb;
+            fwnPacket2<PRECISE>(t, xfPoint(xf, x, y, za), xfPoint(xf, x, y, zb), activeA, activeB, betaSq, scratch + 1, &wa, &wb);
+            if (activeA) out[size_t(za - g.zOut) * sxy + size_t(y) * g.nx + x] = wa;
+            if (activeB) out[size_t(zb - g.zOut) * sxy + size_t(y) * g.nx + x] = wb;
+        }
+    }
+}
+
 // The listed pair steps of a precise gridPairKernel launch: each flagged voxel's closest distance by
 // the precise walk (cpPacket, from maxDistSq), written with its sign bit.  Voxels never listed kept
 // FP32 distances no triangle came near the FP64 re-evaluation for: the precise walk's own.  A list
@@ -1761,6 +1882,10 @@ cudaError_t launchSignColumns(const QueryTree& t, const GridRange& g, const Xf& 
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
                           unsigned* scratch, cudaStream_t s) {
     const TileGrid tg = tileGridFor(g);
+    if (tg.segLen >= 2) {  // work items of two or more tiles: the paired walk
+        if (precise) return launchPersistent(gridFwnPairKernel<true>, tg.numItems, scratch, s, t, g, tg, xf, beta, out, scratch);
+        return launchPersistent(gridFwnPairKernel<false>, tg.numItems, scratch, s, t, g, tg, xf, beta, out, scratch);
+    }
     DistOpts o{0.f, FLT_MAX, 0, 0.5f, beta};
     if (precise)
         return launchPersistent(gridKernel<true, false>, tg.numItems, scratch, s, t, g, tg, xf, o, out, scratch);

@@ -1,0 +1,34 @@
+"""The paired walks (two voxels per lane through one packet traversal): winding-number grids equal the
+one-query walk's values at the same points bit for bit, in both arithmetic modes and for slabs."""
+import numpy as np
+import pytest
+
+from meshlib_gb300 import meshgen as mg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_paired_winding_numbers_equal_point_queries(fwn_lib, precise):
+    import meshlib_gb300 as M
+    v, f = mg.noisy_icosphere(seed=3, level=7)
+    g = M.FastWindingNumber(v, f, precise=precise)
+    dims, xf = mg.grid_for(v, 256)  # work items of several tiles: the paired walk
+    xf = np.asarray(xf, np.float32)
+    wn = g.calcFromGrid(dims, xf).reshape(dims[2], dims[1], dims[0])
+    rng = np.random.default_rng(0)
+    idx = rng.integers(0, [dims[0], dims[1], dims[2]], (200_000, 3))
+    # the voxel centres as the grid computes them (left-to-right dots, FP32)
+    fx, fy, fz = (idx[:, k].astype(np.float32) for k in range(3))
+    pts = np.stack([((xf[0] * fx + xf[1] * fy) + xf[2] * fz) + xf[9], ((xf[3] * fx + xf[4] * fy) + xf[5] * fz) + xf[10],
+                    ((xf[6] * fx + xf[7] * fy) + xf[8] * fz) + xf[11]], 1).astype(np.float32)
+    at = g.calcFromVector(pts)
+    grid_at = wn[idx[:, 2], idx[:, 1], idx[:, 0]]
+    assert np.array_equal(grid_at.view(np.uint32), at.view(np.uint32))
+    # slabs of the same grid
+    import torch
+    z0, z1 = 37, 171
+    sl = torch.empty((z1 - z0) * dims[0] * dims[1], device="cuda")
+    g.calcFromGridSlab_dev(dims, xf, z0, z1, sl.data_ptr(), stream=0)
+    torch.cuda.synchronize()
+    assert np.array_equal(sl.cpu().numpy().reshape(z1 - z0, dims[1], dims[0]).view(np.uint32), wn[z0:z1].view(np.uint32))
