@@ -1442,6 +1442,31 @@ __global__ void __launch_bounds__(kThreads, 4) gridFwnPairKernel(QueryTree t, Gr
     }
 }
 
+// Winding numbers of spatially ordered points, two tiles of 32 per work item (fwnPacket2): lane i takes
+// the i-th point of each tile; the same values as vectorKernel<PRECISE, false>, bit for bit.
+template <bool PRECISE>
+__global__ void __launch_bounds__(kThreads, 4) vectorFwnPairKernel(QueryTree t, const float* __restrict__ pts, int64_t n,
+                                                                   float beta, float* __restrict__ out, unsigned* scratch,
+                                                                   const int32_t* __restrict__ order) {
+    const int lane = threadIdx.x & 31;
+    const float betaSq = __fmul_rn(beta, beta);
+    const uint64_t numPairs = (uint64_t(n) + 63) / 64;
+    for (;;) {
+        const unsigned item = nextTicket(scratch, lane);
+        if (item >= numPairs) break;
+        const int64_t ra = int64_t(item) * 64 + lane, rb = ra + 32;  // ranks in processing order
+        const bool activeA = ra < n, activeB = rb < n;
+        const int64_t ia = activeA ? int64_t(order[ra]) : 0, ib = activeB ? int64_t(order[rb]) : 0;
+        float3 qa = make_float3(0.f, 0.f, 0.f), qb = qa;
+        if (activeA) qa = make_float3(pts[3 * ia], pts[3 * ia + 1], pts[3 * ia + 2]);
+        if (activeB) qb = make_float3(pts[3 * ib], pts[3 * ib + 1], pts[3 * ib + 2]);
+        float wa, wb;
+        fwnPacket2<PRECISE>(t, qa, qb, activeA, activeB, betaSq, scratch + 1, &wa, &wb);
+        if (activeA) out[ia] = wa;
+        if (activeB) out[ib] = wb;
+    }
+}
+
 // The listed pair steps of a precise gridPairKernel launch: each flagged voxel's closest distance by
 // the precise walk (cpPacket, from maxDistSq), written with its sign bit.  Voxels never listed kept
 // FP32 distances no triangle came near the FP64 re-evaluation for: the precise walk's own.  A list
@@ -1953,6 +1978,11 @@ cudaError_t launchVectorFwn(const QueryTree& t, const float* pts, int64_t n, flo
                             float* out, unsigned* scratch, cudaStream_t s, const int32_t* order) {
     DistOpts o{0.f, FLT_MAX, 0, 0.5f, beta};
     const uint64_t tiles = (uint64_t(n) + 31) / 32;
+    if (order && skipFace < 0) {  // spatially ordered points, no face skipped: two tiles per walk
+        const uint64_t pairs = (tiles + 1) / 2;
+        if (precise) return launchPersistent(vectorFwnPairKernel<true>, pairs, scratch, s, t, pts, n, beta, out, scratch, order);
+        return launchPersistent(vectorFwnPairKernel<false>, pairs, scratch, s, t, pts, n, beta, out, scratch, order);
+    }
     if (precise)
         return launchPersistent(vectorKernel<true, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order, 1);
     return launchPersistent(vectorKernel<false, false>, tiles, scratch, s, t, pts, n, o, skipFace, out, scratch, order, 1);

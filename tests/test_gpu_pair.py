@@ -32,3 +32,18 @@ def test_paired_winding_numbers_equal_point_queries(fwn_lib, precise):
     g.calcFromGridSlab_dev(dims, xf, z0, z1, sl.data_ptr(), stream=0)
     torch.cuda.synchronize()
     assert np.array_equal(sl.cpu().numpy().reshape(z1 - z0, dims[1], dims[0]).view(np.uint32), wn[z0:z1].view(np.uint32))
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_paired_point_winding_numbers(fwn_lib, precise):
+    """Large point sets (Morton-ordered, two tiles per walk) give each point the same winding number as
+    small batches of the same points (one tile per walk), bit for bit."""
+    import meshlib_gb300 as M
+    v, f = mg.noisy_icosphere(seed=8, level=6)
+    g = M.FastWindingNumber(v, f, precise=precise)
+    rng = np.random.default_rng(4)
+    pts = np.concatenate([v[rng.integers(0, len(v), 60_000)] * rng.uniform(0.99, 1.01, (60_000, 1)),
+                          rng.uniform(-1.3, 1.3, (40_001, 3))]).astype(np.float32)
+    whole = g.calcFromVector(pts)
+    parts = np.concatenate([g.calcFromVector(pts[i:i + 5000]) for i in range(0, len(pts), 5000)])
+    assert np.array_equal(whole.view(np.uint32), parts.view(np.uint32))
