@@ -141,7 +141,7 @@ __global__ void packKernel(const RefNode* __restrict__ nodes, int64_t nNodes, co
         const float e1x = b.x - a.x, e1y = b.y - a.y, e2x = c.x - a.x, e2y = c.y - a.y;
         const float area2 = fmaf(e1x, e2y, -e1y * e2x);
         const float len2 = fmaf(e1x, e1x, e1y * e1y) + fmaf(e2x, e2x, e2y * e2y) + fmaf(c.x - b.x, c.x - b.x, (c.y - b.y) * (c.y - b.y));
-        const float vertical = fabsf(area2) <= 1e-5f * len2 ? 1.f : 0.f;
+        const float vertical = fabsf(area2) <= 1e-6f * len2 ? 1.f : 0.f;
         tri[3 * int64_t(s) + 0] = make_float4(a.x, a.y, a.z, __int_as_float(nd.l));
         tri[3 * int64_t(s) + 1] = make_float4(b.x, b.y, b.z, vertical);
         tri[3 * int64_t(s) + 2] = make_float4(c.x, c.y, c.z,
