@@ -159,19 +159,19 @@ def cpu_reference_rate(v, f, dims, xf, seconds=12.0, threads=None, want_counts=T
 
 
 # DRAM bytes (read + write) of one launch of the signed-distance grid kernel at 512^3 on this
-# workload: dram__bytes_read.sum 567,815,168 + dram__bytes_write.sum 640,902,400 from one ncu
+# workload: dram__bytes_read.sum 607,253,248 + dram__bytes_write.sum 653,923,328 from one ncu
 # capture of the same kernel (a constant copied from that capture, not measured by this run; the
 # committed profile summary under profiles/ gives the command).  536,870,912 of the written bytes
 # are the output grid.
-KERNEL_DRAM_BYTES_512 = 567_815_168 + 640_902_400
+KERNEL_DRAM_BYTES_512 = 607_253_248 + 653_923_328
 
 
 # Counters of the signed-distance grid kernel at 256^3 on this workload from one ncu capture
 # (constants copied from that capture, not measured by this run): FMA-pipe utilisation
 # (sm__pipe_fma_cycles_active), issue-slot utilisation and active lanes per warp instruction.
-KERNEL_FMA_PIPE_ACTIVE = 0.362
-KERNEL_ISSUE_ACTIVE = 0.878
-KERNEL_LANES_PER_INSTR = 25.09
+KERNEL_FMA_PIPE_ACTIVE = 0.351
+KERNEL_ISSUE_ACTIVE = 0.882
+KERNEL_LANES_PER_INSTR = 24.92
 
 
 def fp32_peak_tflops(device: int = 0, reps: int = 5) -> float:
@@ -749,7 +749,7 @@ def main():
                                     "The bound that holds is instruction issue: dram_frac_actual (measured DRAM bytes "
                                     "per launch / step time / peak) is well under 1 %, issue_active_ncu is the busy "
                                     "fraction of the issue slots (ncu, 256^3 capture)",
-                            "duration": "the timed step's CUDA-event time: the grid kernel (the paired walk, 65.2 ms of the "
+                            "duration": "the timed step's CUDA-event time: the grid kernel (the paired walk, 63.3 ms of the "
                                         "step in the ncu launch list) and, before it, the column sign pass (crossing lists + "
                                         "column sweep, 0.33 ms) and after it the precise re-walk of the listed voxels (0.1 ms)"}
         try:
@@ -765,7 +765,7 @@ def main():
                         "fma_pipe_active_ncu": KERNEL_FMA_PIPE_ACTIVE,
                         "note": "reference-equivalent FLOP/s counts the reference traversal's box tests, projections, "
                                 "dipoles and solid angles per voxel; the packet traversal does far fewer, and ncu shows the "
-                                "FMA pipe 36% busy: the kernel is bound by instruction issue and dependent loads"}
+                                "FMA pipe 35% busy: the kernel is bound by instruction issue and dependent loads"}
         line["cpu_baseline"] = cpu_baseline_fields(rate, thr, desc)
         line["precision"] = precision_vs_fp64(v, f, dims, xf, out, shell, shell_d, extra=prec_extra, M=M, device=local)
     if rank == 0:
