@@ -47,3 +47,26 @@ def test_paired_point_winding_numbers(fwn_lib, precise):
     whole = g.calcFromVector(pts)
     parts = np.concatenate([g.calcFromVector(pts[i:i + 5000]) for i in range(0, len(pts), 5000)])
     assert np.array_equal(whole.view(np.uint32), parts.view(np.uint32))
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_paired_signed_distance_slabs(fwn_lib, precise):
+    """Slabs of a 256^3 signed-distance grid (paired walk, its fix-up pass and the column signs over
+    each slab's own range) stack to the whole grid, bit for bit, unbanded and banded."""
+    import torch
+
+    import meshlib_gb300 as M
+    v, f = mg.noisy_icosphere(seed=9, level=7)
+    g = M.FastWindingNumber(v, f, precise=precise)
+    dims, xf = mg.grid_for(v, 256)
+    n = int(np.prod(dims))
+    for opts in (None, M.DistanceToMeshOptions(maxDistSq=(0.02 * mg.diag(v)) ** 2)):
+        whole = torch.empty(n, device="cuda")
+        g.calcFromGridWithDistances_dev(dims, xf, whole.data_ptr(), options=opts, stream=0)
+        parts = []
+        for z0, z1 in ((0, 90), (90, 200), (200, 256)):
+            t = torch.empty((z1 - z0) * dims[0] * dims[1], device="cuda")
+            g.calcFromGridWithDistancesSlab_dev(dims, xf, z0, z1, t.data_ptr(), options=opts, stream=0)
+            parts.append(t)
+        torch.cuda.synchronize()
+        assert torch.equal(torch.cat(parts).view(torch.int32), whole.view(torch.int32))
