@@ -848,9 +848,10 @@ GBFWN_API size_t gbfwn_from_grid_memory(int64_t nv, int64_t nt, const int32_t di
     const size_t vox = dims ? size_t(std::max(dims[0], 0)) * size_t(std::max(dims[1], 0)) * size_t(std::max(dims[2], 0)) : 0;
     const size_t tiles = (dims && vox) ? size_t(gridTiles(dims[0], dims[1], dims[2])) : 0;
     const size_t items = std::min(tiles, tiles / 16 + size_t(50) * size_t(numSMs()) * 32);
-    // the inside bits of a closed mesh's grid and its columns' crossing lists (72 bytes per column)
+    // the inside bits of a closed mesh's grid, its columns' crossing lists (72 bytes per column) and
+    // the paired walk's fix list (16 bytes per two warp tiles and per work item)
     const size_t bits = dims && vox ? size_t((dims[0] + 31) / 32) * size_t(dims[1]) * size_t(dims[2]) * 4 +
-                                          size_t(dims[0]) * size_t(dims[1]) * 72 + 512
+                                          size_t(dims[0]) * size_t(dims[1]) * 72 + 512 + tiles * 8 + items * 16 + 32
                                     : 0;
     return gbfwn_mesh_memory(nv, nt) + vox * sizeof(float) + items * 32 * sizeof(float) + bits;
 }

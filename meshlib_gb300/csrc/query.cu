@@ -946,8 +946,9 @@ __global__ void __launch_bounds__(kThreads) columnRasterKernel(QueryTree t, Grid
             A = ld4(tr);
             B = ld4(tr + 1);
             C = ld4(tr + 2);
-            // the widened bounds relative to the grid's origin, mapped to index space in FP32 with
-            // their error bound as margin (8 ulps of the terms' magnitudes; FP64 issues far slower)
+            // the widened bounds relative to the grid's origin, mapped to index space in FP32 with a
+            // margin of 1e-6 of the terms' magnitudes (about 17 ulps, several times the mapping's
+            // rounding; FP64 issues far slower)
             const float x0 = __fsub_rn(__fsub_rn(fminf(A.x, fminf(B.x, C.x)), cl.ex), cl.org[0]);
             const float x1 = __fadd_rn(__fsub_rn(fmaxf(A.x, fmaxf(B.x, C.x)), cl.org[0]), cl.ex);
             const float y0 = __fsub_rn(__fsub_rn(fminf(A.y, fminf(B.y, C.y)), cl.ey), cl.org[1]);

@@ -49,9 +49,10 @@ def test_memory_estimators(fwn_lib):
     est = M.memory_estimates(655362, 1310720, dims=(512, 512, 512), npts=4_000_000)
     # the result, the signed-distance columns' hand-over words (128 B per column of >= 16 tiles, or of
     # fewer tiles while under 50 items per resident warp remain), and for closed meshes the inside
-    # bits (1 bit per voxel) and the crossing lists (72 B per grid column)
-    extra = est["from_grid"] - est["mesh"] - 512 ** 3 * 4 - 512 ** 3 // 8 - 512 * 512 * 72 - 512
-    assert 0 < extra <= 512 ** 3 // 4 + 50 * 160 * 32 * 128
+    # bits (1 bit per voxel), the crossing lists (72 B per grid column) and the paired walk's fix list
+    # (16 B per two tiles of 32 voxels and per work item)
+    extra = est["from_grid"] - est["mesh"] - 512 ** 3 * 4 - 512 ** 3 // 8 - 512 * 512 * 72 - 512 - 512 ** 3 // 32 * 8 - 32
+    assert 0 < extra <= (512 ** 3 // 4 + 50 * 160 * 32 * 128) * (1 + 16 / 128)
     # points in and results out, Morton order and its sort scratch
     assert est["from_vector"] - est["mesh"] == 4_000_000 * 40 + 4096
     # the peak is the build: 352 B kept and up to 244 B of work arrays per face, 12 B per vertex
