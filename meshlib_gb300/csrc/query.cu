@@ -1000,8 +1000,9 @@ __global__ void __launch_bounds__(kThreads) columnRasterKernel(QueryTree t, Grid
     }
 }
 
-// For the grid columns of the launch (32 consecutive x per warp, in segments of kColumnSeg layers,
-// each with its own ray): inside = (winding number of the voxel > threshold), written as bits (one
+// For the grid columns of the launch (32 consecutive x per warp, in segments of kColumnSeg layers;
+// the crossings from the columns' lists, or a column's own ray where its list overflowed or there are
+// no lists): inside = (winding number of the voxel > threshold), written as bits (one
 // word per 32 voxels along x, layout (z - zOut, y, x / 32)) or applied to `values` (negated where
 // inside; value index (z - zOut) nx ny + y nx + x).  The range [z0, z1) of dims is covered.
 constexpr int kColumnSeg = 128;
