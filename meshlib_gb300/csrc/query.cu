@@ -1417,6 +1417,8 @@ __global__ void __launch_bounds__(kThreads, kPairBlocks) gridPairKernel(QueryTre
 
 // Winding numbers of a grid two tiles at a time (fwnPacket2): each lane takes its voxel of the lower
 // tile and the one kTZ layers above; the same values as gridKernel<PRECISE, false>, bit for bit.
+// 4 blocks per SM (64 registers): at 512^3 on 1.31 M triangles 19.7 ms, against 20.7 ms at 3 and
+// 29.6 ms at 5 (spills).
 template <bool PRECISE>
 __global__ void __launch_bounds__(kThreads, 4) gridFwnPairKernel(QueryTree t, GridRange g, TileGrid tg, Xf xf, float beta,
                                                                  float* __restrict__ out, unsigned* scratch) {
