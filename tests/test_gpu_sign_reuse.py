@@ -394,3 +394,9 @@ def test_paired_walk_with_voxels_on_the_surface(M, precise):
             g.set_sign_reuse(True)
             _same(*res)
             assert (res[0] == 0).any() or cf is f
+            if opts is not None:  # the banded bricks (exact cull): paired walk over brick runs, fix-up
+                import torch
+                out = torch.full((int(np.prod(d)),), 7.0, device="cuda")
+                g.calcFromGridWithDistancesBanded_dev(d, x, out.data_ptr(), opts, None, stream=0)
+                torch.cuda.synchronize()
+                _same(out.cpu().numpy(), res[1])
