@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden,-ffp-contract=off", "--expt-relaxed-constexpr"]
 # build.cu must round every float operation separately (bit-identical boxes and dipoles)
 PER_FILE = {"build.cu": ["-fmad=false"], "treebuild.cu": ["-fmad=false"]}
-SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "mlp_gemm.cu", "mlp_net.cu", "mlp_train.cu", "surrogate.cu", "batch.cu", "sort.cu",
+SOURCES = ["capi.cu", "build.cu", "treebuild.cu", "query.cu", "columns.cu", "mlp_gemm.cu", "mlp_net.cu", "mlp_train.cu", "surrogate.cu", "batch.cu", "sort.cu",
            "projector.cu", "mc.cu"]
 # measurement support for bench.py (the FP32 FMA peak), kept out of the product library
 BENCH_SOURCES = ["bench/fp32_peak.cu"]

@@ -87,7 +87,7 @@ enum : unsigned {
 };
 
 // ---------------------------------------------------------------------------------------------
-// Kernel launchers (query.cu).  All take a `scratch` pointer to two device words: [0] = work
+// Kernel launchers (query.cu; the column sign pass in columns.cu).  All take a `scratch` pointer to two device words: [0] = work
 // queue ticket counter, [1] = status bits.  The launchers reset the ticket counter themselves.
 cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, float beta, int precise, float* out,
                           unsigned* scratch, cudaStream_t s);
@@ -98,7 +98,7 @@ cudaError_t launchGridFwn(const QueryTree& t, const GridRange& g, const Xf& xf, 
 cudaError_t launchGridSdf(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o, int precise,
                           float* out, unsigned* scratch, cudaStream_t s, float* colState = nullptr, size_t colBytes = 0);
 size_t gridSdfColumnStateBytes(const QueryTree& t, const GridRange& g, const Xf& xf, const DistOpts& o);
-// Signs of a closed mesh's grid from one vertical ray per (x, y) column (query.cu, signColumnsKernel):
+// Signs of a closed mesh's grid from its vertical columns' crossings (columns.cu, signColumnsKernel):
 // applicable when signColumnsApply; writes inside bits (one 32-bit word per 32 voxels along x, layout
 // (z - zOut, y, x / 32)) or negates `values` where the voxel is inside.
 bool signColumnsApply(const QueryTree& t, const Xf& xf, float beta, float threshold);
