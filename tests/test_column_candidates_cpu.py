@@ -1,4 +1,4 @@
-"""The column pass's candidate columns (query.cu, columnRasterKernel and launchSignColumns): for a
+"""The column pass's candidate columns (columns.cu, columnRasterKernel and launchSignColumns): for a
 triangle, the columns whose FP32 centre (x, y) lies in the triangle's closed (x, y) bounds must all be
 candidates, however the grid is placed, scaled or turned about z and however far from the origin.  This
 restates the candidate arithmetic in numpy FP32 (the widening by twice the centres' rounding, the FP32
