@@ -70,3 +70,26 @@ def test_paired_signed_distance_slabs(fwn_lib, precise):
             parts.append(t)
         torch.cuda.synchronize()
         assert torch.equal(torch.cat(parts).view(torch.int32), whole.view(torch.int32))
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_ordered_point_distances(fwn_lib, precise):
+    """Signed distances at large point sets (Morton-ordered and walked in that order) equal those of
+    small batches of the same points (unordered), bit for bit: shell points, points in the box, the
+    mesh's own vertices (on the surface) and, for a self-intersecting closed mesh, points inside both
+    parts.  (A paired walk for points, two tiles per walk with paired rays, measured slower: 4 M shell
+    points 3.94 -> 4.13 ms, so points keep one tile per walk for distances.)"""
+    import meshlib_gb300 as M
+    rng = np.random.default_rng(5)
+    for v, f in (mg.noisy_icosphere(seed=10, level=6), mg.overlapping_spheres(seed=5, level=5)):
+        g = M.FastWindingNumber(v, f, precise=precise)
+        pts = np.concatenate([v[rng.integers(0, len(v), 50_000)] * rng.uniform(0.995, 1.005, (50_000, 1)),
+                              rng.uniform(v.min(0) - 0.2, v.max(0) + 0.2, (40_000, 3)), v[:10_000]]).astype(np.float32)
+        rng.shuffle(pts)
+        for opts in (None, M.DistanceToMeshOptions(maxDistSq=0.01)):
+            whole = g.calcWithDistances(pts, opts)
+            parts = np.concatenate([g.calcWithDistances(pts[i:i + 5000], opts) for i in range(0, len(pts), 5000)])
+            assert np.array_equal(np.isnan(whole), np.isnan(parts))
+            m = ~np.isnan(whole)
+            assert np.array_equal(whole[m].view(np.uint32), parts[m].view(np.uint32))
+            assert (whole[m] == 0).any()
