@@ -22,6 +22,10 @@ def test_batch_matches_single_calls(fwn_lib, tmp_path, monkeypatch):
         g = M.FastWindingNumber(v, f)
         dims, xf = mg.grid_for(v, n)
         dims = (n, n + k, max(3, n - 2 * k))  # uneven, non-cubic
+        if k == 2:  # a tilted grid: the paired variants project the upper voxel on its own
+            c, s_ = np.float32(np.cos(0.3)), np.float32(np.sin(0.3))
+            xf = np.asarray(xf, np.float32).copy()
+            xf[:9] = (xf[:9].reshape(3, 3) @ np.array([[c, 0, s_], [0, 1, 0], [-s_, 0, c]], np.float32)).reshape(-1)
         opts = M.DistanceToMeshOptions(maxDistSq=0.05) if k == 1 else None
         ref = torch.empty(int(np.prod(dims)), device="cuda")
         g.calcFromGridWithDistances_dev(dims, xf, ref.data_ptr(), options=opts, stream=s.cuda_stream)
@@ -77,3 +81,42 @@ def test_mesh_of_live_batch_cannot_be_destroyed(fwn_lib):
     b.close()
     g.close()
     assert not g.handle.value
+
+
+def test_batch_with_a_lower_distance_bound(fwn_lib):
+    """An item with minDistSq > 0: a walk stops at the first distance <= minDistSq it meets (the
+    reference's early stop), so below that bound a value depends on the walk's order and only the
+    bound is guaranteed; every other voxel, and the sign of every voxel, equals the single calls in
+    every variant (the paired ones run as their one-voxel counterparts)."""
+    import torch
+
+    import meshlib_gb300 as M
+    from meshlib_gb300 import meshgen as mg
+    items, refs, outs, lows = [], [], [], []
+    for k, (v, f) in enumerate((mg.noisy_icosphere(seed=6, level=4), mg.noisy_torus(seed=7))):
+        g = M.FastWindingNumber(v, f)
+        dims, xf = mg.grid_for(v, 40)
+        opts = M.DistanceToMeshOptions(minDistSq=0.001, maxDistSq=0.05, nullOutsideMinMax=False) if k == 0 else None
+        lows.append(0.001 if k == 0 else 0.0)
+        ref = torch.empty(int(np.prod(dims)), device="cuda")
+        g.calcFromGridWithDistances_dev(dims, xf, ref.data_ptr(), options=opts, stream=0)
+        out = torch.full_like(ref, 7.0)
+        items.append((g, dims, xf, opts, out.data_ptr()))
+        refs.append(ref)
+        outs.append(out)
+    b = M.Batch(items)
+    torch.cuda.synchronize()
+    for c in range(len(M.Batch.configs())):
+        for o in outs:
+            o.fill_(7.0)
+        b.set_config(c)
+        b.run_dev(stream=0)
+        torch.cuda.synchronize()
+        for r, o, low in zip(refs, outs, lows):
+            assert torch.equal(torch.isnan(r), torch.isnan(o))
+            fin = ~torch.isnan(r)
+            assert torch.equal(torch.signbit(r[fin]), torch.signbit(o[fin])), c
+            above = fin & (r * r >= low)
+            assert torch.equal(r[above], o[above]), c
+            below = fin & (r * r < low)
+            assert bool((o[below] * o[below] <= low).all()), c
